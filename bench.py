@@ -1,0 +1,376 @@
+"""Benchmark of the HairMSNN per-path-vertex hot path on GB300.
+
+python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                [--workload render|vertex]
+
+Workloads (synthetic, seeded):
+  render  full wavefront render of procedural straight hair: 10k strands x
+          64 cubic B-spline control points, head ellipsoid, sky + directional
+          light, 512x512, path_v1=1, path_v2=40, BETA=1, online cache
+          training 2^16 records/frame.  One step = one frame (1 spp, as the
+          reference's render loop: G-buffer paths + train + infer + compose).
+          metric: paths/s.
+  vertex  2^18 hair-vertex queries: BSDF eval + BSDF importance sample +
+          cache-network inference (Freq-12 / OneBlob-32 / Identity -> 5x64).
+          metric: vertex queries/s.
+
+One JSON line is printed by rank 0.  `value` times the kernels with inputs
+resident in HBM (CUDA events per step on the launching stream, L2 flushed
+between steps outside the events); `e2e` times the same step through the
+public API with pinned host inputs copied in and results copied out inside
+the timed region.  Multi-GPU runs are independent replicas (the path has no
+exchange step on one box).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_VERTEX = 1 << 18
+MLP_FLOP_W64 = 2 * (209 * 64 + 4 * 64 * 64 + 64 * 3)  # 59,904 per query
+BSDF_EVAL_BYTES = 40 + 16
+BSDF_SAMPLE_BYTES = 44 + 28
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.isfile(path):
+        p = json.load(open(path))
+        return {"hbm_gbs": p["hbm_gbs"], "bf16_tflops": p["bf16_tflops"],
+                "bf16_tflops_sustained": p.get("bf16_tflops_sustained", p["bf16_tflops"]),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "source": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for i, nm in enumerate(names):
+                if f[5 + i].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ============================================================ vertex workload
+class VertexWorkload:
+    name = "vertex"
+    metric = "hair-vertex queries/s (BSDF eval + importance sample + cache-MLP inference)"
+    unit = "queries/s"
+
+    def __init__(self, torch, n=N_VERTEX):
+        import numpy as np
+        import hairmsnn_gb300 as hm
+        from hairmsnn_gb300 import mlp
+        self.torch, self.hm, self.n = torch, hm, n
+        self.wo, self.wi, self.t, self.h, self.u = hm.gen_bsdf_queries(0, n)
+        rng = np.random.default_rng(0)
+        x = np.zeros((n, 16), np.float32)
+        x[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+        x[:, 3:7] = rng.uniform(0, 1, (n, 4))
+        x[:, 7] = rng.uniform(-1, 1, n)
+        x[:, 8:11] = [0.06, 0.1, 0.2]
+        x[:, 11:13] = 0.3
+        self.x_host = torch.from_numpy(x).pin_memory()
+        self.x = self.x_host.cuda()
+        self.net = mlp.TinyMLP("c1_cache_w64.json", 16, 3, seed=0)
+        self.out = torch.empty((n, 3), device="cuda")
+        self.kernels_per_step = 4  # eval, sample, encode, fused MLP
+        # pinned host copies for the end-to-end leg
+        self.host_in = [a.cpu().pin_memory() for a in (self.wo, self.wi, self.t, self.h, self.u)]
+        self.h2d_bytes = sum(a.numel() * 4 for a in self.host_in) + self.x_host.numel() * 4
+        self.d2h_bytes = (3 * n + n + 3 * n + 3 * n + n) * 4 + n * 3 * 4
+        self.host_out = [torch.empty(s, dtype=torch.float32).pin_memory()
+                         for s in ((3, n), (n,), (3, n), (3, n), (n,), (n, 3))]
+
+    def step(self, events=None):
+        hm = self.hm
+        ev = events
+        if ev: ev[0].record()
+        f, pdf = hm.bsdf_eval(self.wo, self.wi, self.t, self.h)
+        if ev: ev[1].record()
+        wi2, f2, pdf2 = hm.bsdf_sample(self.wo, self.t, self.h, self.u)
+        if ev: ev[2].record()
+        self.net.inference(self.x, self.out)
+        if ev: ev[3].record()
+        return f, pdf, wi2, f2, pdf2
+
+    def e2e_step(self):
+        torch = self.torch
+        dev = [a.to("cuda", non_blocking=True) for a in self.host_in]
+        xd = self.x_host.to("cuda", non_blocking=True)
+        f, pdf = self.hm.bsdf_eval(dev[0], dev[1], dev[2], dev[3])
+        wi2, f2, pdf2 = self.hm.bsdf_sample(dev[0], dev[2], dev[3], dev[4])
+        out = self.net.inference(xd)
+        for h, d in zip(self.host_out, (f, pdf, wi2, f2, pdf2, out)):
+            h.copy_(d, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+
+    def n_events(self):
+        return 4
+
+    def units_per_step(self):
+        return self.n
+
+    def roofline(self, seg_ms, pk):
+        """seg_ms: mean ms of [eval, sample, mlp]; dominant = the longest."""
+        n = self.n
+        segs = {
+            "bsdf_eval_kernel": ("hbm", BSDF_EVAL_BYTES * n / (seg_ms[0] * 1e-3) / 1e9, pk["hbm_gbs"], "GB/s",
+                                 seg_ms[0]),
+            "bsdf_sample_kernel": ("hbm", BSDF_SAMPLE_BYTES * n / (seg_ms[1] * 1e-3) / 1e9, pk["hbm_gbs"], "GB/s",
+                                   seg_ms[1]),
+            "mlp_fwd_kernel<64> (+encode)": ("tensor", MLP_FLOP_W64 * n / (seg_ms[2] * 1e-3) / 1e12,
+                                             pk["bf16_tflops"], "TFLOP/s", seg_ms[2]),
+        }
+        name = max(segs, key=lambda k: segs[k][4])
+        bound, ach, peak, unit, ms = segs[name]
+        return {"kernel": name, "bound": bound, "achieved": round(ach, 3), "peak": peak, "unit": unit,
+                "frac": round(ach / peak, 5), "traffic": None,
+                "note": f"peak = {pk['source']} ({'HBM copy' if bound == 'hbm' else 'cuBLAS bf16 burst'})",
+                "per_kernel_ms": {k: round(v[4], 4) for k, v in segs.items()}}
+
+    def config(self):
+        return {"workload": "vertex: 2^18 hair-vertex queries, BSDF eval+sample (alpha=2deg, beta_m=beta_n=0.3, "
+                            "sigma_a=(0.06,0.1,0.2)) + cache MLP Freq12/OneBlob32/Identity->5x64 FP32",
+                "queries": self.n, "l2": "flushed between timed steps (256 MiB write)",
+                "parallelism": "replicas"}
+
+    def cpu_baseline(self, threads, budget_s=10.0):
+        """Oracle port: BSDF eval + sample (C++ threads) + FP64 numpy MLP, bounded sample."""
+        import numpy as np
+        from oracle import mlp_oracle as mo
+        from oracle import pyoracle as po
+        n = 1 << 14
+        wo, wi, t, h, u = po.gen_bsdf_queries(0, n)
+        cfg = mo.Config(self.net.config_text, 16, 3)
+        params = self.net.params().astype(np.float64)
+        x = self.x_host[:n].numpy()
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            po.hair_eval(wo.T, wi.T, t.T, h, threads=threads)
+            po.hair_sample(wo.T, t.T, h, u.T, threads=threads)
+            mo.forward(cfg, params, x)
+            reps += 1
+            el = time.perf_counter() - t0
+            if el > budget_s or reps >= 50:
+                break
+        return {"value": round(reps * n / el, 1), "unit": self.unit, "cores": threads, "kind": "port",
+                "sample": f"{reps} x {n} queries (eval+sample C++ on {threads} threads, MLP FP64 numpy)"}
+
+
+def make_workload(name, torch):
+    if name == "vertex":
+        return VertexWorkload(torch)
+    from hairmsnn_gb300 import render as _r  # noqa: F401  (render workload)
+    return _r.RenderBenchWorkload(torch)
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU-side restatement (oracle port) of
+    the same workload on all host threads; no GPU work."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+    from oracle import pyoracle as po
+    threads = host_threads()
+    n = 1 << 14
+    wo, wi, t, h, u = po.gen_bsdf_queries(0, n)
+    if args.workload == "vertex":
+        from oracle import mlp_oracle as mo
+        cfg_text = open(os.path.join(ROOT, "hairmsnn_gb300", "configs", "c1_cache_w64.json")).read()
+        cfg = mo.Config(cfg_text, 16, 3)
+        params = np.random.default_rng(0).normal(scale=0.1, size=cfg.n_params)
+        x = np.random.default_rng(1).uniform(0, 1, (n, 16)).astype(np.float32)
+
+        def step():
+            po.hair_eval(wo.T, wi.T, t.T, h, threads=threads)
+            po.hair_sample(wo.T, t.T, h, u.T, threads=threads)
+            mo.forward(cfg, params, x)
+        units, metric, unit = n, VertexWorkload.metric, VertexWorkload.unit
+        sample = f"{n} queries per step (oracle port: C++ BSDF on {threads} threads + FP64 numpy MLP)"
+        cfgd = {"workload": "vertex (bounded sample)", "queries_per_step": n}
+    else:
+        from oracle import render_oracle as ro
+        step, units, sample, cfgd = ro.reference_step_factory(threads)
+        metric, unit = "paths/s at fixed relMSE vs PT", "paths/s"
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    ms = 1e3 * sum(times) / len(times)
+    value = units / (ms * 1e-3)
+    line = {"impl": "reference", "metric": metric, "value": round(value, 2), "unit": unit, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": cfgd,
+            "cpu_baseline": {"value": round(value, 2), "unit": unit, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 2), "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "vertex"),
+                    choices=["render", "vertex"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    from hairmsnn_gb300 import build
+    build.build()
+    wl = make_workload(args.workload, torch)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        wl.step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    ne = wl.n_events()
+    all_events = [[torch.cuda.Event(enable_timing=True) for _ in range(ne)] for _ in range(args.steps)]
+    sampler = ClockSampler(local if ws > 1 else 0)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler.start()
+    time.sleep(0.3)
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)  # > L2 write between steps, outside the step events
+        wl.step(all_events[k])
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    step_ms = [ev[0].elapsed_time(ev[-1]) for ev in all_events]
+    seg_ms = [statistics.mean(ev[i].elapsed_time(ev[i + 1]) for ev in all_events) for i in range(ne - 1)]
+    ms = statistics.mean(step_ms)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    units = wl.units_per_step() * ws
+    value = units / (ms * 1e-3)
+
+    # ---- end-to-end through the public API (pinned host in/out in the timed region)
+    for _ in range(2):
+        wl.e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        wl.e2e_step()
+    torch.cuda.synchronize()
+    e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    if rank != 0:
+        return 0
+    pk = peaks()
+    roof = wl.roofline(seg_ms, pk)
+    line = {"metric": wl.metric, "value": round(value, 2), "unit": wl.unit, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene / queries)",
+            "config": wl.config(),
+            "e2e": {"value": round(wl.units_per_step() * ws / (e2e_ms * 1e-3), 2), "unit": wl.unit,
+                    "h2d_bytes_per_step": wl.h2d_bytes, "d2h_bytes_per_step": wl.d2h_bytes},
+            "gpu_launches": wl.kernels_per_step * args.steps,
+            "roofline": roof, "clocks": clocks}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = wl.cpu_baseline(host_threads())
+    print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

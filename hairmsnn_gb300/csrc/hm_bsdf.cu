@@ -1,0 +1,207 @@
+// Batched hair-BSDF kernels behind the C ABI (include/hairmsnn.h):
+// hm_bsdf_eval / hm_bsdf_sample replace per-hit calls of the reference's
+// disney_hair() / sample_disney_hair() (cuda_headers/disney_hair.cuh:186,277).
+//
+// Data layout: planar structure-of-arrays ([3][n] for vectors), one query per
+// thread, so every warp-wide load or store is one contiguous 128-byte line
+// per plane.  Inputs are read once through the non-coherent path and outputs
+// are written with streaming stores (nothing is re-read).
+#include <math.h>
+
+#include "hm_hair_bsdf.cuh"
+
+namespace hm {
+
+// setupHairShading (disney_hair.cuh:26-41) and every other material-only term,
+// evaluated once on the host in the same single-precision order.
+HairConsts hair_consts_from_params(const hm_hair_params& p) {
+  HairConsts hc;
+  const float bm = p.beta_m, bn = p.beta_n;
+  hc.v[0] = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * powf(bm, 20.f));
+  hc.v[1] = (float)(.25 * (double)hc.v[0]);
+  hc.v[2] = 4.f * hc.v[0];
+  hc.s = kSqrtPiOver8 * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * powf(bn, 22.f));
+  hc.v[3] = hc.s;
+  hc.sin2k[0] = sinf(p.alpha);
+  hc.cos2k[0] = safe_sqrt(1.f - sqr(hc.sin2k[0]));
+  for (int i = 1; i < 3; ++i) {
+    hc.sin2k[i] = 2.f * hc.cos2k[i - 1] * hc.sin2k[i - 1];
+    hc.cos2k[i] = sqr(hc.cos2k[i - 1]) - sqr(hc.sin2k[i - 1]);
+  }
+  for (int i = 0; i < 3; ++i) hc.sigma_a[i] = p.sigma_a[i];
+  hc.gain[0] = p.gain_r;
+  hc.gain[1] = p.gain_tt;
+  hc.gain[2] = p.gain_trt;
+  hc.gain[3] = p.gain_trrt;
+  auto cdf = [&](float x) { return 1.f / (1.f + expf(-x / hc.s)); };  // LogisticCDF :123-125
+  hc.trim_den = cdf(kPi) - cdf(-kPi);
+  hc.cdf_lo = cdf(-kPi);
+  for (int k = 0; k < 3; ++k) {
+    hc.inv_v[k] = 1.f / hc.v[k];
+    hc.mp_logc[k] = logf(1.f / (2.f * hc.v[k]));
+    hc.mp_den[k] = sinhf(1.f / hc.v[k]) * 2.f * hc.v[k];
+  }
+  for (int k = 0; k < 4; ++k) hc.exp_m2v[k] = expf(-2.f / hc.v[k]);
+  hc.fp64_mp = bm < 0.1f ? 1 : 0;
+  return hc;
+}
+
+HM_D float ldg(const float* p) { return __ldg(p); }
+
+__global__ void __launch_bounds__(256) bsdf_eval_kernel(HairConsts hc, const float* __restrict__ wo,
+                                                        const float* __restrict__ wi,
+                                                        const float* __restrict__ t,
+                                                        const float* __restrict__ h,
+                                                        float* __restrict__ f,
+                                                        float* __restrict__ pdf, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const f3 w_o = mk(ldg(wo + i), ldg(wo + n + i), ldg(wo + 2 * n + i));
+    const f3 w_i = mk(ldg(wi + i), ldg(wi + n + i), ldg(wi + 2 * n + i));
+    const f3 tg = mk(ldg(t + i), ldg(t + n + i), ldg(t + 2 * n + i));
+    const Frame fr = hair_frame(w_o, tg);
+    const f3 wol = normalize(to_local(fr, w_o));
+    const f3 wil = normalize(to_local(fr, w_i));
+    const HairEval e = hair_eval(wol, wil, ldg(h + i), hc);
+    __stcs(f + i, e.f.x);
+    __stcs(f + n + i, e.f.y);
+    __stcs(f + 2 * n + i, e.f.z);
+    __stcs(pdf + i, e.pdf);
+  }
+}
+
+__global__ void __launch_bounds__(256) bsdf_sample_kernel(HairConsts hc, const float* __restrict__ wo,
+                                                          const float* __restrict__ t,
+                                                          const float* __restrict__ h,
+                                                          const float* __restrict__ u,
+                                                          float* __restrict__ wi_out,
+                                                          float* __restrict__ f,
+                                                          float* __restrict__ pdf, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const f3 w_o = mk(ldg(wo + i), ldg(wo + n + i), ldg(wo + 2 * n + i));
+    const f3 tg = mk(ldg(t + i), ldg(t + n + i), ldg(t + 2 * n + i));
+    const Frame fr = hair_frame(w_o, tg);
+    const f3 wol = normalize(to_local(fr, w_o));
+    f3 wil;
+    const HairEval e = hair_sample(wol, ldg(h + i), ldg(u + i), ldg(u + n + i), ldg(u + 2 * n + i),
+                                   ldg(u + 3 * n + i), hc, &wil);
+    const f3 w = normalize(to_world(fr, wil));
+    __stcs(wi_out + i, w.x);
+    __stcs(wi_out + n + i, w.y);
+    __stcs(wi_out + 2 * n + i, w.z);
+    __stcs(f + i, e.f.x);
+    __stcs(f + n + i, e.f.y);
+    __stcs(f + 2 * n + i, e.f.z);
+    __stcs(pdf + i, e.pdf);
+  }
+}
+
+// uniformSampleSphere (utils.cuh:115-121)
+HM_D f3 uniform_sample_sphere(float u0, float u1) {
+  float z = 1.f - 2.f * u0;
+  float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+  float phi = 2.f * kPi * u1;
+  return normalize(mk(r * cosf(phi), r * sinf(phi), z));
+}
+
+// Synthetic BSDF workload: one counter-based stream per query
+// (murmur-seeded LCG of random.cuh, pixel index = query index), 11 draws:
+// wo (2), wi (2), tangent (2), h (1), sampling uniforms (4).
+__global__ void __launch_bounds__(256) bsdf_gen_kernel(uint32_t seed, float* __restrict__ wo,
+                                                       float* __restrict__ wi,
+                                                       float* __restrict__ t,
+                                                       float* __restrict__ h,
+                                                       float* __restrict__ u, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t st = rng_seed((int)seed, (uint32_t)i);
+    float r[11];
+#pragma unroll
+    for (int k = 0; k < 11; ++k) r[k] = lcg_next(st);
+    const f3 a = uniform_sample_sphere(r[0], r[1]);
+    const f3 b = uniform_sample_sphere(r[2], r[3]);
+    const f3 c = uniform_sample_sphere(r[4], r[5]);
+    wo[i] = a.x; wo[n + i] = a.y; wo[2 * n + i] = a.z;
+    if (wi) { wi[i] = b.x; wi[n + i] = b.y; wi[2 * n + i] = b.z; }
+    t[i] = c.x; t[n + i] = c.y; t[2 * n + i] = c.z;
+    h[i] = 2.f * r[6] - 1.f;
+    if (u) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) u[k * n + i] = r[7 + k];
+    }
+  }
+}
+
+static int grid_for(int64_t n, int block) {
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = (n + block - 1) / block;
+  int64_t cap = (int64_t)sms * 16;  // persistent-enough grid: 16 x 256-thread CTAs per SM
+  return (int)(blocks < cap ? blocks : cap);
+}
+
+}  // namespace hm
+
+using namespace hm;
+
+static int check_params(const hm_hair_params* p) {
+  if (!p) {
+    hm_set_error("hair params are NULL");
+    return HM_EINVAL;
+  }
+  if (!(p->beta_m > 0.f) || !(p->beta_n > 0.f)) {
+    hm_set_error("beta_m and beta_n must be > 0 (got %g, %g)", p->beta_m, p->beta_n);
+    return HM_EINVAL;
+  }
+  return HM_OK;
+}
+
+extern "C" int hm_bsdf_eval(const hm_bsdf_queries* q, float* f, float* pdf, int64_t n,
+                            const hm_hair_params* params, void* stream) {
+  if (n < 0 || !q) return hm_set_error("hm_bsdf_eval: n < 0 or queries NULL"), HM_EINVAL;
+  if (int s = check_params(params)) return s;
+  if (n == 0) return HM_OK;
+  if (!q->wo || !q->wi || !q->tangent || !q->h || !f || !pdf)
+    return hm_set_error("hm_bsdf_eval: NULL array"), HM_EINVAL;
+  HairConsts hc = hair_consts_from_params(*params);
+  bsdf_eval_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(hc, q->wo, q->wi, q->tangent,
+                                                                        q->h, f, pdf, n);
+  HM_CHECK_LAUNCH("bsdf_eval_kernel");
+  return HM_OK;
+}
+
+extern "C" int hm_bsdf_sample(const hm_bsdf_queries* q, float* wi_out, float* f, float* pdf,
+                              int64_t n, const hm_hair_params* params, void* stream) {
+  if (n < 0 || !q) return hm_set_error("hm_bsdf_sample: n < 0 or queries NULL"), HM_EINVAL;
+  if (int s = check_params(params)) return s;
+  if (n == 0) return HM_OK;
+  if (!q->wo || !q->tangent || !q->h || !q->u || !wi_out || !f || !pdf)
+    return hm_set_error("hm_bsdf_sample: NULL array"), HM_EINVAL;
+  HairConsts hc = hair_consts_from_params(*params);
+  bsdf_sample_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(
+      hc, q->wo, q->tangent, q->h, q->u, wi_out, f, pdf, n);
+  HM_CHECK_LAUNCH("bsdf_sample_kernel");
+  return HM_OK;
+}
+
+extern "C" int hm_bsdf_gen_queries(uint32_t seed, int64_t n, float* wo, float* wi, float* tangent,
+                                   float* h, float* u, void* stream) {
+  if (n < 0 || !wo || !tangent || !h) return hm_set_error("hm_bsdf_gen_queries: bad args"), HM_EINVAL;
+  if (n == 0) return HM_OK;
+  bsdf_gen_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(seed, wo, wi, tangent, h, u, n);
+  HM_CHECK_LAUNCH("bsdf_gen_kernel");
+  return HM_OK;
+}
+
+extern "C" int hm_hair_setup(const hm_hair_params* params, float* out10) {
+  if (int s = check_params(params)) return s;
+  if (!out10) return hm_set_error("hm_hair_setup: out NULL"), HM_EINVAL;
+  HairConsts hc = hair_consts_from_params(*params);
+  for (int i = 0; i < 3; ++i) out10[i] = hc.v[i];
+  out10[3] = hc.s;
+  for (int i = 0; i < 3; ++i) out10[4 + i] = hc.sin2k[i];
+  for (int i = 0; i < 3; ++i) out10[7 + i] = hc.cos2k[i];
+  return HM_OK;
+}

@@ -1,0 +1,82 @@
+// Radiance-cache network: tiny-cuda-nn style config, parameters and the
+// FP32 kernels.  Replaces TINY_MLP (cuda_headers/neural_network.cuh:33-50,
+// cuda/neural_network.cu:17-64) and the tiny-cuda-nn objects it owns
+// (NetworkWithInputEncoding, Trainer, Adam/ExponentialDecay, loss).
+//
+// Semantics follow tiny-cuda-nn's documented behaviour (the library is an
+// absent submodule of the reference, so its source cannot be consulted):
+//  * encodings Identity / Frequency / OneBlob (quartic kernel, periodic on
+//    [0,1)) / HashGrid (multiresolution hash, Mueller et al. 2022) combined by
+//    Composite in input order; the encoded width is padded to a multiple of
+//    16 with ones (the padding acts as a learnable bias: the MLP has none);
+//  * FullyFusedMLP: n_hidden_layers ReLU layers of n_neurons, a linear output
+//    layer padded to 16 outputs, weights row-major [out][in], network
+//    parameters first and encoding parameters after them;
+//  * losses L2, RelativeL2, RelativeL2Luminance (gradient through the
+//    numerator only), averaged over batch x output dims;
+//  * Adam with l2_reg on the matrix weights only and sparse updates (zero
+//    gradient => untouched) of encoding parameters, wrapped by
+//    ExponentialDecay.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "hm_common.cuh"
+
+namespace hm {
+
+enum EncType { ENC_IDENTITY = 0, ENC_FREQUENCY = 1, ENC_ONEBLOB = 2, ENC_HASHGRID = 3 };
+enum LossType { LOSS_L2 = 0, LOSS_REL_L2 = 1, LOSS_REL_L2_LUM = 2 };
+enum Activation { ACT_NONE = 0, ACT_RELU = 1 };
+
+constexpr int kMaxSegs = 8;
+constexpr int kMaxLevels = 24;
+
+struct EncSeg {
+  int type;
+  int in_off, n_dims;   // consumed input dims
+  int out_off, n_out;   // produced features
+  int n_freq;           // Frequency
+  int n_bins;           // OneBlob
+  // HashGrid
+  int n_levels, n_feat, base_res;
+  float log2_scale;     // log2(per_level_scale)
+  int64_t param_off;    // offset of this grid's table inside the encoding params
+  uint32_t level_size[kMaxLevels];    // table entries per level
+  uint32_t level_res[kMaxLevels];     // grid resolution per level
+  float level_scale[kMaxLevels];      // position scale per level
+  uint32_t level_off[kMaxLevels];     // entry offset per level
+};
+
+struct MlpDims {
+  int in_ch, out_ch;
+  int n_enc;      // encoded features before padding
+  int in_pad;     // encoded width padded to 16
+  int width;      // n_neurons
+  int n_hidden;   // n_hidden_layers
+  int out_pad;    // output width padded to 16
+  int n_segs;
+  EncSeg segs[kMaxSegs];
+  int activation, output_activation;
+  int64_t n_net_params;  // matrix weights
+  int64_t n_enc_params;  // hash tables
+  int64_t layer_off[16]; // offset of each weight matrix (layer 0..n_hidden)
+};
+
+struct AdamCfg {
+  float lr, beta1, beta2, eps, l2_reg;
+  int decay_start, decay_interval;
+  float decay_base;
+};
+
+struct MlpConfig {
+  MlpDims d;
+  AdamCfg adam;
+  int loss;
+  std::string init;  // "xavier_uniform" (tcnn default) or "he_normal"
+};
+
+// Parses a tcnn-style JSON config (loss / optimizer / encoding / network).
+MlpConfig mlp_config_from_json(const char* text, int in_ch, int out_ch);
+
+}  // namespace hm

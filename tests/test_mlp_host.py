@@ -1,0 +1,114 @@
+"""Host-side network logic: config parsing (no device work) and the FP64
+oracle's own gradients against central finite differences."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mlp_oracle as mo
+
+CFG_DIR = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                       "hairmsnn_gb300", "configs")
+
+
+def cfg_text(name):
+    return open(os.path.join(CFG_DIR, name)).read()
+
+
+@pytest.mark.parametrize("name,in_ch,enc,pad,params", [
+    ("c1_cache_w64.json", 16, 209, 224, 224 * 64 + 4 * 64 * 64 + 16 * 64),
+    ("c1_cache_w128.json", 16, 209, 224, 224 * 128 + 4 * 128 * 128 + 16 * 128),
+    ("hairmsnn_cache.json", 12, 59, 64, None),
+])
+def test_describe_config_matches_oracle(name, in_ch, enc, pad, params):
+    from hairmsnn_gb300 import build, mlp
+    build.build()
+    d = mlp.describe(name, in_ch, 3)
+    oc = mo.Config(cfg_text(name), in_ch, 3)
+    assert d.encoded_width == enc == oc.n_enc
+    assert d.padded_input_width == pad == oc.in_pad
+    assert d.n_params == oc.n_params
+    assert d.n_network_params == oc.n_net_params
+    if params is not None:
+        assert d.n_network_params == params
+
+
+def test_reference_cache_config_sizes():
+    """The reference's network (HashGrid 16x2, T=2^15, OneBlob(6 dims, 4 bins),
+    Identity(3)) -> 59 features padded to 64; grid levels 0 and 1 are dense."""
+    oc = mo.Config(cfg_text("hairmsnn_cache.json"), 12, 3)
+    grid = oc.segs[0]
+    sizes = [lv[2] for lv in grid["levels"]]
+    assert sizes[0] == 16 ** 3 and sizes[1] == 32 ** 3 and all(s == 1 << 15 for s in sizes[2:])
+    assert oc.n_enc_params == 2 * sum(sizes)
+
+
+def test_reference_config_file_parses_when_present():
+    path = "/root/reference/scenes/straight/tcnn_hairmsnn.json"
+    if not os.path.isfile(path):
+        pytest.skip("reference checkout not present")
+    from hairmsnn_gb300 import build, mlp
+    build.build()
+    a = mlp.describe(path, 12, 3)
+    b = mlp.describe("hairmsnn_cache.json", 12, 3)
+    assert (a.n_params, a.padded_input_width, a.width, a.n_hidden_layers) == \
+        (b.n_params, b.padded_input_width, b.width, b.n_hidden_layers)
+
+
+@pytest.mark.parametrize("bad", [
+    "{", '{"encoding": {"otype": "Spherical"}}', '{"network": {"n_neurons": 48}}',
+    '{"loss": {"otype": "Huber"}}', '{"encoding": {"otype": "OneBlob", "n_dims_to_encode": 99}}',
+])
+def test_bad_configs_are_parse_errors(bad):
+    from hairmsnn_gb300 import build, mlp
+    from hairmsnn_gb300._ffi import HMError
+    build.build()
+    with pytest.raises(HMError) as e:
+        mlp.describe(bad, 12, 3)
+    assert e.value.status == 6
+
+
+def tiny_cfg(enc):
+    return {"loss": {"otype": "RelativeL2Luminance"},
+            "optimizer": {"otype": "Adam", "learning_rate": 0.01, "beta1": 0.9, "beta2": 0.99,
+                          "epsilon": 1e-15, "l2_reg": 1e-6},
+            "encoding": enc,
+            "network": {"n_neurons": 16, "n_hidden_layers": 2}}
+
+
+@pytest.mark.parametrize("enc", [
+    {"otype": "Composite", "nested": [{"otype": "Frequency", "n_dims_to_encode": 3, "n_frequencies": 3},
+                                      {"otype": "OneBlob", "n_dims_to_encode": 2, "n_bins": 8},
+                                      {"otype": "Identity"}]},
+    {"otype": "Composite", "nested": [{"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": 3,
+                                       "log2_hashmap_size": 6, "base_resolution": 2,
+                                       "per_level_scale": 2.0},
+                                      {"otype": "Identity"}]},
+])
+def test_oracle_gradients_match_finite_differences(enc):
+    cfg = mo.Config(tiny_cfg(enc), 6, 3)
+    rng = np.random.default_rng(1)
+    params = rng.normal(scale=0.3, size=cfg.n_params)
+    x = rng.uniform(0.05, 0.95, (32, 6)).astype(np.float32)
+    tgt = rng.uniform(0, 1, (32, 3))
+    _, g = mo.backward(cfg, params, x, tgt)
+    idx = rng.choice(cfg.n_params, 60, replace=False)
+    eps = 1e-6
+    for i in idx:
+        p1, p2 = params.copy(), params.copy()
+        p1[i] += eps
+        p2[i] -= eps
+        l1, _ = mo.loss_and_grad(cfg, mo.forward(cfg, p1, x)[0], tgt)
+        l2, _ = mo.loss_and_grad(cfg, mo.forward(cfg, p2, x)[0], tgt)
+        fd = (l1 - l2) / (2 * eps)
+        # the luminance denominator is held constant in the analytic gradient
+        # (tcnn semantics), so compare against FD of a frozen-denominator loss
+        out1 = mo.forward(cfg, p1, x)[0]
+        out2 = mo.forward(cfg, p2, x)[0]
+        out0 = mo.forward(cfg, params, x)[0]
+        lum = 0.299 * out0[:, 0] + 0.587 * out0[:, 1] + 0.114 * out0[:, 2]
+        den = (lum * lum + 0.01)[:, None]
+        f = lambda o: np.sum((o[:, :3] - tgt) ** 2 / den) / (32 * 3)
+        fd_frozen = (f(out1) - f(out2)) / (2 * eps)
+        assert abs(fd_frozen - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd_frozen, g[i], fd)

@@ -256,9 +256,27 @@ def run_reference(args):
         sample = f"{n} queries per step (oracle port: C++ BSDF on {threads} threads + FP64 numpy MLP)"
         cfgd = {"workload": "vertex (bounded sample)", "queries_per_step": n}
     else:
-        from oracle import render_oracle as ro
-        step, units, sample, cfgd = ro.reference_step_factory(threads)
-        metric, unit = "paths/s at fixed relMSE vs PT", "paths/s"
+        from hairmsnn_gb300 import build as hb
+        from hairmsnn_gb300 import render as hr
+        hb.build()
+        cfg = hr.straight_hair_scene(512, 512)
+        scene = hr.Scene(cfg)  # host-only parse + generation
+        osc = po.OracleScene.from_library(scene)
+        P, R = 512 * 512, 1 << 16
+        n = 8192
+        state = {"p0": (256 * 512), "frame": 0}
+
+        def step():
+            osc.render_pixels(1, beta=1, accum_id=state["frame"], every_nth=P // R, n_train=R, p0=state["p0"], n=n,
+                              threads=threads)
+            state["p0"] = (state["p0"] + n) % (P - n)
+            state["frame"] += 1
+        units = n
+        metric, unit = hr.RenderBenchWorkload.metric, hr.RenderBenchWorkload.unit
+        sample = (f"{n} pixels (1 spp) per step of the 512x512 render: the reference's per-pixel path code "
+                  f"(rayGenCam / msnnPathTrace / msnnTrainingPath, oracle port) on {threads} threads; "
+                  f"cache network not included")
+        cfgd = {"workload": "render (bounded pixel sample per step)", "pixels_per_step": n}
     for _ in range(args.warmup):
         step()
     times = []
@@ -285,7 +303,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "vertex"),
+    ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "render"),
                     choices=["render", "vertex"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

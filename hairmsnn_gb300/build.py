@@ -24,6 +24,17 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3"
                      "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 
 
+# Shading translation units evaluate ill-conditioned expressions of the
+# reference's formulas (1 - sin^2 near grazing angles, cross products of
+# nearly parallel vectors, exp(cos/v) with 1/v up to ~1e3): they are compiled
+# without multiply-add contraction so every non-transcendental operation is
+# rounded exactly as the reference's separately rounded operations.
+PER_FILE_FLAGS = {
+    "hm_bsdf.cu": ["-fmad=false"],
+    "hm_shade.cu": ["-fmad=false"],
+}
+
+
 def nvcc():
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and os.path.isfile(cand):
@@ -40,7 +51,7 @@ def _compile(src, newest_header, verbose, extra):
     obj = os.path.join(OBJ_DIR, os.path.basename(src) + ".o")
     if os.path.isfile(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), newest_header):
         return obj, False
-    cmd = [nvcc(), *NVCC_FLAGS, *extra, "-c", src, "-o", obj]
+    cmd = [nvcc(), *NVCC_FLAGS, *PER_FILE_FLAGS.get(os.path.basename(src), []), *extra, "-c", src, "-o", obj]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -35,3 +35,10 @@ extern "C" const char* hm_status_string(int s) {
 }
 
 extern "C" const char* hm_version(void) { return "hairmsnn-gb300 0.1 sm_103a"; }
+
+extern "C" int hm_copy_to_host(void* host_dst, const void* device_src, int64_t bytes) {
+  if (bytes < 0 || (bytes > 0 && (!host_dst || !device_src))) return hm_set_error("hm_copy_to_host: bad args"), HM_EINVAL;
+  if (bytes == 0) return HM_OK;
+  cudaError_t e = cudaMemcpy(host_dst, device_src, (size_t)bytes, cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_copy_to_host");
+}

@@ -1,0 +1,267 @@
+// Device LBVH over all primitives (hair segments, then head triangles).
+// Replaces the OptiX GAS/IAS builds of the reference (owlGroupBuildAccel,
+// render_hair_msnn.cu:316-384, 412): GB300 has no RT cores.
+//
+//   1. prim_bounds_kernel  per-primitive AABB (segment: hull of its 4 control
+//                          points grown by the largest radius; triangle: its
+//                          3 vertices) + per-block scene bounds
+//   2. morton_kernel       30-bit Morton code of each AABB centre in the
+//                          scene bounds, key = code << 32 | primitive id
+//                          (unique keys: no tie handling needed)
+//   3. radix sort of the 64-bit keys (cub::DeviceRadixSort, setup only)
+//   4. karras_kernel       binary radix tree (Karras, HPG 2012)
+//   5. refit_kernel        bottom-up child AABBs, second arrival continues
+//
+// All float arithmetic uses explicitly rounded intrinsics (no contraction),
+// so the node array is bit-identical to a host build of the same algorithm.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "hm_scene.h"
+
+namespace hm {
+
+struct Aabb {
+  float lo[3], hi[3];
+};
+
+HM_D Aabb prim_aabb(const SceneDev& s, int p) {
+  Aabb b;
+  if (p < s.n_seg) {
+    const float4* c = s.cp + s.seg[p];
+    float4 q0 = c[0], q1 = c[1], q2 = c[2], q3 = c[3];
+    float r = fmaxf(fmaxf(q0.w, q1.w), fmaxf(q2.w, q3.w));
+    b.lo[0] = __fsub_rn(fminf(fminf(q0.x, q1.x), fminf(q2.x, q3.x)), r);
+    b.lo[1] = __fsub_rn(fminf(fminf(q0.y, q1.y), fminf(q2.y, q3.y)), r);
+    b.lo[2] = __fsub_rn(fminf(fminf(q0.z, q1.z), fminf(q2.z, q3.z)), r);
+    b.hi[0] = __fadd_rn(fmaxf(fmaxf(q0.x, q1.x), fmaxf(q2.x, q3.x)), r);
+    b.hi[1] = __fadd_rn(fmaxf(fmaxf(q0.y, q1.y), fmaxf(q2.y, q3.y)), r);
+    b.hi[2] = __fadd_rn(fmaxf(fmaxf(q0.z, q1.z), fmaxf(q2.z, q3.z)), r);
+  } else {
+    int3 t = s.tri[p - s.n_seg];
+    float3 a = s.vtx[t.x], bb = s.vtx[t.y], c = s.vtx[t.z];
+    b.lo[0] = fminf(fminf(a.x, bb.x), c.x);
+    b.lo[1] = fminf(fminf(a.y, bb.y), c.y);
+    b.lo[2] = fminf(fminf(a.z, bb.z), c.z);
+    b.hi[0] = fmaxf(fmaxf(a.x, bb.x), c.x);
+    b.hi[1] = fmaxf(fmaxf(a.y, bb.y), c.y);
+    b.hi[2] = fmaxf(fmaxf(a.z, bb.z), c.z);
+  }
+  return b;
+}
+
+__global__ void prim_bounds_kernel(SceneDev s, int n, float* __restrict__ block_bounds) {
+  __shared__ float red[6][256];
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    Aabb b = prim_aabb(s, p);
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = fminf(lo[k], b.lo[k]);
+      hi[k] = fmaxf(hi[k], b.hi[k]);
+    }
+  }
+  for (int k = 0; k < 3; ++k) {
+    red[k][threadIdx.x] = lo[k];
+    red[3 + k][threadIdx.x] = hi[k];
+  }
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 3; ++k) {
+        red[k][threadIdx.x] = fminf(red[k][threadIdx.x], red[k][threadIdx.x + w]);
+        red[3 + k][threadIdx.x] = fmaxf(red[3 + k][threadIdx.x], red[3 + k][threadIdx.x + w]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) block_bounds[blockIdx.x * 6 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+HM_HD uint32_t expand_bits10(uint32_t v) {
+  v = (v * 0x00010001u) & 0xFF0000FFu;
+  v = (v * 0x00000101u) & 0x0F00F00Fu;
+  v = (v * 0x00000011u) & 0xC30C30C3u;
+  v = (v * 0x00000005u) & 0x49249249u;
+  return v;
+}
+
+HM_D uint32_t quantize10(float c, float lo, float ext) {
+  float q = ext > 0.f ? __fdiv_rn(__fsub_rn(c, lo), ext) : 0.f;
+  float v = fminf(fmaxf(__fmul_rn(q, 1024.f), 0.f), 1023.f);
+  return (uint32_t)v;
+}
+
+__global__ void morton_kernel(SceneDev s, int n, const float* __restrict__ block_bounds, int nblocks,
+                              unsigned long long* __restrict__ keys) {
+  __shared__ float sb[6];
+  if (threadIdx.x < 6) {
+    float v = threadIdx.x < 3 ? INFINITY : -INFINITY;
+    for (int b = 0; b < nblocks; ++b) {
+      float x = block_bounds[b * 6 + threadIdx.x];
+      v = threadIdx.x < 3 ? fminf(v, x) : fmaxf(v, x);
+    }
+    sb[threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    Aabb b = prim_aabb(s, p);
+    uint32_t q[3];
+    for (int k = 0; k < 3; ++k) {
+      float c = __fmul_rn(__fadd_rn(b.lo[k], b.hi[k]), 0.5f);
+      q[k] = quantize10(c, sb[k], __fsub_rn(sb[3 + k], sb[k]));
+    }
+    uint32_t code = (expand_bits10(q[0]) << 2) | (expand_bits10(q[1]) << 1) | expand_bits10(q[2]);
+    keys[p] = ((unsigned long long)code << 32) | (unsigned long long)(uint32_t)p;
+  }
+}
+
+HM_D int delta(const unsigned long long* keys, int n, int i, int j) {
+  if (j < 0 || j >= n) return -1;
+  return __clzll(keys[i] ^ keys[j]);
+}
+
+// Internal node i: children (>= 0 internal, < 0 leaf ~slot), parents.
+__global__ void karras_kernel(const unsigned long long* __restrict__ keys, int n, int2* __restrict__ child,
+                              int* __restrict__ parent_int, int* __restrict__ parent_leaf) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n - 1) return;
+  int d = (delta(keys, n, i, i + 1) - delta(keys, n, i, i - 1)) >= 0 ? 1 : -1;
+  int dmin = delta(keys, n, i, i - d);
+  int lmax = 2;
+  while (delta(keys, n, i, i + lmax * d) > dmin) lmax *= 2;
+  int l = 0;
+  for (int t = lmax / 2; t >= 1; t /= 2)
+    if (delta(keys, n, i, i + (l + t) * d) > dmin) l += t;
+  int j = i + l * d;
+  int dnode = delta(keys, n, i, j);
+  int s = 0;
+  for (int div = 2;; div *= 2) {
+    int t = (l + div - 1) / div;
+    if (delta(keys, n, i, i + (s + t) * d) > dnode) s += t;
+    if (t <= 1) break;
+  }
+  int gamma = i + s * d + min(d, 0);
+  int lo = min(i, j), hi = max(i, j);
+  int left = lo == gamma ? ~gamma : gamma;
+  int right = hi == gamma + 1 ? ~(gamma + 1) : gamma + 1;
+  child[i] = make_int2(left, right);
+  if (left < 0) parent_leaf[~left] = i; else parent_int[left] = i;
+  if (right < 0) parent_leaf[~right] = i; else parent_int[right] = i;
+}
+
+HM_D void write_slot(float4* nodes, int node, int slot, const Aabb& b) {
+  float* f = reinterpret_cast<float*>(nodes + 4 * node);
+  const int o = slot * 6;
+  for (int k = 0; k < 3; ++k) {
+    f[o + k] = b.lo[k];
+    f[o + 3 + k] = b.hi[k];
+  }
+}
+
+__global__ void refit_kernel(SceneDev s, const unsigned long long* __restrict__ keys, int n,
+                             const int2* __restrict__ child, const int* __restrict__ parent_int,
+                             const int* __restrict__ parent_leaf, int* __restrict__ counters,
+                             float4* __restrict__ nodes, int* __restrict__ prim_of_leaf) {
+  int leaf = blockIdx.x * blockDim.x + threadIdx.x;
+  if (leaf >= n) return;
+  int prim = (int)(keys[leaf] & 0xffffffffull);
+  prim_of_leaf[leaf] = prim;
+  Aabb b = prim_aabb(s, prim);
+  int node = parent_leaf[leaf];
+  int slot = (child[node].x == ~leaf) ? 0 : 1;
+  int cur = ~leaf;
+  for (;;) {
+    write_slot(nodes, node, slot, b);
+    __threadfence();
+    if (atomicAdd(counters + node, 1) == 0) return;  // first arrival: the sibling finishes
+    __threadfence();
+    const float* f = reinterpret_cast<const float*>(nodes + 4 * node);
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = fminf(__ldcg(f + k), __ldcg(f + 6 + k));
+      b.hi[k] = fmaxf(__ldcg(f + 3 + k), __ldcg(f + 9 + k));
+    }
+    cur = node;
+    if (node == 0) return;
+    int p = parent_int[node];
+    slot = (child[p].x == cur) ? 0 : 1;
+    node = p;
+  }
+}
+
+__global__ void pack_children_kernel(const int2* __restrict__ child, int n_int, float4* __restrict__ nodes) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_int) return;
+  int2 c = child[i];
+  nodes[4 * i + 3] = make_float4(__int_as_float(c.x), __int_as_float(c.y), 0.f, 0.f);
+}
+
+// Single primitive: a root whose second child is an empty box.
+__global__ void single_leaf_kernel(SceneDev s, float4* nodes, int* prim_of_leaf) {
+  Aabb b = prim_aabb(s, 0);
+  write_slot(nodes, 0, 0, b);
+  Aabb e;
+  for (int k = 0; k < 3; ++k) {
+    e.lo[k] = INFINITY;
+    e.hi[k] = -INFINITY;
+  }
+  write_slot(nodes, 0, 1, e);
+  nodes[3] = make_float4(__int_as_float(~0), __int_as_float(~0), 0.f, 0.f);
+  prim_of_leaf[0] = 0;
+}
+
+int Scene::build_bvh(cudaStream_t st) {
+  const int n = n_prims();
+  if (n <= 0) return hm_set_error("scene has no primitives"), HM_EINVAL;
+  SceneDev sd = dev();
+  const int n_int = std::max(1, n - 1);
+  cudaFree(d_nodes);
+  cudaFree(d_prim_of_leaf);
+  d_nodes = nullptr;
+  d_prim_of_leaf = nullptr;
+  cudaError_t e = cudaMalloc(&d_nodes, (size_t)n_int * 4 * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&d_prim_of_leaf, (size_t)n * sizeof(int));
+  if (e != cudaSuccess) return hm_cuda_status(e, "bvh alloc");
+  n_nodes = n_int;
+  if (n == 1) {
+    sd.nodes = d_nodes;
+    single_leaf_kernel<<<1, 1, 0, st>>>(sd, d_nodes, d_prim_of_leaf);
+    HM_CHECK_LAUNCH("single_leaf_kernel");
+    return HM_OK;
+  }
+  const int nb = std::min(1024, (n + 255) / 256);
+  float* bb = nullptr;
+  unsigned long long *keys = nullptr, *keys_sorted = nullptr;
+  int2* child = nullptr;
+  int *par_i = nullptr, *par_l = nullptr, *cnt = nullptr;
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0;
+  cub::DeviceRadixSort::SortKeys(nullptr, tmp_bytes, keys, keys_sorted, n, 0, 62, st);
+  e = cudaMalloc(&bb, nb * 6 * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&keys, n * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&keys_sorted, n * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&child, n_int * sizeof(int2));
+  if (e == cudaSuccess) e = cudaMalloc(&par_i, n_int * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&par_l, n * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&cnt, n_int * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, tmp_bytes);
+  int status = HM_OK;
+  if (e != cudaSuccess) {
+    status = hm_cuda_status(e, "bvh scratch");
+  } else {
+    prim_bounds_kernel<<<nb, 256, 0, st>>>(sd, n, bb);
+    morton_kernel<<<std::min(4096, (n + 255) / 256), 256, 0, st>>>(sd, n, bb, nb, keys);
+    cub::DeviceRadixSort::SortKeys(tmp, tmp_bytes, keys, keys_sorted, n, 0, 62, st);
+    cudaMemsetAsync(cnt, 0, n_int * sizeof(int), st);
+    cudaMemsetAsync(par_i, 0xff, n_int * sizeof(int), st);
+    karras_kernel<<<(n_int + 255) / 256, 256, 0, st>>>(keys_sorted, n, child, par_i, par_l);
+    refit_kernel<<<(n + 255) / 256, 256, 0, st>>>(sd, keys_sorted, n, child, par_i, par_l, cnt, d_nodes,
+                                                  d_prim_of_leaf);
+    pack_children_kernel<<<(n_int + 255) / 256, 256, 0, st>>>(child, n_int, d_nodes);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) status = hm_cuda_status(e, "bvh build");
+  }
+  cudaFree(bb); cudaFree(keys); cudaFree(keys_sorted); cudaFree(child);
+  cudaFree(par_i); cudaFree(par_l); cudaFree(cnt); cudaFree(tmp);
+  return status;
+}
+
+}  // namespace hm

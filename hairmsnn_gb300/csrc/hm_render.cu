@@ -1,0 +1,592 @@
+// Wavefront frame driver and trace kernels.
+//
+// Per frame (one sample per pixel, as the reference's render loop,
+// render_hair_msnn.cu:699-771):
+//   camera -> [extend -> shade -> shadow -> compact] x bounces -> finalize
+//   MSNN: -> cache training step on the frame's records -> cache inference on
+//   every pixel -> compose (FP64 accumulation)
+// Queues are compacted with a deterministic block scan, so the order of the
+// surviving paths (and therefore every result) does not depend on timing.
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "hm_mlp.cuh"
+#include "hm_render.h"
+#include "hm_trace.cuh"
+
+namespace hm {
+
+int launch_camera(const SceneDev& s, const FrameParams& fp, const PathState& ps, int* queue, int* count,
+                  cudaStream_t st);
+int launch_shade(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
+                 const int* queue, const int* count, int* keep, int grid, cudaStream_t st);
+int launch_finalize(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
+                    cudaStream_t st);
+int launch_compose(const SceneDev& s, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st);
+
+// COUNT: accumulate BVH nodes visited / primitives tested into cnt[0..1]
+// (an untimed instrumentation pass; the timed path uses COUNT = false).
+template <bool COUNT>
+__global__ void __launch_bounds__(128) extend_kernel(SceneDev s, PathState ps, const int* __restrict__ queue,
+                                                     const int* __restrict__ count, int* err,
+                                                     unsigned long long* cnt) {
+  const int n = *count;
+  TraceCount tc{0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int pid = queue[i];
+    const float4 o = ps.ray_o[pid], d = ps.ray_d[pid];
+    Ray r{mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), 0.f, 1e30f};
+    Hit h = trace<false, COUNT>(s, r, err, &tc);
+    ps.hit[pid] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v);
+  }
+  if (COUNT) {
+    atomicAdd(cnt + 0, (unsigned long long)tc.nodes);
+    atomicAdd(cnt + 1, (unsigned long long)tc.prims);
+  }
+}
+
+// Resolves the pending direct-lighting samples: visible sum, NaN check
+// (directLighting, optix_common.cuh:296-308), weighted add to the path
+// radiance.  Explicitly rounded operations: no multiply-add contraction.
+template <bool COUNT>
+__global__ void __launch_bounds__(128) shadow_kernel(SceneDev s, PathState ps, const int* __restrict__ queue,
+                                                     const int* __restrict__ count, int* err,
+                                                     unsigned long long* cnt) {
+  const int n = *count;
+  TraceCount tc{0, 0};
+  uint32_t rays = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int pid = queue[i];
+    const uint32_t flags = ps.flags[pid];
+    if (!(flags & F_DL)) continue;
+    float sx = 0.f, sy = 0.f, sz = 0.f;  // lightSample + bsdfSample
+    const float4 o0 = ps.sh_o0[pid], o1 = ps.sh_o1[pid];
+    float c0x = 0.f, c0y = 0.f, c0z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
+    if (o0.w != 0.f) {
+      const float4 d = ps.sh_d0[pid];
+      Ray r{mk(o0.x, o0.y, o0.z), mk(d.x, d.y, d.z), 0.f, 1e30f};
+      if (COUNT) ++rays;
+      if (trace<true, COUNT>(s, r, err, &tc).prim < 0) {
+        const float4 c = ps.sh_c0[pid];
+        c0x = c.x; c0y = c.y; c0z = c.z;
+      }
+    }
+    if (o1.w != 0.f) {
+      const float4 d = ps.sh_d1[pid];
+      Ray r{mk(o1.x, o1.y, o1.z), mk(d.x, d.y, d.z), 0.f, 1e30f};
+      if (COUNT) ++rays;
+      if (trace<true, COUNT>(s, r, err, &tc).prim < 0) {
+        const float4 c = ps.sh_c1[pid];
+        c1x = c.x; c1y = c.y; c1z = c.z;
+      }
+    }
+    sx = __fadd_rn(0.f, __fadd_rn(c0x, c1x));
+    sy = __fadd_rn(0.f, __fadd_rn(c0y, c1y));
+    sz = __fadd_rn(0.f, __fadd_rn(c0z, c1z));
+    if (isnan(sx) || isnan(sy) || isnan(sz)) sx = sy = sz = 0.f;
+    const float4 w = ps.dl_w[pid];
+    float4 c = ps.col[pid];
+    c.x = __fadd_rn(c.x, __fmul_rn(w.x, sx));
+    c.y = __fadd_rn(c.y, __fmul_rn(w.y, sy));
+    c.z = __fadd_rn(c.z, __fmul_rn(w.z, sz));
+    ps.col[pid] = c;
+    if (flags & F_TRAIN) {
+      const float4 ws = ps.dl_ws[pid];
+      float4 cs = ps.col_s[pid];
+      cs.x = __fadd_rn(cs.x, __fmul_rn(ws.x, sx));
+      cs.y = __fadd_rn(cs.y, __fmul_rn(ws.y, sy));
+      cs.z = __fadd_rn(cs.z, __fmul_rn(ws.z, sz));
+      ps.col_s[pid] = cs;
+    }
+    ps.flags[pid] = flags & ~F_DL;
+  }
+  if (COUNT) {
+    atomicAdd(cnt + 2, (unsigned long long)tc.nodes);
+    atomicAdd(cnt + 3, (unsigned long long)tc.prims);
+    atomicAdd(cnt + 4, (unsigned long long)rays);
+  }
+}
+
+// ---- deterministic compaction: keep[] over count entries -> next queue
+constexpr int kScanBlock = 1024;
+
+__global__ void __launch_bounds__(kScanBlock) scan_count_kernel(const int* __restrict__ keep, const int* __restrict__ count,
+                                                                int* __restrict__ block_sums, int n_blocks_max) {
+  const int n = *count;
+  __shared__ int warp_sums[kScanBlock / 32];
+  for (int b = blockIdx.x; b < n_blocks_max; b += gridDim.x) {
+    const int i = b * kScanBlock + threadIdx.x;
+    const int v = (i < n) ? keep[i] : 0;
+    const int ws = __popc(__ballot_sync(0xffffffffu, v != 0));
+    if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = ws;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int s = 0;
+      for (int w = 0; w < kScanBlock / 32; ++w) s += warp_sums[w];
+      block_sums[b] = s;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void scan_blocks_kernel(int* __restrict__ block_sums, const int* __restrict__ count, int* __restrict__ out_count) {
+  // single block: exclusive scan of ceil(count / kScanBlock) block sums
+  const int n = *count;
+  const int nb = (n + kScanBlock - 1) / kScanBlock;
+  __shared__ int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < nb; base += blockDim.x) {
+    const int i = base + threadIdx.x;
+    int v = i < nb ? block_sums[i] : 0;
+    // inclusive warp scan
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) >= o) x += y;
+    }
+    __shared__ int wsum[32];
+    if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = x;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      int w = threadIdx.x < (int)(blockDim.x >> 5) ? wsum[threadIdx.x] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, w, o);
+        if (threadIdx.x >= o) w += y;
+      }
+      wsum[threadIdx.x] = w;
+    }
+    __syncthreads();
+    const int warp_off = (threadIdx.x >> 5) ? wsum[(threadIdx.x >> 5) - 1] : 0;
+    const int incl = x + warp_off;
+    if (i < nb) block_sums[i] = carry + incl - v;  // exclusive
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry += incl;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out_count = carry;
+}
+
+__global__ void __launch_bounds__(kScanBlock) scatter_kernel(const int* __restrict__ keep, const int* __restrict__ queue,
+                                                             const int* __restrict__ count,
+                                                             const int* __restrict__ block_offsets,
+                                                             int* __restrict__ next, int n_blocks_max) {
+  const int n = *count;
+  __shared__ int warp_off[kScanBlock / 32];
+  for (int b = blockIdx.x; b < n_blocks_max; b += gridDim.x) {
+    const int i = b * kScanBlock + threadIdx.x;
+    const int v = (i < n) ? keep[i] : 0;
+    const unsigned m = __ballot_sync(0xffffffffu, v != 0);
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) warp_off[threadIdx.x >> 5] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int s = 0;
+      for (int w = 0; w < kScanBlock / 32; ++w) {
+        int t = warp_off[w];
+        warp_off[w] = s;
+        s += t;
+      }
+    }
+    __syncthreads();
+    if (v) next[block_offsets[b] + warp_off[threadIdx.x >> 5] + __popc(m & ((1u << lane) - 1u))] = queue[i];
+    __syncthreads();
+  }
+}
+
+// ---- render object
+struct Render {
+  Scene* scene = nullptr;
+  int mode = MODE_MSNN;
+  int beta_knob = 1;
+  int accum_id = 0;
+  int n_train = 16384;
+  int every_nth = 1;
+  int in_ch = 12;
+  bool train = true;
+  uint32_t seed = 0;
+  hm_mlp* mlp = nullptr;
+  int P = 0;
+  PathState ps{};
+  FrameBufs fb{};
+  int *q_a = nullptr, *q_b = nullptr, *keep = nullptr, *block_sums = nullptr, *counts = nullptr, *err = nullptr;
+  int* h_count = nullptr;  // pinned
+  std::vector<void*> allocs;
+  int64_t rays_extend = 0, rays_shadow_paths = 0;
+  int last_bounces = 0;
+  int sm_count = 152;
+  float last_loss = 0.f;
+  float* d_loss = nullptr;
+  // instrumentation
+  bool timing = false, counting = false;
+  unsigned long long* d_cnt = nullptr;  // extend nodes, prims, shadow nodes, prims, shadow rays
+  std::vector<cudaEvent_t> ev;          // pool, reused every frame
+  hm_render_timings tm{};
+
+  ~Render() {
+    for (void* p : allocs) cudaFree(p);
+    if (h_count) cudaFreeHost(h_count);
+    if (mlp) hm_mlp_destroy(mlp);
+    for (auto e : ev) cudaEventDestroy(e);
+  }
+  cudaEvent_t event(size_t i) {
+    while (ev.size() <= i) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      ev.push_back(e);
+    }
+    return ev[i];
+  }
+  template <class T>
+  cudaError_t alloc(T** p, size_t n) {
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e == cudaSuccess) allocs.push_back((void*)*p);
+    return e;
+  }
+};
+
+static const char* kDefaultCacheConfig =
+    "{\"loss\":{\"otype\":\"RelativeL2Luminance\"},"
+    "\"optimizer\":{\"otype\":\"ExponentialDecay\",\"decay_start\":4000,\"decay_interval\":4000,\"decay_base\":0.33,"
+    "\"nested\":{\"otype\":\"Adam\",\"learning_rate\":1e-2,\"beta1\":0.9,\"beta2\":0.99,\"epsilon\":1e-15,\"l2_reg\":1e-6}},"
+    "\"encoding\":{\"otype\":\"Composite\",\"nested\":["
+    "{\"n_dims_to_encode\":3,\"otype\":\"HashGrid\",\"per_level_scale\":2.0,\"log2_hashmap_size\":15,"
+    "\"base_resolution\":16,\"n_levels\":16},"
+    "{\"n_dims_to_encode\":6,\"otype\":\"OneBlob\",\"n_bins\":4},{\"otype\":\"Identity\"}]},"
+    "\"network\":{\"otype\":\"FullyFusedMLP\",\"activation\":\"ReLU\",\"output_activation\":\"None\","
+    "\"n_neurons\":64,\"n_hidden_layers\":2}}";
+
+static int render_setup(Render* r, const hm_render_options* o) {
+  Scene* s = r->scene;
+  if (int st = s->ensure_built()) return st;
+  r->P = s->width * s->height;
+  const int P = r->P;
+  cudaError_t e = cudaSuccess;
+  auto A4 = [&](float4** p) { if (e == cudaSuccess) e = r->alloc(p, P); };
+  if (e == cudaSuccess) e = r->alloc(&r->ps.rng, P);
+  if (e == cudaSuccess) e = r->alloc(&r->ps.flags, P);
+  if (e == cudaSuccess) e = r->alloc(&r->ps.bounce, P);
+  A4(&r->ps.ray_o); A4(&r->ps.ray_d); A4(&r->ps.hit); A4(&r->ps.beta); A4(&r->ps.beta_s);
+  A4(&r->ps.col); A4(&r->ps.col_s); A4(&r->ps.sh_o0); A4(&r->ps.sh_d0); A4(&r->ps.sh_o1);
+  A4(&r->ps.sh_d1); A4(&r->ps.sh_c0); A4(&r->ps.sh_c1); A4(&r->ps.dl_w); A4(&r->ps.dl_ws);
+  A4(&r->fb.gbuf);
+  const int nblocks = (P + kScanBlock - 1) / kScanBlock;
+  if (e == cudaSuccess) e = r->alloc(&r->q_a, P);
+  if (e == cudaSuccess) e = r->alloc(&r->q_b, P);
+  if (e == cudaSuccess) e = r->alloc(&r->keep, P);
+  if (e == cudaSuccess) e = r->alloc(&r->block_sums, nblocks + 1);
+  if (e == cudaSuccess) e = r->alloc(&r->counts, 4);
+  if (e == cudaSuccess) e = r->alloc(&r->err, 1);
+  if (e == cudaSuccess) e = r->alloc(&r->fb.acc_pt, (size_t)P * 3);
+  if (e == cudaSuccess) e = r->alloc(&r->fb.acc_nn, (size_t)P * 3);
+  if (e == cudaSuccess) e = r->alloc(&r->fb.acc_final, (size_t)P * 3);
+  if (e == cudaSuccess) e = r->alloc(&r->d_loss, 1);
+  if (e == cudaSuccess) e = r->alloc(&r->d_cnt, 8);
+  if (e == cudaSuccess) e = cudaMallocHost(&r->h_count, sizeof(int));
+  if (e != cudaSuccess) return hm_cuda_status(e, "render buffers");
+  cudaMemset(r->err, 0, sizeof(int));
+  cudaMemset(r->fb.acc_pt, 0, (size_t)P * 3 * sizeof(double));
+  cudaMemset(r->fb.acc_nn, 0, (size_t)P * 3 * sizeof(double));
+  cudaMemset(r->fb.acc_final, 0, (size_t)P * 3 * sizeof(double));
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (r->mode == MODE_MSNN) {
+    r->n_train = o && o->train_records > 0 ? o->train_records : 16384;
+    // everyNth = frameSize / numTrainRecords (integer division, render_hair_msnn.cu:106), at least 1
+    r->every_nth = std::max(1, P / r->n_train);
+    r->n_train = std::min(r->n_train, (P + r->every_nth - 1) / r->every_nth);
+    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_frame_in, (size_t)P * r->in_ch);
+    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_frame_out, (size_t)P * 3);
+    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_train_in, (size_t)r->n_train * r->in_ch);
+    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_train_out, (size_t)r->n_train * 3);
+    if (e != cudaSuccess) return hm_cuda_status(e, "render cache buffers");
+    cudaMemset(r->fb.nn_train_in, 0, (size_t)r->n_train * r->in_ch * sizeof(float));
+    cudaMemset(r->fb.nn_train_out, 0, (size_t)r->n_train * 3 * sizeof(float));
+    std::string cfg = o && o->cache_config_json ? o->cache_config_json
+                                                : (s->cache_config.empty() ? kDefaultCacheConfig : s->cache_config);
+    int st = 0;
+    r->mlp = hm_mlp_create(cfg.c_str(), r->in_ch, 3, o ? o->cache_precision : HM_PREC_FP32, r->seed, &st);
+    if (!r->mlp) return st;
+  }
+  return HM_OK;
+}
+
+static int render_frame(Render* r, cudaStream_t st) {
+  Scene* s = r->scene;
+  SceneDev sd = s->dev();
+  FrameParams fp{r->mode, r->beta_knob - 1, r->accum_id, r->accum_id + 10007, r->every_nth, r->n_train, r->in_ch};
+  int* q_cur = r->q_a;
+  int* q_next = r->q_b;
+  int* c_cur = r->counts;
+  int* c_next = r->counts + 1;
+  // instrumentation: event pairs per stage (timing) / work counters (counting)
+  size_t ne = 0;
+  std::vector<std::pair<int, size_t>> marks;  // (stage, event index)
+  auto mark = [&](int stage) {
+    if (!r->timing) return;
+    cudaEventRecord(r->event(ne), st);
+    marks.emplace_back(stage, ne++);
+  };
+  enum { S_CAMERA, S_EXTEND, S_SHADE, S_SHADOW, S_COMPACT, S_FINALIZE, S_TRAIN, S_INFER, S_COMPOSE, S_END };
+  if (r->counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
+  mark(S_CAMERA);
+  if (int e = launch_camera(sd, fp, r->ps, q_cur, c_cur, st)) return e;
+  const int grid = r->sm_count * 8;
+  const int nblocks = (r->P + kScanBlock - 1) / kScanBlock;
+  int count = r->P;
+  int bounces = 0;
+  int64_t ext_rays = 0;
+  for (int it = 0; it <= s->path_v2 && count > 0; ++it) {
+    mark(S_EXTEND);
+    if (r->counting)
+      extend_kernel<true><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
+    else
+      extend_kernel<false><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
+    HM_CHECK_LAUNCH("extend_kernel");
+    mark(S_SHADE);
+    if (int e = launch_shade(sd, fp, r->ps, r->fb, q_cur, c_cur, r->keep, grid, st)) return e;
+    mark(S_SHADOW);
+    if (r->counting)
+      shadow_kernel<true><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
+    else
+      shadow_kernel<false><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
+    HM_CHECK_LAUNCH("shadow_kernel");
+    mark(S_COMPACT);
+    scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(r->keep, c_cur, r->block_sums, nblocks);
+    scan_blocks_kernel<<<1, 1024, 0, st>>>(r->block_sums, c_cur, c_next);
+    scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(r->keep, q_cur, c_cur, r->block_sums,
+                                                                              q_next, nblocks);
+    HM_CHECK_LAUNCH("compaction");
+    ext_rays += count;
+    cudaError_t e = cudaMemcpyAsync(r->h_count, c_next, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return hm_cuda_status(e, "bounce count");
+    count = *r->h_count;
+    std::swap(q_cur, q_next);
+    std::swap(c_cur, c_next);
+    ++bounces;
+  }
+  r->rays_extend += ext_rays;
+  r->last_bounces = bounces;
+  mark(S_FINALIZE);
+  if (int e = launch_finalize(sd, fp, r->ps, r->fb, st)) return e;
+  int launches = 1 + 6 * bounces + 1;
+  if (r->mode == MODE_MSNN) {
+    mark(S_TRAIN);
+    if (r->train) {
+      if (int e = hm_mlp_training_step(r->mlp, r->fb.nn_train_in, r->fb.nn_train_out, r->n_train, r->d_loss, st))
+        return e;
+    }
+    mark(S_INFER);
+    if (int e = hm_mlp_inference(r->mlp, r->fb.nn_frame_in, r->fb.nn_frame_out, r->P, st)) return e;
+    mark(S_COMPOSE);
+    if (int e = launch_compose(sd, fp, r->fb, st)) return e;
+    hm_mlp_desc md;
+    hm_mlp_info(r->mlp, &md);
+    const bool grid_enc = md.n_params > md.n_network_params;
+    // training: encode, fwd, bwd, loss reduce, (dw partial + reduce) per layer, [grid bwd], adam
+    launches += (r->train ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 1 : 0) + 1 : 0) + 2 + 1;
+  }
+  mark(S_END);
+  r->accum_id += 1;
+  hm_render_timings& tm = r->tm;
+  memset(&tm, 0, sizeof(tm));
+  tm.bounces = bounces;
+  tm.extension_rays = ext_rays;
+  tm.kernel_launches = launches;
+  if (r->timing) {
+    cudaEventSynchronize(r->event(ne - 1));
+    float* slot[] = {&tm.camera_ms, &tm.extend_ms, &tm.shade_ms, &tm.shadow_ms, &tm.compact_ms,
+                     &tm.finalize_ms, &tm.train_ms, &tm.infer_ms, &tm.compose_ms};
+    for (size_t k = 0; k + 1 < marks.size(); ++k) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, r->event(marks[k].second), r->event(marks[k + 1].second));
+      *slot[marks[k].first] += ms;
+    }
+    cudaEventElapsedTime(&tm.total_ms, r->event(marks.front().second), r->event(marks.back().second));
+  }
+  if (r->counting) {
+    unsigned long long c[8];
+    cudaMemcpyAsync(c, r->d_cnt, sizeof(c), cudaMemcpyDeviceToHost, st);
+    cudaStreamSynchronize(st);
+    tm.extend_nodes = (int64_t)c[0];
+    tm.extend_prims = (int64_t)c[1];
+    tm.shadow_nodes = (int64_t)c[2];
+    tm.shadow_prims = (int64_t)c[3];
+    tm.shadow_rays = (int64_t)c[4];
+  }
+  return HM_OK;
+}
+
+// Trace an arbitrary batch of rays (tests and the traversal benchmark).
+__global__ void trace_batch_kernel(SceneDev s, const float* __restrict__ org, const float* __restrict__ dir, int64_t n,
+                                   float tmin, float tmax, int any_hit, float4* __restrict__ out, int* err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    Ray r{mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]), mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), tmin, tmax};
+    Hit h = any_hit ? trace<true>(s, r, err) : trace<false>(s, r, err);
+    out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v);
+  }
+}
+
+}  // namespace hm
+
+using namespace hm;
+
+extern "C" hm_render* hm_render_create(hm_scene* scene, const hm_render_options* opt, int* status) {
+  int dummy;
+  if (!status) status = &dummy;
+  if (!scene) {
+    *status = HM_EINVAL;
+    hm_set_error("hm_render_create: NULL scene");
+    return nullptr;
+  }
+  Render* r = new Render();
+  r->scene = (Scene*)scene;
+  if (opt) {
+    r->mode = opt->mode;
+    r->beta_knob = opt->beta;
+    r->train = opt->train != 0;
+    r->seed = opt->seed;
+  } else {
+    r->train = r->scene->cache_train;
+  }
+  if (r->mode != MODE_PT && r->mode != MODE_MSNN) {
+    delete r;
+    *status = HM_EINVAL;
+    hm_set_error("hm_render_create: unknown mode");
+    return nullptr;
+  }
+  if (r->beta_knob < 1) {
+    delete r;
+    *status = HM_EINVAL;
+    hm_set_error("hm_render_create: BETA must be >= 1 (internal beta = BETA - 1)");
+    return nullptr;
+  }
+  int st = render_setup(r, opt);
+  if (st != HM_OK) {
+    delete r;
+    *status = st;
+    return nullptr;
+  }
+  *status = HM_OK;
+  return (hm_render*)r;
+}
+
+extern "C" void hm_render_destroy(hm_render* h) { delete (Render*)h; }
+
+extern "C" int hm_render_frame(hm_render* h, void* stream) {
+  Render* r = (Render*)h;
+  if (!r) return hm_set_error("hm_render_frame: NULL"), HM_EINVAL;
+  int st = render_frame(r, (cudaStream_t)stream);
+  if (st != HM_OK) return st;
+  int err = 0;
+  cudaError_t e = cudaMemcpyAsync(&err, r->err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_frame");
+  if (err) return hm_set_error("traversal gave up on some rays (error bits 0x%x)", err), HM_ECAPACITY;
+  return HM_OK;
+}
+
+extern "C" int hm_render_reset(hm_render* h) {
+  Render* r = (Render*)h;
+  if (!r) return HM_EINVAL;
+  r->accum_id = 0;
+  return HM_OK;
+}
+
+extern "C" int hm_render_read(hm_render* h, int which, double* host_rgb) {
+  Render* r = (Render*)h;
+  if (!r || !host_rgb) return hm_set_error("hm_render_read: NULL"), HM_EINVAL;
+  const double* src = which == HM_IMAGE_FINAL ? r->fb.acc_final
+                      : which == HM_IMAGE_SHORT ? r->fb.acc_pt
+                      : which == HM_IMAGE_CACHE ? r->fb.acc_nn : nullptr;
+  if (!src) return hm_set_error("hm_render_read: unknown image %d", which), HM_EINVAL;
+  if (r->mode == MODE_PT && which != HM_IMAGE_FINAL) return hm_set_error("hm_render_read: PT renders have only the final image"), HM_EINVAL;
+  const size_t n = (size_t)r->P * 3;
+  cudaError_t e = cudaMemcpy(host_rgb, src, n * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_read");
+  const double inv = r->accum_id > 0 ? 1.0 / r->accum_id : 0.0;
+  for (size_t i = 0; i < n; ++i) host_rgb[i] *= inv;
+  return HM_OK;
+}
+
+extern "C" int hm_render_get_stats(const hm_render* h, hm_render_stats* out) {
+  const Render* r = (const Render*)h;
+  if (!r || !out) return HM_EINVAL;
+  out->frames = r->accum_id;
+  out->pixels = r->P;
+  out->extension_rays = r->rays_extend;
+  out->last_bounces = r->last_bounces;
+  out->train_records = r->mode == MODE_MSNN ? r->n_train : 0;
+  out->every_nth = r->every_nth;
+  float loss = 0.f;
+  if (r->mlp && r->train && r->accum_id > 0) cudaMemcpy(&loss, r->d_loss, sizeof(float), cudaMemcpyDeviceToHost);
+  out->last_loss = loss;
+  return HM_OK;
+}
+
+extern "C" int hm_render_set_instrumentation(hm_render* h, int timing, int counting) {
+  Render* r = (Render*)h;
+  if (!r) return HM_EINVAL;
+  r->timing = timing != 0;
+  r->counting = counting != 0;
+  return HM_OK;
+}
+
+extern "C" int hm_render_get_timings(const hm_render* h, hm_render_timings* out) {
+  const Render* r = (const Render*)h;
+  if (!r || !out) return HM_EINVAL;
+  *out = r->tm;
+  return HM_OK;
+}
+
+extern "C" hm_mlp* hm_render_cache(hm_render* h) {
+  Render* r = (Render*)h;
+  return r ? r->mlp : nullptr;
+}
+
+// Cache input / target buffers of the last frame (device pointers, valid
+// until the next frame): which 0 = frame inputs [P][12], 1 = frame outputs
+// [P][3], 2 = training inputs [R][12], 3 = training targets [R][3],
+// 4 = G-buffer [P] float4.
+extern "C" int hm_render_buffer(hm_render* h, int which, void** dptr, int64_t* count) {
+  Render* r = (Render*)h;
+  if (!r || !dptr) return HM_EINVAL;
+  switch (which) {
+    case 0: *dptr = r->fb.nn_frame_in; if (count) *count = (int64_t)r->P * r->in_ch; break;
+    case 1: *dptr = r->fb.nn_frame_out; if (count) *count = (int64_t)r->P * 3; break;
+    case 2: *dptr = r->fb.nn_train_in; if (count) *count = (int64_t)r->n_train * r->in_ch; break;
+    case 3: *dptr = r->fb.nn_train_out; if (count) *count = (int64_t)r->n_train * 3; break;
+    case 4: *dptr = r->fb.gbuf; if (count) *count = (int64_t)r->P; break;
+    default: return HM_EINVAL;
+  }
+  return HM_OK;
+}
+
+extern "C" int hm_trace_rays(const hm_scene* h, const float* d_org, const float* d_dir, int64_t n, float tmin,
+                             float tmax, int any_hit, float* d_hits, void* stream) {
+  Scene* s = const_cast<Scene*>((const Scene*)h);  // the device build is a lazily made cache
+  if (!s || n < 0 || (n > 0 && (!d_org || !d_dir || !d_hits))) return hm_set_error("hm_trace_rays: bad args"), HM_EINVAL;
+  if (n == 0) return HM_OK;
+  if (int st = s->ensure_built()) return st;
+  int* err = nullptr;
+  cudaError_t e = cudaMalloc(&err, sizeof(int));
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_trace_rays");
+  cudaMemsetAsync(err, 0, sizeof(int), (cudaStream_t)stream);
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = (int)std::min<int64_t>((n + 127) / 128, (int64_t)sms * 16);
+  trace_batch_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(s->dev(), d_org, d_dir, n, tmin, tmax, any_hit,
+                                                             (float4*)d_hits, err);
+  int herr = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  cudaFree(err);
+  if (e != cudaSuccess) return hm_cuda_status(e, "trace_batch_kernel");
+  if (herr) return hm_set_error("traversal gave up on some rays (error bits 0x%x)", herr), HM_ECAPACITY;
+  return HM_OK;
+}

@@ -1,0 +1,83 @@
+// Wavefront integrator state shared by the shading (hm_shade.cu) and tracing
+// (hm_render.cu) translation units.
+#pragma once
+#include "hm_scene.h"
+
+namespace hm {
+
+enum PathFlags : uint32_t {
+  F_TRAIN = 1u,     // pixel produces a training record this frame
+  F_DL = 2u,        // shadow rays of the current vertex are pending
+  F_PRIM_HIT = 4u,  // primary ray hit something
+  F_PRIM_SURF = 8u  // ... and it was the head surface
+};
+
+enum RenderMode { MODE_PT = 0, MODE_MSNN = 1 };
+
+// Structure-of-arrays path state, one slot per pixel (capacity W*H).
+struct PathState {
+  uint32_t* rng;
+  uint32_t* flags;
+  int* bounce;
+  float4* ray_o;  // extension ray origin (w unused)
+  float4* ray_d;  // extension ray direction
+  float4* hit;    // t, prim (int bits, -1 miss), u, v
+  float4* beta;   // path throughput
+  float4* beta_s; // short-path throughput (training pixels)
+  float4* col;    // path radiance (miss: emitted radiance of the primary ray)
+  float4* col_s;  // short-path radiance (training pixels)
+  float4* sh_o0;  // shadow ray 0 origin, w = 1 if valid
+  float4* sh_d0;
+  float4* sh_o1;  // shadow ray 1
+  float4* sh_d1;
+  float4* sh_c0;  // contributions if unoccluded
+  float4* sh_c1;
+  float4* dl_w;   // weight of the visible direct-lighting sum in col
+  float4* dl_ws;  // ... in col_s
+};
+
+struct FrameParams {
+  int mode;        // RenderMode
+  int beta;        // BETA - 1 (render_hair_msnn.cu:1170)
+  int accum_id;    // frames accumulated so far
+  int frame_seed;  // accum_id + 10007 (hair_msnn.cu:194)
+  int every_nth;   // one training pixel per every_nth pixels
+  int n_train;     // training records per frame
+  int in_ch;       // cache input channels (12)
+};
+
+struct FrameBufs {
+  float* nn_frame_in;   // [P][in_ch]
+  float* nn_frame_out;  // [P][3]
+  float* nn_train_in;   // [R][in_ch]
+  float* nn_train_out;  // [R][3]
+  float4* gbuf;         // path colour; w = 1 hit, 2 surface (bit flags as float)
+  double* acc_pt;       // [P][3] running sums (FP64)
+  double* acc_nn;
+  double* acc_final;
+};
+
+// Training-pixel choice: the reference shuffles a table of 0..R-1 each frame
+// with thrust::shuffle and keeps pixel fbOfs % everyNth == trainIdxs[trOfs] %
+// everyNth.  Here the permutation is a keyed Feistel bijection on [0, R)
+// (cycle-walking for non-powers of two), deterministic per frame.
+HM_HD uint32_t feistel_perm(uint32_t i, uint32_t n, uint32_t key) {
+  uint32_t bits = 1;
+  while ((1u << bits) < n) ++bits;
+  const uint32_t half = (bits + 1) / 2, lo_mask = (1u << half) - 1u;
+  uint32_t x = i;
+  for (int walk = 0; walk < 64; ++walk) {
+    uint32_t l = x >> half, r = x & lo_mask;
+    for (int round = 0; round < 4; ++round) {
+      uint32_t f = murmur_finalize(r ^ (key + 0x9e3779b9u * (uint32_t)(round + 1))) & lo_mask;
+      uint32_t nl = r;
+      r = (l ^ f) & lo_mask;
+      l = nl;
+    }
+    x = ((l << half) | r) & ((1u << (2 * half)) - 1u);
+    if (x < n) return x;
+  }
+  return i % n;
+}
+
+}  // namespace hm

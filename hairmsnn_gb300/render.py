@@ -1,0 +1,393 @@
+"""Scene, renderer and ray-tracing front end over the C ABI.
+
+Mirrors the reference's frame driver (RenderWindow_HairMSNN, render_hair_msnn.cu)
+minus the viewer: a Scene is built from the reference's scene JSON (plus the
+procedural-asset keys), a Renderer runs HairMSNN (or plain path tracing) one
+sample per pixel per frame() and accumulates in FP64.
+"""
+import ctypes
+import json
+import os
+import time
+
+import numpy as np
+
+from ._ffi import check, lib
+
+HM_SCENE = dict(control_points=0, segments=1, vertices=2, normals=3, triangles=4, env=5, env_cpdf=6,
+                env_ccdf=7, env_mpdf=8, env_mcdf=9, dir_lights=10, bvh_nodes=11, bvh_leaves=12, camera=13,
+                materials=14)
+DTYPES = dict(control_points=(np.float32, 4), segments=(np.int32, 1), vertices=(np.float32, 3),
+              normals=(np.float32, 3), triangles=(np.int32, 3), env=(np.float32, 4), env_cpdf=(np.float32, 1),
+              env_ccdf=(np.float32, 1), env_mpdf=(np.float32, 1), env_mcdf=(np.float32, 1),
+              dir_lights=(np.float32, 6), bvh_nodes=(np.float32, 16), bvh_leaves=(np.int32, 1),
+              camera=(np.float32, 12), materials=(np.float32, 16))
+PT, MSNN = 0, 1
+IMAGE_FINAL, IMAGE_SHORT, IMAGE_CACHE = 0, 1, 2
+
+
+class hm_scene_desc(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in (
+        "n_strands", "n_control_points", "n_segments", "n_vertices", "n_triangles", "n_bvh_nodes", "width",
+        "height", "spp", "path_v1", "path_v2", "env_width", "env_height", "n_dir_lights", "mis", "env_pdf",
+        "has_env", "shading_catrom")] + [("scene_scale", ctypes.c_float), ("bounds_min", ctypes.c_float * 3),
+                       ("bounds_max", ctypes.c_float * 3)]
+
+
+class hm_render_options(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int), ("beta", ctypes.c_int), ("train_records", ctypes.c_int),
+                ("train", ctypes.c_int), ("cache_precision", ctypes.c_int), ("seed", ctypes.c_uint32),
+                ("cache_config_json", ctypes.c_char_p)]
+
+
+class hm_render_stats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_int), ("pixels", ctypes.c_int), ("extension_rays", ctypes.c_int64),
+                ("last_bounces", ctypes.c_int), ("train_records", ctypes.c_int), ("every_nth", ctypes.c_int),
+                ("last_loss", ctypes.c_float)]
+
+
+class hm_render_timings(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_float) for n in (
+        "total_ms", "camera_ms", "extend_ms", "shade_ms", "shadow_ms", "compact_ms", "finalize_ms", "train_ms",
+        "infer_ms", "compose_ms")] + [("bounces", ctypes.c_int), ("kernel_launches", ctypes.c_int)] + [
+        (n, ctypes.c_int64) for n in ("extension_rays", "shadow_rays", "extend_nodes", "extend_prims",
+                                      "shadow_nodes", "shadow_prims")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_declared = False
+
+
+def _declare():
+    global _declared
+    if _declared:
+        return
+    L = lib()
+    vp, i32, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64
+    P = ctypes.POINTER
+    L.hm_scene_create.restype = vp
+    L.hm_scene_create.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P(i32)]
+    L.hm_scene_build.argtypes = [vp]
+    L.hm_scene_destroy.restype = None
+    L.hm_scene_destroy.argtypes = [vp]
+    L.hm_scene_info.argtypes = [vp, P(hm_scene_desc)]
+    L.hm_scene_export_size.restype = i64
+    L.hm_scene_export_size.argtypes = [vp, i32]
+    L.hm_scene_export.argtypes = [vp, i32, vp, i64]
+    L.hm_trace_rays.argtypes = [vp, vp, vp, i64, ctypes.c_float, ctypes.c_float, i32, vp, vp]
+    L.hm_render_create.restype = vp
+    L.hm_render_create.argtypes = [vp, P(hm_render_options), P(i32)]
+    L.hm_render_destroy.restype = None
+    L.hm_render_destroy.argtypes = [vp]
+    L.hm_render_frame.argtypes = [vp, vp]
+    L.hm_render_reset.argtypes = [vp]
+    L.hm_render_read.argtypes = [vp, i32, vp]
+    L.hm_render_get_stats.argtypes = [vp, P(hm_render_stats)]
+    L.hm_render_cache.restype = vp
+    L.hm_render_cache.argtypes = [vp]
+    L.hm_render_buffer.argtypes = [vp, i32, P(vp), P(i64)]
+    L.hm_copy_to_host.argtypes = [vp, vp, i64]
+    L.hm_render_set_instrumentation.argtypes = [vp, i32, i32]
+    L.hm_render_get_timings.argtypes = [vp, P(hm_render_timings)]
+    _declared = True
+
+
+def _stream(stream):
+    import torch
+    s = torch.cuda.current_stream() if stream is None else stream
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Scene:
+    """parseScene + asset generation (host); device build on first use."""
+
+    def __init__(self, config, base_dir=None):
+        _declare()
+        text = json.dumps(config) if isinstance(config, dict) else config
+        st = ctypes.c_int(0)
+        h = lib().hm_scene_create(text.encode(), (base_dir or "").encode(), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        self._h = ctypes.c_void_p(h)
+        self.config = config
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hm_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self):
+        check(lib().hm_scene_build(self._h))
+
+    def info(self):
+        d = hm_scene_desc()
+        check(lib().hm_scene_info(self._h, ctypes.byref(d)))
+        return d
+
+    def export(self, name):
+        which = HM_SCENE[name]
+        nbytes = lib().hm_scene_export_size(self._h, which)
+        dt, width = DTYPES[name]
+        out = np.zeros(max(nbytes, 0) // np.dtype(dt).itemsize, dt)
+        if nbytes > 0:
+            check(lib().hm_scene_export(self._h, which, out.ctypes.data_as(ctypes.c_void_p), nbytes))
+        return out.reshape(-1, width) if width > 1 else out
+
+    def trace(self, org, dirs, tmin=0.0, tmax=1e30, any_hit=False, stream=None):
+        """org, dirs: CUDA float32 [n, 3] -> hits [n, 4] (t, prim bits, u, v)."""
+        import torch
+        n = org.shape[0]
+        hits = torch.empty((n, 4), dtype=torch.float32, device=org.device)
+        check(lib().hm_trace_rays(self._h, ctypes.c_void_p(org.data_ptr()), ctypes.c_void_p(dirs.data_ptr()), n,
+                                  tmin, tmax, 1 if any_hit else 0, ctypes.c_void_p(hits.data_ptr()),
+                                  _stream(stream)))
+        return hits
+
+
+class Renderer:
+    """One frame() = one sample per pixel of HairMSNN (mode=MSNN) or plain PT."""
+
+    def __init__(self, scene, mode=MSNN, beta=1, train_records=16384, train=True, precision=0, seed=0,
+                 cache_config=None):
+        _declare()
+        self.scene = scene
+        o = hm_render_options(mode, beta, train_records, 1 if train else 0, precision, seed,
+                              cache_config.encode() if cache_config else None)
+        st = ctypes.c_int(0)
+        h = lib().hm_render_create(scene._h, ctypes.byref(o), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        self._h = ctypes.c_void_p(h)
+        info = scene.info()
+        self.width, self.height = info.width, info.height
+        self.mode = mode
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hm_render_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def frame(self, stream=None):
+        check(lib().hm_render_frame(self._h, _stream(stream)))
+
+    def reset(self):
+        check(lib().hm_render_reset(self._h))
+
+    def read(self, which=IMAGE_FINAL):
+        img = np.zeros((self.height, self.width, 3), np.float64)
+        check(lib().hm_render_read(self._h, which, img.ctypes.data_as(ctypes.c_void_p)))
+        return img
+
+    def stats(self):
+        s = hm_render_stats()
+        check(lib().hm_render_get_stats(self._h, ctypes.byref(s)))
+        return s
+
+    def instrument(self, timing=True, counting=False):
+        check(lib().hm_render_set_instrumentation(self._h, 1 if timing else 0, 1 if counting else 0))
+
+    def timings(self):
+        t = hm_render_timings()
+        check(lib().hm_render_get_timings(self._h, ctypes.byref(t)))
+        return t
+
+    def buffer(self, which):
+        """Host copy of a device buffer of the last frame (see hm_render_buffer):
+        0 cache inputs [P,12], 1 cache outputs [P,3], 2 training inputs [R,12],
+        3 training targets [R,3], 4 G-buffer [P,4]."""
+        p = ctypes.c_void_p()
+        n = ctypes.c_int64()
+        check(lib().hm_render_buffer(self._h, which, ctypes.byref(p), ctypes.byref(n)))
+        width = {0: 12, 1: 3, 2: 12, 3: 3, 4: 4}[which]
+        count = n.value * (4 if which == 4 else 1)
+        host = np.zeros(count, np.float32)
+        check(lib().hm_copy_to_host(host.ctypes.data_as(ctypes.c_void_p), p, count * 4))
+        return host.reshape(-1, width)
+
+
+def relmse(img, ref, eps=1e-2):
+    """mean((x - ref)^2 / (ref^2 + eps)) over pixels and channels."""
+    return float(np.mean((img - ref) ** 2 / (ref ** 2 + eps)))
+
+
+# ----------------------------------------------------------------- workloads
+def straight_hair_scene(width=512, height=512, strands=10000, control_points=64, spp=16, path_v2=40,
+                        seed=1, sky_w=512, sky_h=256, triangles=20000):
+    """The full-render workload: straight procedural hair (10k strands x 64
+    cubic B-spline control points, 20 cm long, radius 0.04 mm, roots on a
+    unit-sphere cap; scene unit = 10 cm), a 20k-triangle head ellipsoid, a
+    Preetham sky (turbidity 3) and a directional light from (3,3,3)."""
+    return {
+        "camera": {"from": [0.0, -3.8, 0.1], "to": [0.0, 0.0, -0.25], "up": [0.0, 0.0, 1.0], "cos_fovy": 0.66},
+        "hair": {"alpha": 2.0, "beta_m": 0.3, "beta_n": 0.3, "type": 1, "sigma_a": [0.06, 0.1, 0.2],
+                 "procedural": {"type": "straight", "strands": strands, "control_points": control_points,
+                                "length": 2.0, "radius": 4e-4, "seed": seed}},
+        "surface": {"procedural": {"type": "ellipsoid", "triangles": triangles, "radii": [0.85, 0.95, 1.0],
+                                   "diffuse": [0.35, 0.25, 0.2]}},
+        "lights": {"sky": {"turbidity": 3.0, "sun": [3, 3, 3], "width": sky_w, "height": sky_h, "scale": 1.0},
+                   "directional": [{"from": [3, 3, 3], "emit": [1, 1, 1]}]},
+        "integrator": {"ENV_PDF": True, "MIS": True, "width": width, "height": height, "spp": spp,
+                       "path_v1": 1, "path_v2": path_v2},
+        "tcnn": {"init_train": True},
+    }
+
+
+RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
+NODE_BYTES = 64               # one BVH node: both child boxes + child indices
+PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
+
+
+class RenderBenchWorkload:
+    """bench.py workload: one frame (1 spp) of the full HairMSNN render per step."""
+
+    name = "render"
+    metric = "paths/s (HairMSNN full wavefront render, 512x512, 1 spp/frame, online cache training 2^16/frame)"
+    unit = "paths/s"
+
+    def __init__(self, torch, width=512, height=512, train_records=1 << 16):
+        self.torch = torch
+        self.width, self.height, self.train_records = width, height, train_records
+        self.cfg = straight_hair_scene(width, height)
+        self.scene = Scene(self.cfg)
+        self.scene.build()
+        self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True)
+        self.r.instrument(timing=True, counting=False)
+        self.P = width * height
+        self.h2d_bytes = 0
+        self.d2h_bytes = self.P * 3 * 8
+        self.host_img = np.zeros((height, width, 3))
+        self.stage_ms = []
+        self.launches = []
+
+    def step(self, events=None):
+        if events:
+            events[0].record()
+        self.r.frame()
+        if events:
+            events[1].record()
+        t = self.r.timings()
+        self.stage_ms.append(t.as_dict())
+        self.launches.append(t.kernel_launches)
+
+    @property
+    def kernels_per_step(self):
+        return int(round(np.mean(self.launches[-8:]))) if self.launches else 0
+
+    def e2e_step(self):
+        # the public API call a user makes: one frame, then the FP64 image read back
+        self.r.frame()
+        self.host_img = self.r.read(IMAGE_FINAL)
+
+    def n_events(self):
+        return 2
+
+    def units_per_step(self):
+        return self.P
+
+    def counted_frame(self):
+        """One untimed frame with traversal work counters."""
+        self.r.instrument(timing=True, counting=True)
+        self.r.frame()
+        t = self.r.timings()
+        self.r.instrument(timing=True, counting=False)
+        return t
+
+    def roofline(self, seg_ms, pk):
+        keys = ["extend_ms", "shade_ms", "shadow_ms", "compact_ms", "train_ms", "infer_ms", "compose_ms",
+                "camera_ms", "finalize_ms"]
+        n = max(1, min(len(self.stage_ms), 16))
+        mean = {k: float(np.mean([s[k] for s in self.stage_ms[-n:]])) for k in keys}
+        c = self.counted_frame()
+        dominant = max(("extend_ms", "shadow_ms", "shade_ms", "train_ms", "infer_ms"), key=lambda k: mean[k])
+        out = {"stage_ms_per_frame": {k: round(v, 4) for k, v in mean.items()},
+               "rays_per_frame": {"extension": int(c.extension_rays), "shadow": int(c.shadow_rays)},
+               "bvh_work_per_frame": {"extend_nodes": int(c.extend_nodes), "extend_prims": int(c.extend_prims),
+                                      "shadow_nodes": int(c.shadow_nodes), "shadow_prims": int(c.shadow_prims)}}
+        if dominant in ("extend_ms", "shadow_ms"):
+            if dominant == "extend_ms":
+                rays, nodes, prims = c.extension_rays, c.extend_nodes, c.extend_prims
+            else:
+                rays, nodes, prims = c.shadow_rays, c.shadow_nodes, c.shadow_prims
+            alg = rays * RAY_RECORD_BYTES + nodes * NODE_BYTES + prims * PRIM_BYTES
+            ach = alg / (mean[dominant] * 1e-3) / 1e9
+            out.update({"kernel": dominant.replace("_ms", "_kernel"), "bound": "hbm", "achieved": round(ach, 2),
+                        "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
+                        "traffic": None, "algorithmic_bytes_per_frame": int(alg),
+                        "note": ("algorithmic bytes = rays x 48 B + BVH nodes visited x 64 B + primitives "
+                                 "tested x 64 B, counted in an untimed frame; the 40 MB BVH and 10 MB of curves "
+                                 "are L2-resident, so this can exceed the HBM copy peak ("
+                                 + pk["source"] + ")")})
+        else:
+            out.update({"kernel": dominant, "bound": "tensor", "achieved": None, "peak": pk["bf16_tflops"],
+                        "unit": "TFLOP/s", "frac": None, "traffic": None})
+        return out
+
+    def config(self):
+        return {"workload": "render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments), "
+                            "20k-tri head, Preetham sky T=3 + directional (3,3,3), 512x512, path_v1=1, path_v2=40, "
+                            "BETA=1, cache FP32 HashGrid/OneBlob MLP 64x2, 2^16 training records/frame",
+                "pixels": self.P, "train_records": self.train_records,
+                "l2": "working set (BVH 40 MB + curves 10 MB + path state 70 MB) exceeds the 256 MiB flush; "
+                      "flushed between timed frames",
+                "parallelism": "replicas"}
+
+    def cpu_baseline(self, threads, budget_s=20.0):
+        """The oracle's reference-structured integrator (rayGenCam G-buffer pass,
+        msnnPathTrace / msnnTrainingPath) on the host cores, bounded sample of
+        pixels of the same scene; cache inference + one training step in FP64 numpy."""
+        import time
+        from oracle import mlp_oracle as mo
+        from oracle import pyoracle as po
+        o = po.OracleScene.from_library(self.scene)
+        net = self.r
+        cfg_text = json.dumps(_default_cache_config())
+        oc = mo.Config(cfg_text, 12, 3)
+        params = np.random.default_rng(0).normal(scale=0.05, size=oc.n_params)
+        every = max(1, self.P // self.train_records)
+        n = 4096
+        t0 = time.perf_counter()
+        done = 0
+        p0 = (self.height // 2) * self.width  # a band through the hair
+        while True:
+            col, nn_in, tr, fl = o.render_pixels(1, beta=1, accum_id=done // self.P, every_nth=every,
+                                                 n_train=self.train_records, p0=p0, n=n, threads=threads)
+            mo.forward(oc, params, nn_in)
+            tmask = (fl & 4) != 0
+            if tmask.any():
+                mo.backward(oc, params, nn_in[tmask], tr[tmask])
+            done += n
+            p0 = (p0 + n) % (self.P - n)
+            if time.perf_counter() - t0 > budget_s:
+                break
+        el = time.perf_counter() - t0
+        return {"value": round(done / el, 1), "unit": self.unit, "cores": threads, "kind": "port",
+                "sample": f"{done} pixels (1 spp) of the same scene: oracle rayGenCam/msnnPathTrace/"
+                          f"msnnTrainingPath on {threads} threads + FP64 numpy cache inference and training"}
+
+
+def _default_cache_config():
+    return {
+        "loss": {"otype": "RelativeL2Luminance"},
+        "optimizer": {"otype": "ExponentialDecay", "decay_start": 4000, "decay_interval": 4000, "decay_base": 0.33,
+                      "nested": {"otype": "Adam", "learning_rate": 1e-2, "beta1": 0.9, "beta2": 0.99,
+                                 "epsilon": 1e-15, "l2_reg": 1e-6}},
+        "encoding": {"otype": "Composite", "nested": [
+            {"n_dims_to_encode": 3, "otype": "HashGrid", "per_level_scale": 2.0, "log2_hashmap_size": 15,
+             "base_resolution": 16, "n_levels": 16},
+            {"n_dims_to_encode": 6, "otype": "OneBlob", "n_bins": 4}, {"otype": "Identity"}]},
+        "network": {"otype": "FullyFusedMLP", "activation": "ReLU", "output_activation": "None",
+                    "n_neurons": 64, "n_hidden_layers": 2}}

@@ -33,6 +33,9 @@ const char* hm_status_string(int status);
 const char* hm_last_error(void);
 /* Library version string and the CUDA arch it was compiled for ("sm_103a"). */
 const char* hm_version(void);
+/* Synchronous device -> host copy helper for callers without a CUDA runtime
+ * binding of their own (no reference counterpart). */
+int hm_copy_to_host(void* host_dst, const void* device_src, int64_t bytes);
 
 /* ------------------------------------------------------------------------
  * Hair material.  Replaces the hair block of the scene JSON as parsed by
@@ -156,6 +159,134 @@ int hm_mlp_get_gradients(const hm_mlp* mlp, float* host_out);
 /* TINY_MLP::loadWeights, neural_network.cu:23-32 (own binary snapshot format). */
 int hm_mlp_save(const hm_mlp* mlp, const char* path);
 int hm_mlp_load(hm_mlp* mlp, const char* path);
+
+/* ------------------------------------------------------------------------
+ * Scene.  Replaces parseScene (scene.cpp:119-339), the OWL geometry and
+ * texture set-up of RenderWindow_HairMSNN::initialize (render_hair_msnn.cu
+ * :98-412) and the OptiX acceleration-structure builds (owlGroupBuildAccel,
+ * :316-384, 412): the scene owns device copies of the hair curves (cubic
+ * B-spline segments), the head mesh, the environment sampling tables
+ * (generateEnvSamplingTables, scene.cpp:349-425) and an LBVH over all
+ * primitives.  json_text uses the reference's keys (camera, hair, integrator,
+ * lights, tcnn, surface) with the same defaults and the same image-size
+ * limits; the missing assets are replaced by generators:
+ *   hair.procedural    {type straight|curly, strands, control_points, length,
+ *                       radius, root_min_z, helix_radius, helix_pitch, seed}
+ *   surface.procedural {type ellipsoid, triangles, radii[3], diffuse[3], alpha}
+ *   lights.sky         {turbidity, sun[3], width, height, scale, rotation}
+ *                      (Preetham et al. 1999 sky baked to a lat-long map)
+ * base_dir resolves relative file names (tcnn.config).  Returns NULL and a
+ * status (HM_EPARSE for bad JSON, HM_EUNSUPPORTED for .hair/.obj/.exr files).
+ * ---------------------------------------------------------------------- */
+typedef struct hm_scene hm_scene;
+
+typedef struct hm_scene_desc {
+  int n_strands, n_control_points, n_segments;
+  int n_vertices, n_triangles, n_bvh_nodes;
+  int width, height, spp, path_v1, path_v2;
+  int env_width, env_height, n_dir_lights;
+  int mis, env_pdf, has_env;
+  int shading_catrom; /* 1: curves shaded as Catmull-Rom (reference closest-hit quirk) */
+  float scene_scale;
+  float bounds_min[3], bounds_max[3];
+} hm_scene_desc;
+
+enum hm_scene_array {
+  HM_SCENE_CONTROL_POINTS = 0, /* float4 (x, y, z, radius) */
+  HM_SCENE_SEGMENTS = 1,       /* int32 first control point of each segment */
+  HM_SCENE_VERTICES = 2,       /* float3 */
+  HM_SCENE_NORMALS = 3,        /* float3 */
+  HM_SCENE_TRIANGLES = 4,      /* int3 */
+  HM_SCENE_ENV = 5,            /* float4 lat-long radiance, z up */
+  HM_SCENE_ENV_CPDF = 6,       /* [H][W+1] */
+  HM_SCENE_ENV_CCDF = 7,
+  HM_SCENE_ENV_MPDF = 8,       /* [H+1] */
+  HM_SCENE_ENV_MCDF = 9,
+  HM_SCENE_DIR_LIGHTS = 10,    /* 6 floats each: normalised from, emit */
+  HM_SCENE_BVH_NODES = 11,     /* 64 bytes each: child AABBs + child indices */
+  HM_SCENE_BVH_LEAVES = 12,    /* int32 primitive of each leaf slot */
+  HM_SCENE_CAMERA = 13,        /* pos, dir_00, dir_du, dir_dv (12 floats) */
+  HM_SCENE_MATERIALS = 14      /* 16 floats: hair params, diffuse, alpha, env scale/rotation */
+};
+
+/* Host-only: parses and generates (no device work). */
+hm_scene* hm_scene_create(const char* json_text, const char* base_dir, int* status);
+/* Uploads the scene and builds its LBVH on the current device (also done on
+ * first use by hm_render_create / hm_trace_rays). */
+int hm_scene_build(hm_scene* scene);
+void hm_scene_destroy(hm_scene* scene);
+int hm_scene_info(const hm_scene* scene, hm_scene_desc* out);
+/* Host copy of one scene array (bytes: hm_scene_export_size). */
+int64_t hm_scene_export_size(const hm_scene* scene, int which);
+int hm_scene_export(const hm_scene* scene, int which, void* host_out, int64_t capacity_bytes);
+
+/* Closest-hit (any_hit = 0) or any-hit traversal of n rays: d_org, d_dir
+ * [n][3]; d_hits [n][4] = (t, primitive id as int bits (-1 miss), u, v):
+ * u is the curve parameter for hair segments (primitives 0..n_segments-1),
+ * (u, v) the barycentrics of vertices 1 and 2 for triangles.  Replaces
+ * owl::traceRay with its closest-hit / any-hit programs. */
+int hm_trace_rays(const hm_scene* scene, const float* d_org, const float* d_dir, int64_t n, float tmin,
+                  float tmax, int any_hit, float* d_hits, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Renderer.  Replaces RenderWindow_HairMSNN::render (render_hair_msnn.cu
+ * :699-771) with the device programs of cuda/hair_msnn.cu (rayGenCam,
+ * msnnPathTrace, msnnTrainingPath) and, in HM_MODE_PT, the plain path tracer
+ * of render_path_tracing.cu / cuda/path_tracing.cu.  One hm_render_frame is
+ * one sample per pixel: wavefront paths -> (MSNN) cache training step on
+ * the frame's records -> cache inference -> compose; images accumulate in
+ * FP64.  `beta` is the BETA command-line knob (render_hair_msnn.cu:1154,
+ * internal beta = BETA - 1).
+ * ---------------------------------------------------------------------- */
+typedef struct hm_render hm_render;
+
+enum hm_render_mode { HM_MODE_PT = 0, HM_MODE_MSNN = 1 };
+enum hm_image { HM_IMAGE_FINAL = 0, HM_IMAGE_SHORT = 1, HM_IMAGE_CACHE = 2 };
+
+typedef struct hm_render_options {
+  int mode;                      /* hm_render_mode */
+  int beta;                      /* BETA >= 1 */
+  int train_records;             /* per frame; 0 = 16384 (render_hair_msnn.h:127-129) */
+  int train;                     /* online cache training on/off (tcnn.init_train) */
+  int cache_precision;           /* HM_PREC_* */
+  uint32_t seed;                 /* cache initialisation */
+  const char* cache_config_json; /* NULL: the scene's tcnn.config, else the built-in one */
+} hm_render_options;
+
+typedef struct hm_render_stats {
+  int frames, pixels;
+  int64_t extension_rays;
+  int last_bounces;
+  int train_records, every_nth;
+  float last_loss;
+} hm_render_stats;
+
+hm_render* hm_render_create(hm_scene* scene, const hm_render_options* options, int* status);
+void hm_render_destroy(hm_render* render);
+int hm_render_frame(hm_render* render, void* stream);
+/* Restart accumulation (the reference's cameraChanged resets accumId). */
+int hm_render_reset(hm_render* render);
+/* Average of the accumulated frames, FP64 [H][W][3], row 0 = bottom. */
+int hm_render_read(hm_render* render, int which, double* host_rgb);
+int hm_render_get_stats(const hm_render* render, hm_render_stats* out);
+/* Per-frame instrumentation (the reference's renderTime / trainTime /
+ * inferTime, render_hair_msnn.cu:649-770, measured with CUDA events on the
+ * render stream).  timing: event pairs around every stage of each frame;
+ * counting: traversal work counters (slower kernels; for an untimed pass). */
+typedef struct hm_render_timings {
+  float total_ms, camera_ms, extend_ms, shade_ms, shadow_ms, compact_ms, finalize_ms;
+  float train_ms, infer_ms, compose_ms;
+  int bounces, kernel_launches;
+  int64_t extension_rays, shadow_rays;
+  int64_t extend_nodes, extend_prims, shadow_nodes, shadow_prims;
+} hm_render_timings;
+int hm_render_set_instrumentation(hm_render* render, int timing, int counting);
+int hm_render_get_timings(const hm_render* render, hm_render_timings* out);
+/* The render's cache network (owned by the render; NULL in PT mode). */
+hm_mlp* hm_render_cache(hm_render* render);
+/* Device buffers of the last frame: 0 cache inputs [P][12], 1 cache outputs
+ * [P][3], 2 training inputs [R][12], 3 training targets [R][3], 4 G-buffer. */
+int hm_render_buffer(hm_render* render, int which, void** dptr, int64_t* count);
 
 #ifdef __cplusplus
 }

@@ -105,6 +105,168 @@ def hair_sample(wo, t, h, u, hp=C1_HAIR, threads=1):
     return wi, f, pdf, margin
 
 
+def _declare_render(L):
+    if getattr(L, "_render_declared", False):
+        return
+    i32, f32, vp = ctypes.c_int, ctypes.c_float, ctypes.c_void_p
+    L.hmo_scene_new.restype = vp
+    L.hmo_scene_new.argtypes = [F32P, i32, I32P, i32, F32P, F32P, i32, I32P, i32, F32P, i32, i32, F32P, F32P,
+                                F32P, F32P, F32P, i32, F32P, F32P, I32P, f32]
+    L.hmo_scene_free.restype = None
+    L.hmo_scene_free.argtypes = [vp]
+    L.hmo_bvh_sizes.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.hmo_bvh_export.restype = None
+    L.hmo_bvh_export.argtypes = [vp, F32P, I32P]
+    L.hmo_trace_rays.restype = None
+    L.hmo_trace_rays.argtypes = [vp, F32P, F32P, i32, f32, f32, i32, F32P]
+    L.hmo_render_pixels.restype = None
+    L.hmo_render_pixels.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, F32P, F32P, F32P, I32P, i32]
+    L._render_declared = True
+
+
+class OracleScene:
+    """The oracle's copy of a scene: same arrays as the library's, its own LBVH."""
+
+    def __init__(self, arrays, settings, scene_scale):
+        L = lib()
+        _declare_render(L)
+        a = {k: np.ascontiguousarray(v) for k, v in arrays.items()}
+        self._keep = a
+        env_w, env_h = int(settings["env_w"]), int(settings["env_h"])
+        empty = np.zeros(4, np.float32)
+        g = lambda k: a[k] if a[k].size else empty
+        sets = np.array([settings["width"], settings["height"], settings["path_v1"], settings["path_v2"],
+                         settings["mis"], settings["env_pdf"], settings["has_env"], settings["catrom"]], np.int32)
+        self.h = L.hmo_scene_new(
+            a["control_points"].astype(np.float32).ravel(), len(a["control_points"]),
+            a["segments"].astype(np.int32).ravel(), len(a["segments"]),
+            a["vertices"].astype(np.float32).ravel(), a["normals"].astype(np.float32).ravel(), len(a["vertices"]),
+            a["triangles"].astype(np.int32).ravel(), len(a["triangles"]),
+            g("env").astype(np.float32).ravel(), env_w, env_h,
+            g("env_cpdf").ravel(), g("env_ccdf").ravel(), g("env_mpdf").ravel(), g("env_mcdf").ravel(),
+            g("dir_lights").astype(np.float32).ravel(), len(a["dir_lights"]),
+            a["camera"].astype(np.float32).ravel(), a["materials"].astype(np.float32).ravel(), sets,
+            float(scene_scale))
+        self.width, self.height = int(settings["width"]), int(settings["height"])
+
+    @classmethod
+    def from_library(cls, scene):
+        """scene: hairmsnn_gb300.render.Scene (host arrays only, no device)."""
+        names = ["control_points", "segments", "vertices", "normals", "triangles", "env", "env_cpdf",
+                 "env_ccdf", "env_mpdf", "env_mcdf", "dir_lights", "camera", "materials"]
+        arrays = {k: scene.export(k) for k in names}
+        i = scene.info()
+        settings = dict(width=i.width, height=i.height, path_v1=i.path_v1, path_v2=i.path_v2, mis=i.mis,
+                        env_pdf=i.env_pdf, has_env=i.has_env, catrom=i.shading_catrom, env_w=i.env_width,
+                        env_h=i.env_height)
+        return cls(arrays, settings, i.scene_scale)
+
+    def __del__(self):
+        try:
+            lib().hmo_scene_free(self.h)
+        except Exception:
+            pass
+
+    def bvh(self):
+        L = lib()
+        nn, nl = ctypes.c_int(), ctypes.c_int()
+        L.hmo_bvh_sizes(self.h, ctypes.byref(nn), ctypes.byref(nl))
+        nodes = np.zeros(nn.value * 16, np.float32)
+        leaves = np.zeros(nl.value, np.int32)
+        L.hmo_bvh_export(self.h, nodes, leaves)
+        return nodes.reshape(-1, 16), leaves
+
+    def trace(self, org, dirs, tmin=0.0, tmax=1e30, any_hit=False):
+        org, dirs = f32(org), f32(dirs)
+        hits = np.zeros((org.shape[0], 4), np.float32)
+        lib().hmo_trace_rays(self.h, org, dirs, org.shape[0], tmin, tmax, 1 if any_hit else 0, hits)
+        return hits
+
+    def render_pixels(self, mode, beta=1, accum_id=0, every_nth=1, n_train=0, p0=0, n=None, threads=8):
+        """One frame of rayGenCam for pixels [p0, p0+n): mode 0 PT, 1 MSNN G-buffer."""
+        n = self.width * self.height - p0 if n is None else n
+        color = np.zeros((n, 3), np.float32)
+        nn_in = np.zeros((n, 12), np.float32)
+        train = np.zeros((n, 3), np.float32)
+        flags = np.zeros(n, np.int32)
+        lib().hmo_render_pixels(self.h, mode, beta, accum_id, every_nth, n_train, p0, n, color, nn_in, train, flags,
+                                threads)
+        return color, nn_in, train, flags
+
+
+def env_tables(env, w, h):
+    """generateEnvSamplingTables (scene.cpp:349-425), single precision, order kept."""
+    env = np.asarray(env, np.float32).reshape(h, w, 4)
+    cw = w + 1
+    cpdf = np.zeros((h, cw), np.float32)
+    ccdf = np.zeros((h, cw), np.float32)
+    third = np.float32(1.0) / np.float32(3.0)
+    for y in range(h):
+        s = _sinf(np.float32(3.14159) * (np.float32(y) + np.float32(0.5)) / np.float32(h))
+        for x in range(w):
+            c = env[y, x]
+            avg = np.float32((np.float32(c[0] + c[1]) + c[2]) * third)
+            cpdf[y, x] = np.float32(avg * s)
+            if x > 0:
+                ccdf[y, x] = np.float32(ccdf[y, x - 1] + np.float32(cpdf[y, x - 1] / np.float32(w)))
+        total = np.float32(ccdf[y, w - 1] + np.float32(cpdf[y, w - 1] / np.float32(w)))
+        cpdf[y, w] = total
+        if total > 0:
+            inv = np.float32(np.float32(1.0) / total)
+            ccdf[y, 1:w] = (ccdf[y, 1:w] * inv).astype(np.float32)
+        ccdf[y, w] = 1.0
+    mpdf = np.zeros(h + 1, np.float32)
+    mcdf = np.zeros(h + 1, np.float32)
+    mpdf[0] = cpdf[0, w]
+    for i in range(1, h):
+        mpdf[i] = cpdf[i, w]
+        mcdf[i] = np.float32(mcdf[i - 1] + np.float32(mpdf[i - 1] / np.float32(h)))
+    total = np.float32(mcdf[h - 1] + np.float32(mpdf[h - 1] / np.float32(h)))
+    mpdf[h] = total
+    if total > 0:
+        mcdf[1:h] = (mcdf[1:h] / total).astype(np.float32)
+    mcdf[h] = 1.0
+    return cpdf.ravel(), ccdf.ravel(), mpdf, mcdf
+
+
+def _sinf(x):
+    """C sinf (float in, float out) through the oracle library's libm."""
+    return np.float32(_libm().sinf(ctypes.c_float(float(x))))
+
+
+_libm_h = None
+
+
+def _libm():
+    global _libm_h
+    if _libm_h is None:
+        _libm_h = ctypes.CDLL("libm.so.6")
+        _libm_h.sinf.restype = ctypes.c_float
+        _libm_h.sinf.argtypes = [ctypes.c_float]
+    return _libm_h
+
+
+def camera_vectors(frm, at, up, cos_fovy, width, height):
+    """cameraChanged (render_hair_msnn.cu:1093-1118) in float32."""
+    f = lambda v: np.asarray(v, np.float32)
+
+    def normalize(v):
+        v = f(v)
+        d = np.float32(np.float32(v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
+        return (v * np.float32(np.float32(1.0) / np.float32(np.sqrt(d)))).astype(np.float32)
+
+    def cross(a, b):
+        return f([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]])
+
+    d00 = normalize(f(at) - f(frm))
+    aspect = np.float32(np.float32(width) / np.float32(height))
+    ddu = (np.float32(cos_fovy) * aspect * normalize(cross(d00, f(up)))).astype(np.float32)
+    ddv = (np.float32(cos_fovy) * normalize(cross(ddu, d00))).astype(np.float32)
+    d00 = (d00 - np.float32(0.5) * ddu).astype(np.float32)
+    d00 = (d00 - np.float32(0.5) * ddv).astype(np.float32)
+    return f(frm), d00, ddu, ddv
+
+
 def gen_bsdf_queries(seed, n):
     """Synthetic BSDF workload, planar layouts: wo/wi/t [3,n], h [n], u [4,n]."""
     wo = np.zeros((3, n), np.float32)

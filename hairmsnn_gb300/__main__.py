@@ -1,0 +1,97 @@
+"""Command line: the reference's `render_hair_msnn [scene.json] [BETA]`
+(render_hair_msnn.cu:1146-1175) without the viewer.
+
+  python -m hairmsnn_gb300 render [scene.json] [BETA] [--frames N] [--mode msnn|pt]
+                                  [--width W --height H] [--out image.pfm] [--stats out.json]
+
+Without a scene file the built-in straight-hair scene is used.  Frames
+accumulate in FP64; --out writes the average as a little-endian PFM
+(bottom row first, the renderer's own row order).  --stats writes per-frame
+timings (the reference's renderTime/trainTime/inferTime) and the cache loss
+as JSON (the reference parses integrator.stats_output but never writes it).
+"""
+import argparse
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+
+def write_pfm(path, img):
+    """img: [H, W, 3] float, row 0 = bottom (PFM stores bottom-to-top)."""
+    h, w, _ = img.shape
+    with open(path, "wb") as f:
+        f.write(f"PF\n{w} {h}\n-1.0\n".encode())
+        f.write(np.ascontiguousarray(img, dtype="<f4").tobytes())
+
+
+def read_pfm(path):
+    with open(path, "rb") as f:
+        assert f.readline().strip() == b"PF"
+        w, h = (int(x) for x in f.readline().split())
+        scale = float(f.readline())
+        dt = "<f4" if scale < 0 else ">f4"
+        return np.frombuffer(f.read(), dtype=dt).reshape(h, w, 3).astype(np.float32)
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m hairmsnn_gb300")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    r = sub.add_parser("render")
+    r.add_argument("scene", nargs="?", default=None)
+    r.add_argument("beta", nargs="?", type=int, default=1)
+    r.add_argument("--frames", type=int, default=None, help="default: integrator.spp")
+    r.add_argument("--mode", choices=["msnn", "pt"], default="msnn")
+    r.add_argument("--width", type=int, default=None)
+    r.add_argument("--height", type=int, default=None)
+    r.add_argument("--strands", type=int, default=None, help="built-in scene only")
+    r.add_argument("--train-records", type=int, default=16384)
+    r.add_argument("--out", default=None)
+    r.add_argument("--stats", default=None)
+    a = ap.parse_args(argv)
+
+    from . import build, render
+    build.build()
+    if a.scene:
+        cfg = json.load(open(a.scene))
+        base = os.path.dirname(os.path.abspath(a.scene))
+    else:
+        cfg = render.straight_hair_scene(a.width or 512, a.height or 512,
+                                         **({"strands": a.strands} if a.strands else {}))
+        base = None
+    if a.width:
+        cfg.setdefault("integrator", {})["width"] = a.width
+    if a.height:
+        cfg.setdefault("integrator", {})["height"] = a.height
+    scene = render.Scene(cfg, base)
+    rd = render.Renderer(scene, render.MSNN if a.mode == "msnn" else render.PT, beta=a.beta,
+                         train_records=a.train_records, train=cfg.get("tcnn", {}).get("init_train", True))
+    rd.instrument(timing=True)
+    frames = a.frames if a.frames is not None else scene.info().spp
+    log = []
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        rd.frame()
+        t = rd.timings().as_dict()
+        t["loss"] = rd.stats().last_loss
+        log.append(t)
+    wall = time.perf_counter() - t0
+    img = rd.read(render.IMAGE_FINAL)
+    out = a.out or cfg.get("integrator", {}).get("image_output") or None
+    if out:
+        if not out.endswith(".pfm"):
+            out = os.path.splitext(out)[0] + ".pfm"
+        write_pfm(out, img)
+    summary = {"frames": frames, "wall_s": wall, "paths_per_s": frames * img.shape[0] * img.shape[1] / wall,
+               "mean_radiance": float(img.mean())}
+    print(json.dumps(summary))
+    stats_path = a.stats or cfg.get("integrator", {}).get("stats_output") or None
+    if stats_path:
+        json.dump({"summary": summary, "frames": log}, open(stats_path, "w"), indent=1)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -260,9 +260,20 @@ __global__ void __launch_bounds__(256) encode_kernel(const float* __restrict__ i
   for (int k = d.n_enc; k < d.in_pad; ++k) xo[k] = 1.f;
 }
 
+// Hash-grid gradients are scattered as 64-bit fixed-point integers (2^-40
+// resolution, range +-2^23): integer addition is associative, so the sum does
+// not depend on the order the atomics land in and training stays bitwise
+// reproducible.
+constexpr double kGridFix = 1099511627776.0;  // 2^40
+
+__global__ void grid_fix_to_float_kernel(const long long* __restrict__ acc, float* __restrict__ out, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)((double)acc[i] * (1.0 / kGridFix));
+}
+
 // Hash-grid backward: dX columns of the grid features -> table gradients.
 __global__ void __launch_bounds__(256) grid_bwd_kernel(const float* __restrict__ in, const float* __restrict__ dX,
-                                                       float* __restrict__ enc_grad, int64_t n) {
+                                                       long long* __restrict__ enc_grad, int64_t n) {
   const MlpDims& d = c_dims[0];
   const int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (q >= n) return;
@@ -271,7 +282,7 @@ __global__ void __launch_bounds__(256) grid_bwd_kernel(const float* __restrict__
   for (int si = 0; si < d.n_segs; ++si) {
     const EncSeg& s = d.segs[si];
     if (s.type != ENC_HASHGRID) continue;
-    float* tg = enc_grad + s.param_off;
+    long long* tg = enc_grad + s.param_off;
     float px = xin[s.in_off], py = xin[s.in_off + 1], pz = xin[s.in_off + 2];
     for (int l = 0; l < s.n_levels; ++l) {
       const float sc = s.level_scale[l];
@@ -285,7 +296,10 @@ __global__ void __launch_bounds__(256) grid_bwd_kernel(const float* __restrict__
         uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
         for (int f = 0; f < s.n_feat; ++f) {
           float gv = g[s.out_off + l * s.n_feat + f];
-          if (gv != 0.f) atomicAdd(tg + (int64_t)e * s.n_feat + f, w * gv);
+          if (gv != 0.f) {
+            const long long q = __double2ll_rn((double)(w * gv) * kGridFix);
+            if (q != 0) atomicAdd((unsigned long long*)(tg + (int64_t)e * s.n_feat + f), (unsigned long long)q);
+          }
         }
       }
     }
@@ -655,6 +669,7 @@ struct Mlp {
   int64_t dw_part_cap = 0;
   float* loss_part = nullptr;
   float* loss_dev = nullptr;
+  long long* grid_acc = nullptr;  // fixed-point hash-grid gradient accumulator
   int64_t last_n = 0;        // batch of the last forward()
   const float* last_in = nullptr;
 };
@@ -841,6 +856,7 @@ extern "C" void hm_mlp_destroy(hm_mlp* h) {
   cudaFree(m->adam_v);
   cudaFree(m->dw_part);
   cudaFree(m->loss_dev);
+  cudaFree(m->grid_acc);
   delete m;
 }
 
@@ -975,10 +991,16 @@ extern "C" int hm_mlp_backward(hm_mlp* h, const float* d_target, int64_t n, floa
     HM_CHECK_LAUNCH("dw_reduce_kernel");
   }
   if (d.n_enc_params > 0) {
-    cudaError_t e = cudaMemsetAsync(m->grads + d.n_net_params, 0, d.n_enc_params * sizeof(float), st);
+    if (!m->grid_acc) {
+      cudaError_t e = cudaMalloc(&m->grid_acc, d.n_enc_params * sizeof(long long));
+      if (e != cudaSuccess) return hm_cuda_status(e, "grid grad accumulator");
+    }
+    cudaError_t e = cudaMemsetAsync(m->grid_acc, 0, d.n_enc_params * sizeof(long long), st);
     if (e != cudaSuccess) return hm_cuda_status(e, "grid grad clear");
-    grid_bwd_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(m->last_in, m->dX, m->grads + d.n_net_params, n);
+    grid_bwd_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(m->last_in, m->dX, m->grid_acc, n);
     HM_CHECK_LAUNCH("grid_bwd_kernel");
+    grid_fix_to_float_kernel<<<1024, 256, 0, st>>>(m->grid_acc, m->grads + d.n_net_params, d.n_enc_params);
+    HM_CHECK_LAUNCH("grid_fix_to_float_kernel");
   }
   if (d_loss) {
     cudaError_t e = cudaMemcpyAsync(d_loss, m->loss_dev, sizeof(float), cudaMemcpyDeviceToDevice, st);

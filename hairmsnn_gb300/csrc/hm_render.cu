@@ -387,7 +387,7 @@ static int render_frame(Render* r, cudaStream_t st) {
     hm_mlp_info(r->mlp, &md);
     const bool grid_enc = md.n_params > md.n_network_params;
     // training: encode, fwd, bwd, loss reduce, (dw partial + reduce) per layer, [grid bwd], adam
-    launches += (r->train ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 1 : 0) + 1 : 0) + 2 + 1;
+    launches += (r->train ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 2 : 0) + 1 : 0) + 2 + 1;
   }
   mark(S_END);
   r->accum_id += 1;

@@ -100,12 +100,16 @@ def test_training_gradients_and_adam_match_oracle(mlpmod, cfg, in_ch, gen):
     assert np.abs((p1 - p0) - (ref_p1 - p0)).max() <= 1e-3 * oc.lr
 
 
-def test_training_is_bitwise_deterministic(mlpmod):
-    x = torch.from_numpy(c1_inputs(4096, seed=4)).cuda()
+@pytest.mark.parametrize("cfg,in_ch,gen", [("c1_cache_w64.json", 16, c1_inputs),
+                                           ("hairmsnn_cache.json", 12, ref_inputs)])
+def test_training_is_bitwise_deterministic(mlpmod, cfg, in_ch, gen):
+    """Fixed-order weight-gradient reduction and fixed-point hash-grid
+    gradient atomics: repeated training is bit-identical."""
+    x = torch.from_numpy(gen(4096, seed=4)).cuda()
     t = torch.from_numpy(np.random.default_rng(3).uniform(0, 2, (4096, 3)).astype(np.float32)).cuda()
     runs = []
     for _ in range(2):
-        net = mlpmod.TinyMLP("c1_cache_w64.json", 16, 3, seed=1)
+        net = mlpmod.TinyMLP(cfg, in_ch, 3, seed=1)
         for _ in range(5):
             net.training_step(x, t)
         runs.append(net.params())

@@ -25,65 +25,154 @@ int launch_finalize(const SceneDev& s, const FrameParams& fp, const PathState& p
                     cudaStream_t st);
 int launch_compose(const SceneDev& s, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st);
 
-// COUNT: accumulate BVH nodes visited / primitives tested into cnt[0..1]
-// (an untimed instrumentation pass; the timed path uses COUNT = false).
-template <bool COUNT>
-__global__ void __launch_bounds__(128) extend_kernel(SceneDev s, PathState ps, const int* __restrict__ queue,
-                                                     const int* __restrict__ count, int* err,
-                                                     unsigned long long* cnt) {
-  const int n = *count;
-  TraceCount tc{0, 0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+// ---- persistent traversal with warp-aggregated dynamic ray fetching
+// Ray sources: extension rays (one per queued path), shadow rays (two slots
+// per queued path, empty slots finish at once), and plain ray batches.
+struct ExtendRays {
+  PathState ps;
+  const int* queue;
+  const int* count;
+  HM_D int n() const { return *count; }
+  HM_D bool ray(int i, f3* o, f3* d) const {
     const int pid = queue[i];
-    const float4 o = ps.ray_o[pid], d = ps.ray_d[pid];
-    Ray r{mk(o.x, o.y, o.z), mk(d.x, d.y, d.z), 0.f, 1e30f};
-    Hit h = trace<false, COUNT>(s, r, err, &tc);
-    ps.hit[pid] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v);
+    const float4 a = ps.ray_o[pid], b = ps.ray_d[pid];
+    *o = mk(a.x, a.y, a.z);
+    *d = mk(b.x, b.y, b.z);
+    return true;
+  }
+  HM_D void write(int i, const Hit& h) const {
+    ps.hit[queue[i]] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v);
+  }
+};
+
+struct ShadowRays {
+  PathState ps;
+  const int* queue;
+  const int* count;
+  uint8_t* vis;  // [P][2]: 1 = unoccluded
+  HM_D int n() const { return 2 * *count; }
+  HM_D bool ray(int i, f3* o, f3* d) const {
+    const int pid = queue[i >> 1];
+    if (!(ps.flags[pid] & F_DL)) return false;
+    const float4 a = (i & 1) ? ps.sh_o1[pid] : ps.sh_o0[pid];
+    if (a.w == 0.f) return false;
+    const float4 b = (i & 1) ? ps.sh_d1[pid] : ps.sh_d0[pid];
+    *o = mk(a.x, a.y, a.z);
+    *d = mk(b.x, b.y, b.z);
+    return true;
+  }
+  HM_D void write(int i, const Hit& h) const { vis[2 * queue[i >> 1] + (i & 1)] = h.prim < 0 ? 1 : 0; }
+};
+
+struct BatchRays {
+  const float* org;
+  const float* dir;
+  int64_t count;
+  float tmin, tmax;
+  float4* out;
+  HM_D int n() const { return (int)count; }
+  HM_D bool ray(int i, f3* o, f3* d) const {
+    *o = mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]);
+    *d = mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
+    return true;
+  }
+  HM_D void write(int i, const Hit& h) const { out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v); }
+};
+
+// COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
+// cnt[0..2] (an untimed instrumentation pass; timed frames use COUNT = false).
+template <class Src, bool ANY_HIT, bool COUNT>
+__global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev s, float tmin, float tmax,
+                                                               int* __restrict__ fetch, int* err,
+                                                               unsigned long long* cnt) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int n = src.n();
+  int stack[kStack];
+  TravState t;
+  TraceCount tc{0, 0};
+  uint32_t rays = 0;
+  int cur = -1;
+  bool exhausted = false;
+  for (;;) {
+    const unsigned idle = __ballot_sync(FULL, cur < 0);
+    if (idle && !exhausted) {
+      const int leader = __ffs(idle) - 1;
+      const int want = __popc(idle);
+      int base = 0;
+      if (lane == leader) base = atomicAdd(fetch, want);
+      base = __shfl_sync(FULL, base, leader);
+      exhausted = base + want >= n;
+      if (cur < 0) {
+        const int my = base + __popc(idle & ((1u << lane) - 1u));
+        if (my < n) {
+          f3 o, d;
+          if (src.ray(my, &o, &d)) {
+            trav_init(t, o, d, tmin, tmax);
+            cur = my;
+            if (COUNT) ++rays;
+          } else {
+            src.write(my, Hit{tmax, -1, 0.f, 0.f});
+          }
+        }
+      }
+    }
+    if (exhausted && __all_sync(FULL, cur < 0)) break;
+    if (cur >= 0 && trav_step<ANY_HIT, COUNT>(s, t, stack, err, &tc)) {
+      src.write(cur, t.h);
+      cur = -1;
+    }
   }
   if (COUNT) {
     atomicAdd(cnt + 0, (unsigned long long)tc.nodes);
     atomicAdd(cnt + 1, (unsigned long long)tc.prims);
+    atomicAdd(cnt + 2, (unsigned long long)rays);
   }
 }
 
-// Resolves the pending direct-lighting samples: visible sum, NaN check
-// (directLighting, optix_common.cuh:296-308), weighted add to the path
-// radiance.  Explicitly rounded operations: no multiply-add contraction.
-template <bool COUNT>
-__global__ void __launch_bounds__(128) shadow_kernel(SceneDev s, PathState ps, const int* __restrict__ queue,
-                                                     const int* __restrict__ count, int* err,
-                                                     unsigned long long* cnt) {
+template <class Src, bool ANY_HIT>
+static int launch_persistent(const Src& src, const SceneDev& s, float tmin, float tmax, int* fetch, int* err,
+                             unsigned long long* cnt, bool counting, int max_blocks, cudaStream_t st) {
+  if (counting)
+    persistent_trace_kernel<Src, ANY_HIT, true><<<max_blocks, 128, 0, st>>>(src, s, tmin, tmax, fetch, err, cnt);
+  else
+    persistent_trace_kernel<Src, ANY_HIT, false><<<max_blocks, 128, 0, st>>>(src, s, tmin, tmax, fetch, err, cnt);
+  HM_CHECK_LAUNCH("persistent_trace_kernel");
+  return HM_OK;
+}
+
+template <class Src, bool ANY_HIT>
+static int persistent_blocks() {
+  int dev = 0, sms = 152, per_sm = 4;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_trace_kernel<Src, ANY_HIT, false>, 128, 0);
+  return sms * std::max(1, per_sm);
+}
+
+// Resolves the pending direct-lighting samples of each queued path: visible
+// sum, NaN check (directLighting, optix_common.cuh:296-308), weighted add to
+// the path radiance.  Explicitly rounded operations: no contraction.
+__global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const int* __restrict__ queue,
+                                                             const int* __restrict__ count,
+                                                             const uint8_t* __restrict__ vis) {
   const int n = *count;
-  TraceCount tc{0, 0};
-  uint32_t rays = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int pid = queue[i];
     const uint32_t flags = ps.flags[pid];
     if (!(flags & F_DL)) continue;
-    float sx = 0.f, sy = 0.f, sz = 0.f;  // lightSample + bsdfSample
-    const float4 o0 = ps.sh_o0[pid], o1 = ps.sh_o1[pid];
     float c0x = 0.f, c0y = 0.f, c0z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
-    if (o0.w != 0.f) {
-      const float4 d = ps.sh_d0[pid];
-      Ray r{mk(o0.x, o0.y, o0.z), mk(d.x, d.y, d.z), 0.f, 1e30f};
-      if (COUNT) ++rays;
-      if (trace<true, COUNT>(s, r, err, &tc).prim < 0) {
-        const float4 c = ps.sh_c0[pid];
-        c0x = c.x; c0y = c.y; c0z = c.z;
-      }
+    if (ps.sh_o0[pid].w != 0.f && vis[2 * pid]) {
+      const float4 c = ps.sh_c0[pid];
+      c0x = c.x; c0y = c.y; c0z = c.z;
     }
-    if (o1.w != 0.f) {
-      const float4 d = ps.sh_d1[pid];
-      Ray r{mk(o1.x, o1.y, o1.z), mk(d.x, d.y, d.z), 0.f, 1e30f};
-      if (COUNT) ++rays;
-      if (trace<true, COUNT>(s, r, err, &tc).prim < 0) {
-        const float4 c = ps.sh_c1[pid];
-        c1x = c.x; c1y = c.y; c1z = c.z;
-      }
+    if (ps.sh_o1[pid].w != 0.f && vis[2 * pid + 1]) {
+      const float4 c = ps.sh_c1[pid];
+      c1x = c.x; c1y = c.y; c1z = c.z;
     }
-    sx = __fadd_rn(0.f, __fadd_rn(c0x, c1x));
-    sy = __fadd_rn(0.f, __fadd_rn(c0y, c1y));
-    sz = __fadd_rn(0.f, __fadd_rn(c0z, c1z));
+    float sx = __fadd_rn(0.f, __fadd_rn(c0x, c1x));
+    float sy = __fadd_rn(0.f, __fadd_rn(c0y, c1y));
+    float sz = __fadd_rn(0.f, __fadd_rn(c0z, c1z));
     if (isnan(sx) || isnan(sy) || isnan(sz)) sx = sy = sz = 0.f;
     const float4 w = ps.dl_w[pid];
     float4 c = ps.col[pid];
@@ -100,11 +189,6 @@ __global__ void __launch_bounds__(128) shadow_kernel(SceneDev s, PathState ps, c
       ps.col_s[pid] = cs;
     }
     ps.flags[pid] = flags & ~F_DL;
-  }
-  if (COUNT) {
-    atomicAdd(cnt + 2, (unsigned long long)tc.nodes);
-    atomicAdd(cnt + 3, (unsigned long long)tc.prims);
-    atomicAdd(cnt + 4, (unsigned long long)rays);
   }
 }
 
@@ -216,6 +300,10 @@ struct Render {
   int64_t rays_extend = 0, rays_shadow_paths = 0;
   int last_bounces = 0;
   int sm_count = 152;
+  int* fetch = nullptr;  // ray-fetch counters of the persistent traversals, 2 per bounce
+  int fetch_slots = 0;
+  uint8_t* vis = nullptr;  // shadow-ray visibility [P][2]
+  int blocks_extend = 0, blocks_shadow = 0;
   float last_loss = 0.f;
   float* d_loss = nullptr;
   // instrumentation
@@ -283,6 +371,11 @@ static int render_setup(Render* r, const hm_render_options* o) {
   if (e == cudaSuccess) e = r->alloc(&r->fb.acc_final, (size_t)P * 3);
   if (e == cudaSuccess) e = r->alloc(&r->d_loss, 1);
   if (e == cudaSuccess) e = r->alloc(&r->d_cnt, 8);
+  r->fetch_slots = 2 * (s->path_v2 + 2);
+  if (e == cudaSuccess) e = r->alloc(&r->fetch, r->fetch_slots);
+  if (e == cudaSuccess) e = r->alloc(&r->vis, (size_t)P * 2);
+  r->blocks_extend = persistent_blocks<ExtendRays, false>();
+  r->blocks_shadow = persistent_blocks<ShadowRays, true>();
   if (e == cudaSuccess) e = cudaMallocHost(&r->h_count, sizeof(int));
   if (e != cudaSuccess) return hm_cuda_status(e, "render buffers");
   cudaMemset(r->err, 0, sizeof(int));
@@ -331,6 +424,7 @@ static int render_frame(Render* r, cudaStream_t st) {
   };
   enum { S_CAMERA, S_EXTEND, S_SHADE, S_SHADOW, S_COMPACT, S_FINALIZE, S_TRAIN, S_INFER, S_COMPOSE, S_END };
   if (r->counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
+  cudaMemsetAsync(r->fetch, 0, r->fetch_slots * sizeof(int), st);
   mark(S_CAMERA);
   if (int e = launch_camera(sd, fp, r->ps, q_cur, c_cur, st)) return e;
   const int grid = r->sm_count * 8;
@@ -340,19 +434,19 @@ static int render_frame(Render* r, cudaStream_t st) {
   int64_t ext_rays = 0;
   for (int it = 0; it <= s->path_v2 && count > 0; ++it) {
     mark(S_EXTEND);
-    if (r->counting)
-      extend_kernel<true><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
-    else
-      extend_kernel<false><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
-    HM_CHECK_LAUNCH("extend_kernel");
+    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{r->ps, q_cur, c_cur}, sd, 0.f, 1e30f,
+                                                     r->fetch + 2 * it, r->err, r->d_cnt, r->counting,
+                                                     r->blocks_extend, st))
+      return e;
     mark(S_SHADE);
     if (int e = launch_shade(sd, fp, r->ps, r->fb, q_cur, c_cur, r->keep, grid, st)) return e;
     mark(S_SHADOW);
-    if (r->counting)
-      shadow_kernel<true><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
-    else
-      shadow_kernel<false><<<grid, 128, 0, st>>>(sd, r->ps, q_cur, c_cur, r->err, r->d_cnt);
-    HM_CHECK_LAUNCH("shadow_kernel");
+    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{r->ps, q_cur, c_cur, r->vis}, sd, 0.f, 1e30f,
+                                                    r->fetch + 2 * it + 1, r->err, r->d_cnt + 3, r->counting,
+                                                    r->blocks_shadow, st))
+      return e;
+    shadow_resolve_kernel<<<grid, 256, 0, st>>>(r->ps, q_cur, c_cur, r->vis);
+    HM_CHECK_LAUNCH("shadow_resolve_kernel");
     mark(S_COMPACT);
     scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(r->keep, c_cur, r->block_sums, nblocks);
     scan_blocks_kernel<<<1, 1024, 0, st>>>(r->block_sums, c_cur, c_next);
@@ -372,7 +466,7 @@ static int render_frame(Render* r, cudaStream_t st) {
   r->last_bounces = bounces;
   mark(S_FINALIZE);
   if (int e = launch_finalize(sd, fp, r->ps, r->fb, st)) return e;
-  int launches = 1 + 6 * bounces + 1;
+  int launches = 1 + 7 * bounces + 1;
   if (r->mode == MODE_MSNN) {
     mark(S_TRAIN);
     if (r->train) {
@@ -413,21 +507,11 @@ static int render_frame(Render* r, cudaStream_t st) {
     cudaStreamSynchronize(st);
     tm.extend_nodes = (int64_t)c[0];
     tm.extend_prims = (int64_t)c[1];
-    tm.shadow_nodes = (int64_t)c[2];
-    tm.shadow_prims = (int64_t)c[3];
-    tm.shadow_rays = (int64_t)c[4];
+    tm.shadow_nodes = (int64_t)c[3];
+    tm.shadow_prims = (int64_t)c[4];
+    tm.shadow_rays = (int64_t)c[5];
   }
   return HM_OK;
-}
-
-// Trace an arbitrary batch of rays (tests and the traversal benchmark).
-__global__ void trace_batch_kernel(SceneDev s, const float* __restrict__ org, const float* __restrict__ dir, int64_t n,
-                                   float tmin, float tmax, int any_hit, float4* __restrict__ out, int* err) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    Ray r{mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]), mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]), tmin, tmax};
-    Hit h = any_hit ? trace<true>(s, r, err) : trace<false>(s, r, err);
-    out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v);
-  }
 }
 
 }  // namespace hm
@@ -571,22 +655,25 @@ extern "C" int hm_trace_rays(const hm_scene* h, const float* d_org, const float*
   if (!s || n < 0 || (n > 0 && (!d_org || !d_dir || !d_hits))) return hm_set_error("hm_trace_rays: bad args"), HM_EINVAL;
   if (n == 0) return HM_OK;
   if (int st = s->ensure_built()) return st;
-  int* err = nullptr;
-  cudaError_t e = cudaMalloc(&err, sizeof(int));
+  if (n > INT32_MAX) return hm_set_error("hm_trace_rays: at most 2^31-1 rays per call"), HM_ECAPACITY;
+  int* err = nullptr;  // [0] error bits, [1] ray-fetch counter
+  cudaError_t e = cudaMalloc(&err, 2 * sizeof(int));
   if (e != cudaSuccess) return hm_cuda_status(e, "hm_trace_rays");
-  cudaMemsetAsync(err, 0, sizeof(int), (cudaStream_t)stream);
-  int dev = 0, sms = 152;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int grid = (int)std::min<int64_t>((n + 127) / 128, (int64_t)sms * 16);
-  trace_batch_kernel<<<grid, 128, 0, (cudaStream_t)stream>>>(s->dev(), d_org, d_dir, n, tmin, tmax, any_hit,
-                                                             (float4*)d_hits, err);
+  cudaMemsetAsync(err, 0, 2 * sizeof(int), (cudaStream_t)stream);
+  BatchRays src{d_org, d_dir, n, tmin, tmax, (float4*)d_hits};
+  int st = any_hit ? launch_persistent<BatchRays, true>(src, s->dev(), tmin, tmax, err + 1, err, nullptr, false,
+                                                        persistent_blocks<BatchRays, true>(), (cudaStream_t)stream)
+                   : launch_persistent<BatchRays, false>(src, s->dev(), tmin, tmax, err + 1, err, nullptr, false,
+                                                         persistent_blocks<BatchRays, false>(), (cudaStream_t)stream);
+  if (st != HM_OK) {
+    cudaFree(err);
+    return st;
+  }
   int herr = 0;
-  e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
   cudaFree(err);
-  if (e != cudaSuccess) return hm_cuda_status(e, "trace_batch_kernel");
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_trace_rays");
   if (herr) return hm_set_error("traversal gave up on some rays (error bits 0x%x)", herr), HM_ECAPACITY;
   return HM_OK;
 }

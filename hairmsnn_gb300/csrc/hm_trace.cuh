@@ -193,6 +193,85 @@ struct TraceCount {
   uint32_t nodes, prims;
 };
 
+// Resumable traversal: one node visit per trav_step(), so a persistent
+// kernel can hand a lane a new ray as soon as its previous ray finishes
+// (dynamic ray fetching, Aila & Laine, HPG 2009).
+struct TravState {
+  f3 o, d, inv;
+  float tmin;
+  Hit h;
+  int node;
+  int sp;
+  int visits;
+};
+
+HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
+  t.o = o;
+  t.d = d;
+  t.inv = mk(fabsf(d.x) > 1e-20f ? 1.f / d.x : copysignf(1e20f, d.x),
+             fabsf(d.y) > 1e-20f ? 1.f / d.y : copysignf(1e20f, d.y),
+             fabsf(d.z) > 1e-20f ? 1.f / d.z : copysignf(1e20f, d.z));
+  t.tmin = tmin;
+  t.h = Hit{tmax, -1, 0.f, 0.f};
+  t.node = 0;
+  t.sp = 0;
+  t.visits = 0;
+}
+
+HM_D bool prim_intersect(const SceneDev& s, int prim, const Ray& r, float tmax, float* t, float* u, float* v);
+
+// Returns true when the ray is finished (result in t.h).
+template <bool ANY_HIT, bool COUNT>
+HM_D bool trav_step(const SceneDev& s, TravState& t, int* stack, int* err, TraceCount* cnt) {
+  if (++t.visits > kMaxVisits) {
+    atomicOr(err, TRACE_ERR_STEPS);
+    return true;
+  }
+  const Ray r{t.o, t.d, t.tmin, t.h.t};
+  float t0, t1;
+  int c0, c1;
+  node_test(s.nodes, t.node, t.o, t.inv, t.tmin, t.h.t, &t0, &t1, &c0, &c1);
+  if (COUNT) cnt->nodes += 1;
+  if (COUNT) cnt->prims += (c0 < 0 && t0 < INFINITY) + (c1 < 0 && t1 < INFINITY);
+  if (c0 < 0 && t0 < INFINITY) {
+    float th, u, v;
+    const int prim = __ldg(s.prim_of_leaf + ~c0);
+    if (prim_intersect(s, prim, r, t.h.t, &th, &u, &v)) {
+      t.h = Hit{th, prim, u, v};
+      if (ANY_HIT) return true;
+    }
+    t0 = INFINITY;
+    if (t1 > t.h.t) t1 = INFINITY;
+  }
+  if (c1 < 0 && t1 < INFINITY) {
+    float th, u, v;
+    const int prim = __ldg(s.prim_of_leaf + ~c1);
+    if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v)) {
+      t.h = Hit{th, prim, u, v};
+      if (ANY_HIT) return true;
+    }
+    t1 = INFINITY;
+    if (t0 > t.h.t) t0 = INFINITY;
+  }
+  const bool go0 = t0 < INFINITY, go1 = t1 < INFINITY;
+  if (go0 && go1) {
+    if (t.sp >= kStack) {
+      atomicOr(err, TRACE_ERR_STACK);
+      return true;
+    }
+    stack[t.sp++] = t0 <= t1 ? c1 : c0;
+    t.node = t0 <= t1 ? c0 : c1;
+  } else if (go0) {
+    t.node = c0;
+  } else if (go1) {
+    t.node = c1;
+  } else {
+    if (t.sp == 0) return true;
+    t.node = stack[--t.sp];
+  }
+  return false;
+}
+
 // ANY_HIT == true: return at the first hit in (tmin, tmax) (shadow rays).
 template <bool ANY_HIT, bool COUNT = false>
 HM_D Hit trace(const SceneDev& s, const Ray& r, int* err, TraceCount* cnt = nullptr) {

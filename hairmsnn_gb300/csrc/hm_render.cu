@@ -79,6 +79,8 @@ struct BatchRays {
   HM_D void write(int i, const Hit& h) const { out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v); }
 };
 
+constexpr int kStragglers = 2;  // lanes a warp does not wait for before its leaf phase
+
 // COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
 // cnt[0..2] (an untimed instrumentation pass; timed frames use COUNT = false).
 template <class Src, bool ANY_HIT, bool COUNT>
@@ -118,9 +120,20 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
       }
     }
     if (exhausted && __all_sync(FULL, cur < 0)) break;
-    if (cur >= 0 && trav_step<ANY_HIT, COUNT>(s, t, stack, err, &tc)) {
-      src.write(cur, t.h);
-      cur = -1;
+    // box phase: walk inner nodes until all but a few lanes have parked a leaf
+    // (or finished); stragglers continue in the next round
+    for (;;) {
+      const bool need = cur >= 0 && trav_needs_step(t);
+      if (__popc(__ballot_sync(FULL, need)) <= kStragglers) break;
+      if (need) trav_inner_step<COUNT>(s, t, stack, err, &tc);
+    }
+    // leaf phase: the parked curve / triangle tests run together
+    if (cur >= 0) {
+      const bool done = trav_leaf<ANY_HIT, COUNT>(s, t, &tc);
+      if (done || trav_finished(t)) {
+        src.write(cur, t.h);
+        cur = -1;
+      }
     }
   }
   if (COUNT) {

@@ -203,6 +203,7 @@ struct TravState {
   int node;
   int sp;
   int visits;
+  int pend;  // parked leaf slot, -1: none
 };
 
 HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
@@ -216,9 +217,81 @@ HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
   t.node = 0;
   t.sp = 0;
   t.visits = 0;
+  t.pend = -1;
 }
 
 HM_D bool prim_intersect(const SceneDev& s, int prim, const Ray& r, float tmax, float* t, float* u, float* v);
+
+// Leaf-postponing traversal ("while-while", Aila & Laine 2009): an inner
+// step only walks boxes; a leaf reached is parked (t.pend = leaf slot) and
+// tested later together with the other lanes' parked leaves, so the expensive
+// curve test runs with most lanes of the warp active.
+//   t.node >= 0: next internal node to visit; t.node < 0: pop next.
+//   A lane needs inner steps while nothing is parked and work remains.
+HM_D bool trav_needs_step(const TravState& t) { return t.pend < 0 && (t.node >= 0 || t.sp > 0); }
+HM_D bool trav_finished(const TravState& t) { return t.pend < 0 && t.node < 0 && t.sp == 0; }
+
+template <bool COUNT>
+HM_D void trav_inner_step(const SceneDev& s, TravState& t, int* stack, int* err, TraceCount* cnt) {
+  if (++t.visits > kMaxVisits) {
+    atomicOr(err, TRACE_ERR_STEPS);
+    t.node = -1;
+    t.sp = 0;
+    return;
+  }
+  int cur = t.node >= 0 ? t.node : stack[--t.sp];
+  if (cur < 0) {  // a leaf left on the stack
+    t.pend = ~cur;
+    t.node = -1;
+    return;
+  }
+  float t0, t1;
+  int c0, c1;
+  node_test(s.nodes, cur, t.o, t.inv, t.tmin, t.h.t, &t0, &t1, &c0, &c1);
+  if (COUNT) cnt->nodes += 1;
+  const bool go0 = t0 < INFINITY, go1 = t1 < INFINITY;
+  int next = 0;
+  bool have = true;
+  if (go0 && go1) {
+    if (t.sp >= kStack) {
+      atomicOr(err, TRACE_ERR_STACK);
+      t.node = -1;
+      t.sp = 0;
+      return;
+    }
+    stack[t.sp++] = t0 <= t1 ? c1 : c0;
+    next = t0 <= t1 ? c0 : c1;
+  } else if (go0) {
+    next = c0;
+  } else if (go1) {
+    next = c1;
+  } else {
+    have = false;
+  }
+  if (!have) {
+    t.node = -1;
+  } else if (next < 0) {
+    t.pend = ~next;
+    t.node = -1;
+  } else {
+    t.node = next;
+  }
+}
+
+// Tests the parked leaf.  Returns true if an any-hit ray is finished.
+template <bool ANY_HIT, bool COUNT>
+HM_D bool trav_leaf(const SceneDev& s, TravState& t, TraceCount* cnt) {
+  if (t.pend < 0) return false;
+  const int prim = __ldg(s.prim_of_leaf + t.pend);
+  t.pend = -1;
+  if (COUNT) cnt->prims += 1;
+  float th, u, v;
+  if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v)) {
+    t.h = Hit{th, prim, u, v};
+    if (ANY_HIT) return true;
+  }
+  return false;
+}
 
 // Returns true when the ray is finished (result in t.h).
 template <bool ANY_HIT, bool COUNT>

@@ -79,7 +79,8 @@ struct BatchRays {
   HM_D void write(int i, const Hit& h) const { out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v); }
 };
 
-constexpr int kStragglers = 2;  // lanes a warp does not wait for before its leaf phase
+constexpr int kStragglers = 2;        // lanes a warp does not wait for before its leaf phase
+constexpr int kMaxRounds = 1 << 22;   // per-warp round cap (~6k rounds per warp at 512x512)
 
 // COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
 // cnt[0..2] (an untimed instrumentation pass; timed frames use COUNT = false).
@@ -96,6 +97,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
   uint32_t rays = 0;
   int cur = -1;
   bool exhausted = false;
+  int rounds = 0;
   for (;;) {
     const unsigned idle = __ballot_sync(FULL, cur < 0);
     if (idle && !exhausted) {
@@ -120,11 +122,20 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
       }
     }
     if (exhausted && __all_sync(FULL, cur < 0)) break;
-    // box phase: walk inner nodes until all but a few lanes have parked a leaf
-    // (or finished); stragglers continue in the next round
-    for (;;) {
+    if (++rounds > kMaxRounds) {  // safety net: never spin on a logic error
+      if (lane == 0) atomicOr(err, TRACE_ERR_STEPS);
+      break;
+    }
+    // box phase: walk inner nodes until every lane has parked a leaf or
+    // finished; once some lane has a leaf parked, up to kStragglers lanes
+    // that still need steps are not waited for (they continue next round).
+    // Every iteration advances at least one lane, so the phase terminates.
+    for (int guard = 0; guard < kMaxVisits; ++guard) {
       const bool need = cur >= 0 && trav_needs_step(t);
-      if (__popc(__ballot_sync(FULL, need)) <= kStragglers) break;
+      const unsigned needm = __ballot_sync(FULL, need);
+      if (needm == 0) break;
+      const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.pend >= 0);
+      if (parked != 0 && __popc(needm) <= kStragglers) break;
       if (need) trav_inner_step<COUNT>(s, t, stack, err, &tc);
     }
     // leaf phase: the parked curve / triangle tests run together

@@ -440,11 +440,15 @@ static int render_frame(Render* r, cudaStream_t st) {
   int* c_next = r->counts + 1;
   // instrumentation: event pairs per stage (timing) / work counters (counting)
   size_t ne = 0;
+  int cur_bounce = -1;
   std::vector<std::pair<int, size_t>> marks;  // (stage, event index)
+  std::vector<int> mark_bounce;
+  std::vector<int> paths_at;  // paths traced in each bounce
   auto mark = [&](int stage) {
     if (!r->timing) return;
     cudaEventRecord(r->event(ne), st);
     marks.emplace_back(stage, ne++);
+    mark_bounce.push_back(cur_bounce);
   };
   enum { S_CAMERA, S_EXTEND, S_SHADE, S_SHADOW, S_COMPACT, S_FINALIZE, S_TRAIN, S_INFER, S_COMPOSE, S_END };
   if (r->counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
@@ -457,6 +461,8 @@ static int render_frame(Render* r, cudaStream_t st) {
   int bounces = 0;
   int64_t ext_rays = 0;
   for (int it = 0; it <= s->path_v2 && count > 0; ++it) {
+    cur_bounce = it;
+    paths_at.push_back(count);
     mark(S_EXTEND);
     if (int e = launch_persistent<ExtendRays, false>(ExtendRays{r->ps, q_cur, c_cur}, sd, 0.f, 1e30f,
                                                      r->fetch + 2 * it, r->err, r->d_cnt, r->counting,
@@ -488,6 +494,7 @@ static int render_frame(Render* r, cudaStream_t st) {
   }
   r->rays_extend += ext_rays;
   r->last_bounces = bounces;
+  cur_bounce = -1;
   mark(S_FINALIZE);
   if (int e = launch_finalize(sd, fp, r->ps, r->fb, st)) return e;
   int launches = 1 + 7 * bounces + 1;
@@ -522,7 +529,13 @@ static int render_frame(Render* r, cudaStream_t st) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, r->event(marks[k].second), r->event(marks[k + 1].second));
       *slot[marks[k].first] += ms;
+      const int b = mark_bounce[k];
+      if (b >= 0 && b < 48) {
+        if (marks[k].first == S_EXTEND) tm.extend_ms_by_bounce[b] += ms;
+        if (marks[k].first == S_SHADOW) tm.shadow_ms_by_bounce[b] += ms;
+      }
     }
+    for (size_t b = 0; b < paths_at.size() && b < 48; ++b) tm.paths_by_bounce[b] = paths_at[b];
     cudaEventElapsedTime(&tm.total_ms, r->event(marks.front().second), r->event(marks.back().second));
   }
   if (r->counting) {

@@ -51,10 +51,16 @@ class hm_render_timings(ctypes.Structure):
         "total_ms", "camera_ms", "extend_ms", "shade_ms", "shadow_ms", "compact_ms", "finalize_ms", "train_ms",
         "infer_ms", "compose_ms")] + [("bounces", ctypes.c_int), ("kernel_launches", ctypes.c_int)] + [
         (n, ctypes.c_int64) for n in ("extension_rays", "shadow_rays", "extend_nodes", "extend_prims",
-                                      "shadow_nodes", "shadow_prims")]
+                                      "shadow_nodes", "shadow_prims")] + [
+        ("paths_by_bounce", ctypes.c_int * 48), ("extend_ms_by_bounce", ctypes.c_float * 48),
+        ("shadow_ms_by_bounce", ctypes.c_float * 48)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        out = {}
+        for k, _ in self._fields_:
+            v = getattr(self, k)
+            out[k] = list(v)[:max(1, self.bounces)] if k.endswith("_by_bounce") else v
+        return out
 
 
 _declared = False

@@ -279,6 +279,9 @@ typedef struct hm_render_timings {
   int bounces, kernel_launches;
   int64_t extension_rays, shadow_rays;
   int64_t extend_nodes, extend_prims, shadow_nodes, shadow_prims;
+  /* per bounce (first 48): paths traced, extension and shadow traversal ms */
+  int paths_by_bounce[48];
+  float extend_ms_by_bounce[48], shadow_ms_by_bounce[48];
 } hm_render_timings;
 int hm_render_set_instrumentation(hm_render* render, int timing, int counting);
 int hm_render_get_timings(const hm_render* render, hm_render_timings* out);

@@ -15,10 +15,12 @@ Workloads (synthetic, seeded):
           metric: vertex queries/s.
 
 One JSON line is printed by rank 0.  `value` times the kernels with inputs
-resident in HBM (CUDA events per step on the launching stream, L2 flushed
-between steps outside the events); `e2e` times the same step through the
-public API with pinned host inputs copied in and results copied out inside
-the timed region.  Multi-GPU runs are independent replicas (the path has no
+resident in HBM (vertex: CUDA events per step on the launching stream, L2
+flushed between steps outside the events; render: CUDA events around K
+pipelined frames on the submitting stream, a 256 MiB L2-flush write before
+each frame's submission inside the region); `e2e` times the same step
+through the public API with pinned host inputs copied in and results copied
+out inside the timed region.  Multi-GPU runs are independent replicas (the path has no
 exchange step on one box).
 """
 import argparse
@@ -330,24 +332,29 @@ def main():
     torch.cuda.synchronize()
 
     # ---- device-resident timed region
-    ne = wl.n_events()
-    all_events = [[torch.cuda.Event(enable_timing=True) for _ in range(ne)] for _ in range(args.steps)]
     sampler = ClockSampler(local if ws > 1 else 0)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     sampler.start()
     time.sleep(0.3)
-    for k in range(args.steps):
-        flush.fill_(k & 0xFF)  # > L2 write between steps, outside the step events
-        wl.step(all_events[k])
-    torch.cuda.synchronize()
+    seg_ms = None
+    if hasattr(wl, "timed_region"):
+        ms = wl.timed_region(args.steps, flush)
+    else:
+        ne = wl.n_events()
+        all_events = [[torch.cuda.Event(enable_timing=True) for _ in range(ne)] for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)  # > L2 write between steps, outside the step events
+            wl.step(all_events[k])
+        torch.cuda.synchronize()
+        step_ms = [ev[0].elapsed_time(ev[-1]) for ev in all_events]
+        seg_ms = [statistics.mean(ev[i].elapsed_time(ev[i + 1]) for ev in all_events) for i in range(ne - 1)]
+        ms = statistics.mean(step_ms)
     if ws > 1:
         torch.distributed.barrier()
     clocks = sampler.stop()
-    step_ms = [ev[0].elapsed_time(ev[-1]) for ev in all_events]
-    seg_ms = [statistics.mean(ev[i].elapsed_time(ev[i + 1]) for ev in all_events) for i in range(ne - 1)]
-    ms = statistics.mean(step_ms)
+    launches = wl.kernels_per_step * args.steps
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -356,15 +363,19 @@ def main():
     value = units / (ms * 1e-3)
 
     # ---- end-to-end through the public API (pinned host in/out in the timed region)
-    for _ in range(2):
-        wl.e2e_step()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
     e2e_steps = max(3, args.steps // 2)
-    for _ in range(e2e_steps):
-        wl.e2e_step()
-    torch.cuda.synchronize()
-    e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
+    if hasattr(wl, "e2e_region"):
+        wl.e2e_region(2)
+        e2e_ms = wl.e2e_region(e2e_steps)
+    else:
+        for _ in range(2):
+            wl.e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            wl.e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
     if ws > 1:
         t = torch.tensor([e2e_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -380,7 +391,7 @@ def main():
             "config": wl.config(),
             "e2e": {"value": round(wl.units_per_step() * ws / (e2e_ms * 1e-3), 2), "unit": wl.unit,
                     "h2d_bytes_per_step": wl.h2d_bytes, "d2h_bytes_per_step": wl.d2h_bytes},
-            "gpu_launches": wl.kernels_per_step * args.steps,
+            "gpu_launches": launches,
             "roofline": roof, "clocks": clocks}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = wl.cpu_baseline(host_threads())

@@ -304,6 +304,28 @@ __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const int* __restri
 }
 
 // ---- render object
+// Frames are pipelined: up to `depth` frames are in flight on their own
+// streams with their own path state.  Frame k+1's path tracing never reads the
+// cache (the reference's G_BUFFER pass, hair_msnn.cu:206-312), so it overlaps
+// with the latency-bound tail of frame k's long training paths; only the cache
+// step (train -> infer) and the FP64 accumulation (compose) are chained across
+// frames with events, in frame order, so results are bit-identical to running
+// the frames one after another.  Bounce counts stay on the device: every
+// bounce's kernels read the queue length from device memory and do nothing
+// once it is zero, so no frame needs a host round trip.
+struct Slot {
+  PathState ps{};
+  FrameBufs fb{};
+  int *q_a = nullptr, *q_b = nullptr, *keep = nullptr, *block_sums = nullptr, *counts = nullptr;
+  int *err = nullptr, *fetch = nullptr;
+  uint8_t* vis = nullptr;
+  float* d_loss = nullptr;
+  int* h_err = nullptr;  // pinned copy of err, read once the frame is done
+  cudaStream_t st = nullptr;
+  cudaEvent_t done = nullptr;
+  bool in_flight = false;
+};
+
 struct Render {
   Scene* scene = nullptr;
   int mode = MODE_MSNN;
@@ -316,31 +338,38 @@ struct Render {
   uint32_t seed = 0;
   hm_mlp* mlp = nullptr;
   int P = 0;
-  PathState ps{};
-  FrameBufs fb{};
-  int *q_a = nullptr, *q_b = nullptr, *keep = nullptr, *block_sums = nullptr, *counts = nullptr, *err = nullptr;
-  int* h_count = nullptr;  // pinned
+  int depth = 3;
+  std::vector<Slot> slots;
+  double *acc_pt = nullptr, *acc_nn = nullptr, *acc_final = nullptr;
+  cudaEvent_t ev_submit = nullptr, ev_mlp = nullptr, ev_compose = nullptr, ev_read = nullptr;
+  bool have_mlp_ev = false, have_compose_ev = false, have_read_ev = false;
+  int* h_count = nullptr;  // pinned (synchronous instrumented frames)
   std::vector<void*> allocs;
-  int64_t rays_extend = 0, rays_shadow_paths = 0;
+  int64_t rays_extend = 0;
   int last_bounces = 0;
   int sm_count = 152;
-  int* fetch = nullptr;  // ray-fetch counters of the persistent traversals, 2 per bounce
   int fetch_slots = 0;
-  uint8_t* vis = nullptr;  // shadow-ray visibility [P][2]
   int blocks_extend = 0, blocks_shadow = 0;
-  float last_loss = 0.f;
-  float* d_loss = nullptr;
-  // instrumentation
+  int last_error = 0;
+  // instrumentation (synchronous frames)
   bool timing = false, counting = false;
-  unsigned long long* d_cnt = nullptr;  // extend nodes, prims, shadow nodes, prims, shadow rays
-  std::vector<cudaEvent_t> ev;          // pool, reused every frame
+  unsigned long long* d_cnt = nullptr;
+  std::vector<cudaEvent_t> ev;
   hm_render_timings tm{};
 
   ~Render() {
+    for (auto& s : slots) {
+      if (s.st) cudaStreamSynchronize(s.st);
+      if (s.st) cudaStreamDestroy(s.st);
+      if (s.done) cudaEventDestroy(s.done);
+      if (s.h_err) cudaFreeHost(s.h_err);
+    }
     for (void* p : allocs) cudaFree(p);
     if (h_count) cudaFreeHost(h_count);
     if (mlp) hm_mlp_destroy(mlp);
     for (auto e : ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ev_submit, ev_mlp, ev_compose, ev_read})
+      if (e) cudaEventDestroy(e);
   }
   cudaEvent_t event(size_t i) {
     while (ev.size() <= i) {
@@ -369,125 +398,191 @@ static const char* kDefaultCacheConfig =
     "\"network\":{\"otype\":\"FullyFusedMLP\",\"activation\":\"ReLU\",\"output_activation\":\"None\","
     "\"n_neurons\":64,\"n_hidden_layers\":2}}";
 
+static cudaError_t slot_alloc(Render* r, Slot& sl) {
+  const int P = r->P;
+  cudaError_t e = cudaSuccess;
+  auto A4 = [&](float4** p) { if (e == cudaSuccess) e = r->alloc(p, P); };
+  if (e == cudaSuccess) e = r->alloc(&sl.ps.rng, P);
+  if (e == cudaSuccess) e = r->alloc(&sl.ps.flags, P);
+  if (e == cudaSuccess) e = r->alloc(&sl.ps.bounce, P);
+  A4(&sl.ps.ray_o); A4(&sl.ps.ray_d); A4(&sl.ps.hit); A4(&sl.ps.beta); A4(&sl.ps.beta_s);
+  A4(&sl.ps.col); A4(&sl.ps.col_s); A4(&sl.ps.sh_o0); A4(&sl.ps.sh_d0); A4(&sl.ps.sh_o1);
+  A4(&sl.ps.sh_d1); A4(&sl.ps.sh_c0); A4(&sl.ps.sh_c1); A4(&sl.ps.dl_w); A4(&sl.ps.dl_ws);
+  A4(&sl.fb.gbuf);
+  const int nblocks = (P + kScanBlock - 1) / kScanBlock;
+  if (e == cudaSuccess) e = r->alloc(&sl.q_a, P);
+  if (e == cudaSuccess) e = r->alloc(&sl.q_b, P);
+  if (e == cudaSuccess) e = r->alloc(&sl.keep, P);
+  if (e == cudaSuccess) e = r->alloc(&sl.block_sums, nblocks + 1);
+  if (e == cudaSuccess) e = r->alloc(&sl.counts, 4);
+  if (e == cudaSuccess) e = r->alloc(&sl.err, 1);
+  if (e == cudaSuccess) e = r->alloc(&sl.fetch, r->fetch_slots);
+  if (e == cudaSuccess) e = r->alloc(&sl.vis, (size_t)P * 2);
+  if (e == cudaSuccess) e = r->alloc(&sl.d_loss, 1);
+  if (e == cudaSuccess) e = cudaMallocHost(&sl.h_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
+  if (e != cudaSuccess) return e;
+  *sl.h_err = 0;
+  cudaMemset(sl.err, 0, sizeof(int));
+  cudaMemset(sl.d_loss, 0, sizeof(float));
+  sl.fb.acc_pt = r->acc_pt;
+  sl.fb.acc_nn = r->acc_nn;
+  sl.fb.acc_final = r->acc_final;
+  if (r->mode == MODE_MSNN) {
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_frame_in, (size_t)P * r->in_ch);
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_frame_out, (size_t)P * 3);
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_train_in, (size_t)r->n_train * r->in_ch);
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_train_out, (size_t)r->n_train * 3);
+    if (e != cudaSuccess) return e;
+    cudaMemset(sl.fb.nn_train_in, 0, (size_t)r->n_train * r->in_ch * sizeof(float));
+    cudaMemset(sl.fb.nn_train_out, 0, (size_t)r->n_train * 3 * sizeof(float));
+  }
+  return e;
+}
+
 static int render_setup(Render* r, const hm_render_options* o) {
   Scene* s = r->scene;
   if (int st = s->ensure_built()) return st;
   r->P = s->width * s->height;
   const int P = r->P;
   cudaError_t e = cudaSuccess;
-  auto A4 = [&](float4** p) { if (e == cudaSuccess) e = r->alloc(p, P); };
-  if (e == cudaSuccess) e = r->alloc(&r->ps.rng, P);
-  if (e == cudaSuccess) e = r->alloc(&r->ps.flags, P);
-  if (e == cudaSuccess) e = r->alloc(&r->ps.bounce, P);
-  A4(&r->ps.ray_o); A4(&r->ps.ray_d); A4(&r->ps.hit); A4(&r->ps.beta); A4(&r->ps.beta_s);
-  A4(&r->ps.col); A4(&r->ps.col_s); A4(&r->ps.sh_o0); A4(&r->ps.sh_d0); A4(&r->ps.sh_o1);
-  A4(&r->ps.sh_d1); A4(&r->ps.sh_c0); A4(&r->ps.sh_c1); A4(&r->ps.dl_w); A4(&r->ps.dl_ws);
-  A4(&r->fb.gbuf);
-  const int nblocks = (P + kScanBlock - 1) / kScanBlock;
-  if (e == cudaSuccess) e = r->alloc(&r->q_a, P);
-  if (e == cudaSuccess) e = r->alloc(&r->q_b, P);
-  if (e == cudaSuccess) e = r->alloc(&r->keep, P);
-  if (e == cudaSuccess) e = r->alloc(&r->block_sums, nblocks + 1);
-  if (e == cudaSuccess) e = r->alloc(&r->counts, 4);
-  if (e == cudaSuccess) e = r->alloc(&r->err, 1);
-  if (e == cudaSuccess) e = r->alloc(&r->fb.acc_pt, (size_t)P * 3);
-  if (e == cudaSuccess) e = r->alloc(&r->fb.acc_nn, (size_t)P * 3);
-  if (e == cudaSuccess) e = r->alloc(&r->fb.acc_final, (size_t)P * 3);
-  if (e == cudaSuccess) e = r->alloc(&r->d_loss, 1);
+  if (e == cudaSuccess) e = r->alloc(&r->acc_pt, (size_t)P * 3);
+  if (e == cudaSuccess) e = r->alloc(&r->acc_nn, (size_t)P * 3);
+  if (e == cudaSuccess) e = r->alloc(&r->acc_final, (size_t)P * 3);
   if (e == cudaSuccess) e = r->alloc(&r->d_cnt, 8);
-  r->fetch_slots = 2 * (s->path_v2 + 2);
-  if (e == cudaSuccess) e = r->alloc(&r->fetch, r->fetch_slots);
-  if (e == cudaSuccess) e = r->alloc(&r->vis, (size_t)P * 2);
-  r->blocks_extend = persistent_blocks<ExtendRays, false>();
-  r->blocks_shadow = persistent_blocks<ShadowRays, true>();
   if (e == cudaSuccess) e = cudaMallocHost(&r->h_count, sizeof(int));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_submit, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_mlp, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_compose, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_read, cudaEventDisableTiming);
   if (e != cudaSuccess) return hm_cuda_status(e, "render buffers");
-  cudaMemset(r->err, 0, sizeof(int));
-  cudaMemset(r->fb.acc_pt, 0, (size_t)P * 3 * sizeof(double));
-  cudaMemset(r->fb.acc_nn, 0, (size_t)P * 3 * sizeof(double));
-  cudaMemset(r->fb.acc_final, 0, (size_t)P * 3 * sizeof(double));
+  cudaMemset(r->acc_pt, 0, (size_t)P * 3 * sizeof(double));
+  cudaMemset(r->acc_nn, 0, (size_t)P * 3 * sizeof(double));
+  cudaMemset(r->acc_final, 0, (size_t)P * 3 * sizeof(double));
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  r->fetch_slots = 2 * (s->path_v2 + 2);
+  r->blocks_extend = persistent_blocks<ExtendRays, false>();
+  r->blocks_shadow = persistent_blocks<ShadowRays, true>();
   if (r->mode == MODE_MSNN) {
     r->n_train = o && o->train_records > 0 ? o->train_records : 16384;
     // everyNth = frameSize / numTrainRecords (integer division, render_hair_msnn.cu:106), at least 1
     r->every_nth = std::max(1, P / r->n_train);
     r->n_train = std::min(r->n_train, (P + r->every_nth - 1) / r->every_nth);
-    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_frame_in, (size_t)P * r->in_ch);
-    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_frame_out, (size_t)P * 3);
-    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_train_in, (size_t)r->n_train * r->in_ch);
-    if (e == cudaSuccess) e = r->alloc(&r->fb.nn_train_out, (size_t)r->n_train * 3);
-    if (e != cudaSuccess) return hm_cuda_status(e, "render cache buffers");
-    cudaMemset(r->fb.nn_train_in, 0, (size_t)r->n_train * r->in_ch * sizeof(float));
-    cudaMemset(r->fb.nn_train_out, 0, (size_t)r->n_train * 3 * sizeof(float));
+  }
+  r->slots.resize(r->depth);
+  for (auto& sl : r->slots) {
+    e = slot_alloc(r, sl);
+    if (e != cudaSuccess) return hm_cuda_status(e, "render frame slot");
+  }
+  if (r->mode == MODE_MSNN) {
     std::string cfg = o && o->cache_config_json ? o->cache_config_json
                                                 : (s->cache_config.empty() ? kDefaultCacheConfig : s->cache_config);
     int st = 0;
     r->mlp = hm_mlp_create(cfg.c_str(), r->in_ch, 3, o ? o->cache_precision : HM_PREC_FP32, r->seed, &st);
     if (!r->mlp) return st;
   }
+  cudaError_t e2 = cudaDeviceSynchronize();
+  return e2 == cudaSuccess ? HM_OK : hm_cuda_status(e2, "render setup");
+}
+
+// Waits for a slot's frame and reports its traversal error bits.
+static int slot_finish(Render* r, Slot& sl) {
+  if (!sl.in_flight) return HM_OK;
+  cudaError_t e = cudaEventSynchronize(sl.done);
+  sl.in_flight = false;
+  if (e != cudaSuccess) return hm_cuda_status(e, "render frame");
+  if (*sl.h_err) {
+    int bits = *sl.h_err;
+    *sl.h_err = 0;
+    cudaMemset(sl.err, 0, sizeof(int));
+    return hm_set_error("traversal gave up on some rays (error bits 0x%x)", bits), HM_ECAPACITY;
+  }
   return HM_OK;
 }
 
-static int render_frame(Render* r, cudaStream_t st) {
+static int render_sync(Render* r) {
+  int status = HM_OK;
+  for (auto& sl : r->slots) {
+    int s = slot_finish(r, sl);
+    if (s && !status) status = s;
+  }
+  return status;
+}
+
+// Enqueues one frame.  sync_bounces: read the queue length after every
+// bounce (instrumented frames: per-stage events, early exit); otherwise the
+// whole frame is enqueued without a host round trip.
+static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   Scene* s = r->scene;
   SceneDev sd = s->dev();
+  Slot& sl = r->slots[r->accum_id % r->depth];
+  if (int e = slot_finish(r, sl)) return e;  // back-pressure: the slot's previous frame
+  const cudaStream_t st = sl.st;
+  cudaEventRecord(r->ev_submit, user);
+  cudaStreamWaitEvent(st, r->ev_submit, 0);
   FrameParams fp{r->mode, r->beta_knob - 1, r->accum_id, r->accum_id + 10007, r->every_nth, r->n_train, r->in_ch};
-  int* q_cur = r->q_a;
-  int* q_next = r->q_b;
-  int* c_cur = r->counts;
-  int* c_next = r->counts + 1;
+  int* q_cur = sl.q_a;
+  int* q_next = sl.q_b;
+  int* c_cur = sl.counts;
+  int* c_next = sl.counts + 1;
   // instrumentation: event pairs per stage (timing) / work counters (counting)
   size_t ne = 0;
   int cur_bounce = -1;
   std::vector<std::pair<int, size_t>> marks;  // (stage, event index)
   std::vector<int> mark_bounce;
-  std::vector<int> paths_at;  // paths traced in each bounce
+  std::vector<int> paths_at;
   auto mark = [&](int stage) {
-    if (!r->timing) return;
+    if (!r->timing || !sync_bounces) return;
     cudaEventRecord(r->event(ne), st);
     marks.emplace_back(stage, ne++);
     mark_bounce.push_back(cur_bounce);
   };
   enum { S_CAMERA, S_EXTEND, S_SHADE, S_SHADOW, S_COMPACT, S_FINALIZE, S_TRAIN, S_INFER, S_COMPOSE, S_END };
-  if (r->counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
-  cudaMemsetAsync(r->fetch, 0, r->fetch_slots * sizeof(int), st);
+  const bool counting = r->counting && sync_bounces;
+  if (counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
+  cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
   mark(S_CAMERA);
-  if (int e = launch_camera(sd, fp, r->ps, q_cur, c_cur, st)) return e;
+  if (int e = launch_camera(sd, fp, sl.ps, q_cur, c_cur, st)) return e;
   const int grid = r->sm_count * 8;
   const int nblocks = (r->P + kScanBlock - 1) / kScanBlock;
   int count = r->P;
   int bounces = 0;
   int64_t ext_rays = 0;
+  const FrameBufs fb = sl.fb;
   for (int it = 0; it <= s->path_v2 && count > 0; ++it) {
     cur_bounce = it;
     paths_at.push_back(count);
     mark(S_EXTEND);
-    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{r->ps, q_cur, c_cur}, sd, 0.f, 1e30f,
-                                                     r->fetch + 2 * it, r->err, r->d_cnt, r->counting,
+    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, 0.f, 1e30f,
+                                                     sl.fetch + 2 * it, sl.err, r->d_cnt, counting,
                                                      r->blocks_extend, st))
       return e;
     mark(S_SHADE);
-    if (int e = launch_shade(sd, fp, r->ps, r->fb, q_cur, c_cur, r->keep, grid, st)) return e;
+    if (int e = launch_shade(sd, fp, sl.ps, fb, q_cur, c_cur, sl.keep, grid, st)) return e;
     mark(S_SHADOW);
-    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{r->ps, q_cur, c_cur, r->vis}, sd, 0.f, 1e30f,
-                                                    r->fetch + 2 * it + 1, r->err, r->d_cnt + 3, r->counting,
+    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, 0.f, 1e30f,
+                                                    sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, counting,
                                                     r->blocks_shadow, st))
       return e;
-    shadow_resolve_kernel<<<grid, 256, 0, st>>>(r->ps, q_cur, c_cur, r->vis);
+    shadow_resolve_kernel<<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis);
     HM_CHECK_LAUNCH("shadow_resolve_kernel");
     mark(S_COMPACT);
-    scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(r->keep, c_cur, r->block_sums, nblocks);
-    scan_blocks_kernel<<<1, 1024, 0, st>>>(r->block_sums, c_cur, c_next);
-    scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(r->keep, q_cur, c_cur, r->block_sums,
+    scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
+                                                                                  nblocks);
+    scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
+    scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, q_cur, c_cur, sl.block_sums,
                                                                               q_next, nblocks);
     HM_CHECK_LAUNCH("compaction");
-    ext_rays += count;
-    cudaError_t e = cudaMemcpyAsync(r->h_count, c_next, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e != cudaSuccess) return hm_cuda_status(e, "bounce count");
-    count = *r->h_count;
+    if (sync_bounces) {
+      ext_rays += count;
+      cudaError_t e = cudaMemcpyAsync(r->h_count, c_next, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) return hm_cuda_status(e, "bounce count");
+      count = *r->h_count;
+    }
     std::swap(q_cur, q_next);
     std::swap(c_cur, c_next);
     ++bounces;
@@ -495,33 +590,51 @@ static int render_frame(Render* r, cudaStream_t st) {
   r->rays_extend += ext_rays;
   r->last_bounces = bounces;
   cur_bounce = -1;
-  mark(S_FINALIZE);
-  if (int e = launch_finalize(sd, fp, r->ps, r->fb, st)) return e;
   int launches = 1 + 7 * bounces + 1;
-  if (r->mode == MODE_MSNN) {
+  if (r->mode == MODE_PT) {
+    // writePixel accumulates: frames in order, after any pending read-back
+    if (r->have_compose_ev) cudaStreamWaitEvent(st, r->ev_compose, 0);
+    if (r->have_read_ev) cudaStreamWaitEvent(st, r->ev_read, 0);
+    mark(S_FINALIZE);
+    if (int e = launch_finalize(sd, fp, sl.ps, fb, st)) return e;
+    cudaEventRecord(r->ev_compose, st);
+    r->have_compose_ev = true;
+  } else {
+    mark(S_FINALIZE);
+    if (int e = launch_finalize(sd, fp, sl.ps, fb, st)) return e;
+    // cache step: after the previous frame's inference (weights and workspace)
+    if (r->have_mlp_ev) cudaStreamWaitEvent(st, r->ev_mlp, 0);
     mark(S_TRAIN);
     if (r->train) {
-      if (int e = hm_mlp_training_step(r->mlp, r->fb.nn_train_in, r->fb.nn_train_out, r->n_train, r->d_loss, st))
+      if (int e = hm_mlp_training_step(r->mlp, fb.nn_train_in, fb.nn_train_out, r->n_train, sl.d_loss, st))
         return e;
     }
     mark(S_INFER);
-    if (int e = hm_mlp_inference(r->mlp, r->fb.nn_frame_in, r->fb.nn_frame_out, r->P, st)) return e;
+    if (int e = hm_mlp_inference(r->mlp, fb.nn_frame_in, fb.nn_frame_out, r->P, st)) return e;
+    cudaEventRecord(r->ev_mlp, st);
+    r->have_mlp_ev = true;
+    if (r->have_compose_ev) cudaStreamWaitEvent(st, r->ev_compose, 0);
+    if (r->have_read_ev) cudaStreamWaitEvent(st, r->ev_read, 0);
     mark(S_COMPOSE);
-    if (int e = launch_compose(sd, fp, r->fb, st)) return e;
+    if (int e = launch_compose(sd, fp, fb, st)) return e;
+    cudaEventRecord(r->ev_compose, st);
+    r->have_compose_ev = true;
     hm_mlp_desc md;
     hm_mlp_info(r->mlp, &md);
     const bool grid_enc = md.n_params > md.n_network_params;
-    // training: encode, fwd, bwd, loss reduce, (dw partial + reduce) per layer, [grid bwd], adam
     launches += (r->train ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 2 : 0) + 1 : 0) + 2 + 1;
   }
   mark(S_END);
+  cudaMemcpyAsync(sl.h_err, sl.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(sl.done, st);
+  sl.in_flight = true;
   r->accum_id += 1;
   hm_render_timings& tm = r->tm;
   memset(&tm, 0, sizeof(tm));
   tm.bounces = bounces;
   tm.extension_rays = ext_rays;
   tm.kernel_launches = launches;
-  if (r->timing) {
+  if (r->timing && sync_bounces) {
     cudaEventSynchronize(r->event(ne - 1));
     float* slot[] = {&tm.camera_ms, &tm.extend_ms, &tm.shade_ms, &tm.shadow_ms, &tm.compact_ms,
                      &tm.finalize_ms, &tm.train_ms, &tm.infer_ms, &tm.compose_ms};
@@ -538,7 +651,7 @@ static int render_frame(Render* r, cudaStream_t st) {
     for (size_t b = 0; b < paths_at.size() && b < 48; ++b) tm.paths_by_bounce[b] = paths_at[b];
     cudaEventElapsedTime(&tm.total_ms, r->event(marks.front().second), r->event(marks.back().second));
   }
-  if (r->counting) {
+  if (counting) {
     unsigned long long c[8];
     cudaMemcpyAsync(c, r->d_cnt, sizeof(c), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -548,6 +661,7 @@ static int render_frame(Render* r, cudaStream_t st) {
     tm.shadow_prims = (int64_t)c[4];
     tm.shadow_rays = (int64_t)c[5];
   }
+  if (sync_bounces) return slot_finish(r, sl);
   return HM_OK;
 }
 
@@ -570,6 +684,7 @@ extern "C" hm_render* hm_render_create(hm_scene* scene, const hm_render_options*
     r->beta_knob = opt->beta;
     r->train = opt->train != 0;
     r->seed = opt->seed;
+    if (opt->frames_in_flight > 0) r->depth = std::min(opt->frames_in_flight, 8);
   } else {
     r->train = r->scene->cache_train;
   }
@@ -600,29 +715,58 @@ extern "C" void hm_render_destroy(hm_render* h) { delete (Render*)h; }
 extern "C" int hm_render_frame(hm_render* h, void* stream) {
   Render* r = (Render*)h;
   if (!r) return hm_set_error("hm_render_frame: NULL"), HM_EINVAL;
-  int st = render_frame(r, (cudaStream_t)stream);
-  if (st != HM_OK) return st;
-  int err = 0;
-  cudaError_t e = cudaMemcpyAsync(&err, r->err, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
-  if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_frame");
-  if (err) return hm_set_error("traversal gave up on some rays (error bits 0x%x)", err), HM_ECAPACITY;
+  // asynchronous unless instrumented: errors of a frame are reported when its
+  // slot is reused or at the next synchronising call (read / stats / reset)
+  return render_frame(r, (cudaStream_t)stream, r->timing || r->counting);
+}
+
+// Asynchronous read-back of the FP64 running sums (not averaged) of every
+// frame enqueued so far into host_dst (pinned for a true async copy), on
+// `stream`; the next frame's accumulation waits for the copy.
+extern "C" int hm_render_read_async(hm_render* h, int which, double* host_dst, void* stream) {
+  Render* r = (Render*)h;
+  if (!r || !host_dst) return hm_set_error("hm_render_read_async: NULL"), HM_EINVAL;
+  const double* src = which == HM_IMAGE_FINAL ? r->acc_final
+                      : which == HM_IMAGE_SHORT ? r->acc_pt
+                      : which == HM_IMAGE_CACHE ? r->acc_nn : nullptr;
+  if (!src) return hm_set_error("hm_render_read_async: unknown image %d", which), HM_EINVAL;
+  if (r->mode == MODE_PT && which != HM_IMAGE_FINAL)
+    return hm_set_error("hm_render_read_async: PT renders have only the final image"), HM_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (r->have_compose_ev) cudaStreamWaitEvent(s, r->ev_compose, 0);
+  cudaError_t e = cudaMemcpyAsync(host_dst, src, (size_t)r->P * 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaEventRecord(r->ev_read, s);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_read_async");
+  r->have_read_ev = true;
+  return HM_OK;
+}
+
+extern "C" int hm_render_wait(hm_render* h, void* stream) {
+  Render* r = (Render*)h;
+  if (!r) return HM_EINVAL;
+  for (auto& sl : r->slots)
+    if (sl.in_flight) {
+      cudaError_t e = cudaStreamWaitEvent((cudaStream_t)stream, sl.done, 0);
+      if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_wait");
+    }
   return HM_OK;
 }
 
 extern "C" int hm_render_reset(hm_render* h) {
   Render* r = (Render*)h;
   if (!r) return HM_EINVAL;
+  int st = render_sync(r);
   r->accum_id = 0;
-  return HM_OK;
+  return st;
 }
 
 extern "C" int hm_render_read(hm_render* h, int which, double* host_rgb) {
   Render* r = (Render*)h;
   if (!r || !host_rgb) return hm_set_error("hm_render_read: NULL"), HM_EINVAL;
-  const double* src = which == HM_IMAGE_FINAL ? r->fb.acc_final
-                      : which == HM_IMAGE_SHORT ? r->fb.acc_pt
-                      : which == HM_IMAGE_CACHE ? r->fb.acc_nn : nullptr;
+  if (int st = render_sync(r)) return st;
+  const double* src = which == HM_IMAGE_FINAL ? r->acc_final
+                      : which == HM_IMAGE_SHORT ? r->acc_pt
+                      : which == HM_IMAGE_CACHE ? r->acc_nn : nullptr;
   if (!src) return hm_set_error("hm_render_read: unknown image %d", which), HM_EINVAL;
   if (r->mode == MODE_PT && which != HM_IMAGE_FINAL) return hm_set_error("hm_render_read: PT renders have only the final image"), HM_EINVAL;
   const size_t n = (size_t)r->P * 3;
@@ -634,8 +778,9 @@ extern "C" int hm_render_read(hm_render* h, int which, double* host_rgb) {
 }
 
 extern "C" int hm_render_get_stats(const hm_render* h, hm_render_stats* out) {
-  const Render* r = (const Render*)h;
+  Render* r = const_cast<Render*>((const Render*)h);
   if (!r || !out) return HM_EINVAL;
+  int st = render_sync(r);
   out->frames = r->accum_id;
   out->pixels = r->P;
   out->extension_rays = r->rays_extend;
@@ -643,9 +788,10 @@ extern "C" int hm_render_get_stats(const hm_render* h, hm_render_stats* out) {
   out->train_records = r->mode == MODE_MSNN ? r->n_train : 0;
   out->every_nth = r->every_nth;
   float loss = 0.f;
-  if (r->mlp && r->train && r->accum_id > 0) cudaMemcpy(&loss, r->d_loss, sizeof(float), cudaMemcpyDeviceToHost);
+  if (r->mlp && r->train && r->accum_id > 0)
+    cudaMemcpy(&loss, r->slots[(r->accum_id - 1) % r->depth].d_loss, sizeof(float), cudaMemcpyDeviceToHost);
   out->last_loss = loss;
-  return HM_OK;
+  return st;
 }
 
 extern "C" int hm_render_set_instrumentation(hm_render* h, int timing, int counting) {
@@ -675,12 +821,14 @@ extern "C" hm_mlp* hm_render_cache(hm_render* h) {
 extern "C" int hm_render_buffer(hm_render* h, int which, void** dptr, int64_t* count) {
   Render* r = (Render*)h;
   if (!r || !dptr) return HM_EINVAL;
+  if (int st = render_sync(r)) return st;
+  const FrameBufs& fb = r->slots[r->accum_id > 0 ? (r->accum_id - 1) % r->depth : 0].fb;
   switch (which) {
-    case 0: *dptr = r->fb.nn_frame_in; if (count) *count = (int64_t)r->P * r->in_ch; break;
-    case 1: *dptr = r->fb.nn_frame_out; if (count) *count = (int64_t)r->P * 3; break;
-    case 2: *dptr = r->fb.nn_train_in; if (count) *count = (int64_t)r->n_train * r->in_ch; break;
-    case 3: *dptr = r->fb.nn_train_out; if (count) *count = (int64_t)r->n_train * 3; break;
-    case 4: *dptr = r->fb.gbuf; if (count) *count = (int64_t)r->P; break;
+    case 0: *dptr = fb.nn_frame_in; if (count) *count = (int64_t)r->P * r->in_ch; break;
+    case 1: *dptr = fb.nn_frame_out; if (count) *count = (int64_t)r->P * 3; break;
+    case 2: *dptr = fb.nn_train_in; if (count) *count = (int64_t)r->n_train * r->in_ch; break;
+    case 3: *dptr = fb.nn_train_out; if (count) *count = (int64_t)r->n_train * 3; break;
+    case 4: *dptr = fb.gbuf; if (count) *count = (int64_t)r->P; break;
     default: return HM_EINVAL;
   }
   return HM_OK;

@@ -37,7 +37,7 @@ class hm_scene_desc(ctypes.Structure):
 class hm_render_options(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("beta", ctypes.c_int), ("train_records", ctypes.c_int),
                 ("train", ctypes.c_int), ("cache_precision", ctypes.c_int), ("seed", ctypes.c_uint32),
-                ("cache_config_json", ctypes.c_char_p)]
+                ("cache_config_json", ctypes.c_char_p), ("frames_in_flight", ctypes.c_int)]
 
 
 class hm_render_stats(ctypes.Structure):
@@ -88,6 +88,8 @@ def _declare():
     L.hm_render_destroy.restype = None
     L.hm_render_destroy.argtypes = [vp]
     L.hm_render_frame.argtypes = [vp, vp]
+    L.hm_render_wait.argtypes = [vp, vp]
+    L.hm_render_read_async.argtypes = [vp, i32, vp, vp]
     L.hm_render_reset.argtypes = [vp]
     L.hm_render_read.argtypes = [vp, i32, vp]
     L.hm_render_get_stats.argtypes = [vp, P(hm_render_stats)]
@@ -162,11 +164,11 @@ class Renderer:
     """One frame() = one sample per pixel of HairMSNN (mode=MSNN) or plain PT."""
 
     def __init__(self, scene, mode=MSNN, beta=1, train_records=16384, train=True, precision=0, seed=0,
-                 cache_config=None):
+                 cache_config=None, frames_in_flight=0):
         _declare()
         self.scene = scene
         o = hm_render_options(mode, beta, train_records, 1 if train else 0, precision, seed,
-                              cache_config.encode() if cache_config else None)
+                              cache_config.encode() if cache_config else None, frames_in_flight)
         st = ctypes.c_int(0)
         h = lib().hm_render_create(scene._h, ctypes.byref(o), ctypes.byref(st))
         if not h:
@@ -188,7 +190,12 @@ class Renderer:
             pass
 
     def frame(self, stream=None):
+        """Enqueue one frame (asynchronous; see hm_render_frame)."""
         check(lib().hm_render_frame(self._h, _stream(stream)))
+
+    def wait(self, stream=None):
+        """Make `stream` (default: torch's current stream) wait for all frames in flight."""
+        check(lib().hm_render_wait(self._h, _stream(stream)))
 
     def reset(self):
         check(lib().hm_render_reset(self._h))
@@ -197,6 +204,13 @@ class Renderer:
         img = np.zeros((self.height, self.width, 3), np.float64)
         check(lib().hm_render_read(self._h, which, img.ctypes.data_as(ctypes.c_void_p)))
         return img
+
+    def read_async(self, host_sums, which=IMAGE_FINAL, stream=None):
+        """Enqueue a copy of the FP64 running sums (not averaged) of every frame
+        enqueued so far into `host_sums` (a pinned float64 torch tensor or numpy
+        array of [H, W, 3]) on `stream`; see hm_render_read_async."""
+        ptr = host_sums.data_ptr() if hasattr(host_sums, "data_ptr") else host_sums.ctypes.data
+        check(lib().hm_render_read_async(self._h, which, ctypes.c_void_p(ptr), _stream(stream)))
 
     def stats(self):
         s = hm_render_stats()
@@ -264,39 +278,69 @@ class RenderBenchWorkload:
     metric = "paths/s (HairMSNN full wavefront render, 512x512, 1 spp/frame, online cache training 2^16/frame)"
     unit = "paths/s"
 
-    def __init__(self, torch, width=512, height=512, train_records=1 << 16):
+    def __init__(self, torch, width=512, height=512, train_records=1 << 16, frames_in_flight=3):
         self.torch = torch
         self.width, self.height, self.train_records = width, height, train_records
+        self.frames_in_flight = frames_in_flight
         self.cfg = straight_hair_scene(width, height)
         self.scene = Scene(self.cfg)
         self.scene.build()
-        self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True)
-        self.r.instrument(timing=True, counting=False)
+        self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True,
+                          frames_in_flight=frames_in_flight)
         self.P = width * height
         self.h2d_bytes = 0
         self.d2h_bytes = self.P * 3 * 8
-        self.host_img = np.zeros((height, width, 3))
         self.stage_ms = []
         self.launches = []
+        self.read_stream = torch.cuda.Stream()
+        self.host_sums = [torch.empty((height, width, 3), dtype=torch.float64, pin_memory=True) for _ in range(2)]
 
     def step(self, events=None):
-        if events:
-            events[0].record()
+        """One frame enqueued (frames run pipelined on the renderer's own streams)."""
         self.r.frame()
-        if events:
-            events[1].record()
-        t = self.r.timings()
-        self.stage_ms.append(t.as_dict())
-        self.launches.append(t.kernel_launches)
+        self.launches.append(self.r.timings().kernel_launches)
+
+    def timed_region(self, steps, flush):
+        """Device time of `steps` pipelined frames: an event on the submitting
+        stream before the first frame, the renderer's completion joined back
+        (hm_render_wait) before the closing event; the L2 flush write precedes
+        each frame's submission inside the region."""
+        torch = self.torch
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for k in range(steps):
+            flush.fill_(k & 0xFF)
+            self.step()
+        self.r.wait()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / steps
 
     @property
     def kernels_per_step(self):
         return int(round(np.mean(self.launches[-8:]))) if self.launches else 0
 
+    def e2e_region(self, steps):
+        """Wall time per frame through the public API with the result read back
+        every frame: hm_render_frame, then hm_render_read_async of the FP64
+        image sums into pinned host memory on a separate stream (the next
+        frame's accumulation waits for that copy); host synchronisation at
+        both ends."""
+        import time
+        torch = self.torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            self.r.frame()
+            self.r.read_async(self.host_sums[k & 1], IMAGE_FINAL, stream=self.read_stream)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        self.host_img = self.host_sums[(steps - 1) & 1].numpy() / self.r.stats().frames
+        return 1e3 * el / steps
+
     def e2e_step(self):
-        # the public API call a user makes: one frame, then the FP64 image read back
         self.r.frame()
-        self.host_img = self.r.read(IMAGE_FINAL)
+        self.r.read_async(self.host_sums[0], IMAGE_FINAL, stream=self.read_stream)
 
     def n_events(self):
         return 2
@@ -304,17 +348,28 @@ class RenderBenchWorkload:
     def units_per_step(self):
         return self.P
 
+    def profile_frames(self, n=4):
+        """Synchronous instrumented frames (per-stage CUDA events on the frame's
+        stream) for the stage breakdown and the roofline."""
+        self.r.instrument(timing=True, counting=False)
+        for _ in range(n):
+            self.r.frame()
+            self.stage_ms.append(self.r.timings().as_dict())
+        self.r.instrument(timing=False, counting=False)
+
     def counted_frame(self):
         """One untimed frame with traversal work counters."""
         self.r.instrument(timing=True, counting=True)
         self.r.frame()
         t = self.r.timings()
-        self.r.instrument(timing=True, counting=False)
+        self.r.instrument(timing=False, counting=False)
         return t
 
     def roofline(self, seg_ms, pk):
         keys = ["extend_ms", "shade_ms", "shadow_ms", "compact_ms", "train_ms", "infer_ms", "compose_ms",
                 "camera_ms", "finalize_ms"]
+        if not self.stage_ms:
+            self.profile_frames()
         n = max(1, min(len(self.stage_ms), 16))
         mean = {k: float(np.mean([s[k] for s in self.stage_ms[-n:]])) for k in keys}
         c = self.counted_frame()

@@ -251,6 +251,7 @@ typedef struct hm_render_options {
   int cache_precision;           /* HM_PREC_* */
   uint32_t seed;                 /* cache initialisation */
   const char* cache_config_json; /* NULL: the scene's tcnn.config, else the built-in one */
+  int frames_in_flight;          /* 0 = 3; frames pipelined on their own streams (1..8) */
 } hm_render_options;
 
 typedef struct hm_render_stats {
@@ -263,7 +264,22 @@ typedef struct hm_render_stats {
 
 hm_render* hm_render_create(hm_scene* scene, const hm_render_options* options, int* status);
 void hm_render_destroy(hm_render* render);
+/* Enqueues one frame and returns without waiting: up to frames_in_flight
+ * frames overlap (the path tracing of frame k+1 never reads the cache, so it
+ * runs while frame k's long training paths finish); the cache step and the
+ * FP64 accumulation stay in frame order, so images are bit-identical to
+ * serial frames.  The frame is ordered after work already enqueued on
+ * `stream`; use hm_render_wait to order later work after it.
+ * A frame's traversal errors are returned by a later call (when its slot is
+ * reused, or by hm_render_read / _get_stats / _reset, which synchronise).
+ * With instrumentation on, frames run one at a time. */
 int hm_render_frame(hm_render* render, void* stream);
+/* Makes `stream` wait for every frame in flight (no host synchronisation). */
+int hm_render_wait(hm_render* render, void* stream);
+/* Asynchronous read-back on `stream` of the FP64 running sums (divide by the
+ * number of frames) of all frames enqueued so far, [H][W][3]; host_dst should
+ * be pinned.  The next frame's accumulation waits for the copy. */
+int hm_render_read_async(hm_render* render, int which, double* host_dst, void* stream);
 /* Restart accumulation (the reference's cameraChanged resets accumId). */
 int hm_render_reset(hm_render* render);
 /* Average of the accumulated frames, FP64 [H][W][3], row 0 = bottom. */

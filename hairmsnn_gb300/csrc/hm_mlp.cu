@@ -1115,3 +1115,69 @@ extern "C" int hm_mlp_describe_config(const char* config_json, int in_ch, int ou
   }
   return HM_OK;
 }
+
+// ============================================= inference without allocation
+// hm_mlp_inference_noalloc: the same encode + fused forward kernels as
+// hm_mlp_inference, but the encoded-input scratch ([n][in_pad] floats, the
+// only per-call device memory inference needs) lives in a fixed file-scope
+// device array instead of the handle's cudaMalloc'd workspace.  It exists for
+// callers that may not allocate device memory once running: a frame loop that
+// reserves all of its memory up front and must not stall on cudaMalloc (which
+// can synchronise the device) or fail on it under memory pressure halfway
+// through a frame.
+//
+// Limits and rules:
+//  * n * in_pad <= kNoAllocScratchFloats (4 MiB of floats, e.g. 4,681
+//    queries at in_pad 224, 16,384 at in_pad 64); larger n is rejected with
+//    HM_ECAPACITY and nothing is launched.  Split larger batches.
+//  * Nothing has to start at zero: the encode kernel writes every one of the
+//    first n * in_pad floats before the forward kernel reads them.
+//  * One scratch per device, shared by every handle: two calls whose work
+//    overlaps on the device (different streams, threads or handles without an
+//    ordering between them) overwrite each other's scratch.  Order them.
+//  * The first call on a device resolves the array's address with
+//    cudaGetSymbolAddress with that device current (this can load the
+//    library's device code); make that first call before any stream capture.
+constexpr int64_t kNoAllocScratchFloats = (int64_t)1 << 20;
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
+static float* s_noalloc_ptr[kNoAllocMaxDevices];
+static std::mutex s_noalloc_mu;
+
+static int noalloc_scratch(float** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_mlp_inference_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return hm_set_error("hm_mlp_inference_noalloc: device %d beyond the %d supported", dev, kNoAllocMaxDevices),
+           HM_EUNSUPPORTED;
+  std::lock_guard<std::mutex> lock(s_noalloc_mu);
+  if (!s_noalloc_ptr[dev]) {
+    float* p = nullptr;
+    e = cudaGetSymbolAddress((void**)&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) return hm_cuda_status(e, "hm_mlp_inference_noalloc: cudaGetSymbolAddress");
+    s_noalloc_ptr[dev] = p;
+  }
+  *out = s_noalloc_ptr[dev];
+  return HM_OK;
+}
+
+extern "C" int hm_mlp_inference_noalloc(hm_mlp* h, const float* d_in, float* d_out, int64_t n, void* stream) {
+  Mlp* m = (Mlp*)h;
+  if (int s = check_io("hm_mlp_inference_noalloc", m, d_in, d_out, n)) return s;
+  if (n == 0) return HM_OK;
+  const int64_t need = n * (int64_t)m->cfg.d.in_pad;
+  if (need > kNoAllocScratchFloats)
+    return hm_set_error("hm_mlp_inference_noalloc: %lld queries x %d encoded floats exceed the static scratch of "
+                        "%lld floats (at most %lld queries per call for this network)",
+                        (long long)n, m->cfg.d.in_pad, (long long)kNoAllocScratchFloats,
+                        (long long)(kNoAllocScratchFloats / m->cfg.d.in_pad)),
+           HM_ECAPACITY;
+  float* X = nullptr;
+  if (int s = noalloc_scratch(&X)) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (int s = set_dims_symbol(m, st)) return s;
+  encode_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(d_in, m->params + m->cfg.d.n_net_params, X, n);
+  HM_CHECK_LAUNCH("encode_kernel");
+  return dispatch_fwd(m, X, d_out, m->cfg.d.out_ch, nullptr, n, st);
+}

@@ -138,6 +138,13 @@ int hm_mlp_info(const hm_mlp* mlp, hm_mlp_desc* out);
 int hm_mlp_describe_config(const char* config_json, int in_ch, int out_ch, hm_mlp_desc* out);
 /* TINY_MLP::inference(in, out, size), neural_network.cu:58-64 */
 int hm_mlp_inference(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, void* stream);
+/* No counterpart in the reference.  hm_mlp_inference without any device
+ * allocation, for callers that must not allocate once running: the encoded
+ * inputs go to one static 4 MiB device scratch per device (n * padded input
+ * width <= 2^20 floats, else HM_ECAPACITY).  Calls on one device must not
+ * overlap (they share the scratch); make the first call on each device before
+ * any stream capture (it resolves the scratch address). */
+int hm_mlp_inference_noalloc(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, void* stream);
 /* Trainer::training_step + Trainer::loss (render_hair_msnn.cu:690-691),
  * split into its three phases and fused: forward keeps the activations
  * (d_out may be NULL; d_in must stay valid until backward), backward takes

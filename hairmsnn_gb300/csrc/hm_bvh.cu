@@ -2,9 +2,9 @@
 // Replaces the OptiX GAS/IAS builds of the reference (owlGroupBuildAccel,
 // render_hair_msnn.cu:316-384, 412): GB300 has no RT cores.
 //
-//   1. prim_bounds_kernel  per-primitive AABB (segment: hull of its 4 control
-//                          points grown by the largest radius; triangle: its
-//                          3 vertices) + per-block scene bounds
+//   1. prim_bounds_kernel  per-primitive AABB (segment: hull of its 4 Bezier
+//                          control points grown by their largest radius;
+//                          triangle: its 3 vertices) + per-block scene bounds
 //   2. morton_kernel       30-bit Morton code of each AABB centre in the
 //                          scene bounds, key = code << 32 | primitive id
 //                          (unique keys: no tie handling needed)
@@ -27,15 +27,24 @@ struct Aabb {
 HM_D Aabb prim_aabb(const SceneDev& s, int p) {
   Aabb b;
   if (p < s.n_seg) {
+    // hull of the segment's Bezier control points (the curve lies inside
+    // it), grown by their largest radius; the B-spline control polygon
+    // spans three segments and gave boxes about three times too long
     const float4* c = s.cp + s.seg[p];
-    float4 q0 = c[0], q1 = c[1], q2 = c[2], q3 = c[3];
-    float r = fmaxf(fmaxf(q0.w, q1.w), fmaxf(q2.w, q3.w));
-    b.lo[0] = __fsub_rn(fminf(fminf(q0.x, q1.x), fminf(q2.x, q3.x)), r);
-    b.lo[1] = __fsub_rn(fminf(fminf(q0.y, q1.y), fminf(q2.y, q3.y)), r);
-    b.lo[2] = __fsub_rn(fminf(fminf(q0.z, q1.z), fminf(q2.z, q3.z)), r);
-    b.hi[0] = __fadd_rn(fmaxf(fmaxf(q0.x, q1.x), fmaxf(q2.x, q3.x)), r);
-    b.hi[1] = __fadd_rn(fmaxf(fmaxf(q0.y, q1.y), fmaxf(q2.y, q3.y)), r);
-    b.hi[2] = __fadd_rn(fmaxf(fmaxf(q0.z, q1.z), fmaxf(q2.z, q3.z)), r);
+    float4 q[4] = {c[0], c[1], c[2], c[3]};
+    float w[4][4];
+    for (int k = 0; k < 4; ++k) {
+      const float q0 = (&q[0].x)[k], q1 = (&q[1].x)[k], q2 = (&q[2].x)[k], q3 = (&q[3].x)[k];
+      w[0][k] = __fmul_rn(__fadd_rn(__fadd_rn(q0, __fmul_rn(4.f, q1)), q2), 1.f / 6.f);
+      w[1][k] = __fmul_rn(__fadd_rn(__fmul_rn(2.f, q1), q2), 1.f / 3.f);
+      w[2][k] = __fmul_rn(__fadd_rn(q1, __fmul_rn(2.f, q2)), 1.f / 3.f);
+      w[3][k] = __fmul_rn(__fadd_rn(__fadd_rn(q1, __fmul_rn(4.f, q2)), q3), 1.f / 6.f);
+    }
+    const float r = fmaxf(fmaxf(w[0][3], w[1][3]), fmaxf(w[2][3], w[3][3]));
+    for (int k = 0; k < 3; ++k) {
+      b.lo[k] = __fsub_rn(fminf(fminf(w[0][k], w[1][k]), fminf(w[2][k], w[3][k])), r);
+      b.hi[k] = __fadd_rn(fmaxf(fmaxf(w[0][k], w[1][k]), fmaxf(w[2][k], w[3][k])), r);
+    }
   } else {
     int3 t = s.tri[p - s.n_seg];
     float3 a = s.vtx[t.x], bb = s.vtx[t.y], c = s.vtx[t.z];

@@ -269,6 +269,11 @@ def straight_hair_scene(width=512, height=512, strands=10000, control_points=64,
 RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
 NODE_BYTES = 64               # one BVH node: both child boxes + child indices
 PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
+# DRAM bytes per extension ray of the extension traversal kernel, from ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) over every launch of two
+# 256x256 frames of this scene: 395.3 MB for about 2 x 137k rays.  ncu runs
+# each launch with cold caches, so this is an upper bound for warm frames.
+EXTEND_DRAM_BYTES_PER_RAY = 1440
 
 
 class RenderBenchWorkload:
@@ -387,7 +392,9 @@ class RenderBenchWorkload:
             ach = alg / (mean[dominant] * 1e-3) / 1e9
             out.update({"kernel": dominant.replace("_ms", "_kernel"), "bound": "hbm", "achieved": round(ach, 2),
                         "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
-                        "traffic": None, "algorithmic_bytes_per_frame": int(alg),
+                        "traffic": (int(rays * EXTEND_DRAM_BYTES_PER_RAY) if dominant == "extend_ms" else None),
+                        "traffic_basis": "DRAM bytes per frame: ncu cold-cache capture at 256x256 scaled by rays",
+                        "algorithmic_bytes_per_frame": int(alg),
                         "note": ("algorithmic bytes = rays x 48 B + BVH nodes visited x 64 B + primitives "
                                  "tested x 64 B, counted in an untimed frame; the 40 MB BVH and 10 MB of curves "
                                  "are L2-resident, so this can exceed the HBM copy peak ("

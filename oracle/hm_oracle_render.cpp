@@ -63,11 +63,21 @@ struct OScene {
 Box prim_box(const OScene& s, int p) {
   Box b;
   if (p < s.n_seg()) {
+    // hull of the Bezier control points of the segment, grown by their
+    // largest radius (same operation order as the device build)
     const float* c = &s.cp[4 * s.seg[p]];
-    float r = fmaxf(fmaxf(c[3], c[7]), fmaxf(c[11], c[15]));
+    float w[4][4];
+    for (int k = 0; k < 4; ++k) {
+      const float q0 = c[k], q1 = c[4 + k], q2 = c[8 + k], q3 = c[12 + k];
+      w[0][k] = ((q0 + 4.f * q1) + q2) * (1.f / 6.f);
+      w[1][k] = (2.f * q1 + q2) * (1.f / 3.f);
+      w[2][k] = (q1 + 2.f * q2) * (1.f / 3.f);
+      w[3][k] = ((q1 + 4.f * q2) + q3) * (1.f / 6.f);
+    }
+    const float r = fmaxf(fmaxf(w[0][3], w[1][3]), fmaxf(w[2][3], w[3][3]));
     for (int k = 0; k < 3; ++k) {
-      b.lo[k] = fminf(fminf(c[k], c[4 + k]), fminf(c[8 + k], c[12 + k])) - r;
-      b.hi[k] = fmaxf(fmaxf(c[k], c[4 + k]), fmaxf(c[8 + k], c[12 + k])) + r;
+      b.lo[k] = fminf(fminf(w[0][k], w[1][k]), fminf(w[2][k], w[3][k])) - r;
+      b.hi[k] = fmaxf(fmaxf(w[0][k], w[1][k]), fmaxf(w[2][k], w[3][k])) + r;
     }
   } else {
     const int* t = &s.tri[3 * (p - s.n_seg())];

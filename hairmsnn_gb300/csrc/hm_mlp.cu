@@ -173,36 +173,6 @@ MlpConfig mlp_config_from_json(const char* text, int in_ch, int out_ch) {
 // ====================================================================== encoding
 __constant__ MlpDims c_dims[1];
 
-// OneBlob quartic-kernel CDF with radius one bin (inv_radius = n_bins).
-HM_D float quartic_cdf(float x, float inv_radius) {
-  float u = x * inv_radius;
-  float u2 = u * u;
-  float u4 = u2 * u2;
-  return fminf(fmaxf((1.0f / 16.0f) * u * (15.0f - 10.0f * u2 + 3.0f * u4) + 0.5f, 0.f), 1.f);
-}
-// Periodic (on [0,1)) cumulative mass left of `boundary` for a blob at x.
-HM_D float oneblob_cdf(float boundary, float x, float nb) {
-  return quartic_cdf(boundary - x, nb) + quartic_cdf(boundary - x - 1.0f, nb) +
-         quartic_cdf(boundary - x + 1.0f, nb);
-}
-
-HM_D uint32_t grid_index(const EncSeg& s, int l, uint32_t x, uint32_t y, uint32_t z) {
-  const uint32_t size = s.level_size[l], res = s.level_res[l];
-  uint32_t stride = 1, index = 0;
-  index += x * stride;
-  stride *= res;
-  if (stride <= size) {
-    index += y * stride;
-    stride *= res;
-    if (stride <= size) {
-      index += z * stride;
-      stride *= res;
-    }
-  }
-  if (size < stride) index = (x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u);
-  return index % size;
-}
-
 // One thread per (query, encoded feature group): writes X[q][*].
 __global__ void __launch_bounds__(256) encode_kernel(const float* __restrict__ in, const float* __restrict__ enc_params,
                                                      float* __restrict__ X, int64_t n) {
@@ -672,6 +642,12 @@ struct Mlp {
   long long* grid_acc = nullptr;  // fixed-point hash-grid gradient accumulator
   int64_t last_n = 0;        // batch of the last forward()
   const float* last_in = nullptr;
+  // tensor-core inference (precision != FP32): packed weights, refreshed
+  // when the FP32 master parameters change (params_version)
+  TcPack tc;
+  int64_t params_version = 1, packed_version = 0;
+  int* tc_err_host = nullptr;  // host-mapped timeout flag of the kernel
+  int* tc_err_dev = nullptr;
 };
 
 }  // namespace hm
@@ -803,11 +779,6 @@ extern "C" hm_mlp* hm_mlp_create(const char* config_json, int in_ch, int out_ch,
                                  uint32_t seed, int* status) {
   int dummy;
   if (!status) status = &dummy;
-  if (precision != HM_PREC_FP32) {
-    *status = HM_EUNSUPPORTED;
-    hm_set_error("hm_mlp_create: precision %d is not available for this network", precision);
-    return nullptr;
-  }
   Mlp* m = new Mlp();
   try {
     m->cfg = mlp_config_from_json(config_json, in_ch, out_ch);
@@ -816,6 +787,15 @@ extern "C" hm_mlp* hm_mlp_create(const char* config_json, int in_ch, int out_ch,
     delete m;
     *status = HM_EPARSE;
     return nullptr;
+  }
+  if (precision != HM_PREC_FP32) {
+    std::string why;
+    if (!tc_supported(m->cfg.d, precision, &why)) {
+      delete m;
+      *status = HM_EUNSUPPORTED;
+      hm_set_error("hm_mlp_create: precision %d is not available for this network (%s)", precision, why.c_str());
+      return nullptr;
+    }
   }
   m->precision = precision;
   m->n_params = m->cfg.d.n_net_params + m->cfg.d.n_enc_params;
@@ -826,6 +806,17 @@ extern "C" hm_mlp* hm_mlp_create(const char* config_json, int in_ch, int out_ch,
   if (e == cudaSuccess) e = cudaMalloc(&m->adam_m, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&m->adam_v, bytes);
   if (e == cudaSuccess) e = cudaMalloc(&m->loss_dev, sizeof(float));
+  if (e == cudaSuccess && precision != HM_PREC_FP32) {
+    e = cudaHostAlloc(&m->tc_err_host, sizeof(int), cudaHostAllocMapped);
+    if (e == cudaSuccess) {
+      *m->tc_err_host = 0;
+      e = cudaHostGetDevicePointer(&m->tc_err_dev, m->tc_err_host, 0);
+    }
+    if (e == cudaSuccess) {
+      int st = tc_pack_alloc(m->cfg.d, precision, &m->tc);
+      if (st != HM_OK) e = cudaErrorMemoryAllocation;
+    }
+  }
   if (e != cudaSuccess) {
     *status = hm_cuda_status(e, "hm_mlp_create");
     hm_mlp_destroy((hm_mlp*)m);
@@ -857,6 +848,8 @@ extern "C" void hm_mlp_destroy(hm_mlp* h) {
   cudaFree(m->dw_part);
   cudaFree(m->loss_dev);
   cudaFree(m->grid_acc);
+  tc_pack_free(&m->tc);
+  if (m->tc_err_host) cudaFreeHost(m->tc_err_host);
   delete m;
 }
 
@@ -890,6 +883,7 @@ extern "C" int hm_mlp_set_params(hm_mlp* h, const float* host_in) {
   Mlp* m = (Mlp*)h;
   if (!m || !host_in) return hm_set_error("hm_mlp_set_params: NULL"), HM_EINVAL;
   cudaError_t e = cudaMemcpy(m->params, host_in, m->n_params * sizeof(float), cudaMemcpyHostToDevice);
+  m->params_version += 1;
   return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_mlp_set_params");
 }
 
@@ -910,7 +904,24 @@ extern "C" int hm_mlp_reset(hm_mlp* h) {
   if (e == cudaSuccess) e = cudaMemset(m->adam_v, 0, bytes);
   m->step = 0;
   m->lr = m->cfg.adam.lr;
+  m->params_version += 1;
   return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_mlp_reset");
+}
+
+// Inference on the tensor cores (FP16 / BF16 / E4M3 operands, FP32
+// accumulation); encoding fused, no per-call allocation.  A bounded wait
+// that expired in an earlier call is reported here.
+static int tc_inference(Mlp* m, const float* d_in, float* d_out, int64_t n, cudaStream_t st) {
+  if (*(volatile int*)m->tc_err_host) {
+    *m->tc_err_host = 0;
+    return hm_set_error("mlp: a tensor-core wait expired in an earlier call"), HM_ETIMEOUT;
+  }
+  if (m->packed_version != m->params_version) {
+    if (int s = tc_pack(m->cfg.d, m->params, m->tc, st)) return s;
+    m->packed_version = m->params_version;
+  }
+  return tc_forward(m->cfg.d, m->tc, m->params + m->cfg.d.n_net_params, d_in, d_out, m->cfg.d.out_ch, n,
+                    m->tc_err_dev, st);
 }
 
 static int check_io(const char* who, Mlp* m, const void* a, const void* b, int64_t n) {
@@ -928,6 +939,7 @@ extern "C" int hm_mlp_inference(hm_mlp* h, const float* d_in, float* d_out, int6
   if (int s = check_io("hm_mlp_inference", m, d_in, d_out, n)) return s;
   if (n == 0) return HM_OK;
   cudaStream_t st = (cudaStream_t)stream;
+  if (m->precision != HM_PREC_FP32) return tc_inference(m, d_in, d_out, n, st);
   if (int s = ensure_ws(m, n)) return s;
   if (int s = encode(m, d_in, n, st)) return s;
   return dispatch_fwd(m, m->X, d_out, m->cfg.d.out_ch, nullptr, n, st);
@@ -1024,6 +1036,7 @@ extern "C" int hm_mlp_optimizer_step(hm_mlp* h, float loss_scale, void* stream) 
                                                       m->cfg.d.n_net_params, lr_t, a.beta1, a.beta2, a.eps,
                                                       a.l2_reg, loss_scale);
   HM_CHECK_LAUNCH("adam_kernel");
+  m->params_version += 1;
   return HM_OK;
 }
 
@@ -1166,6 +1179,7 @@ extern "C" int hm_mlp_inference_noalloc(hm_mlp* h, const float* d_in, float* d_o
   Mlp* m = (Mlp*)h;
   if (int s = check_io("hm_mlp_inference_noalloc", m, d_in, d_out, n)) return s;
   if (n == 0) return HM_OK;
+  if (m->precision != HM_PREC_FP32) return tc_inference(m, d_in, d_out, n, (cudaStream_t)stream);
   const int64_t need = n * (int64_t)m->cfg.d.in_pad;
   if (need > kNoAllocScratchFloats)
     return hm_set_error("hm_mlp_inference_noalloc: %lld queries x %d encoded floats exceed the static scratch of "

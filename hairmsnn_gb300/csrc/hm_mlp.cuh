@@ -79,4 +79,63 @@ struct MlpConfig {
 // Parses a tcnn-style JSON config (loss / optimizer / encoding / network).
 MlpConfig mlp_config_from_json(const char* text, int in_ch, int out_ch);
 
+
+// ---- encoding helpers shared by the FP32 and tensor-core kernels
+// OneBlob quartic-kernel CDF with radius one bin (inv_radius = n_bins).
+HM_D float quartic_cdf(float x, float inv_radius) {
+  float u = x * inv_radius;
+  float u2 = u * u;
+  float u4 = u2 * u2;
+  return fminf(fmaxf((1.0f / 16.0f) * u * (15.0f - 10.0f * u2 + 3.0f * u4) + 0.5f, 0.f), 1.f);
+}
+// Periodic (on [0,1)) cumulative mass left of `boundary` for a blob at x.
+HM_D float oneblob_cdf(float boundary, float x, float nb) {
+  return quartic_cdf(boundary - x, nb) + quartic_cdf(boundary - x - 1.0f, nb) +
+         quartic_cdf(boundary - x + 1.0f, nb);
+}
+
+HM_D uint32_t grid_index(const EncSeg& s, int l, uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t size = s.level_size[l], res = s.level_res[l];
+  uint32_t stride = 1, index = 0;
+  index += x * stride;
+  stride *= res;
+  if (stride <= size) {
+    index += y * stride;
+    stride *= res;
+    if (stride <= size) {
+      index += z * stride;
+      stride *= res;
+    }
+  }
+  if (size < stride) index = (x * 1u) ^ (y * 2654435761u) ^ (z * 805459861u);
+  return index % size;
+}
+
+
+// ---- tensor-core (tcgen05) forward for HM_PREC_FP16 / BF16 / FP8_E4M3
+// Weights are repacked from the FP32 master copy into the operand layout of
+// the MMA (K-major, 8-row x 16-byte core matrices) whenever they change.
+struct TcPack {
+  int precision = 0;
+  int elem_bytes = 2;
+  int kinst = 16;           // K of one MMA instruction (elements)
+  int n_layers = 0;         // hidden layers + output
+  int N[16], K[16];         // per layer: output rows, padded input columns
+  int64_t boff[16];         // byte offset of each layer in the blob
+  int64_t bytes = 0;
+  uint8_t* blob = nullptr;  // device
+  float* scales = nullptr;  // device [16]: 1/weight scale per layer; [15]: hash-grid amax
+};
+
+// Whether the tensor-core path covers this network at this precision.
+bool tc_supported(const MlpDims& d, int precision, std::string* why);
+// Layout, allocation (once) and repacking of the weights.
+int tc_pack_alloc(const MlpDims& d, int precision, TcPack* pk);
+int tc_pack(const MlpDims& d, const float* params, TcPack& pk, cudaStream_t st);
+void tc_pack_free(TcPack* pk);
+// Encoding + all layers of n queries on the tensor cores: in [n][in_ch],
+// out [n][out_stride] (the first out_ch columns written).
+int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
+               int out_stride, int64_t n, int* err_flag, cudaStream_t st);
+
 }  // namespace hm

@@ -1,0 +1,608 @@
+// Radiance-cache network forward on the 5th-generation tensor cores.
+//
+// One persistent CTA of 128 threads per SM slot; each CTA keeps every layer's
+// weights in shared memory (loaded once) and walks 128-query tiles:
+//   encode   thread t computes the encoded input row of query t of the tile
+//            (same per-feature arithmetic as the FP32 encode kernel) and
+//            stores it, rounded to FP16 / BF16 / E4M3, as the A operand
+//   layers   thread 0 issues tcgen05.mma (M=128, N=width or 16, K=16/32 per
+//            instruction) with A and B in shared memory and the FP32
+//            accumulator in tensor memory, then tcgen05.commit to an mbarrier
+//   epilogue every thread reads its row of the accumulator (tcgen05.ld
+//            32x32b), applies ReLU and stores it as the next layer's A
+//   output   the 16-column accumulator of the last layer -> out (FP32)
+// Layer 0 is split along K into chunks when the encoded row does not fit
+// next to the weights.
+//
+// Operand layout (both A and B, K-major, no swizzle): 8-row x 16-byte core
+// matrices; for an R-row operand the byte at (row, kb) sits at
+//   ((kb / 16) * (R / 8) + row / 8) * 128 + (row % 8) * 16 + kb % 16,
+// so core matrices adjacent in K are 16*R bytes apart (leading byte offset)
+// and those adjacent in M/N 128 bytes apart (stride byte offset).
+//
+// E4M3: weights carry one scale per layer (448 / amax of the layer), the
+// activations one scale per query row (448 / amax of the row; for the
+// encoded input an upper bound: 1 for Frequency/OneBlob/padding, |x| for
+// Identity inputs, the table amax for hash grids).  Scaling rows of A scales
+// rows of D, so the epilogue owning the row undoes it exactly.
+//
+// Every wait on the mbarrier is bounded; on expiry the kernel records the
+// fact in a host-mapped flag, stops issuing work, frees its tensor memory
+// and returns.
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_fp8.h>
+
+#include <algorithm>
+#include <string>
+
+#include "hm_mlp.cuh"
+
+namespace hm {
+
+enum { TC_FP16 = 1, TC_BF16 = 2, TC_E4M3 = 3 };
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 128;
+constexpr int kTcSmemMax = 227 * 1024;
+constexpr int kTcSlack = 16 * 1024;  // guard band after the operands
+constexpr uint32_t kTcWaitLimit = 1u << 20;
+constexpr float kE4M3Max = 448.f;
+
+// ------------------------------------------------------------- PTX wrappers
+HM_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+HM_D void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+HM_D void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+HM_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+HM_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kTcWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+HM_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+HM_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+HM_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// warp-collective
+HM_D void tmem_alloc(uint32_t* holder, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(holder)),
+               "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+HM_D void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+
+template <bool F8>
+HM_D void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+  if (F8)
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+  else
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+HM_D void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+// 16 consecutive FP32 columns of this thread's lane; the wait is in the same
+// statement so no use of the registers can be scheduled before it.
+HM_D void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+      "tcgen05.wait::ld.sync.aligned;\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Instruction descriptor: D = F32, A/B K-major, formats (kind::f16: 0 F16,
+// 1 BF16; kind::f8f6f4: 0 E4M3), N >> 3 at bit 17, M >> 4 at bit 24.
+HM_HD uint32_t tc_idesc(int m, int n, int fmt) {
+  return (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+// Shared-memory descriptor, no swizzle: start, leading (K) and stride (M/N)
+// byte offsets in 16-byte units, descriptor version 1.
+HM_D uint64_t tc_sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+}
+
+HM_HD int64_t op_offset(int rows, int row, int kb) {
+  return ((int64_t)(kb >> 4) * (rows >> 3) + (row >> 3)) * 128 + (row & 7) * 16 + (kb & 15);
+}
+
+// ------------------------------------------------------------ quantisation
+template <int PREC>
+HM_D uint32_t pack2(float a, float b) {
+  if (PREC == TC_BF16) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+  } else {
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+  }
+}
+HM_D uint32_t pack4_e4m3(float a, float b, float c, float d) {
+  const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(a, b), __NV_SATFINITE, __NV_E4M3);
+  const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(c, d), __NV_SATFINITE, __NV_E4M3);
+  return (lo & 0xFFFFu) | (hi << 16);
+}
+
+// ---------------------------------------------------------------- encoding
+// Feature k of the encoded row (k >= n_enc: padding 1; k >= in_pad: 0, the
+// extra K columns of the E4M3 layout carry zero weights).  Same arithmetic,
+// feature by feature, as encode_kernel.
+HM_D float enc_feature(const MlpDims& d, const float* __restrict__ xin, const float* __restrict__ enc_params, int k) {
+  if (k >= d.in_pad) return 0.f;
+  if (k >= d.n_enc) return 1.f;
+  int si = 0;
+  while (si + 1 < d.n_segs && k >= d.segs[si + 1].out_off) ++si;
+  const EncSeg& s = d.segs[si];
+  const int j = k - s.out_off;
+  if (s.type == ENC_IDENTITY) return xin[s.in_off + j];
+  if (s.type == ENC_FREQUENCY) {
+    const int dim = j / (2 * s.n_freq), rem = j % (2 * s.n_freq), f = rem >> 1;
+    const float a = ldexpf(xin[s.in_off + dim], f) * kPi;
+    return (rem & 1) ? sinf(a + 0.5f * kPi) : sinf(a);
+  }
+  if (s.type == ENC_ONEBLOB) {
+    const int dim = j / s.n_bins, b = j % s.n_bins;
+    const float nb = (float)s.n_bins, x = xin[s.in_off + dim];
+    const float c0 = oneblob_cdf(0.f, x, nb);
+    const float left = b == 0 ? c0 : oneblob_cdf((float)b / nb, x, nb);
+    const float right = (b == s.n_bins - 1) ? c0 + 1.f : oneblob_cdf((float)(b + 1) / nb, x, nb);
+    return right - left;
+  }
+  // hash grid: level l, feature f
+  const int l = j / s.n_feat, f = j % s.n_feat;
+  const float* table = enc_params + s.param_off;
+  const float px = xin[s.in_off], py = xin[s.in_off + 1], pz = xin[s.in_off + 2];
+  const float sc = s.level_scale[l];
+  const float fx = fmaf(sc, px, 0.5f), fy = fmaf(sc, py, 0.5f), fz = fmaf(sc, pz, 0.5f);
+  const float gx = floorf(fx), gy = floorf(fy), gz = floorf(fz);
+  const float wx = fx - gx, wy = fy - gy, wz = fz - gz;
+  const uint32_t ix = (uint32_t)(int)gx, iy = (uint32_t)(int)gy, iz = (uint32_t)(int)gz;
+  float acc = 0.f;
+  for (int c = 0; c < 8; ++c) {
+    const uint32_t cx = ix + (c & 1), cy = iy + ((c >> 1) & 1), cz = iz + ((c >> 2) & 1);
+    const float w = ((c & 1) ? wx : 1.f - wx) * (((c >> 1) & 1) ? wy : 1.f - wy) * (((c >> 2) & 1) ? wz : 1.f - wz);
+    const uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
+    acc += w * __ldg(table + (int64_t)e * s.n_feat + f);
+  }
+  return acc;
+}
+
+// Upper bound of |feature| over the row (E4M3 input scale).
+HM_D float enc_row_bound(const MlpDims& d, const float* __restrict__ xin, float grid_amax) {
+  float m = 1.f;
+  for (int si = 0; si < d.n_segs; ++si) {
+    const EncSeg& s = d.segs[si];
+    if (s.type == ENC_IDENTITY)
+      for (int k = 0; k < s.n_dims; ++k) m = fmaxf(m, fabsf(xin[s.in_off + k]));
+    else if (s.type == ENC_HASHGRID)
+      m = fmaxf(m, grid_amax);
+  }
+  return m;
+}
+
+// --------------------------------------------------------------- the kernel
+struct TcArgs {
+  MlpDims d;
+  const uint8_t* blob;
+  int64_t blob_bytes;
+  int64_t boff[16];
+  int N[16], K[16];
+  int n_layers;
+  int kc0;  // layer-0 K chunk (elements)
+  const float* scales;
+  const float* enc_params;
+  const float* in;
+  float* out;
+  int out_stride;
+  int64_t n;
+  int* err;  // host-mapped
+  int a_bytes;
+  int slack;  // guard band between the weights and the barrier (bytes)
+  int ncols;
+};
+
+template <int PREC, int W>
+__global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_constant__ TcArgs p) {
+  constexpr bool F8 = PREC == TC_E4M3;
+  constexpr int EB = F8 ? 1 : 2;       // bytes per element
+  constexpr int KI = 32 / EB;          // K per MMA instruction
+  constexpr int CK = 16 / EB;          // elements per 16-byte core-matrix row
+  constexpr int FMT = PREC == TC_BF16 ? 1 : 0;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* A = smem;
+  uint8_t* Wt = smem + p.a_bytes;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(Wt + ((p.blob_bytes + 127) & ~(int64_t)127) + p.slack);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const MlpDims& d = p.d;
+  const int L = p.n_layers - 1;  // index of the output layer
+
+  for (int64_t i = tid; i < p.blob_bytes / 16; i += kTcThreads)
+    reinterpret_cast<uint4*>(Wt)[i] = __ldg(reinterpret_cast<const uint4*>(p.blob) + i);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(holder, p.ncols);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *holder;
+  const uint32_t row_taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t a_base = smem_u32(A), w_base = smem_u32(Wt);
+  const uint32_t a_lbo = 16 * kTcRows;
+  uint32_t phase = 0;
+  bool failed = false;
+  auto w_inv = [&](int l) { return F8 ? __ldg(p.scales + l) : 1.f; };
+  const float grid_amax = F8 ? p.scales[15] : 0.f;
+
+  // issue the MMAs of one layer (or layer-0 chunk) and wait for them
+  auto run_layer = [&](int l, int k_begin, int k_count, bool accumulate_first) -> bool {
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t idesc = tc_idesc(kTcRows, p.N[l], FMT);
+      const uint32_t b_lbo = 16 * p.N[l];
+      const uint32_t b_base = w_base + (uint32_t)p.boff[l];
+      for (int ks = 0; ks < k_count / KI; ++ks) {
+        const uint64_t ad = tc_sdesc(a_base + (uint32_t)ks * 2 * a_lbo, a_lbo, 128);
+        const uint64_t bd = tc_sdesc(b_base + (uint32_t)((k_begin / KI) + ks) * 2 * b_lbo, b_lbo, 128);
+        tc_mma<F8>(tmem, ad, bd, idesc, (accumulate_first || ks > 0) ? 1u : 0u);
+      }
+      tc_commit(bar);
+    }
+    const bool ok = mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    const bool bad = __syncthreads_or(!ok);
+    tc_fence_after();
+    return !bad;
+  };
+
+  const int64_t n_tiles = (p.n + kTcRows - 1) / kTcRows;
+  for (int64_t tile = blockIdx.x; tile < n_tiles && !failed; tile += gridDim.x) {
+    const int64_t q = tile * kTcRows + tid;
+    const bool valid = q < p.n;
+    const float* xin = p.in + (valid ? q : 0) * d.in_ch;
+    float row_inv = 1.f;  // 1 / activation scale of this thread's A row
+    float row_scale = 1.f;
+    if (F8) {
+      const float bound = valid ? enc_row_bound(d, xin, grid_amax) : 1.f;
+      row_scale = kE4M3Max / bound;
+      row_inv = bound / kE4M3Max;
+    }
+    // ---- layer 0, in K chunks
+    const int K0 = p.K[0];
+    for (int kc = 0; kc < K0 && !failed; kc += p.kc0) {
+      const int kn = min(p.kc0, K0 - kc);
+      for (int g = 0; g < kn / CK; ++g) {
+        const int k0 = kc + g * CK;
+        uint32_t word[4];
+        if (F8) {
+#pragma unroll
+          for (int w4 = 0; w4 < 4; ++w4) {
+            float v[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) v[e] = valid ? enc_feature(d, xin, p.enc_params, k0 + 4 * w4 + e) : 0.f;
+            word[w4] = pack4_e4m3(v[0] * row_scale, v[1] * row_scale, v[2] * row_scale, v[3] * row_scale);
+          }
+        } else {
+#pragma unroll
+          for (int w2 = 0; w2 < 4; ++w2) {
+            const float a = valid ? enc_feature(d, xin, p.enc_params, k0 + 2 * w2) : 0.f;
+            const float b = valid ? enc_feature(d, xin, p.enc_params, k0 + 2 * w2 + 1) : 0.f;
+            word[w2] = pack2<PREC>(a, b);
+          }
+        }
+        *reinterpret_cast<uint4*>(A + op_offset(kTcRows, tid, g * 16)) =
+            make_uint4(word[0], word[1], word[2], word[3]);
+      }
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (!run_layer(0, kc, kn, kc > 0)) failed = true;
+    }
+    // ---- hidden epilogues and the following layers
+    for (int l = 1; l <= L && !failed; ++l) {
+      const float sc = row_inv * w_inv(l - 1);
+      if (F8) {
+        float v[W];
+#pragma unroll
+        for (int c = 0; c < W / 16; ++c) {
+          float t[16];
+          tmem_ld16(row_taddr + c * 16, t);
+#pragma unroll
+          for (int e = 0; e < 16; ++e) v[c * 16 + e] = fmaxf(t[e] * sc, 0.f);
+        }
+        float amax = 0.f;
+#pragma unroll
+        for (int e = 0; e < W; ++e) amax = fmaxf(amax, v[e]);
+        const float s = amax > 0.f ? kE4M3Max / amax : 1.f;
+        row_inv = amax > 0.f ? amax / kE4M3Max : 1.f;
+#pragma unroll
+        for (int g = 0; g < W / 16; ++g) {
+          uint32_t word[4];
+#pragma unroll
+          for (int w4 = 0; w4 < 4; ++w4)
+            word[w4] = pack4_e4m3(v[g * 16 + 4 * w4] * s, v[g * 16 + 4 * w4 + 1] * s, v[g * 16 + 4 * w4 + 2] * s,
+                                  v[g * 16 + 4 * w4 + 3] * s);
+          *reinterpret_cast<uint4*>(A + op_offset(kTcRows, tid, g * 16)) =
+              make_uint4(word[0], word[1], word[2], word[3]);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < W / 16; ++c) {
+          float t[16];
+          tmem_ld16(row_taddr + c * 16, t);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            uint32_t word[4];
+#pragma unroll
+            for (int w2 = 0; w2 < 4; ++w2)
+              word[w2] = pack2<PREC>(fmaxf(t[h * 8 + 2 * w2], 0.f), fmaxf(t[h * 8 + 2 * w2 + 1], 0.f));
+            *reinterpret_cast<uint4*>(A + op_offset(kTcRows, tid, (c * 2 + h) * 16)) =
+                make_uint4(word[0], word[1], word[2], word[3]);
+          }
+        }
+      }
+      tc_fence_before();
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (!run_layer(l, 0, p.K[l], false)) failed = true;
+    }
+    if (failed) break;
+    // ---- output layer accumulator -> out
+    {
+      float t[16];
+      tmem_ld16(row_taddr, t);
+      const float sc = row_inv * w_inv(L);
+      if (valid)
+        for (int o = 0; o < d.out_ch && o < p.out_stride; ++o) p.out[q * p.out_stride + o] = t[o] * sc;
+    }
+    tc_fence_before();
+    __syncthreads();
+  }
+  if (failed && tid == 0) atomicOr(p.err, 1);
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, p.ncols);
+}
+
+// ------------------------------------------------------------ weight packing
+__global__ void tc_scales_kernel(MlpDims d, const float* __restrict__ params, int n_layers, float* __restrict__ scales) {
+  // block l < n_layers: amax of layer l's weights -> 1 / (448 / amax);
+  // block n_layers: amax of the encoding parameters (hash tables)
+  __shared__ float red[256];
+  const int l = blockIdx.x;
+  int64_t begin, count;
+  if (l < n_layers) {
+    const int fan_in = l == 0 ? d.in_pad : d.width;
+    const int fan_out = l == n_layers - 1 ? d.out_pad : d.width;
+    begin = d.layer_off[l];
+    count = (int64_t)fan_in * fan_out;
+  } else {
+    begin = d.n_net_params;
+    count = d.n_enc_params;
+  }
+  float m = 0.f;
+  for (int64_t i = threadIdx.x; i < count; i += blockDim.x) m = fmaxf(m, fabsf(params[begin + i]));
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) red[threadIdx.x] = fmaxf(red[threadIdx.x], red[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (l < n_layers)
+      scales[l] = red[0] > 0.f ? red[0] / kE4M3Max : 1.f;
+    else
+      scales[15] = red[0];
+  }
+}
+
+template <int PREC>
+__global__ void tc_pack_kernel(MlpDims d, const float* __restrict__ params, int layer, int N, int K,
+                               int64_t boff, const float* __restrict__ scales, uint8_t* __restrict__ blob) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)N * K) return;
+  const int n = (int)(i / K), k = (int)(i % K);
+  const int fan_in = layer == 0 ? d.in_pad : d.width;
+  const float w = k < fan_in ? params[d.layer_off[layer] + (int64_t)n * fan_in + k] : 0.f;
+  if (PREC == TC_E4M3) {
+    const float s = 1.f / scales[layer];
+    const uint32_t v = __nv_cvt_float2_to_fp8x2(make_float2(w * s, 0.f), __NV_SATFINITE, __NV_E4M3);
+    blob[boff + op_offset(N, n, k)] = (uint8_t)(v & 0xFF);
+  } else if (PREC == TC_BF16) {
+    __nv_bfloat16 h = __float2bfloat16_rn(w);
+    *reinterpret_cast<__nv_bfloat16*>(blob + boff + op_offset(N, n, 2 * k)) = h;
+  } else {
+    __half h = __float2half_rn(w);
+    *reinterpret_cast<__half*>(blob + boff + op_offset(N, n, 2 * k)) = h;
+  }
+}
+
+// ------------------------------------------------------------------ host API
+static int tc_kinst(int precision) { return precision == HM_PREC_FP8_E4M3 ? 32 : 16; }
+static int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+bool tc_supported(const MlpDims& d, int precision, std::string* why) {
+  if (precision != HM_PREC_FP16 && precision != HM_PREC_BF16 && precision != HM_PREC_FP8_E4M3) {
+    if (why) *why = "unknown precision";
+    return false;
+  }
+  if (precision == HM_PREC_FP8_E4M3 && d.width < 32) {
+    if (why) *why = "E4M3 needs n_neurons >= 32 (K of one MMA is 32)";
+    return false;
+  }
+  if (d.n_hidden + 1 > 15) {
+    if (why) *why = "too many layers";
+    return false;
+  }
+  TcPack pk;
+  pk.precision = precision;
+  pk.elem_bytes = precision == HM_PREC_FP8_E4M3 ? 1 : 2;
+  const int KI = tc_kinst(precision);
+  int64_t blob = 0;
+  for (int l = 0; l <= d.n_hidden; ++l) {
+    const int N = l == d.n_hidden ? d.out_pad : d.width;
+    const int K = round_up(l == 0 ? d.in_pad : d.width, KI);
+    blob += (int64_t)N * K * pk.elem_bytes;
+  }
+  const int64_t a_min = (int64_t)kTcRows * std::max(KI, d.width) * pk.elem_bytes;
+  if (((blob + 127) & ~127) + a_min + 64 > kTcSmemMax) {
+    if (why) *why = "weights do not fit in shared memory";
+    return false;
+  }
+  return true;
+}
+
+int tc_pack_alloc(const MlpDims& d, int precision, TcPack* pk) {
+  pk->precision = precision;
+  pk->elem_bytes = precision == HM_PREC_FP8_E4M3 ? 1 : 2;
+  pk->kinst = tc_kinst(precision);
+  pk->n_layers = d.n_hidden + 1;
+  int64_t off = 0;
+  for (int l = 0; l < pk->n_layers; ++l) {
+    pk->N[l] = l == d.n_hidden ? d.out_pad : d.width;
+    pk->K[l] = round_up(l == 0 ? d.in_pad : d.width, pk->kinst);
+    pk->boff[l] = off;
+    off += (int64_t)pk->N[l] * pk->K[l] * pk->elem_bytes;
+  }
+  pk->bytes = off;
+  cudaError_t e = cudaMalloc(&pk->blob, (size_t)off);
+  if (e == cudaSuccess) e = cudaMalloc(&pk->scales, 16 * sizeof(float));
+  if (e != cudaSuccess) return hm_cuda_status(e, "tensor-core weight blob");
+  cudaMemset(pk->scales, 0, 16 * sizeof(float));
+  return HM_OK;
+}
+
+void tc_pack_free(TcPack* pk) {
+  cudaFree(pk->blob);
+  cudaFree(pk->scales);
+  pk->blob = nullptr;
+  pk->scales = nullptr;
+}
+
+int tc_pack(const MlpDims& d, const float* params, TcPack& pk, cudaStream_t st) {
+  if (pk.precision == HM_PREC_FP8_E4M3) {
+    tc_scales_kernel<<<pk.n_layers + 1, 256, 0, st>>>(d, params, pk.n_layers, pk.scales);
+    HM_CHECK_LAUNCH("tc_scales_kernel");
+  }
+  for (int l = 0; l < pk.n_layers; ++l) {
+    const int64_t cnt = (int64_t)pk.N[l] * pk.K[l];
+    const int blocks = (int)((cnt + 255) / 256);
+    if (pk.precision == HM_PREC_FP8_E4M3)
+      tc_pack_kernel<TC_E4M3><<<blocks, 256, 0, st>>>(d, params, l, pk.N[l], pk.K[l], pk.boff[l], pk.scales, pk.blob);
+    else if (pk.precision == HM_PREC_BF16)
+      tc_pack_kernel<TC_BF16><<<blocks, 256, 0, st>>>(d, params, l, pk.N[l], pk.K[l], pk.boff[l], pk.scales, pk.blob);
+    else
+      tc_pack_kernel<TC_FP16><<<blocks, 256, 0, st>>>(d, params, l, pk.N[l], pk.K[l], pk.boff[l], pk.scales, pk.blob);
+    HM_CHECK_LAUNCH("tc_pack_kernel");
+  }
+  return HM_OK;
+}
+
+template <int PREC, int W>
+static int tc_launch(const TcArgs& a, size_t smem, cudaStream_t st) {
+  auto kern = mlp_tc_fwd_kernel<PREC, W>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return hm_cuda_status(e, "mlp_tc_fwd_kernel smem");
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, smem);
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  per_sm = std::max(1, std::min(per_sm, 512 / a.ncols));  // tensor-memory columns per SM
+  const int64_t tiles = (a.n + kTcRows - 1) / kTcRows;
+  const int blocks = (int)std::min<int64_t>(tiles, (int64_t)sms * per_sm);
+  kern<<<blocks, kTcThreads, smem, st>>>(a);
+  HM_CHECK_LAUNCH("mlp_tc_fwd_kernel");
+  return HM_OK;
+}
+
+int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
+               int out_stride, int64_t n, int* err_flag, cudaStream_t st) {
+  if (n <= 0) return HM_OK;
+  TcArgs a;
+  a.d = d;
+  a.blob = pk.blob;
+  a.blob_bytes = pk.bytes;
+  for (int l = 0; l < 16; ++l) {
+    a.boff[l] = l < pk.n_layers ? pk.boff[l] : 0;
+    a.N[l] = l < pk.n_layers ? pk.N[l] : 0;
+    a.K[l] = l < pk.n_layers ? pk.K[l] : 0;
+  }
+  a.n_layers = pk.n_layers;
+  a.scales = pk.scales;
+  a.enc_params = enc_params;
+  a.in = in;
+  a.out = out;
+  a.out_stride = out_stride;
+  a.n = n;
+  a.err = err_flag;
+  int ncols = 32;
+  while (ncols < std::max(d.width, 16)) ncols *= 2;
+  a.ncols = ncols;
+  // shared memory: A tile + weights (+ guard band when it fits) + barrier
+  const int eb = pk.elem_bytes;
+  const int64_t wbytes = (pk.bytes + 127) & ~(int64_t)127;
+  const int64_t misc = 64;
+  int64_t slack = kTcSlack;
+  int kc0 = pk.K[0];
+  auto a_bytes_for = [&](int kc) { return (int64_t)kTcRows * std::max(kc, d.width) * eb; };
+  auto fits = [&](int kc) { return a_bytes_for(kc) + wbytes + slack + misc <= kTcSmemMax; };
+  while (!fits(kc0) && kc0 > pk.kinst) kc0 -= pk.kinst;
+  if (!fits(kc0)) {  // no room for the guard band
+    slack = 0;
+    kc0 = pk.K[0];
+    while (!fits(kc0) && kc0 > pk.kinst) kc0 -= pk.kinst;
+  }
+  if (!fits(kc0)) return hm_set_error("mlp: tensor-core tile does not fit"), HM_EUNSUPPORTED;
+  a.kc0 = kc0;
+  a.a_bytes = (int)a_bytes_for(kc0);
+  a.slack = (int)slack;
+  const size_t smem = (size_t)(a.a_bytes + wbytes + slack + misc);
+  const int W = d.width;
+  switch (pk.precision) {
+    case HM_PREC_BF16:
+      return W == 16 ? tc_launch<TC_BF16, 16>(a, smem, st) : W == 32 ? tc_launch<TC_BF16, 32>(a, smem, st)
+             : W == 64 ? tc_launch<TC_BF16, 64>(a, smem, st) : tc_launch<TC_BF16, 128>(a, smem, st);
+    case HM_PREC_FP16:
+      return W == 16 ? tc_launch<TC_FP16, 16>(a, smem, st) : W == 32 ? tc_launch<TC_FP16, 32>(a, smem, st)
+             : W == 64 ? tc_launch<TC_FP16, 64>(a, smem, st) : tc_launch<TC_FP16, 128>(a, smem, st);
+    default:
+      return W == 32 ? tc_launch<TC_E4M3, 32>(a, smem, st) : W == 64 ? tc_launch<TC_E4M3, 64>(a, smem, st)
+             : tc_launch<TC_E4M3, 128>(a, smem, st);
+  }
+}
+
+}  // namespace hm

@@ -99,7 +99,11 @@ int hm_bsdf_gen_queries(uint32_t seed, int64_t n, float* wo, float* wi, float* t
  *                TINY_MLP; read the file and pass its contents)
  *   in_ch/out_ch input / output channels (the reference uses 12 / 3,
  *                headers/render_hair_msnn.h:145)
- *   precision    HM_PREC_*; seed: parameter initialisation stream
+ *   precision    HM_PREC_*; seed: parameter initialisation stream.
+ *                FP16 / BF16 / FP8_E4M3 run inference on the tensor cores
+ *                (operands rounded to that type, FP32 accumulation; E4M3
+ *                with per-layer weight scales and per-query activation
+ *                scales); parameters, gradients and training stay FP32.
  * Device buffers are row-major per query: in [n][in_ch], out [n][out_ch]
  * (tiny-cuda-nn's column-major GPUMatrix(ptr, ch, n)).  Any n >= 0 is
  * accepted (the reference needs n % 128 == 0, scene.cpp:300-306).  The
@@ -141,7 +145,8 @@ int hm_mlp_inference(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, vo
 /* No counterpart in the reference.  hm_mlp_inference without any device
  * allocation, for callers that must not allocate once running: the encoded
  * inputs go to one static 4 MiB device scratch per device (n * padded input
- * width <= 2^20 floats, else HM_ECAPACITY).  Calls on one device must not
+ * width <= 2^20 floats, else HM_ECAPACITY; FP16/BF16/E4M3 handles encode
+ * inside the tensor-core kernel and use no scratch).  Calls on one device must not
  * overlap (they share the scratch); make the first call on each device before
  * any stream capture (it resolves the scratch address). */
 int hm_mlp_inference_noalloc(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, void* stream);

@@ -218,9 +218,149 @@ class VertexWorkload:
                 "sample": f"{reps} x {n} queries (eval+sample C++ on {threads} threads, MLP FP64 numpy)"}
 
 
+# ========================================================= precision workload
+class PrecisionWorkload:
+    """Cache-network precision sweep: 2^20 hair-vertex queries (the vertex
+    workload's 16-D inputs), Freq12/OneBlob32/Identity -> 5 hidden layers of
+    64 or 128 -> 3, FP32 SIMT against FP16/BF16/E4M3 tensor-core inference
+    (FP32 accumulation).  One step = one inference pass of the chosen form
+    (FP16, width 64) over the 2^20 queries; the sweep reports every
+    precision and width with its error against the FP64 oracle."""
+    name = "precision"
+    metric = "cache-MLP inference queries/s (2^20 queries, width 64, FP16 tensor cores)"
+    unit = "queries/s"
+    WIDTHS = (64, 128)
+    PRECS = ("fp32", "fp16", "bf16", "fp8")
+
+    def __init__(self, torch, n=1 << 20):
+        import numpy as np
+        from hairmsnn_gb300 import mlp
+        self.torch, self.np, self.mlp, self.n = torch, np, mlp, n
+        rng = np.random.default_rng(0)
+        x = np.zeros((n, 16), np.float32)
+        x[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+        x[:, 3:7] = rng.uniform(0, 1, (n, 4))
+        x[:, 7] = rng.uniform(-1, 1, n)
+        x[:, 8:11] = [0.06, 0.1, 0.2]
+        x[:, 11:13] = 0.3
+        self.x_np = x
+        self.targets = rng.lognormal(0.0, 1.5, (n, 3)).astype(np.float32)
+        self.x_host = torch.from_numpy(x).pin_memory()
+        self.x = self.x_host.cuda()
+        self.out = torch.empty((n, 3), device="cuda")
+        self.host_out = torch.empty((n, 3), dtype=torch.float32).pin_memory()
+        self.net = mlp.TinyMLP("c1_cache_w64.json", 16, 3, precision="fp16", seed=0)
+        self.kernels_per_step = 1
+        self.h2d_bytes = n * 16 * 4
+        self.d2h_bytes = n * 3 * 4
+
+    def step(self, events=None):
+        if events: events[0].record()
+        self.net.inference(self.x, self.out)
+        if events: events[1].record()
+
+    def e2e_step(self):
+        xd = self.x_host.to("cuda", non_blocking=True)
+        out = self.net.inference(xd)
+        self.host_out.copy_(out, non_blocking=True)
+        self.torch.cuda.current_stream().synchronize()
+
+    def n_events(self):
+        return 2
+
+    def units_per_step(self):
+        return self.n
+
+    @staticmethod
+    def flops(width):
+        # algorithmic: 209 encoded features, 4 hidden-to-hidden layers, 3 outputs
+        return 2 * (209 * width + 4 * width * width + width * 3)
+
+    def _time(self, fn, reps=10):
+        torch = self.torch
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(3):
+            fn()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for a, b in ev:
+            flush.fill_(1)
+            a.record()
+            fn()
+            b.record()
+        torch.cuda.synchronize()
+        return sum(a.elapsed_time(b) for a, b in ev) / reps
+
+    def sweep(self, pk):
+        np, torch = self.np, self.torch
+        from oracle import mlp_oracle as mo
+        sub = 8192
+        xs = self.x_np[:sub]
+        out = {}
+        for w in self.WIDTHS:
+            cfg = f"c1_cache_w{w}.json"
+            ref = None
+            for prec in self.PRECS:
+                net = self.mlp.TinyMLP(cfg, 16, 3, precision=prec, seed=0)
+                if ref is None:
+                    oc = mo.Config(net.config_text, 16, 3)
+                    ref = mo.forward(oc, net.params().astype(np.float64), xs)[0][:, :3]
+                y = torch.empty((self.n, 3), device="cuda")
+                ms = self._time(lambda: net.inference(self.x, y))
+                tgt = torch.from_numpy(self.targets[:1 << 16]).cuda()
+                xin = self.x[:1 << 16]
+                tms = self._time(lambda: net.training_step(xin, tgt), reps=5)
+                got = y[:sub].cpu().numpy().astype(np.float64)
+                err = got - ref
+                rms_ref = float(np.sqrt(np.mean(ref ** 2)))
+                tf = self.flops(w) * self.n / (ms * 1e-3) / 1e12
+                out[f"w{w}_{prec}"] = {
+                    "inference_ms": round(ms, 4), "queries_per_s": round(self.n / (ms * 1e-3), 1),
+                    "tflops": round(tf, 2), "frac_of_bf16_peak": round(tf / pk["bf16_tflops"], 4),
+                    "training_step_ms_2^16": round(tms, 4),
+                    "err_rms_rel": float(f"{np.sqrt(np.mean(err ** 2)) / rms_ref:.3e}"),
+                    "err_max_rel": float(f"{np.abs(err).max() / rms_ref:.3e}")}
+                net.close()
+        return out
+
+    def roofline(self, seg_ms, pk):
+        ms = seg_ms[0]
+        tf = self.flops(64) * self.n / (ms * 1e-3) / 1e12
+        return {"kernel": "mlp_tc_fwd_kernel<FP16, 64> (encoding fused)", "bound": "tensor",
+                "achieved": round(tf, 3), "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": round(tf / pk["bf16_tflops"], 5), "traffic": None,
+                "flop_per_query": self.flops(64),
+                "note": f"peak = dense bf16 cuBLAS burst ({pk['source']}); FP16 has the same tensor rate",
+                "sweep": self.sweep(pk)}
+
+    def config(self):
+        return {"workload": "precision: 2^20 hair-vertex queries, cache MLP Freq12/OneBlob32/Identity (224) -> "
+                            "5x64 -> 3, FP16 operands on tcgen05, FP32 accumulation; sweep over widths 64/128 and "
+                            "FP32/FP16/BF16/E4M3 with errors against the FP64 oracle on 8192 queries",
+                "queries": self.n, "l2": "flushed between timed steps (256 MiB write)",
+                "parallelism": "replicas"}
+
+    def cpu_baseline(self, threads, budget_s=10.0):
+        np = self.np
+        from oracle import mlp_oracle as mo
+        oc = mo.Config(self.net.config_text, 16, 3)
+        params = self.net.params().astype(np.float64)
+        n = 1 << 14
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            mo.forward(oc, params, self.x_np[:n])
+            reps += 1
+            el = time.perf_counter() - t0
+            if el > budget_s or reps >= 50:
+                break
+        return {"value": round(reps * n / el, 1), "unit": self.unit, "cores": threads, "kind": "port",
+                "sample": f"{reps} x {n} queries, FP64 numpy forward of the same network"}
+
+
 def make_workload(name, torch):
     if name == "vertex":
         return VertexWorkload(torch)
+    if name == "precision":
+        return PrecisionWorkload(torch)
     from hairmsnn_gb300 import render as _r  # noqa: F401  (render workload)
     return _r.RenderBenchWorkload(torch)
 
@@ -306,7 +446,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "render"),
-                    choices=["render", "vertex"])
+                    choices=["render", "vertex", "precision"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

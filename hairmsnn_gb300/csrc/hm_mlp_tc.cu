@@ -42,9 +42,8 @@ namespace hm {
 
 enum { TC_FP16 = 1, TC_BF16 = 2, TC_E4M3 = 3 };
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;
 constexpr int kTcSmemMax = 227 * 1024;
-constexpr int kTcSlack = 16 * 1024;  // guard band after the operands
 constexpr uint32_t kTcWaitLimit = 1u << 20;
 constexpr float kE4M3Max = 448.f;
 
@@ -155,47 +154,151 @@ HM_D uint32_t pack4_e4m3(float a, float b, float c, float d) {
 }
 
 // ---------------------------------------------------------------- encoding
-// Feature k of the encoded row (k >= n_enc: padding 1; k >= in_pad: 0, the
-// extra K columns of the E4M3 layout carry zero weights).  Same arithmetic,
-// feature by feature, as encode_kernel.
-HM_D float enc_feature(const MlpDims& d, const float* __restrict__ xin, const float* __restrict__ enc_params, int k) {
-  if (k >= d.in_pad) return 0.f;
-  if (k >= d.n_enc) return 1.f;
-  int si = 0;
-  while (si + 1 < d.n_segs && k >= d.segs[si + 1].out_off) ++si;
-  const EncSeg& s = d.segs[si];
-  const int j = k - s.out_off;
-  if (s.type == ENC_IDENTITY) return xin[s.in_off + j];
-  if (s.type == ENC_FREQUENCY) {
-    const int dim = j / (2 * s.n_freq), rem = j % (2 * s.n_freq), f = rem >> 1;
-    const float a = ldexpf(xin[s.in_off + dim], f) * kPi;
-    return (rem & 1) ? sinf(a + 0.5f * kPi) : sinf(a);
+// Features are produced in increasing order and packed through a 128-bit
+// shift register into 16-byte groups, one conflict-free shared-memory store
+// per group (the 32 rows of a warp are 32 consecutive 16-byte core-matrix
+// rows).
+template <int PREC>
+struct RowPacker {
+  static constexpr int kPer = PREC == TC_E4M3 ? 16 : 8;  // values per 16 bytes
+  uint32_t w0 = 0, w1 = 0, w2 = 0, w3 = 0;
+  int cnt = 0, group;
+  uint8_t* A;
+  int row;
+  float scale;
+  HM_D RowPacker(uint8_t* a, int r, int first_group, float sc) : group(first_group), A(a), row(r), scale(sc) {}
+  HM_D void push(float v) {
+    constexpr int SH = PREC == TC_E4M3 ? 8 : 16;
+    uint32_t h;
+    if (PREC == TC_E4M3)
+      h = (uint32_t)__nv_cvt_float_to_fp8(v * scale, __NV_SATFINITE, __NV_E4M3);
+    else if (PREC == TC_BF16)
+      h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+    else
+      h = (uint32_t)__half_as_ushort(__float2half_rn(v));
+    w0 = __funnelshift_r(w0, w1, SH);
+    w1 = __funnelshift_r(w1, w2, SH);
+    w2 = __funnelshift_r(w2, w3, SH);
+    w3 = (w3 >> SH) | (h << (32 - SH));
+    if (++cnt == kPer) {
+      *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, group * 16)) = make_uint4(w0, w1, w2, w3);
+      ++group;
+      cnt = 0;
+    }
   }
-  if (s.type == ENC_ONEBLOB) {
-    const int dim = j / s.n_bins, b = j % s.n_bins;
-    const float nb = (float)s.n_bins, x = xin[s.in_off + dim];
-    const float c0 = oneblob_cdf(0.f, x, nb);
-    const float left = b == 0 ? c0 : oneblob_cdf((float)b / nb, x, nb);
-    const float right = (b == s.n_bins - 1) ? c0 + 1.f : oneblob_cdf((float)(b + 1) / nb, x, nb);
-    return right - left;
+};
+
+// Encoded features [kb, ke) of one row (k >= n_enc: padding 1; k >= in_pad:
+// 0, the extra K columns of the E4M3 layout carry zero weights).
+// Identity / OneBlob / hash grid values use the arithmetic of encode_kernel;
+// the Frequency pair (sin, cos) of 2^f * pi * x comes from sincospif, whose
+// reduction is exact (encode_kernel forms the phase 2^f * x * 3.1415926 in
+// FP32 and adds pi/2 for the cosine: at most ~5e-4 apart at 2^11, below the
+// 16-bit operand rounding).  OneBlob bins more than two
+// bins away from x (circularly) are exactly 0 in encode_kernel's formula and
+// are not evaluated.
+template <int PREC>
+HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float* __restrict__ enc_params, int kb,
+                    int ke, RowPacker<PREC>& pk) {
+  for (int si = 0; si < d.n_segs; ++si) {
+    const EncSeg& s = d.segs[si];
+    const int lo = max(kb, s.out_off), hi = min(ke, s.out_off + s.n_out);
+    if (lo >= hi) continue;
+    const int j0 = lo - s.out_off, j1 = hi - s.out_off;
+    if (s.type == ENC_IDENTITY) {
+      for (int j = j0; j < j1; ++j) pk.push(xin[s.in_off + j]);
+    } else if (s.type == ENC_FREQUENCY) {
+      int u = j0 >> 1;
+      int dim = u / s.n_freq, f = u - dim * s.n_freq;
+      for (int j = j0; j < j1;) {
+        float sn, cs;
+        sincospif(ldexpf(xin[s.in_off + dim], f), &sn, &cs);
+        if (!(j & 1)) {
+          pk.push(sn);
+          ++j;
+        }
+        if (j < j1) {
+          pk.push(cs);
+          ++j;
+        }
+        if (++f == s.n_freq) {
+          f = 0;
+          ++dim;
+        }
+      }
+    } else if (s.type == ENC_ONEBLOB) {
+      // the five bins around x (circularly) are evaluated once per input
+      // dimension, without branches that would diverge across the rows of
+      // a warp; every other bin is 0
+      const float nb = (float)s.n_bins;
+      int dim = j0 / s.n_bins, b = j0 - dim * s.n_bins;
+      int b0 = 0;
+      float wv[5];
+      auto window = [&](int dm) {
+        const float x = xin[s.in_off + dm];
+        // bin of x on the period [0, 1) (x itself may lie outside it)
+        b0 = (((int)floorf(x * nb)) % s.n_bins + s.n_bins) % s.n_bins;
+        const float c0 = oneblob_cdf(0.f, x, nb);
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+          const int wb = ((b0 - 2 + t) % s.n_bins + s.n_bins) % s.n_bins;
+          const float left = wb == 0 ? c0 : oneblob_cdf((float)wb / nb, x, nb);
+          const float right = (wb == s.n_bins - 1) ? c0 + 1.f : oneblob_cdf((float)(wb + 1) / nb, x, nb);
+          wv[t] = right - left;
+        }
+      };
+      window(dim);
+      for (int j = j0; j < j1; ++j) {
+        int dd = b - b0;
+        if (dd > (s.n_bins >> 1)) dd -= s.n_bins;
+        if (dd < -(s.n_bins >> 1)) dd += s.n_bins;
+        float v = 0.f;
+        v = dd == -2 ? wv[0] : v;
+        v = dd == -1 ? wv[1] : v;
+        v = dd == 0 ? wv[2] : v;
+        v = dd == 1 ? wv[3] : v;
+        v = dd == 2 ? wv[4] : v;
+        pk.push(v);
+        if (++b == s.n_bins && j + 1 < j1) {
+          b = 0;
+          ++dim;
+          window(dim);
+        }
+      }
+    } else {  // hash grid
+      const float* table = enc_params + s.param_off;
+      const float px = xin[s.in_off], py = xin[s.in_off + 1], pz = xin[s.in_off + 2];
+      int l = j0 / s.n_feat, f0 = j0 - l * s.n_feat;
+      for (int j = j0; j < j1; ++l) {
+        const float sc = s.level_scale[l];
+        const float fx = fmaf(sc, px, 0.5f), fy = fmaf(sc, py, 0.5f), fz = fmaf(sc, pz, 0.5f);
+        const float gx = floorf(fx), gy = floorf(fy), gz = floorf(fz);
+        const float wx = fx - gx, wy = fy - gy, wz = fz - gz;
+        const uint32_t ix = (uint32_t)(int)gx, iy = (uint32_t)(int)gy, iz = (uint32_t)(int)gz;
+        float acc[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[q] = 0.f;
+        for (int c = 0; c < 8; ++c) {
+          const uint32_t cx = ix + (c & 1), cy = iy + ((c >> 1) & 1), cz = iz + ((c >> 2) & 1);
+          const float w = ((c & 1) ? wx : 1.f - wx) * (((c >> 1) & 1) ? wy : 1.f - wy) *
+                          (((c >> 2) & 1) ? wz : 1.f - wz);
+          const uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
+          const float* tv = table + (int64_t)e * s.n_feat;
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+            if (q < s.n_feat) acc[q] += w * __ldg(tv + q);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          if (q >= f0 && q < s.n_feat && j < j1) {
+            pk.push(acc[q]);
+            ++j;
+          }
+        f0 = 0;
+      }
+    }
   }
-  // hash grid: level l, feature f
-  const int l = j / s.n_feat, f = j % s.n_feat;
-  const float* table = enc_params + s.param_off;
-  const float px = xin[s.in_off], py = xin[s.in_off + 1], pz = xin[s.in_off + 2];
-  const float sc = s.level_scale[l];
-  const float fx = fmaf(sc, px, 0.5f), fy = fmaf(sc, py, 0.5f), fz = fmaf(sc, pz, 0.5f);
-  const float gx = floorf(fx), gy = floorf(fy), gz = floorf(fz);
-  const float wx = fx - gx, wy = fy - gy, wz = fz - gz;
-  const uint32_t ix = (uint32_t)(int)gx, iy = (uint32_t)(int)gy, iz = (uint32_t)(int)gz;
-  float acc = 0.f;
-  for (int c = 0; c < 8; ++c) {
-    const uint32_t cx = ix + (c & 1), cy = iy + ((c >> 1) & 1), cz = iz + ((c >> 2) & 1);
-    const float w = ((c & 1) ? wx : 1.f - wx) * (((c >> 1) & 1) ? wy : 1.f - wy) * (((c >> 2) & 1) ? wz : 1.f - wz);
-    const uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
-    acc += w * __ldg(table + (int64_t)e * s.n_feat + f);
-  }
-  return acc;
+  for (int k = max(kb, d.n_enc); k < ke; ++k) pk.push(k < d.in_pad ? 1.f : 0.f);
 }
 
 // Upper bound of |feature| over the row (E4M3 input scale).
@@ -228,24 +331,31 @@ struct TcArgs {
   int64_t n;
   int* err;  // host-mapped
   int a_bytes;
-  int slack;  // guard band between the weights and the barrier (bytes)
   int ncols;
 };
 
+// 256 threads: thread (warp w, lane i) owns row 32 * (w % 4) + i of the tile
+// (tensor-memory lanes are split by warp quadrant) and half h = w / 4 of the
+// work on that row: every other 16-byte feature group when encoding, and
+// accumulator columns [h * W/2, (h + 1) * W/2) in the epilogues.
 template <int PREC, int W>
-__global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_constant__ TcArgs p) {
+__global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_constant__ TcArgs p) {
   constexpr bool F8 = PREC == TC_E4M3;
   constexpr int EB = F8 ? 1 : 2;       // bytes per element
   constexpr int KI = 32 / EB;          // K per MMA instruction
   constexpr int CK = 16 / EB;          // elements per 16-byte core-matrix row
   constexpr int FMT = PREC == TC_BF16 ? 1 : 0;
+  constexpr int HW = W / 2;            // accumulator columns per half
   extern __shared__ __align__(1024) uint8_t smem[];
   uint8_t* A = smem;
   uint8_t* Wt = smem + p.a_bytes;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(Wt + ((p.blob_bytes + 127) & ~(int64_t)127) + p.slack);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(Wt + ((p.blob_bytes + 127) & ~(int64_t)127));
   uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 1);
+  float* amax_x = reinterpret_cast<float*>(holder + 4);  // [2][128] E4M3 row maxima
 
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = ((warp & 3) << 5) | (tid & 31);
+  const int half = warp >> 2;
   const MlpDims& d = p.d;
   const int L = p.n_layers - 1;  // index of the output layer
 
@@ -261,7 +371,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *holder;
-  const uint32_t row_taddr = tmem + ((uint32_t)(warp * 32) << 16);
+  const uint32_t row_taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   const uint32_t a_base = smem_u32(A), w_base = smem_u32(Wt);
   const uint32_t a_lbo = 16 * kTcRows;
   uint32_t phase = 0;
@@ -292,10 +402,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_
 
   const int64_t n_tiles = (p.n + kTcRows - 1) / kTcRows;
   for (int64_t tile = blockIdx.x; tile < n_tiles && !failed; tile += gridDim.x) {
-    const int64_t q = tile * kTcRows + tid;
+    const int64_t q = tile * kTcRows + row;
     const bool valid = q < p.n;
     const float* xin = p.in + (valid ? q : 0) * d.in_ch;
-    float row_inv = 1.f;  // 1 / activation scale of this thread's A row
+    float row_inv = 1.f;  // 1 / activation scale of this row of A
     float row_scale = 1.f;
     if (F8) {
       const float bound = valid ? enc_row_bound(d, xin, grid_amax) : 1.f;
@@ -306,27 +416,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_
     const int K0 = p.K[0];
     for (int kc = 0; kc < K0 && !failed; kc += p.kc0) {
       const int kn = min(p.kc0, K0 - kc);
-      for (int g = 0; g < kn / CK; ++g) {
-        const int k0 = kc + g * CK;
-        uint32_t word[4];
-        if (F8) {
-#pragma unroll
-          for (int w4 = 0; w4 < 4; ++w4) {
-            float v[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) v[e] = valid ? enc_feature(d, xin, p.enc_params, k0 + 4 * w4 + e) : 0.f;
-            word[w4] = pack4_e4m3(v[0] * row_scale, v[1] * row_scale, v[2] * row_scale, v[3] * row_scale);
-          }
+      {
+        // the two halves of the row: groups [0, G/2) and [G/2, G) of the chunk
+        const int G = kn / CK, gsplit = (G + 1) >> 1;
+        const int g0 = half ? gsplit : 0, g1 = half ? G : gsplit;
+        RowPacker<PREC> pk(A, row, g0, row_scale);
+        if (valid) {
+          enc_range<PREC>(d, xin, p.enc_params, kc + g0 * CK, kc + g1 * CK, pk);
         } else {
-#pragma unroll
-          for (int w2 = 0; w2 < 4; ++w2) {
-            const float a = valid ? enc_feature(d, xin, p.enc_params, k0 + 2 * w2) : 0.f;
-            const float b = valid ? enc_feature(d, xin, p.enc_params, k0 + 2 * w2 + 1) : 0.f;
-            word[w2] = pack2<PREC>(a, b);
-          }
+          for (int k = g0 * CK; k < g1 * CK; ++k) pk.push(0.f);
         }
-        *reinterpret_cast<uint4*>(A + op_offset(kTcRows, tid, g * 16)) =
-            make_uint4(word[0], word[1], word[2], word[3]);
       }
       fence_proxy_async_smem();
       __syncthreads();
@@ -335,44 +434,41 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_
     // ---- hidden epilogues and the following layers
     for (int l = 1; l <= L && !failed; ++l) {
       const float sc = row_inv * w_inv(l - 1);
+      float v[HW];
+#pragma unroll
+      for (int c = 0; c < HW / 16; ++c) {
+        float t[16];
+        tmem_ld16(row_taddr + half * HW + c * 16, t);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) v[c * 16 + e] = fmaxf(F8 ? t[e] * sc : t[e], 0.f);
+      }
       if (F8) {
-        float v[W];
-#pragma unroll
-        for (int c = 0; c < W / 16; ++c) {
-          float t[16];
-          tmem_ld16(row_taddr + c * 16, t);
-#pragma unroll
-          for (int e = 0; e < 16; ++e) v[c * 16 + e] = fmaxf(t[e] * sc, 0.f);
-        }
         float amax = 0.f;
 #pragma unroll
-        for (int e = 0; e < W; ++e) amax = fmaxf(amax, v[e]);
+        for (int e = 0; e < HW; ++e) amax = fmaxf(amax, v[e]);
+        amax_x[half * kTcRows + row] = amax;
+        __syncthreads();
+        amax = fmaxf(amax_x[row], amax_x[kTcRows + row]);
         const float s = amax > 0.f ? kE4M3Max / amax : 1.f;
         row_inv = amax > 0.f ? amax / kE4M3Max : 1.f;
 #pragma unroll
-        for (int g = 0; g < W / 16; ++g) {
+        for (int g = 0; g < HW / 16; ++g) {
           uint32_t word[4];
 #pragma unroll
           for (int w4 = 0; w4 < 4; ++w4)
             word[w4] = pack4_e4m3(v[g * 16 + 4 * w4] * s, v[g * 16 + 4 * w4 + 1] * s, v[g * 16 + 4 * w4 + 2] * s,
                                   v[g * 16 + 4 * w4 + 3] * s);
-          *reinterpret_cast<uint4*>(A + op_offset(kTcRows, tid, g * 16)) =
+          *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, half * HW + g * 16)) =
               make_uint4(word[0], word[1], word[2], word[3]);
         }
       } else {
 #pragma unroll
-        for (int c = 0; c < W / 16; ++c) {
-          float t[16];
-          tmem_ld16(row_taddr + c * 16, t);
+        for (int g = 0; g < HW / 8; ++g) {
+          uint32_t word[4];
 #pragma unroll
-          for (int h = 0; h < 2; ++h) {
-            uint32_t word[4];
-#pragma unroll
-            for (int w2 = 0; w2 < 4; ++w2)
-              word[w2] = pack2<PREC>(fmaxf(t[h * 8 + 2 * w2], 0.f), fmaxf(t[h * 8 + 2 * w2 + 1], 0.f));
-            *reinterpret_cast<uint4*>(A + op_offset(kTcRows, tid, (c * 2 + h) * 16)) =
-                make_uint4(word[0], word[1], word[2], word[3]);
-          }
+          for (int w2 = 0; w2 < 4; ++w2) word[w2] = pack2<PREC>(v[g * 8 + 2 * w2], v[g * 8 + 2 * w2 + 1]);
+          *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, (half * HW + g * 8) * 2)) =
+              make_uint4(word[0], word[1], word[2], word[3]);
         }
       }
       tc_fence_before();
@@ -381,8 +477,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_fwd_kernel(const __grid_
       if (!run_layer(l, 0, p.K[l], false)) failed = true;
     }
     if (failed) break;
-    // ---- output layer accumulator -> out
-    {
+    // ---- output layer accumulator -> out (columns 0..15, first half of the warps)
+    if (half == 0) {
       float t[16];
       tmem_ld16(row_taddr, t);
       const float sc = row_inv * w_inv(L);
@@ -479,7 +575,7 @@ bool tc_supported(const MlpDims& d, int precision, std::string* why) {
     blob += (int64_t)N * K * pk.elem_bytes;
   }
   const int64_t a_min = (int64_t)kTcRows * std::max(KI, d.width) * pk.elem_bytes;
-  if (((blob + 127) & ~127) + a_min + 64 > kTcSmemMax) {
+  if (((blob + 127) & ~127) + a_min + 1152 > kTcSmemMax) {
     if (why) *why = "weights do not fit in shared memory";
     return false;
   }
@@ -536,11 +632,18 @@ template <int PREC, int W>
 static int tc_launch(const TcArgs& a, size_t smem, cudaStream_t st) {
   auto kern = mlp_tc_fwd_kernel<PREC, W>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
   if (e != cudaSuccess) return hm_cuda_status(e, "mlp_tc_fwd_kernel smem");
-  int per_sm = 0, dev = 0, sms = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kTcThreads, smem);
+  int dev = 0, sms = 0, smem_sm = 0, smem_res = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  cudaDeviceGetAttribute(&smem_res, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  cudaFuncAttributes fa;
+  cudaFuncGetAttributes(&fa, kern);
+  int per_sm = smem_sm / (int)(smem + smem_res);
+  per_sm = std::min(per_sm, 65536 / std::max(1, fa.numRegs * kTcThreads));
   per_sm = std::max(1, std::min(per_sm, 512 / a.ncols));  // tensor-memory columns per SM
   const int64_t tiles = (a.n + kTcRows - 1) / kTcRows;
   const int blocks = (int)std::min<int64_t>(tiles, (int64_t)sms * per_sm);
@@ -575,22 +678,21 @@ int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, cons
   // shared memory: A tile + weights (+ guard band when it fits) + barrier
   const int eb = pk.elem_bytes;
   const int64_t wbytes = (pk.bytes + 127) & ~(int64_t)127;
-  const int64_t misc = 64;
-  int64_t slack = kTcSlack;
-  int kc0 = pk.K[0];
+  const int64_t misc = 1152;  // barrier, tensor-memory address, E4M3 row maxima
   auto a_bytes_for = [&](int kc) { return (int64_t)kTcRows * std::max(kc, d.width) * eb; };
-  auto fits = [&](int kc) { return a_bytes_for(kc) + wbytes + slack + misc <= kTcSmemMax; };
-  while (!fits(kc0) && kc0 > pk.kinst) kc0 -= pk.kinst;
-  if (!fits(kc0)) {  // no room for the guard band
-    slack = 0;
+  auto total = [&](int kc) { return a_bytes_for(kc) + wbytes + misc; };
+  // prefer a layer-0 chunk that leaves room for two CTAs per SM
+  const int64_t two_per_sm = 113 * 1024;
+  int kc0 = pk.K[0];
+  while (total(kc0) > two_per_sm && kc0 > pk.kinst) kc0 -= pk.kinst;
+  if (total(kc0) > two_per_sm) {
     kc0 = pk.K[0];
-    while (!fits(kc0) && kc0 > pk.kinst) kc0 -= pk.kinst;
+    while (total(kc0) > kTcSmemMax && kc0 > pk.kinst) kc0 -= pk.kinst;
   }
-  if (!fits(kc0)) return hm_set_error("mlp: tensor-core tile does not fit"), HM_EUNSUPPORTED;
+  if (total(kc0) > kTcSmemMax) return hm_set_error("mlp: tensor-core tile does not fit"), HM_EUNSUPPORTED;
   a.kc0 = kc0;
   a.a_bytes = (int)a_bytes_for(kc0);
-  a.slack = (int)slack;
-  const size_t smem = (size_t)(a.a_bytes + wbytes + slack + misc);
+  const size_t smem = (size_t)(a.a_bytes + wbytes + misc);
   const int W = d.width;
   switch (pk.precision) {
     case HM_PREC_BF16:

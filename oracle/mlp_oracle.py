@@ -153,8 +153,12 @@ def _grid_corners(s, lvl, p):
     return corners
 
 
-def encode(cfg, params, x):
-    """x [n, in_ch] -> X [n, in_pad] float64."""
+def encode(cfg, params, x, exact_phase=False):
+    """x [n, in_ch] -> X [n, in_pad] float64.
+
+    exact_phase: Frequency features as sin / cos of pi * (2^f x) evaluated
+    in float64 without the FP32 rounding of the phase (the tensor-core
+    kernels' sincospif form); default: the FP32 encode kernel's form."""
     x = np.asarray(x, np.float32)
     n = x.shape[0]
     X = np.ones((n, cfg.in_pad))
@@ -169,6 +173,11 @@ def encode(cfg, params, x):
             xs = x[:, s["in_off"]:s["in_off"] + s["n_dims"]]
             for d in range(s["n_dims"]):
                 for f in range(F):
+                    if exact_phase:
+                        y = xs[:, d].astype(np.float64) * 2.0 ** f
+                        X[:, o + (d * F + f) * 2] = np.sin(np.pi * np.mod(y, 2.0))
+                        X[:, o + (d * F + f) * 2 + 1] = np.cos(np.pi * np.mod(y, 2.0))
+                        continue
                     # the phase is formed in FP32 exactly as the kernel does;
                     # only the sine itself is evaluated in FP64
                     a = (xs[:, d] * np.float32(2.0 ** f)).astype(np.float32) * PI

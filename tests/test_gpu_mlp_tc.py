@@ -4,7 +4,8 @@ accumulation.
 Two references on the same parameters and inputs:
   * an emulation of the kernel's rounding in float64 (operands rounded to the
     type exactly where the kernel rounds them, E4M3 with the kernel's
-    per-layer weight and per-query activation scales): the kernel must agree
+    per-layer weight and per-query activation scales, Frequency features
+    from the exact phase as the kernel's sincospif): the kernel must agree
     up to accumulation order, which can flip the rounding of an activation
     that lies on a rounding boundary;
       FP16/BF16: 99.9% of outputs within 3e-3 * rms + 3e-3 * |ref|, all
@@ -66,7 +67,7 @@ def _e4m3(a):
 def emulate(oc, params, x, prec):
     """The kernel's arithmetic in float64 with its roundings."""
     p64 = np.asarray(params, np.float64)
-    X = mo.encode(oc, p64, x).astype(np.float32)
+    X = mo.encode(oc, p64, x, exact_phase=True).astype(np.float32)
     Ws = [w.astype(np.float32) for w in mo.weights(oc, p64)]
     if prec in TORCH_DT:
         dt = TORCH_DT[prec]
@@ -111,7 +112,8 @@ def check_vs_emulation(out, emu, prec):
 # per-output error against the FP64 oracle: rms(error) / rms(ref) at most
 ORACLE_REL = {"fp16": 2e-3, "bf16": 1.5e-2, "fp8": 1.2e-1}
 
-CASES = [("hairmsnn_cache.json", 12, ref_inputs), ("c1_cache_w64.json", 16, c1_inputs)]
+CASES = [("hairmsnn_cache.json", 12, ref_inputs), ("c1_cache_w64.json", 16, c1_inputs),
+         ("c1_cache_w128.json", 16, c1_inputs)]  # width 128: layer 0 in two K chunks
 
 
 @pytest.mark.parametrize("prec", ["bf16", "fp16", "fp8"])

@@ -4,6 +4,12 @@
   python -m hairmsnn_gb300 render [scene.json] [BETA] [--frames N] [--mode msnn|pt]
                                   [--width W --height H] [--out image.pfm] [--stats out.json]
 
+  python -m hairmsnn_gb300 infer [--config c1_cache_w64.json] [--precision fp16]
+                                 [--queries N] [--repeat R]
+
+`infer` times cache-network inference on N synthetic hair-vertex queries
+(16-D: position, angles, h, sigma_a, beta) and prints the time per call.
+
 Without a scene file the built-in straight-hair scene is used.  Frames
 accumulate in FP64; --out writes the average as a little-endian PFM
 (bottom row first, the renderer's own row order).  --stats writes per-frame
@@ -50,7 +56,14 @@ def main(argv=None):
     r.add_argument("--train-records", type=int, default=16384)
     r.add_argument("--out", default=None)
     r.add_argument("--stats", default=None)
+    q = sub.add_parser("infer")
+    q.add_argument("--config", default="c1_cache_w64.json")
+    q.add_argument("--precision", choices=["fp32", "fp16", "bf16", "fp8"], default="fp16")
+    q.add_argument("--queries", type=int, default=1 << 18)
+    q.add_argument("--repeat", type=int, default=1)
     a = ap.parse_args(argv)
+    if a.cmd == "infer":
+        return infer(a)
 
     from . import build, render
     build.build()
@@ -90,6 +103,42 @@ def main(argv=None):
     stats_path = a.stats or cfg.get("integrator", {}).get("stats_output") or None
     if stats_path:
         json.dump({"summary": summary, "frames": log}, open(stats_path, "w"), indent=1)
+    return 0
+
+
+def vertex_queries(n, seed=0):
+    """Synthetic 16-D cache inputs of hair vertices: position in [-1,1]^3,
+    four angles in [0,1], h in [-1,1], sigma_a (0.06, 0.1, 0.2), beta 0.3."""
+    rng = np.random.default_rng(seed)
+    x = np.zeros((n, 16), np.float32)
+    x[:, 0:3] = rng.uniform(-1, 1, (n, 3))
+    x[:, 3:7] = rng.uniform(0, 1, (n, 4))
+    x[:, 7] = rng.uniform(-1, 1, n)
+    x[:, 8:11] = [0.06, 0.1, 0.2]
+    x[:, 11:13] = 0.3
+    return x
+
+
+def infer(a):
+    import torch
+    from . import build, mlp
+    build.build()
+    d = mlp.describe(a.config, 16, 3)
+    net = mlp.TinyMLP(a.config, 16, 3, precision=a.precision, seed=0)
+    x = torch.from_numpy(vertex_queries(a.queries)).cuda()
+    y = torch.empty((a.queries, 3), device="cuda")
+    net.inference(x, y)
+    torch.cuda.synchronize()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for _ in range(a.repeat):
+        net.inference(x, y)
+    t1.record()
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1) / a.repeat
+    print(json.dumps({"config": a.config, "precision": a.precision, "width": d.width, "queries": a.queries,
+                      "ms": round(ms, 4), "queries_per_s": round(a.queries / (ms * 1e-3), 1),
+                      "mean_abs_out": float(y.abs().mean())}))
     return 0
 
 

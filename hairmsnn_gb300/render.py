@@ -447,6 +447,69 @@ class RenderBenchWorkload:
                           f"msnnTrainingPath on {threads} threads + FP64 numpy cache inference and training"}
 
 
+class RenderQualityWorkload(RenderBenchWorkload):
+    """HairMSNN (BETA=1, online cache training) against plain path tracing on
+    the render workload's scene: relMSE of each at 16 spp against a
+    converged PT reference of the same scene, their frame times, and the PT
+    sample count (and time) needed to reach HairMSNN's relMSE, assuming PT's
+    relMSE falls as 1/spp (it is unbiased).  The reference uses frames
+    16 .. 16 + ref_spp of one PT run, so it shares no random numbers with
+    the 16-spp estimates (the path RNG is seeded by the frame index, as in
+    the reference).  One step = one HairMSNN frame, as the render workload."""
+
+    name = "quality"
+    metric = "paths/s at fixed relMSE vs PT (HairMSNN BETA=1, 512x512, 16 spp, online cache training 2^16/frame)"
+
+    def __init__(self, torch, width=512, height=512, train_records=1 << 16, spp=16, ref_spp=1024):
+        super().__init__(torch, width, height, train_records)
+        self.spp, self.ref_spp = spp, ref_spp
+
+    def _timed_frames(self, r, n):
+        torch = self.torch
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(n):
+            r.frame()
+        r.wait()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / n
+
+    def quality(self):
+        spp = self.spp
+        pt = Renderer(self.scene, PT, frames_in_flight=self.frames_in_flight)
+        pt_ms = self._timed_frames(pt, spp)
+        pt_img = pt.read(IMAGE_FINAL)
+        ref_ms = self._timed_frames(pt, self.ref_spp)
+        total = pt.read(IMAGE_FINAL) * (spp + self.ref_spp)
+        ref = (total - pt_img * spp) / self.ref_spp
+        pt.close()
+        ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
+                      frames_in_flight=self.frames_in_flight)
+        ms_ms = self._timed_frames(ms, spp)
+        ms_img = ms.read(IMAGE_FINAL)
+        ms.close()
+        e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
+        eq_spp = spp * e_pt / e_ms
+        return {"spp": spp, "reference_spp": self.ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
+                "msnn": {"relmse": round(e_ms, 6), "ms_per_frame": round(ms_ms, 3),
+                         "paths_per_s": round(self.P / (ms_ms * 1e-3), 1)},
+                "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
+                       "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
+                "pt_spp_for_msnn_relmse": round(eq_spp, 2),
+                "speedup_at_equal_relmse": round(eq_spp * pt_ms / (spp * ms_ms), 3)}
+
+    def roofline(self, seg_ms, pk):
+        out = super().roofline(seg_ms, pk)
+        out["quality"] = self.quality()
+        return out
+
+    def config(self):
+        c = super().config()
+        c["workload"] = "quality: " + c["workload"] + f"; relMSE at {self.spp} spp vs PT {self.ref_spp} spp"
+        return c
+
+
 def _default_cache_config():
     return {
         "loss": {"otype": "RelativeL2Luminance"},

@@ -11,10 +11,19 @@
 //   3. radix sort of the 64-bit keys (cub::DeviceRadixSort, setup only)
 //   4. karras_kernel       binary radix tree (Karras, HPG 2012)
 //   5. refit_kernel        bottom-up child AABBs, second arrival continues
+//   6. wide_gather_kernel / wide_link_kernel
+//                          collapse into 4-wide nodes, breadth first: the
+//                          wide node of binary node r holds r's children,
+//                          each internal child replaced by its own two
+//                          children; wide nodes are numbered level by level
+//                          in the order their parents list them (an
+//                          exclusive scan per level), so the array is the
+//                          same on every run and equals the host build
 //
 // All float arithmetic uses explicitly rounded intrinsics (no contraction),
 // so the node array is bit-identical to a host build of the same algorithm.
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "hm_scene.h"
 
@@ -216,6 +225,128 @@ __global__ void single_leaf_kernel(SceneDev s, float4* nodes, int* prim_of_leaf)
   prim_of_leaf[0] = 0;
 }
 
+// ---- 4-wide collapse
+HM_D void read_child(const float4* nodes, int node, int slot, float* lo, float* hi, int* code) {
+  const float* f = reinterpret_cast<const float*>(nodes + 4 * (int64_t)node);
+  for (int k = 0; k < 3; ++k) {
+    lo[k] = f[6 * slot + k];
+    hi[k] = f[6 * slot + 3 + k];
+  }
+  *code = __float_as_int(f[12 + slot]);
+}
+
+// One thread per wide node of the level (binary root roots[i]).  Writes the
+// boxes and leaf codes; internal children keep their binary index for now
+// (wide_link_kernel renumbers them) and are counted in n_internal[i].
+__global__ void wide_gather_kernel(const float4* __restrict__ bnodes, const int* __restrict__ roots, int n, int wbase,
+                                   float4* __restrict__ wnodes, int* __restrict__ n_internal) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = roots[i];
+  float lo[4][3], hi[4][3];
+  int code[4];
+  int k = 0, ni = 0;
+  for (int slot = 0; slot < 2; ++slot) {
+    float l[3], h[3];
+    int c;
+    read_child(bnodes, r, slot, l, h, &c);
+    if (c < 0) {
+      for (int a = 0; a < 3; ++a) { lo[k][a] = l[a]; hi[k][a] = h[a]; }
+      code[k++] = c;
+    } else {
+      for (int s2 = 0; s2 < 2; ++s2) {
+        int c2;
+        read_child(bnodes, c, s2, lo[k], hi[k], &c2);
+        code[k++] = c2;
+        ni += c2 >= 0;
+      }
+    }
+  }
+  for (; k < 4; ++k) {
+    for (int a = 0; a < 3; ++a) lo[k][a] = hi[k][a] = INFINITY;
+    code[k] = -1;
+  }
+  float* w = reinterpret_cast<float*>(wnodes + 8 * (int64_t)(wbase + i));
+  for (int j = 0; j < 4; ++j) {
+    w[0 + j] = lo[j][0];
+    w[4 + j] = hi[j][0];
+    w[8 + j] = lo[j][1];
+    w[12 + j] = hi[j][1];
+    w[16 + j] = lo[j][2];
+    w[20 + j] = hi[j][2];
+    w[24 + j] = __int_as_float(code[j]);
+    w[28 + j] = 0.f;
+  }
+  n_internal[i] = ni;
+}
+
+// Internal children of wide node wbase + i become the wide nodes
+// next_base + offs[i] + 0, 1, ... (in slot order) and the next level's roots.
+__global__ void wide_link_kernel(const int* __restrict__ offs, int n, int wbase, int next_base, float4* __restrict__ wnodes,
+                                 int* __restrict__ next_roots) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int* child = reinterpret_cast<int*>(wnodes + 8 * (int64_t)(wbase + i) + 6);
+  int m = offs[i];
+  for (int j = 0; j < 4; ++j) {
+    const int c = child[j];
+    if (c >= 0) {
+      next_roots[m] = c;
+      child[j] = next_base + m;
+      ++m;
+    }
+  }
+}
+
+int build_wide(Scene& sc, cudaStream_t st) {
+  const int n_int = std::max(1, sc.n_prims() - 1);
+  cudaFree(sc.d_wnodes);
+  sc.d_wnodes = nullptr;
+  sc.n_wnodes = 0;
+  int *ra = nullptr, *rb = nullptr, *cnt = nullptr, *offs = nullptr;
+  void* tmp = nullptr;
+  size_t tmp_bytes = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, cnt, offs, n_int + 1, st);
+  cudaError_t e = cudaMalloc(&sc.d_wnodes, (size_t)n_int * 8 * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&ra, n_int * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&rb, n_int * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&cnt, (n_int + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&offs, (n_int + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&tmp, tmp_bytes);
+  int status = HM_OK;
+  if (e != cudaSuccess) {
+    status = hm_cuda_status(e, "wide bvh alloc");
+  } else {
+    const int zero = 0;
+    cudaMemcpyAsync(ra, &zero, sizeof(int), cudaMemcpyHostToDevice, st);
+    int wbase = 0, n = 1;
+    for (int level = 0; n > 0 && status == HM_OK; ++level) {
+      if (wbase + n > n_int) {
+        hm_set_error("wide bvh: node count overflow");
+        status = HM_ECAPACITY;
+        break;
+      }
+      wide_gather_kernel<<<(n + 255) / 256, 256, 0, st>>>(sc.d_nodes, ra, n, wbase, sc.d_wnodes, cnt);
+      cudaMemsetAsync(cnt + n, 0, sizeof(int), st);
+      cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, cnt, offs, n + 1, st);
+      wide_link_kernel<<<(n + 255) / 256, 256, 0, st>>>(offs, n, wbase, wbase + n, sc.d_wnodes, rb);
+      int next = 0;
+      e = cudaMemcpyAsync(&next, offs + n, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) {
+        status = hm_cuda_status(e, "wide bvh level");
+        break;
+      }
+      wbase += n;
+      n = next;
+      std::swap(ra, rb);
+    }
+    sc.n_wnodes = wbase;
+  }
+  cudaFree(ra); cudaFree(rb); cudaFree(cnt); cudaFree(offs); cudaFree(tmp);
+  return status;
+}
+
 int Scene::build_bvh(cudaStream_t st) {
   const int n = n_prims();
   if (n <= 0) return hm_set_error("scene has no primitives"), HM_EINVAL;
@@ -233,7 +364,7 @@ int Scene::build_bvh(cudaStream_t st) {
     sd.nodes = d_nodes;
     single_leaf_kernel<<<1, 1, 0, st>>>(sd, d_nodes, d_prim_of_leaf);
     HM_CHECK_LAUNCH("single_leaf_kernel");
-    return HM_OK;
+    return build_wide(*this, st);
   }
   const int nb = std::min(1024, (n + 255) / 256);
   float* bb = nullptr;
@@ -270,6 +401,7 @@ int Scene::build_bvh(cudaStream_t st) {
   }
   cudaFree(bb); cudaFree(keys); cudaFree(keys_sorted); cudaFree(child);
   cudaFree(par_i); cudaFree(par_l); cudaFree(cnt); cudaFree(tmp);
+  if (status == HM_OK) status = build_wide(*this, st);
   return status;
 }
 

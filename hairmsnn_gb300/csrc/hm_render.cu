@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int n = src.n();
-  int stack[kStack];
+  int2 stack[kStack];
   TravState t;
   TraceCount tc{0, 0};
   uint32_t rays = 0;

@@ -396,7 +396,7 @@ int Scene::upload() {
 Scene::~Scene() {
   cudaFree(d_cp); cudaFree(d_seg); cudaFree(d_vtx); cudaFree(d_nrm); cudaFree(d_tri);
   cudaFree(d_env); cudaFree(d_cpdf); cudaFree(d_ccdf); cudaFree(d_mpdf); cudaFree(d_mcdf);
-  cudaFree(d_dlights); cudaFree(d_nodes); cudaFree(d_prim_of_leaf);
+  cudaFree(d_dlights); cudaFree(d_nodes); cudaFree(d_prim_of_leaf); cudaFree(d_wnodes);
 }
 
 SceneDev Scene::dev() const {
@@ -415,6 +415,8 @@ SceneDev Scene::dev() const {
   d.nodes = d_nodes;
   d.n_nodes = n_nodes;
   d.prim_of_leaf = d_prim_of_leaf;
+  d.wnodes = d_wnodes;
+  d.n_wnodes = n_wnodes;
   d.has_env = has_env;
   d.env_pdf_sampling = env_pdf;
   d.env = d_env;
@@ -501,6 +503,7 @@ extern "C" int hm_scene_info(const hm_scene* h, hm_scene_desc* out) {
   out->n_vertices = (int)s->vtx.size();
   out->n_triangles = (int)s->tri.size();
   out->n_bvh_nodes = s->n_nodes;
+  out->n_bvh_wide_nodes = s->n_wnodes;
   out->width = s->width;
   out->height = s->height;
   out->spp = s->spp;
@@ -545,6 +548,7 @@ extern "C" int64_t hm_scene_export_size(const hm_scene* h, int which) {
     case HM_SCENE_DIR_LIGHTS: return (int64_t)s->dlights.size() * 4;
     case HM_SCENE_BVH_NODES: return (int64_t)s->n_nodes * 64;
     case HM_SCENE_BVH_LEAVES: return (int64_t)s->n_prims() * 4;
+    case HM_SCENE_BVH_WIDE_NODES: return (int64_t)s->n_wnodes * 128;
     case HM_SCENE_CAMERA: return 12 * 4;
     case HM_SCENE_MATERIALS: return 16 * 4;
     default: return -1;
@@ -567,11 +571,14 @@ extern "C" int hm_scene_export(const hm_scene* h, int which, void* out, int64_t 
     case HM_SCENE_ENV_MCDF: return export_vec(s->mcdf, out, cap);
     case HM_SCENE_DIR_LIGHTS: return export_vec(s->dlights, out, cap);
     case HM_SCENE_BVH_NODES:
-    case HM_SCENE_BVH_LEAVES: {
+    case HM_SCENE_BVH_LEAVES:
+    case HM_SCENE_BVH_WIDE_NODES: {
       if (!s->built) return hm_set_error("hm_scene_export: call hm_scene_build first"), HM_EINVAL;
-      int64_t bytes = which == HM_SCENE_BVH_NODES ? (int64_t)s->n_nodes * 64 : (int64_t)s->n_prims() * 4;
+      int64_t bytes = which == HM_SCENE_BVH_NODES ? (int64_t)s->n_nodes * 64
+                      : which == HM_SCENE_BVH_LEAVES ? (int64_t)s->n_prims() * 4 : (int64_t)s->n_wnodes * 128;
       if (cap < bytes) return hm_set_error("hm_scene_export: buffer too small"), HM_ECAPACITY;
-      const void* src = which == HM_SCENE_BVH_NODES ? (const void*)s->d_nodes : (const void*)s->d_prim_of_leaf;
+      const void* src = which == HM_SCENE_BVH_NODES ? (const void*)s->d_nodes
+                        : which == HM_SCENE_BVH_LEAVES ? (const void*)s->d_prim_of_leaf : (const void*)s->d_wnodes;
       if (!bytes) return HM_OK;
       cudaError_t e = cudaMemcpy(out, src, bytes, cudaMemcpyDeviceToHost);
       return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_scene_export bvh");

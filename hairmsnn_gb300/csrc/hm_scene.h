@@ -36,6 +36,11 @@ struct SceneDev {
   const float4* nodes;  // 4 float4 per node
   int n_nodes;
   const int* prim_of_leaf;  // leaf slot -> primitive id
+  // the same tree collapsed to 4-wide nodes (what the traversal walks):
+  // 8 float4 per node, lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
+  // child[4] (>= 0 wide node, < 0 leaf ~slot), padding
+  const float4* wnodes;
+  int n_wnodes;
   // environment (lat-long, z up) and its sampling tables
   int has_env, env_pdf_sampling;
   const float4* env;
@@ -98,6 +103,8 @@ struct Scene {
   float4* d_nodes = nullptr;
   int* d_prim_of_leaf = nullptr;
   int n_nodes = 0;
+  float4* d_wnodes = nullptr;
+  int n_wnodes = 0;
   bool built = false;
 
   ~Scene();

@@ -2,11 +2,13 @@
 // round-cubic curve and triangle intersectors, which the reference reaches
 // through owl::traceRay in hair_msnn.cu:62 and optix_common.cuh:189,257).
 //
-// Node layout (64 B, 4 x float4): child 0 AABB, child 1 AABB, child indices
-// (>= 0 internal node, < 0 leaf slot ~i).  A stack of 64 entries per ray; a
-// ray whose stack would overflow or whose node count passes a fixed cap is
-// reported through the error word instead of looping or writing out of
-// bounds.
+// The kernels walk the LBVH collapsed to 4-wide nodes (128 B, 8 x float4:
+// lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] padding; child
+// >= 0 wide node, < 0 leaf slot ~i; empty slots hold a box that every ray
+// misses).  Children hit are visited nearest first; the others go on a
+// 96-entry stack with their entry distance.  A ray whose stack would
+// overflow or whose visit count passes a fixed cap is reported through the
+// error word instead of looping or writing out of bounds.
 //
 // Curves: uniform cubic B-spline segments (4 control points with radius).
 // The intersector transforms the segment's Bezier control points into ray
@@ -33,7 +35,7 @@ struct Hit {
 };
 
 enum { TRACE_ERR_STACK = 1, TRACE_ERR_STEPS = 2 };
-constexpr int kStack = 64;
+constexpr int kStack = 96;  // (child, distance) entries of the 4-wide traversal
 constexpr int kMaxVisits = 1 << 20;
 
 
@@ -149,37 +151,6 @@ HM_D bool curve_intersect(const SceneDev& s, int seg_idx, const Ray& r, float tm
   return found;
 }
 
-HM_D f3 safe_inv(f3 d) {
-  auto inv = [](float x) { return fabsf(x) > 1e-20f ? 1.f / x : copysignf(1e20f, x); };
-  return mk(inv(d.x), inv(d.y), inv(d.z));
-}
-
-// Slab test of both children of a node; returns entry distances (inf: miss).
-HM_D void node_test(const float4* nodes, int ni, const f3& o, const f3& inv, float tmin, float tmax, float* t0,
-                    float* t1, int* c0, int* c1) {
-  const float4 a = __ldg(nodes + 4 * ni), b = __ldg(nodes + 4 * ni + 1), c = __ldg(nodes + 4 * ni + 2),
-               d = __ldg(nodes + 4 * ni + 3);
-  // child 0: lo (a.x, a.y, a.z) hi (a.w, b.x, b.y); child 1: lo (b.z, b.w, c.x) hi (c.y, c.z, c.w)
-  {
-    float tx0 = (a.x - o.x) * inv.x, tx1 = (a.w - o.x) * inv.x;
-    float ty0 = (a.y - o.y) * inv.y, ty1 = (b.x - o.y) * inv.y;
-    float tz0 = (a.z - o.z) * inv.z, tz1 = (b.y - o.z) * inv.z;
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-    *t0 = tn <= tf ? tn : INFINITY;
-  }
-  {
-    float tx0 = (b.z - o.x) * inv.x, tx1 = (c.y - o.x) * inv.x;
-    float ty0 = (b.w - o.y) * inv.y, ty1 = (c.z - o.y) * inv.y;
-    float tz0 = (c.x - o.z) * inv.z, tz1 = (c.w - o.z) * inv.z;
-    float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-    *t1 = tn <= tf ? tn : INFINITY;
-  }
-  *c0 = __float_as_int(d.x);
-  *c1 = __float_as_int(d.y);
-}
-
 HM_D bool prim_intersect(const SceneDev& s, int prim, const Ray& r, float tmax, float* t, float* u, float* v) {
   if (prim < s.n_seg) {
     *v = 0.f;
@@ -193,9 +164,48 @@ struct TraceCount {
   uint32_t nodes, prims;
 };
 
-// Resumable traversal: one node visit per trav_step(), so a persistent
-// kernel can hand a lane a new ray as soon as its previous ray finishes
-// (dynamic ray fetching, Aila & Laine, HPG 2009).
+// Slab test of the four children of wide node ni: entry distance per child
+// (INFINITY: missed or empty slot) and the child codes.
+HM_D void wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, float tmin, float tmax, float (&t)[4],
+                     int (&c)[4]) {
+  const float4* p = wn + 8 * (int64_t)ni;
+  const float4 lx = __ldg(p), hx = __ldg(p + 1), ly = __ldg(p + 2), hy = __ldg(p + 3), lz = __ldg(p + 4),
+               hz = __ldg(p + 5);
+  const int4 ch = __ldg(reinterpret_cast<const int4*>(p + 6));
+  const float alx[4] = {lx.x, lx.y, lx.z, lx.w}, ahx[4] = {hx.x, hx.y, hx.z, hx.w};
+  const float aly[4] = {ly.x, ly.y, ly.z, ly.w}, ahy[4] = {hy.x, hy.y, hy.z, hy.w};
+  const float alz[4] = {lz.x, lz.y, lz.z, lz.w}, ahz[4] = {hz.x, hz.y, hz.z, hz.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const float tx0 = (alx[k] - o.x) * inv.x, tx1 = (ahx[k] - o.x) * inv.x;
+    const float ty0 = (aly[k] - o.y) * inv.y, ty1 = (ahy[k] - o.y) * inv.y;
+    const float tz0 = (alz[k] - o.z) * inv.z, tz1 = (ahz[k] - o.z) * inv.z;
+    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
+    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
+    t[k] = tn <= tf ? tn : INFINITY;
+  }
+  c[0] = ch.x;
+  c[1] = ch.y;
+  c[2] = ch.z;
+  c[3] = ch.w;
+}
+
+HM_D void cswap(float (&t)[4], int (&c)[4], int i, int j) {
+  if (t[j] < t[i]) {
+    const float tt = t[i];
+    t[i] = t[j];
+    t[j] = tt;
+    const int cc = c[i];
+    c[i] = c[j];
+    c[j] = cc;
+  }
+}
+
+// Resumable traversal of the 4-wide tree: one node visit per inner step, so
+// a persistent kernel can hand a lane a new ray as soon as its previous ray
+// finishes (dynamic ray fetching, Aila & Laine, HPG 2009).  The stack holds
+// (child code, entry distance) pairs; entries beyond the closest hit found
+// so far are dropped when popped.
 struct TravState {
   f3 o, d, inv;
   float tmin;
@@ -220,61 +230,71 @@ HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
   t.pend = -1;
 }
 
-HM_D bool prim_intersect(const SceneDev& s, int prim, const Ray& r, float tmax, float* t, float* u, float* v);
-
 // Leaf-postponing traversal ("while-while", Aila & Laine 2009): an inner
 // step only walks boxes; a leaf reached is parked (t.pend = leaf slot) and
 // tested later together with the other lanes' parked leaves, so the expensive
 // curve test runs with most lanes of the warp active.
-//   t.node >= 0: next internal node to visit; t.node < 0: pop next.
+//   t.node >= 0: next wide node to visit; t.node < 0: pop next.
 //   A lane needs inner steps while nothing is parked and work remains.
 HM_D bool trav_needs_step(const TravState& t) { return t.pend < 0 && (t.node >= 0 || t.sp > 0); }
 HM_D bool trav_finished(const TravState& t) { return t.pend < 0 && t.node < 0 && t.sp == 0; }
 
 template <bool COUNT>
-HM_D void trav_inner_step(const SceneDev& s, TravState& t, int* stack, int* err, TraceCount* cnt) {
+HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err, TraceCount* cnt) {
   if (++t.visits > kMaxVisits) {
     atomicOr(err, TRACE_ERR_STEPS);
     t.node = -1;
     t.sp = 0;
     return;
   }
-  int cur = t.node >= 0 ? t.node : stack[--t.sp];
-  if (cur < 0) {  // a leaf left on the stack
-    t.pend = ~cur;
+  int cur;
+  if (t.node >= 0) {
+    cur = t.node;
+  } else {
+    bool popped = false;
+    cur = 0;
+    while (t.sp > 0) {
+      const int2 e = stack[--t.sp];
+      if (__int_as_float(e.y) > t.h.t) continue;
+      cur = e.x;
+      popped = true;
+      break;
+    }
+    if (!popped) return;  // finished
+    if (cur < 0) {        // a leaf left on the stack
+      t.pend = ~cur;
+      return;
+    }
+  }
+  float tt[4];
+  int cc[4];
+  wnode_test(s.wnodes, cur, t.o, t.inv, t.tmin, t.h.t, tt, cc);
+  if (COUNT) cnt->nodes += 1;
+  // ascending by entry distance (misses sort last)
+  cswap(tt, cc, 0, 1);
+  cswap(tt, cc, 2, 3);
+  cswap(tt, cc, 0, 2);
+  cswap(tt, cc, 1, 3);
+  cswap(tt, cc, 1, 2);
+  const int hits = (tt[0] < INFINITY) + (tt[1] < INFINITY) + (tt[2] < INFINITY) + (tt[3] < INFINITY);
+  if (hits == 0) {
     t.node = -1;
     return;
   }
-  float t0, t1;
-  int c0, c1;
-  node_test(s.nodes, cur, t.o, t.inv, t.tmin, t.h.t, &t0, &t1, &c0, &c1);
-  if (COUNT) cnt->nodes += 1;
-  const bool go0 = t0 < INFINITY, go1 = t1 < INFINITY;
-  int next = 0;
-  bool have = true;
-  if (go0 && go1) {
-    if (t.sp >= kStack) {
-      atomicOr(err, TRACE_ERR_STACK);
-      t.node = -1;
-      t.sp = 0;
-      return;
-    }
-    stack[t.sp++] = t0 <= t1 ? c1 : c0;
-    next = t0 <= t1 ? c0 : c1;
-  } else if (go0) {
-    next = c0;
-  } else if (go1) {
-    next = c1;
-  } else {
-    have = false;
+  if (t.sp + hits - 1 > kStack) {
+    atomicOr(err, TRACE_ERR_STACK);
+    t.node = -1;
+    t.sp = 0;
+    return;
   }
-  if (!have) {
-    t.node = -1;
-  } else if (next < 0) {
-    t.pend = ~next;
+#pragma unroll
+  for (int k = 3; k >= 1; --k)
+    if (k < hits) stack[t.sp++] = make_int2(cc[k], __float_as_int(tt[k]));
+  if (cc[0] < 0) {
+    t.pend = ~cc[0];
     t.node = -1;
   } else {
-    t.node = next;
+    t.node = cc[0];
   }
 }
 
@@ -291,120 +311,6 @@ HM_D bool trav_leaf(const SceneDev& s, TravState& t, TraceCount* cnt) {
     if (ANY_HIT) return true;
   }
   return false;
-}
-
-// Returns true when the ray is finished (result in t.h).
-template <bool ANY_HIT, bool COUNT>
-HM_D bool trav_step(const SceneDev& s, TravState& t, int* stack, int* err, TraceCount* cnt) {
-  if (++t.visits > kMaxVisits) {
-    atomicOr(err, TRACE_ERR_STEPS);
-    return true;
-  }
-  const Ray r{t.o, t.d, t.tmin, t.h.t};
-  float t0, t1;
-  int c0, c1;
-  node_test(s.nodes, t.node, t.o, t.inv, t.tmin, t.h.t, &t0, &t1, &c0, &c1);
-  if (COUNT) cnt->nodes += 1;
-  if (COUNT) cnt->prims += (c0 < 0 && t0 < INFINITY) + (c1 < 0 && t1 < INFINITY);
-  if (c0 < 0 && t0 < INFINITY) {
-    float th, u, v;
-    const int prim = __ldg(s.prim_of_leaf + ~c0);
-    if (prim_intersect(s, prim, r, t.h.t, &th, &u, &v)) {
-      t.h = Hit{th, prim, u, v};
-      if (ANY_HIT) return true;
-    }
-    t0 = INFINITY;
-    if (t1 > t.h.t) t1 = INFINITY;
-  }
-  if (c1 < 0 && t1 < INFINITY) {
-    float th, u, v;
-    const int prim = __ldg(s.prim_of_leaf + ~c1);
-    if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v)) {
-      t.h = Hit{th, prim, u, v};
-      if (ANY_HIT) return true;
-    }
-    t1 = INFINITY;
-    if (t0 > t.h.t) t0 = INFINITY;
-  }
-  const bool go0 = t0 < INFINITY, go1 = t1 < INFINITY;
-  if (go0 && go1) {
-    if (t.sp >= kStack) {
-      atomicOr(err, TRACE_ERR_STACK);
-      return true;
-    }
-    stack[t.sp++] = t0 <= t1 ? c1 : c0;
-    t.node = t0 <= t1 ? c0 : c1;
-  } else if (go0) {
-    t.node = c0;
-  } else if (go1) {
-    t.node = c1;
-  } else {
-    if (t.sp == 0) return true;
-    t.node = stack[--t.sp];
-  }
-  return false;
-}
-
-// ANY_HIT == true: return at the first hit in (tmin, tmax) (shadow rays).
-template <bool ANY_HIT, bool COUNT = false>
-HM_D Hit trace(const SceneDev& s, const Ray& r, int* err, TraceCount* cnt = nullptr) {
-  Hit h{r.tmax, -1, 0.f, 0.f};
-  const f3 inv = safe_inv(r.d);
-  int stack[kStack];
-  int sp = 0;
-  int node = 0;
-  int visits = 0;
-  for (;;) {
-    if (++visits > kMaxVisits) {
-      atomicOr(err, TRACE_ERR_STEPS);
-      return h;
-    }
-    float t0, t1;
-    int c0, c1;
-    node_test(s.nodes, node, r.o, inv, r.tmin, h.t, &t0, &t1, &c0, &c1);
-    if (COUNT) cnt->nodes += 1;
-    if (COUNT) cnt->prims += (c0 < 0 && t0 < INFINITY) + (c1 < 0 && t1 < INFINITY);
-    // leaves first
-    if (c0 < 0 && t0 < INFINITY) {
-      float t, u, v;
-      int prim = __ldg(s.prim_of_leaf + ~c0);
-      if (prim_intersect(s, prim, r, h.t, &t, &u, &v)) {
-        h = Hit{t, prim, u, v};
-        if (ANY_HIT) return h;
-      }
-      t0 = INFINITY;
-      if (t1 > h.t) t1 = INFINITY;
-    }
-    if (c1 < 0 && t1 < INFINITY) {
-      float t, u, v;
-      int prim = __ldg(s.prim_of_leaf + ~c1);
-      if (prim_intersect(s, prim, r, h.t, &t, &u, &v)) {
-        h = Hit{t, prim, u, v};
-        if (ANY_HIT) return h;
-      }
-      t1 = INFINITY;
-      if (t0 > h.t) t0 = INFINITY;
-    }
-    const bool go0 = t0 < INFINITY, go1 = t1 < INFINITY;
-    if (go0 && go1) {
-      int near = t0 <= t1 ? c0 : c1, far = t0 <= t1 ? c1 : c0;
-      if (sp >= kStack) {
-        atomicOr(err, TRACE_ERR_STACK);
-        return h;
-      }
-      stack[sp++] = far;
-      node = near;
-    } else if (go0) {
-      node = c0;
-    } else if (go1) {
-      node = c1;
-    } else {
-      // pop, skipping entries beyond the current closest hit is not possible
-      // without their distances; they are re-tested (cheap, child boxes inline)
-      if (sp == 0) return h;
-      node = stack[--sp];
-    }
-  }
 }
 
 }  // namespace hm

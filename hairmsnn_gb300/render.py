@@ -16,12 +16,12 @@ from ._ffi import check, lib
 
 HM_SCENE = dict(control_points=0, segments=1, vertices=2, normals=3, triangles=4, env=5, env_cpdf=6,
                 env_ccdf=7, env_mpdf=8, env_mcdf=9, dir_lights=10, bvh_nodes=11, bvh_leaves=12, camera=13,
-                materials=14)
+                materials=14, bvh_wide_nodes=15)
 DTYPES = dict(control_points=(np.float32, 4), segments=(np.int32, 1), vertices=(np.float32, 3),
               normals=(np.float32, 3), triangles=(np.int32, 3), env=(np.float32, 4), env_cpdf=(np.float32, 1),
               env_ccdf=(np.float32, 1), env_mpdf=(np.float32, 1), env_mcdf=(np.float32, 1),
               dir_lights=(np.float32, 6), bvh_nodes=(np.float32, 16), bvh_leaves=(np.int32, 1),
-              camera=(np.float32, 12), materials=(np.float32, 16))
+              camera=(np.float32, 12), materials=(np.float32, 16), bvh_wide_nodes=(np.float32, 32))
 PT, MSNN = 0, 1
 IMAGE_FINAL, IMAGE_SHORT, IMAGE_CACHE = 0, 1, 2
 
@@ -31,7 +31,7 @@ class hm_scene_desc(ctypes.Structure):
         "n_strands", "n_control_points", "n_segments", "n_vertices", "n_triangles", "n_bvh_nodes", "width",
         "height", "spp", "path_v1", "path_v2", "env_width", "env_height", "n_dir_lights", "mis", "env_pdf",
         "has_env", "shading_catrom")] + [("scene_scale", ctypes.c_float), ("bounds_min", ctypes.c_float * 3),
-                       ("bounds_max", ctypes.c_float * 3)]
+                       ("bounds_max", ctypes.c_float * 3), ("n_bvh_wide_nodes", ctypes.c_int)]
 
 
 class hm_render_options(ctypes.Structure):
@@ -267,7 +267,7 @@ def straight_hair_scene(width=512, height=512, strands=10000, control_points=64,
 
 
 RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
-NODE_BYTES = 64               # one BVH node: both child boxes + child indices
+NODE_BYTES = 128              # one 4-wide BVH node: four child boxes + child codes
 PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
 # DRAM bytes per extension ray of the extension traversal kernel, from ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum) over every launch of two
@@ -395,7 +395,7 @@ class RenderBenchWorkload:
                         "traffic": (int(rays * EXTEND_DRAM_BYTES_PER_RAY) if dominant == "extend_ms" else None),
                         "traffic_basis": "DRAM bytes per frame: ncu cold-cache capture at 256x256 scaled by rays",
                         "algorithmic_bytes_per_frame": int(alg),
-                        "note": ("algorithmic bytes = rays x 48 B + BVH nodes visited x 64 B + primitives "
+                        "note": ("algorithmic bytes = rays x 48 B + 4-wide BVH nodes visited x 128 B + primitives "
                                  "tested x 64 B, counted in an untimed frame; the 40 MB BVH and 10 MB of curves "
                                  "are L2-resident, so this can exceed the HBM copy peak ("
                                  + pk["source"] + ")")})

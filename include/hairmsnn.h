@@ -201,6 +201,7 @@ typedef struct hm_scene_desc {
   int shading_catrom; /* 1: curves shaded as Catmull-Rom (reference closest-hit quirk) */
   float scene_scale;
   float bounds_min[3], bounds_max[3];
+  int n_bvh_wide_nodes; /* 4-wide nodes traversed by the kernels (0 before the build) */
 } hm_scene_desc;
 
 enum hm_scene_array {
@@ -218,7 +219,10 @@ enum hm_scene_array {
   HM_SCENE_BVH_NODES = 11,     /* 64 bytes each: child AABBs + child indices */
   HM_SCENE_BVH_LEAVES = 12,    /* int32 primitive of each leaf slot */
   HM_SCENE_CAMERA = 13,        /* pos, dir_00, dir_du, dir_dv (12 floats) */
-  HM_SCENE_MATERIALS = 14      /* 16 floats: hair params, diffuse, alpha, env scale/rotation */
+  HM_SCENE_MATERIALS = 14,     /* 16 floats: hair params, diffuse, alpha, env scale/rotation */
+  HM_SCENE_BVH_WIDE_NODES = 15 /* 128 bytes each: lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
+                                  child[4] (>= 0 wide node, < 0 leaf ~slot) + 16 bytes of padding;
+                                  empty slots hold the box [+inf, +inf] */
 };
 
 /* Host-only: parses and generates (no device work). */

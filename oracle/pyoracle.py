@@ -194,6 +194,58 @@ class OracleScene:
         return color, nn_in, train, flags
 
 
+def wide_collapse(nodes):
+    """The 4-wide tree the kernels traverse, built from the binary LBVH
+    (nodes [n, 16] float32: child-0 box, child-1 box, child codes) the way
+    the library collapses it: breadth first, the wide node of binary node r
+    holds r's children with every internal child replaced by its own two
+    children; wide nodes are numbered level by level in the order their
+    parents list them.  Returns [n_wide, 32] float32: lo.x[4] hi.x[4]
+    lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] (int bits; >= 0 wide node,
+    < 0 leaf ~slot, -1 in empty slots whose box is [+inf, +inf]) padding."""
+    nodes = np.ascontiguousarray(nodes, np.float32)
+    codes = nodes.view(np.int32)[:, 12:14]
+    boxes = nodes[:, :12].reshape(-1, 2, 6)
+    out = []
+    roots = np.array([0], np.int64)
+    base = 0
+    while len(roots):
+        n = len(roots)
+        lo = np.full((n, 4, 3), np.inf, np.float32)
+        hi = np.full((n, 4, 3), np.inf, np.float32)
+        kc = np.full((n, 4), -1, np.int32)
+        k = np.zeros(n, np.int64)
+        rows = np.arange(n)
+        for slot in (0, 1):
+            c = codes[roots, slot]
+            leaf = c < 0
+            i = rows[leaf]
+            lo[i, k[i]] = boxes[roots[i], slot, :3]
+            hi[i, k[i]] = boxes[roots[i], slot, 3:]
+            kc[i, k[i]] = c[leaf]
+            k[i] += 1
+            i = rows[~leaf]
+            ci = c[~leaf]
+            for s2 in (0, 1):
+                lo[i, k[i]] = boxes[ci, s2, :3]
+                hi[i, k[i]] = boxes[ci, s2, 3:]
+                kc[i, k[i]] = codes[ci, s2]
+                k[i] += 1
+        internal = kc >= 0
+        nxt = kc[internal].astype(np.int64)
+        kc = kc.copy()
+        kc[internal] = base + n + np.arange(len(nxt), dtype=np.int32)
+        w = np.zeros((n, 32), np.float32)
+        for a in range(3):
+            w[:, 8 * a:8 * a + 4] = lo[:, :, a]
+            w[:, 8 * a + 4:8 * a + 8] = hi[:, :, a]
+        w[:, 24:28] = kc.view(np.float32)
+        out.append(w)
+        base += n
+        roots = nxt
+    return np.concatenate(out)
+
+
 def env_tables(env, w, h):
     """generateEnvSamplingTables (scene.cpp:349-425), single precision, order kept."""
     env = np.asarray(env, np.float32).reshape(h, w, 4)

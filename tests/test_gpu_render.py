@@ -1,6 +1,7 @@
 """GPU parity of the scene LBVH, traversal and wavefront integrator.
 
-* BVH: device node array == the oracle's host build, bit for bit.
+* BVH: device node array == the oracle's host build, bit for bit; so is
+  the 4-wide collapse the kernels traverse.
 * Traversal: same closest primitive for >= 99.5% of rays; t within
   1e-4 relative where the primitive matches (the device contracts
   multiply-adds in traversal; the oracle does not).
@@ -44,6 +45,9 @@ def test_bvh_matches_host_build_bit_exact(R, strands):
     on, ol = o.bvh()
     assert np.array_equal(leaves, ol)
     assert np.array_equal(nodes.view(np.uint32), on.view(np.uint32))
+    wide = s.export("bvh_wide_nodes")
+    assert s.info().n_bvh_wide_nodes == wide.shape[0]
+    assert np.array_equal(wide.view(np.uint32), po.wide_collapse(on).view(np.uint32))
 
 
 def camera_rays(o, cfg, res):

@@ -91,6 +91,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int n = src.n();
+  if (n <= 0) return;  // an empty bounce: no ray-fetch atomics at all
   int2 stack[kStack];
   TravState t;
   TraceCount tc{0, 0};
@@ -222,8 +223,9 @@ constexpr int kScanBlock = 1024;
 __global__ void __launch_bounds__(kScanBlock) scan_count_kernel(const int* __restrict__ keep, const int* __restrict__ count,
                                                                 int* __restrict__ block_sums, int n_blocks_max) {
   const int n = *count;
+  const int nb = min(n_blocks_max, (n + kScanBlock - 1) / kScanBlock);
   __shared__ int warp_sums[kScanBlock / 32];
-  for (int b = blockIdx.x; b < n_blocks_max; b += gridDim.x) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const int i = b * kScanBlock + threadIdx.x;
     const int v = (i < n) ? keep[i] : 0;
     const int ws = __popc(__ballot_sync(0xffffffffu, v != 0));
@@ -281,8 +283,9 @@ __global__ void __launch_bounds__(kScanBlock) scatter_kernel(const int* __restri
                                                              const int* __restrict__ block_offsets,
                                                              int* __restrict__ next, int n_blocks_max) {
   const int n = *count;
+  const int nb = min(n_blocks_max, (n + kScanBlock - 1) / kScanBlock);
   __shared__ int warp_off[kScanBlock / 32];
-  for (int b = blockIdx.x; b < n_blocks_max; b += gridDim.x) {
+  for (int b = blockIdx.x; b < nb; b += gridDim.x) {
     const int i = b * kScanBlock + threadIdx.x;
     const int v = (i < n) ? keep[i] : 0;
     const unsigned m = __ballot_sync(0xffffffffu, v != 0);
@@ -338,7 +341,7 @@ struct Render {
   uint32_t seed = 0;
   hm_mlp* mlp = nullptr;
   int P = 0;
-  int depth = 3;
+  int depth = 0;  // 0: chosen from the frame size in render_setup
   std::vector<Slot> slots;
   double *acc_pt = nullptr, *acc_nn = nullptr, *acc_final = nullptr;
   cudaEvent_t ev_submit = nullptr, ev_mlp = nullptr, ev_compose = nullptr, ev_read = nullptr;
@@ -471,6 +474,12 @@ static int render_setup(Render* r, const hm_render_options* o) {
     // everyNth = frameSize / numTrainRecords (integer division, render_hair_msnn.cu:106), at least 1
     r->every_nth = std::max(1, P / r->n_train);
     r->n_train = std::min(r->n_train, (P + r->every_nth - 1) / r->every_nth);
+  }
+  if (r->depth <= 0) {
+    // default: up to 6 frames in flight (the measured optimum at 512x512),
+    // keeping the per-slot path state and queues under about 2 GB in total
+    const int64_t slot_bytes = (int64_t)P * 360;
+    r->depth = (int)std::max<int64_t>(2, std::min<int64_t>(6, ((int64_t)2 << 30) / std::max<int64_t>(1, slot_bytes)));
   }
   r->slots.resize(r->depth);
   for (auto& sl : r->slots) {
@@ -739,6 +748,11 @@ extern "C" int hm_render_read_async(hm_render* h, int which, double* host_dst, v
   if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_read_async");
   r->have_read_ev = true;
   return HM_OK;
+}
+
+extern "C" int hm_render_frames_in_flight(const hm_render* h) {
+  const Render* r = (const Render*)h;
+  return r ? r->depth : 0;
 }
 
 extern "C" int hm_render_wait(hm_render* h, void* stream) {

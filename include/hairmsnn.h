@@ -267,7 +267,8 @@ typedef struct hm_render_options {
   int cache_precision;           /* HM_PREC_* */
   uint32_t seed;                 /* cache initialisation */
   const char* cache_config_json; /* NULL: the scene's tcnn.config, else the built-in one */
-  int frames_in_flight;          /* 0 = 3; frames pipelined on their own streams (1..8) */
+  int frames_in_flight;          /* frames pipelined on their own streams (1..8); 0: up to 6,
+                                    fewer when their path state would pass ~2 GB */
 } hm_render_options;
 
 typedef struct hm_render_stats {
@@ -290,6 +291,8 @@ void hm_render_destroy(hm_render* render);
  * reused, or by hm_render_read / _get_stats / _reset, which synchronise).
  * With instrumentation on, frames run one at a time. */
 int hm_render_frame(hm_render* render, void* stream);
+/* Frames the renderer keeps in flight (the resolved frames_in_flight). */
+int hm_render_frames_in_flight(const hm_render* render);
 /* Makes `stream` wait for every frame in flight (no host synchronisation). */
 int hm_render_wait(hm_render* render, void* stream);
 /* Asynchronous read-back on `stream` of the FP64 running sums (divide by the

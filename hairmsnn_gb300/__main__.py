@@ -11,14 +11,17 @@
 (16-D: position, angles, h, sigma_a, beta) and prints the time per call.
 
 Without a scene file the built-in straight-hair scene is used.  Frames
-accumulate in FP64; --out writes the average as a little-endian PFM
-(bottom row first, the renderer's own row order).  --stats writes per-frame
+accumulate in FP64; --out writes the average as OpenEXR (.exr: float
+RGB, uncompressed, top row first as the reference's screenShotEXR) or as a
+little-endian PFM (any other name: bottom row first, the renderer's own row
+order).  --stats writes per-frame
 timings (the reference's renderTime/trainTime/inferTime) and the cache loss
 as JSON (the reference parses integrator.stats_output but never writes it).
 """
 import argparse
 import json
 import os
+import struct
 import sys
 import time
 
@@ -40,6 +43,76 @@ def read_pfm(path):
         scale = float(f.readline())
         dt = "<f4" if scale < 0 else ">f4"
         return np.frombuffer(f.read(), dtype=dt).reshape(h, w, 3).astype(np.float32)
+
+
+def _exr_attr(name, typ, payload):
+    return name.encode() + b"\0" + typ.encode() + b"\0" + struct.pack("<i", len(payload)) + payload
+
+
+def write_exr(path, img):
+    """img: [H, W, 3] float, row 0 = bottom (the renderer's order), written as
+    an uncompressed single-part scanline OpenEXR file with FLOAT channels
+    B, G, R (top row first), as the reference's screenShotEXR writes its
+    accumulation buffer (model.cpp:366-383) minus the compression."""
+    h, w, _ = img.shape
+    top_first = np.ascontiguousarray(img[::-1], dtype="<f4")
+    chans = b"".join(c.encode() + b"\0" + struct.pack("<iB3xii", 2, 0, 1, 1) for c in "BGR") + b"\0"
+    header = b"".join([
+        _exr_attr("channels", "chlist", chans),
+        _exr_attr("compression", "compression", b"\0"),
+        _exr_attr("dataWindow", "box2i", struct.pack("<4i", 0, 0, w - 1, h - 1)),
+        _exr_attr("displayWindow", "box2i", struct.pack("<4i", 0, 0, w - 1, h - 1)),
+        _exr_attr("lineOrder", "lineOrder", b"\0"),
+        _exr_attr("pixelAspectRatio", "float", struct.pack("<f", 1.0)),
+        _exr_attr("screenWindowCenter", "v2f", struct.pack("<2f", 0.0, 0.0)),
+        _exr_attr("screenWindowWidth", "float", struct.pack("<f", 1.0)),
+    ]) + b"\0"
+    prefix = struct.pack("<ii", 20000630, 2) + header
+    row_bytes = 8 + 3 * w * 4
+    first = len(prefix) + 8 * h
+    offsets = struct.pack(f"<{h}Q", *(first + y * row_bytes for y in range(h)))
+    rows = []
+    for y in range(h):
+        line = top_first[y]
+        rows.append(struct.pack("<ii", y, 3 * w * 4) + line[:, 2].tobytes() + line[:, 1].tobytes() +
+                    line[:, 0].tobytes())
+    with open(path, "wb") as f:
+        f.write(prefix + offsets + b"".join(rows))
+
+
+def read_exr(path):
+    """Reads what write_exr writes (uncompressed FLOAT B, G, R scanlines);
+    returns [H, W, 3] float32, row 0 = bottom."""
+    data = open(path, "rb").read()
+    magic, version = struct.unpack_from("<ii", data, 0)
+    assert magic == 20000630 and (version & 0xFF) == 2
+    pos, attrs = 8, {}
+    while data[pos] != 0:
+        e = data.index(b"\0", pos)
+        name = data[pos:e].decode()
+        e2 = data.index(b"\0", e + 1)
+        size, = struct.unpack_from("<i", data, e2 + 1)
+        attrs[name] = data[e2 + 5:e2 + 5 + size]
+        pos = e2 + 5 + size
+    pos += 1
+    assert attrs["compression"] == b"\0"
+    x0, y0, x1, y1 = struct.unpack("<4i", attrs["dataWindow"])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    names, c = [], 0
+    ch = attrs["channels"]
+    while ch[c] != 0:
+        e = ch.index(b"\0", c)
+        names.append(ch[c:e].decode())
+        c = e + 1 + 16
+    offsets = struct.unpack_from(f"<{h}Q", data, pos)
+    img = np.zeros((h, w, 3), np.float32)
+    for off in offsets:
+        y, n = struct.unpack_from("<ii", data, off)
+        vals = np.frombuffer(data, "<f4", n // 4, off + 8).reshape(len(names), w)
+        for k, nm in enumerate(names):
+            if nm in "RGB":
+                img[y - y0, :, "RGB".index(nm)] = vals[k]
+    return img[::-1].copy()
 
 
 def main(argv=None):
@@ -94,9 +167,12 @@ def main(argv=None):
     img = rd.read(render.IMAGE_FINAL)
     out = a.out or cfg.get("integrator", {}).get("image_output") or None
     if out:
-        if not out.endswith(".pfm"):
-            out = os.path.splitext(out)[0] + ".pfm"
-        write_pfm(out, img)
+        if out.endswith(".exr"):
+            write_exr(out, img)
+        else:
+            if not out.endswith(".pfm"):
+                out = os.path.splitext(out)[0] + ".pfm"
+            write_pfm(out, img)
     summary = {"frames": frames, "wall_s": wall, "paths_per_s": frames * img.shape[0] * img.shape[1] / wall,
                "mean_radiance": float(img.mean())}
     print(json.dumps(summary))

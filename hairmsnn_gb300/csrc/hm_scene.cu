@@ -97,6 +97,178 @@ static void gen_hair(const HairGen& g, f3 head_r, Scene* s) {
   }
 }
 
+// ------------------------------------------------------------ .hair files
+// Cem Yuksel's HAIR format (its published description): a 128-byte header
+// ("HAIR", strand count, point count, a bit field of the arrays present,
+// default segments / thickness / transparency / colour, 88 bytes of text),
+// then the arrays present, in order: segments (uint16 per strand), points
+// (3 floats per point), thickness (float per point), transparency (float per
+// point), colours (3 floats per point).  Strands become cubic B-splines as in
+// Scene::extractHairData (scene.cpp:10-73): a phantom point p0 + (p0 - p1)
+// before each strand and pN + (pN - pN-1) after it, one segment starting at
+// the phantom and at every point but the last two, radius 0.2 x thickness.
+// The bounds (and so the scene scale) are those of the file's own points.
+static int load_hair_file(const std::string& path, Scene* s, f3* raw_lo, f3* raw_hi) {
+  std::string data;
+  if (!read_file(path, &data)) return hm_set_error("scene: cannot read hair file %s", path.c_str()), HM_EINVAL;
+  if (data.size() < 128 || data.compare(0, 4, "HAIR") != 0)
+    return hm_set_error("scene: %s is not a HAIR file", path.c_str()), HM_EPARSE;
+  auto u32 = [&](size_t off) {
+    uint32_t v;
+    memcpy(&v, data.data() + off, 4);
+    return v;
+  };
+  auto f32 = [&](size_t off) {
+    float v;
+    memcpy(&v, data.data() + off, 4);
+    return v;
+  };
+  const uint32_t n_strands = u32(4), n_points = u32(8), flags = u32(12), d_segments = u32(16);
+  const float d_thickness = f32(20);
+  size_t off = 128;
+  const size_t seg_bytes = (flags & 1) ? (size_t)n_strands * 2 : 0;
+  const size_t pts_bytes = (flags & 2) ? (size_t)n_points * 12 : 0;
+  const size_t thk_bytes = (flags & 4) ? (size_t)n_points * 4 : 0;
+  if (!(flags & 2)) return hm_set_error("scene: %s has no points array", path.c_str()), HM_EPARSE;
+  if (data.size() < off + seg_bytes + pts_bytes + thk_bytes)
+    return hm_set_error("scene: %s is truncated", path.c_str()), HM_EPARSE;
+  const uint8_t* base = reinterpret_cast<const uint8_t*>(data.data());
+  const uint8_t* segs = (flags & 1) ? base + off : nullptr;
+  off += seg_bytes;
+  const uint8_t* pts = base + off;
+  off += pts_bytes;
+  const uint8_t* thk = (flags & 4) ? base + off : nullptr;
+  auto point = [&](int64_t i) {
+    i = std::min<int64_t>(std::max<int64_t>(i, 0), (int64_t)n_points - 1);
+    float v[3];
+    memcpy(v, pts + 12 * i, 12);
+    return mk(v[0], v[1], v[2]);
+  };
+  auto width = [&](int64_t i) {
+    if (!thk) return d_thickness;
+    float v;
+    memcpy(&v, thk + 4 * i, 4);
+    return v;
+  };
+  f3 lo = mk(1e30f, 1e30f, 1e30f), hi = mk(-1e30f, -1e30f, -1e30f);
+  uint32_t strand = 0;
+  int left = -1;
+  s->cp.clear();
+  s->seg.clear();
+  for (int64_t i = 0; i < (int64_t)n_points; ++i) {
+    const f3 p = point(i);
+    const float w = width(i);
+    lo = mk(fminf(lo.x, p.x), fminf(lo.y, p.y), fminf(lo.z, p.z));
+    hi = mk(fmaxf(hi.x, p.x), fmaxf(hi.y, p.y), fmaxf(hi.z, p.z));
+    bool first = false;
+    if (left == -1) {
+      if (strand == n_strands) break;
+      uint16_t ns = (uint16_t)d_segments;
+      if (segs) memcpy(&ns, segs + 2 * strand, 2);
+      left = ns;
+      ++strand;
+      first = true;
+    }
+    if (first) {
+      const f3 q = p + (p - point(i + 1));
+      s->cp.push_back(make_float4(q.x, q.y, q.z, 0.2f * w));
+      s->seg.push_back((int)s->cp.size() - 1);
+    }
+    s->cp.push_back(make_float4(p.x, p.y, p.z, 0.2f * w));
+    if (left > 1) {
+      s->seg.push_back((int)s->cp.size() - 1);
+    } else if (left == 0) {
+      const f3 q = p + (p - point(i - 1));
+      s->cp.push_back(make_float4(q.x, q.y, q.z, 0.2f * w));
+    }
+    --left;
+  }
+  // a strand cut short by the point count leaves segments without their
+  // last control points: drop them
+  while (!s->seg.empty() && s->seg.back() + 3 >= (int)s->cp.size()) s->seg.pop_back();
+  s->n_strands = (int)strand;
+  if (s->seg.empty()) return hm_set_error("scene: %s has no complete segment", path.c_str()), HM_EPARSE;
+  *raw_lo = lo;
+  *raw_hi = hi;
+  return HM_OK;
+}
+
+// ------------------------------------------------------------ .obj files
+// Wavefront OBJ: "v", "vn" and "f" records (1-based or negative indices,
+// v, v/vt, v//vn, v/vt/vn), polygons split into fans.  As loadOBJ
+// (model.cpp:233-345) does, every triangle gets its own three vertices and
+// the file's normals; a face without normals gets its geometric normal.
+static int load_obj_file(const std::string& path, Scene* s) {
+  std::string data;
+  if (!read_file(path, &data)) return hm_set_error("scene: cannot read OBJ file %s", path.c_str()), HM_EINVAL;
+  std::vector<f3> v, vn;
+  s->vtx.clear();
+  s->nrm.clear();
+  s->tri.clear();
+  size_t pos = 0;
+  while (pos < data.size()) {
+    size_t end = data.find('\n', pos);
+    if (end == std::string::npos) end = data.size();
+    std::string line = data.substr(pos, end - pos);
+    pos = end + 1;
+    if (line.size() < 2) continue;
+    if (line[0] == 'v' && (line[1] == ' ' || line[1] == '\t')) {
+      float x = 0, y = 0, z = 0;
+      if (sscanf(line.c_str() + 2, "%f %f %f", &x, &y, &z) == 3) v.push_back(mk(x, y, z));
+    } else if (line[0] == 'v' && line[1] == 'n') {
+      float x = 0, y = 0, z = 0;
+      if (sscanf(line.c_str() + 3, "%f %f %f", &x, &y, &z) == 3) vn.push_back(mk(x, y, z));
+    } else if (line[0] == 'f' && (line[1] == ' ' || line[1] == '\t')) {
+      std::vector<int> fv, fn;
+      const char* c = line.c_str() + 2;
+      while (*c) {
+        while (*c == ' ' || *c == '\t' || *c == '\r') ++c;
+        if (!*c) break;
+        int a = 0, b = 0, n = 0;
+        int got = 0;
+        char* e = nullptr;
+        a = (int)strtol(c, &e, 10);
+        got = e != c;
+        c = e;
+        if (*c == '/') {
+          ++c;
+          if (*c != '/') {
+            b = (int)strtol(c, &e, 10);
+            c = e;
+          }
+          if (*c == '/') {
+            ++c;
+            n = (int)strtol(c, &e, 10);
+            c = e;
+          }
+        }
+        (void)b;
+        while (*c && *c != ' ' && *c != '\t') ++c;
+        if (!got) break;
+        const int vi = a > 0 ? a - 1 : (int)v.size() + a;
+        const int ni = n > 0 ? n - 1 : (n < 0 ? (int)vn.size() + n : -1);
+        if (vi < 0 || vi >= (int)v.size()) return hm_set_error("scene: %s: vertex index out of range", path.c_str()), HM_EPARSE;
+        fv.push_back(vi);
+        fn.push_back(ni >= 0 && ni < (int)vn.size() ? ni : -1);
+      }
+      for (size_t k = 1; k + 1 < fv.size(); ++k) {
+        const int ids[3] = {fv[0], fv[k], fv[k + 1]};
+        const int nid[3] = {fn[0], fn[k], fn[k + 1]};
+        const f3 gn = normalize(cross(v[ids[1]] - v[ids[0]], v[ids[2]] - v[ids[0]]));
+        const int b0 = (int)s->vtx.size();
+        for (int q = 0; q < 3; ++q) {
+          s->vtx.push_back(make_float3(v[ids[q]].x, v[ids[q]].y, v[ids[q]].z));
+          const f3 nn = nid[q] >= 0 ? vn[nid[q]] : gn;
+          s->nrm.push_back(make_float3(nn.x, nn.y, nn.z));
+        }
+        s->tri.push_back(make_int3(b0, b0 + 1, b0 + 2));
+      }
+    }
+  }
+  if (s->tri.empty()) return hm_set_error("scene: %s has no faces", path.c_str()), HM_EPARSE;
+  return HM_OK;
+}
+
 // ------------------------------------------------------------ head ellipsoid
 static void gen_ellipsoid(int triangles, f3 radii, Scene* s) {
   int nu = std::max(3, (int)lrintf(sqrtf((float)triangles / 2.f)));
@@ -234,6 +406,8 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
     return HM_EPARSE;
   }
   const std::string base = base_dir ? base_dir : "";
+  f3 hair_lo = mk(0, 0, 0), hair_hi = mk(0, 0, 0);
+  bool hair_from_file = false;
   try {
     // ---- surface (head)
     const Json& surf = j["surface"];
@@ -248,9 +422,10 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
       s->alpha_raw = (float)p.number_or("alpha", 1.0);
       has_surface = true;
     } else if (surf.has("geometry")) {
-      hm_set_error("scene: OBJ surface geometry (%s) is not supported; use surface.procedural",
-                   surf["geometry"].as_string().c_str());
-      return HM_EUNSUPPORTED;
+      if (int st = load_obj_file(join_path(base, surf["geometry"].as_string()), s)) return st;
+      s->diffuse = f3_of(surf["diffuse"], mk(0.35f, 0.25f, 0.2f));
+      s->alpha_raw = (float)surf.number_or("alpha", 1.0);
+      has_surface = true;
     }
     // ---- hair geometry
     const Json& hair = j["hair"];
@@ -271,9 +446,9 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
       gen_hair(g, head_r, s);
       has_hair = true;
     } else if (hair.has("geometry")) {
-      hm_set_error("scene: .hair geometry (%s) is not supported; use hair.procedural",
-                   hair["geometry"].as_string().c_str());
-      return HM_EUNSUPPORTED;
+      if (int st = load_hair_file(join_path(base, hair["geometry"].as_string()), s, &hair_lo, &hair_hi)) return st;
+      hair_from_file = true;
+      has_hair = true;
     }
     if (!has_surface && !has_hair) throw JsonError("scene: either hair or surface must be defined");
     // ---- camera (required)
@@ -356,7 +531,12 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
   for (auto& v : s->vtx) grow(lo, hi, mk(v.x, v.y, v.z));
   float surf_scale = s->vtx.empty() ? 0.f : length(hi - lo);
   f3 hlo = mk(1e30f, 1e30f, 1e30f), hhi = mk(-1e30f, -1e30f, -1e30f);
-  for (auto& c : s->cp) grow(hlo, hhi, mk(c.x, c.y, c.z));
+  if (hair_from_file) {  // extractHairData's bounds: the file's points, not the phantoms
+    hlo = hair_lo;
+    hhi = hair_hi;
+  } else {
+    for (auto& c : s->cp) grow(hlo, hhi, mk(c.x, c.y, c.z));
+  }
   float hair_scale = s->cp.empty() ? 0.f : length(hhi - hlo);
   if (!s->cp.empty()) {
     grow(lo, hi, hlo);

@@ -464,7 +464,9 @@ class RenderQualityWorkload(RenderBenchWorkload):
     relMSE falls as 1/spp (it is unbiased).  The reference uses frames
     16 .. 16 + ref_spp of one PT run, so it shares no random numbers with
     the 16-spp estimates (the path RNG is seeded by the frame index, as in
-    the reference).  One step = one HairMSNN frame, as the render workload."""
+    the reference).  The HairMSNN relMSE is also reported with the cache's
+    inference in FP16, BF16 and E4M3 on the tensor cores (training FP32).
+    One step = one HairMSNN frame, as the render workload."""
 
     name = "quality"
     metric = "paths/s at fixed relMSE vs PT (HairMSNN BETA=1, 512x512, 16 spp, online cache training 2^16/frame)"
@@ -493,11 +495,16 @@ class RenderQualityWorkload(RenderBenchWorkload):
         total = pt.read(IMAGE_FINAL) * (spp + self.ref_spp)
         ref = (total - pt_img * spp) / self.ref_spp
         pt.close()
-        ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
-                      frames_in_flight=self.frames_in_flight)
-        ms_ms = self._timed_frames(ms, spp)
-        ms_img = ms.read(IMAGE_FINAL)
-        ms.close()
+        by_prec = {}
+        for name, prec in (("fp32", 0), ("fp16", 1), ("bf16", 2), ("fp8", 3)):
+            ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
+                          precision=prec, frames_in_flight=self.frames_in_flight)
+            t_ms = self._timed_frames(ms, spp)
+            img = ms.read(IMAGE_FINAL)
+            ms.close()
+            by_prec[name] = {"relmse": round(relmse(img, ref), 6), "ms_per_frame": round(t_ms, 3)}
+            if name == "fp32":
+                ms_ms, ms_img = t_ms, img
         e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
         eq_spp = spp * e_pt / e_ms
         return {"spp": spp, "reference_spp": self.ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
@@ -505,6 +512,7 @@ class RenderQualityWorkload(RenderBenchWorkload):
                          "paths_per_s": round(self.P / (ms_ms * 1e-3), 1)},
                 "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
                        "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
+                "msnn_by_cache_precision": by_prec,
                 "pt_spp_for_msnn_relmse": round(eq_spp, 2),
                 "speedup_at_equal_relmse": round(eq_spp * pt_ms / (spp * ms_ms), 3)}
 

@@ -188,7 +188,8 @@ int hm_mlp_load(hm_mlp* mlp, const char* path);
  *   lights.sky         {turbidity, sun[3], width, height, scale, rotation}
  *                      (Preetham et al. 1999 sky baked to a lat-long map)
  * base_dir resolves relative file names (tcnn.config).  Returns NULL and a
- * status (HM_EPARSE for bad JSON, HM_EUNSUPPORTED for .hair/.obj/.exr files).
+ * status (HM_EPARSE for bad JSON or a malformed .hair/.obj file, HM_EINVAL for a
+ * missing file, HM_EUNSUPPORTED for .exr environment maps).
  * ---------------------------------------------------------------------- */
 typedef struct hm_scene hm_scene;
 

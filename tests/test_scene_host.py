@@ -73,8 +73,8 @@ def test_reference_defaults(R):
     (lambda c: c["integrator"].update(width=100, height=100), 6),  # not a multiple of 128 pixels
     (lambda c: c["integrator"].update(width=4096, height=4096), 6),
     (lambda c: c.pop("integrator"), 6),
-    (lambda c: c["hair"].update(geometry="wStraight.hair") or c["hair"].pop("procedural"), 7),
-    (lambda c: c["surface"].update(geometry="head.obj") or c["surface"].pop("procedural"), 7),
+    (lambda c: c["hair"].update(geometry="wStraight.hair") or c["hair"].pop("procedural"), 1),  # missing file: HM_EINVAL
+    (lambda c: c["surface"].update(geometry="head.obj") or c["surface"].pop("procedural"), 1),
 ])
 def test_scene_errors(R, mutate, status):
     from hairmsnn_gb300._ffi import HMError

@@ -51,6 +51,22 @@ def bsdf_eval(wo, wi, tangent, h, hp=None, stream=None):
     return f, pdf
 
 
+def bsdf_eval_grad(wo, wi, tangent, h, hp=None, stream=None):
+    """bsdf_eval plus derivatives with respect to (sigma_a r, g, b, beta_m,
+    beta_n, alpha): returns f [3,n], pdf [n], df [6,3,n], dpdf [6,n]."""
+    import torch
+    n = h.shape[0]
+    f = torch.empty((3, n), dtype=torch.float32, device=h.device)
+    pdf = torch.empty((n,), dtype=torch.float32, device=h.device)
+    df = torch.empty((6, 3, n), dtype=torch.float32, device=h.device)
+    dpdf = torch.empty((6, n), dtype=torch.float32, device=h.device)
+    q = hm_bsdf_queries(_ptr(wo), _ptr(wi), _ptr(tangent), _ptr(h), None)
+    p = hair_params(hp)
+    check(lib().hm_bsdf_eval_grad(ctypes.byref(q), _ptr(f), _ptr(pdf), _ptr(df), _ptr(dpdf), n, ctypes.byref(p),
+                                  _stream(stream)))
+    return f, pdf, df, dpdf
+
+
 def bsdf_sample(wo, tangent, h, u, hp=None, stream=None):
     """wo/tangent [3,n], h [n], u [4,n] -> wi [3,n], f [3,n], pdf [n]."""
     import torch

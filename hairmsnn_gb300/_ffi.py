@@ -81,6 +81,7 @@ def lib():
     L.hm_hair_setup.argtypes = [P(hm_hair_params), vp]
     L.hm_bsdf_eval.argtypes = [P(hm_bsdf_queries), vp, vp, i64, P(hm_hair_params), vp]
     L.hm_bsdf_sample.argtypes = [P(hm_bsdf_queries), vp, vp, vp, i64, P(hm_hair_params), vp]
+    L.hm_bsdf_eval_grad.argtypes = [P(hm_bsdf_queries), vp, vp, vp, vp, i64, P(hm_hair_params), vp]
     L.hm_bsdf_gen_queries.argtypes = [u32, i64, vp, vp, vp, vp, vp, vp]
     # radiance-cache network
     L.hm_mlp_create.restype = vp

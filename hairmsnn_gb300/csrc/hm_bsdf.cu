@@ -9,6 +9,7 @@
 #include <math.h>
 
 #include "hm_hair_bsdf.cuh"
+#include "hm_hair_grad.cuh"
 
 namespace hm {
 
@@ -169,6 +170,47 @@ extern "C" int hm_bsdf_eval(const hm_bsdf_queries* q, float* f, float* pdf, int6
   bsdf_eval_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(hc, q->wo, q->wi, q->tangent,
                                                                         q->h, f, pdf, n);
   HM_CHECK_LAUNCH("bsdf_eval_kernel");
+  return HM_OK;
+}
+
+// f, pdf and their partials with respect to (sigma_a r, g, b, beta_m, beta_n,
+// alpha): df [6][3][n], dpdf [6][n] (dpdf may be NULL).
+__global__ void __launch_bounds__(256) bsdf_eval_grad_kernel(hm_hair_params p, const float* __restrict__ wo,
+                                                             const float* __restrict__ wi,
+                                                             const float* __restrict__ t,
+                                                             const float* __restrict__ h,
+                                                             float* __restrict__ f, float* __restrict__ pdf,
+                                                             float* __restrict__ df, float* __restrict__ dpdf,
+                                                             int64_t n) {
+  const float gain[4] = {p.gain_r, p.gain_tt, p.gain_trt, p.gain_trrt};
+  const HairConstsD hc = hair_consts_dual(p.sigma_a, p.beta_m, p.beta_n, p.alpha, gain);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const f3 w_o = mk(ldg(wo + i), ldg(wo + n + i), ldg(wo + 2 * n + i));
+    const f3 w_i = mk(ldg(wi + i), ldg(wi + n + i), ldg(wi + 2 * n + i));
+    const f3 tg = mk(ldg(t + i), ldg(t + n + i), ldg(t + 2 * n + i));
+    const Frame fr = hair_frame(w_o, tg);
+    const HairEvalD e = hair_eval_dual(normalize(to_local(fr, w_o)), normalize(to_local(fr, w_i)), ldg(h + i), hc);
+    for (int c = 0; c < 3; ++c) {
+      f[c * n + i] = e.f[c].v;
+      for (int j = 0; j < kNd; ++j) df[(j * 3 + c) * n + i] = e.f[c].d[j];
+    }
+    pdf[i] = e.pdf.v;
+    if (dpdf)
+      for (int j = 0; j < kNd; ++j) dpdf[j * n + i] = e.pdf.d[j];
+  }
+}
+
+extern "C" int hm_bsdf_eval_grad(const hm_bsdf_queries* q, float* f, float* pdf, float* df, float* dpdf, int64_t n,
+                                 const hm_hair_params* params, void* stream) {
+  if (n < 0 || !q) return hm_set_error("hm_bsdf_eval_grad: n < 0 or queries NULL"), HM_EINVAL;
+  if (int s = check_params(params)) return s;
+  if (n == 0) return HM_OK;
+  if (!q->wo || !q->wi || !q->tangent || !q->h || !f || !pdf || !df)
+    return hm_set_error("hm_bsdf_eval_grad: NULL array"), HM_EINVAL;
+  bsdf_eval_grad_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(*params, q->wo, q->wi, q->tangent, q->h,
+                                                                             f, pdf, df, dpdf, n);
+  HM_CHECK_LAUNCH("bsdf_eval_grad_kernel");
   return HM_OK;
 }
 

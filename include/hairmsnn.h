@@ -81,6 +81,14 @@ int hm_bsdf_eval(const hm_bsdf_queries* q, float* f, float* pdf, int64_t n,
                  const hm_hair_params* params, void* stream);
 int hm_bsdf_sample(const hm_bsdf_queries* q, float* wi_out, float* f, float* pdf, int64_t n,
                    const hm_hair_params* params, void* stream);
+/* disney_hair (disney_hair.cuh:186) with its derivatives with respect to the
+ * material, for appearance fitting (no reference counterpart: the
+ * reference does not differentiate).  Parameters in this order: sigma_a r,
+ * g, b, beta_m, beta_n, alpha (radians).  f [3][n] and pdf [n] as
+ * hm_bsdf_eval; df [6][3][n] = d f[c] / d param[j] at df[(j*3 + c)*n + i];
+ * dpdf [6][n] (may be NULL).  Forward-mode (dual-number) evaluation. */
+int hm_bsdf_eval_grad(const hm_bsdf_queries* q, float* f, float* pdf, float* df, float* dpdf, int64_t n,
+                      const hm_hair_params* params, void* stream);
 
 /* Synthetic BSDF workload generator (no reference counterpart: the
  * benchmark's input).  Per query one murmur-seeded LCG stream (the

@@ -340,6 +340,9 @@ struct Render {
   bool train = true;
   uint32_t seed = 0;
   hm_mlp* mlp = nullptr;
+  float4* d_samples = nullptr;  // scene-sample training pass: points on the hair
+  int n_samples = 0;
+  int pretrain_passes = 0;
   int P = 0;
   int depth = 0;  // 0: chosen from the frame size in render_setup
   std::vector<Slot> slots;
@@ -368,6 +371,7 @@ struct Render {
       if (s.h_err) cudaFreeHost(s.h_err);
     }
     for (void* p : allocs) cudaFree(p);
+    if (d_samples) cudaFree(d_samples);
     if (h_count) cudaFreeHost(h_count);
     if (mlp) hm_mlp_destroy(mlp);
     for (auto e : ev) cudaEventDestroy(e);
@@ -532,7 +536,8 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   const cudaStream_t st = sl.st;
   cudaEventRecord(r->ev_submit, user);
   cudaStreamWaitEvent(st, r->ev_submit, 0);
-  FrameParams fp{r->mode, r->beta_knob - 1, r->accum_id, r->accum_id + 10007, r->every_nth, r->n_train, r->in_ch};
+  FrameParams fp{r->mode, r->beta_knob - 1, r->accum_id, r->accum_id + 10007, r->every_nth, r->n_train, r->in_ch,
+                 0, nullptr, 0, 0u};
   int* q_cur = sl.q_a;
   int* q_next = sl.q_b;
   int* c_cur = sl.counts;
@@ -764,6 +769,123 @@ extern "C" int hm_render_wait(hm_render* h, void* stream) {
       if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_wait");
     }
   return HM_OK;
+}
+
+// ---- scene-sample training pass (initialize(), render_hair_msnn.cu:641-650)
+// Points on the hair: fetchSceneSamples (render_hair_msnn.cu:34-97) gives
+// each segment int(length / total length * 1e6) uniform samples, at least
+// one, with length = |p1 - p0| + |p2 - p1| + |p3 - p2| of its control points
+// (:359-367).  The reference evaluates the points on the Catmull-Rom
+// interpretation of the control points; they only aim the training rays,
+// which then hit whatever hair lies that way, and here they are taken on
+// the B-spline curve that is intersected.  (The reference also looks the
+// lengths up by control-point index instead of segment number; each
+// segment's own length is used here.)
+static int build_scene_samples(Render* r) {
+  const Scene* sc = r->scene;
+  const int n_seg = (int)sc->seg.size();
+  if (n_seg == 0) return hm_set_error("hm_render_pretrain: the scene has no hair"), HM_EINVAL;
+  std::vector<float> len(n_seg);
+  double total = 0.0;
+  auto pt = [&](int i) { const float4 c = sc->cp[i]; return mk(c.x, c.y, c.z); };
+  for (int k = 0; k < n_seg; ++k) {
+    const int i = sc->seg[k];
+    len[k] = length(pt(i) - pt(i + 1)) + length(pt(i + 2) - pt(i + 1)) + length(pt(i + 3) - pt(i + 2));
+    total += len[k];
+  }
+  const double wanted = 1e6;
+  std::vector<float4> samples;
+  samples.reserve((size_t)wanted + n_seg);
+  uint32_t st = rng_seed((int)r->seed, 0x5a3u);
+  for (int k = 0; k < n_seg; ++k) {
+    int m = (int)((double)len[k] / total * wanted);
+    if (m == 0) m = 1;
+    const int i = sc->seg[k];
+    const f3 q0 = pt(i), q1 = pt(i + 1), q2 = pt(i + 2), q3 = pt(i + 3);
+    for (int j = 0; j < m; ++j) {
+      const float u = lcg_next(st), v = 1.f - u;
+      // uniform cubic B-spline basis
+      const float b0 = v * v * v / 6.f, b1 = (3.f * u * u * u - 6.f * u * u + 4.f) / 6.f;
+      const float b2 = (-3.f * u * u * u + 3.f * u * u + 3.f * u + 1.f) / 6.f, b3 = u * u * u / 6.f;
+      const f3 p = q0 * b0 + q1 * b1 + q2 * b2 + q3 * b3;
+      samples.push_back(make_float4(p.x, p.y, p.z, 0.f));
+    }
+  }
+  cudaError_t e = cudaMalloc(&r->d_samples, samples.size() * sizeof(float4));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(r->d_samples, samples.data(), samples.size() * sizeof(float4), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return hm_cuda_status(e, "scene samples");
+  r->n_samples = (int)samples.size();
+  return HM_OK;
+}
+
+// `passes` rounds of: n_train training paths aimed at scene samples (the
+// TRAIN_DATA_GEN pass, hair_msnn.cu:222-233, 240-272), then one training
+// step (train(), render_hair_msnn.cu:666-697).  The reference repeats this
+// for one second of wall time; here the count is explicit.  Each pass uses a
+// new permutation of the samples and the RNG seed of its pass number, like
+// the reference's accumId during initial training.
+static int render_pretrain(Render* r, int passes, cudaStream_t user) {
+  if (r->mode != MODE_MSNN) return hm_set_error("hm_render_pretrain: HairMSNN renderers only"), HM_EINVAL;
+  if (int e = render_sync(r)) return e;
+  if (!r->d_samples)
+    if (int e = build_scene_samples(r)) return e;
+  Scene* s = r->scene;
+  const SceneDev sd = s->dev();
+  Slot& sl = r->slots[0];
+  const cudaStream_t st = sl.st;
+  cudaEventRecord(r->ev_submit, user);
+  cudaStreamWaitEvent(st, r->ev_submit, 0);
+  const int grid = r->sm_count * 8;
+  const int nblocks = (r->n_train + kScanBlock - 1) / kScanBlock;
+  for (int pass = 0; pass < passes; ++pass) {
+    const int id = r->pretrain_passes++;
+    FrameParams fp{r->mode, r->beta_knob - 1, id, id + 10007, 1, r->n_train, r->in_ch,
+                   1, r->d_samples, r->n_samples, 0x9e37u + (uint32_t)id};
+    int* q_cur = sl.q_a;
+    int* q_next = sl.q_b;
+    int* c_cur = sl.counts;
+    int* c_next = sl.counts + 1;
+    cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
+    if (int e = launch_camera(sd, fp, sl.ps, q_cur, c_cur, st)) return e;
+    for (int it = 0; it <= s->path_v2; ++it) {
+      if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, 0.f, 1e30f,
+                                                       sl.fetch + 2 * it, sl.err, r->d_cnt, false,
+                                                       r->blocks_extend, st))
+        return e;
+      if (int e = launch_shade(sd, fp, sl.ps, sl.fb, q_cur, c_cur, sl.keep, grid, st)) return e;
+      if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, 0.f, 1e30f,
+                                                      sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, false,
+                                                      r->blocks_shadow, st))
+        return e;
+      shadow_resolve_kernel<<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis);
+      scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
+                                                                                    nblocks);
+      scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
+      scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, q_cur, c_cur,
+                                                                                sl.block_sums, q_next, nblocks);
+      HM_CHECK_LAUNCH("pretrain bounce");
+      std::swap(q_cur, q_next);
+      std::swap(c_cur, c_next);
+    }
+    if (int e = launch_finalize(sd, fp, sl.ps, sl.fb, st)) return e;
+    if (r->have_mlp_ev) cudaStreamWaitEvent(st, r->ev_mlp, 0);
+    if (int e = hm_mlp_training_step(r->mlp, sl.fb.nn_train_in, sl.fb.nn_train_out, r->n_train, sl.d_loss, st))
+      return e;
+    cudaEventRecord(r->ev_mlp, st);
+    r->have_mlp_ev = true;
+  }
+  cudaMemcpyAsync(sl.h_err, sl.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(sl.done, st);
+  sl.in_flight = true;
+  return slot_finish(r, sl);
+}
+
+extern "C" int hm_render_pretrain(hm_render* h, int passes, void* stream) {
+  Render* r = (Render*)h;
+  if (!r || passes < 0) return hm_set_error("hm_render_pretrain: bad arguments"), HM_EINVAL;
+  if (passes == 0) return HM_OK;
+  return render_pretrain(r, passes, (cudaStream_t)stream);
 }
 
 extern "C" int hm_render_reset(hm_render* h) {

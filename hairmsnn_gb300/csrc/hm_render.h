@@ -44,6 +44,13 @@ struct FrameParams {
   int every_nth;   // one training pixel per every_nth pixels
   int n_train;     // training records per frame
   int in_ch;       // cache input channels (12)
+  // scene-sample training pass (TRAIN_DATA_GEN, hair_msnn.cu:222-233): the
+  // paths are n_train camera rays towards points sampled on the hair, all
+  // training paths; 0 for ordinary frames
+  int pretrain;
+  const float4* samples;  // points on the hair curves (xyz)
+  int n_samples;
+  uint32_t sample_key;    // permutation of the samples for this pass
 };
 
 struct FrameBufs {

@@ -22,12 +22,30 @@ HM_D f3 ld3(const float4* p, int i) {
 }
 HM_D void st3(float4* p, int i, f3 v, float w = 0.f) { p[i] = make_float4(v.x, v.y, v.z, w); }
 
+// Camera rays of one frame, or (fp.pretrain) the rays of the scene-sample
+// training pass: record r aims from the camera at sample perm(r) (the
+// reference's sceneIndices[trOfs], a shuffled index, hair_msnn.cu:222-233).
 __global__ void __launch_bounds__(256) camera_kernel(SceneDev s, FrameParams fp, PathState ps, int* queue,
                                                      int* count) {
-  const int P = s.width * s.height;
+  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid == 0) *count = P;
   if (pid >= P) return;
+  if (fp.pretrain) {
+    const uint32_t si = feistel_perm((uint32_t)pid, (uint32_t)fp.n_samples, fp.sample_key);
+    const float4 sp = fp.samples[si];
+    ps.rng[pid] = rng_seed(fp.frame_seed, (uint32_t)pid);
+    ps.flags[pid] = F_TRAIN;
+    ps.bounce[pid] = 0;
+    st3(ps.ray_o, pid, s.cam_pos);
+    st3(ps.ray_d, pid, normalize(mk(sp.x, sp.y, sp.z) - s.cam_pos));
+    st3(ps.beta, pid, splat(1.f));
+    st3(ps.beta_s, pid, splat(1.f));
+    st3(ps.col, pid, splat(0.f));
+    st3(ps.col_s, pid, splat(0.f));
+    queue[pid] = pid;
+    return;
+  }
   const int x = pid % s.width, y = pid / s.width;
   uint32_t rng = rng_seed(fp.frame_seed, (uint32_t)pid);
   uint32_t flags = 0;
@@ -168,7 +186,7 @@ HM_D bool anynan(f3 c) { return isnan(c.x) || isnan(c.y) || isnan(c.z); }
 HM_D bool anyinf(f3 c) { return isinf(c.x) || isinf(c.y) || isinf(c.z); }
 
 __global__ void __launch_bounds__(256) finalize_kernel(SceneDev s, FrameParams fp, PathState ps, FrameBufs fb) {
-  const int P = s.width * s.height;
+  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid >= P) return;
   const uint32_t flags = ps.flags[pid];
@@ -198,6 +216,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(SceneDev s, FrameParams f
     t[2] = c.z - sc.z;
     color = hit ? c : color;  // a miss keeps Le
   }
+  if (fp.pretrain) return;  // training records only
   const float w = (hit ? 1.f : 0.f) + ((flags & F_PRIM_SURF) ? 2.f : 0.f);
   fb.gbuf[pid] = make_float4(color.x, color.y, color.z, w);
 }
@@ -233,7 +252,7 @@ __global__ void __launch_bounds__(256) compose_kernel(SceneDev s, FrameParams fp
 
 int launch_camera(const SceneDev& s, const FrameParams& fp, const PathState& ps, int* queue, int* count,
                   cudaStream_t st) {
-  const int P = s.width * s.height;
+  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
   camera_kernel<<<(P + 255) / 256, 256, 0, st>>>(s, fp, ps, queue, count);
   HM_CHECK_LAUNCH("camera_kernel");
   return HM_OK;
@@ -248,7 +267,7 @@ int launch_shade(const SceneDev& s, const FrameParams& fp, const PathState& ps, 
 
 int launch_finalize(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
                     cudaStream_t st) {
-  const int P = s.width * s.height;
+  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
   finalize_kernel<<<(P + 255) / 256, 256, 0, st>>>(s, fp, ps, fb);
   HM_CHECK_LAUNCH("finalize_kernel");
   return HM_OK;

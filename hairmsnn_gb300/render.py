@@ -90,6 +90,7 @@ def _declare():
     L.hm_render_frame.argtypes = [vp, vp]
     L.hm_render_wait.argtypes = [vp, vp]
     L.hm_render_frames_in_flight.argtypes = [vp]
+    L.hm_render_pretrain.argtypes = [vp, i32, vp]
     L.hm_render_read_async.argtypes = [vp, i32, vp, vp]
     L.hm_render_reset.argtypes = [vp]
     L.hm_render_read.argtypes = [vp, i32, vp]
@@ -193,6 +194,10 @@ class Renderer:
     def frame(self, stream=None):
         """Enqueue one frame (asynchronous; see hm_render_frame)."""
         check(lib().hm_render_frame(self._h, _stream(stream)))
+
+    def pretrain(self, passes, stream=None):
+        """Scene-sample training of the cache (see hm_render_pretrain)."""
+        check(lib().hm_render_pretrain(self._h, int(passes), _stream(stream)))
 
     def depth(self):
         """Frames in flight (hm_render_options.frames_in_flight as resolved)."""
@@ -471,9 +476,10 @@ class RenderQualityWorkload(RenderBenchWorkload):
     name = "quality"
     metric = "paths/s at fixed relMSE vs PT (HairMSNN BETA=1, 512x512, 16 spp, online cache training 2^16/frame)"
 
-    def __init__(self, torch, width=512, height=512, train_records=1 << 16, spp=16, ref_spp=1024):
+    def __init__(self, torch, width=512, height=512, train_records=1 << 16, spp=16, ref_spp=1024,
+                 pretrain_passes=256):
         super().__init__(torch, width, height, train_records)
-        self.spp, self.ref_spp = spp, ref_spp
+        self.spp, self.ref_spp, self.pretrain_passes = spp, ref_spp, pretrain_passes
 
     def _timed_frames(self, r, n):
         torch = self.torch
@@ -505,6 +511,20 @@ class RenderQualityWorkload(RenderBenchWorkload):
             by_prec[name] = {"relmse": round(relmse(img, ref), 6), "ms_per_frame": round(t_ms, 3)}
             if name == "fp32":
                 ms_ms, ms_img = t_ms, img
+        # the reference's initial training before the first frame (one second
+        # of scene-sample passes there; a fixed pass count here)
+        ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
+                      frames_in_flight=self.frames_in_flight)
+        torch = self.torch
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        ms.pretrain(self.pretrain_passes)
+        t1.record()
+        torch.cuda.synchronize()
+        pre_ms = t0.elapsed_time(t1)
+        t_pre = self._timed_frames(ms, spp)
+        e_pre = relmse(ms.read(IMAGE_FINAL), ref)
+        ms.close()
         e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
         eq_spp = spp * e_pt / e_ms
         return {"spp": spp, "reference_spp": self.ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
@@ -513,6 +533,10 @@ class RenderQualityWorkload(RenderBenchWorkload):
                 "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
                        "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
                 "msnn_by_cache_precision": by_prec,
+                "msnn_after_scene_sample_training": {
+                    "passes": self.pretrain_passes, "training_ms": round(pre_ms, 1), "relmse": round(e_pre, 6),
+                    "ms_per_frame": round(t_pre, 3), "pt_spp_for_same_relmse": round(spp * e_pt / e_pre, 2),
+                    "speedup_at_equal_relmse": round((spp * e_pt / e_pre) * pt_ms / (spp * t_pre), 3)},
                 "pt_spp_for_msnn_relmse": round(eq_spp, 2),
                 "speedup_at_equal_relmse": round(eq_spp * pt_ms / (spp * ms_ms), 3)}
 

@@ -300,6 +300,15 @@ void hm_render_destroy(hm_render* render);
  * reused, or by hm_render_read / _get_stats / _reset, which synchronise).
  * With instrumentation on, frames run one at a time. */
 int hm_render_frame(hm_render* render, void* stream);
+/* Scene-sample training of the cache before rendering: the reference's
+ * initial training (render_hair_msnn.cu:641-650: genTrainingData + train for
+ * one second of wall time, TRAIN_DATA_GEN pass hair_msnn.cu:222-233) as an
+ * explicit number of passes.  Each pass traces train_records training paths
+ * aimed from the camera at points sampled on the hair (about 10^6, placed
+ * by segment length as fetchSceneSamples, render_hair_msnn.cu:34-97) and
+ * takes one training step.  HairMSNN renderers only; waits for frames in
+ * flight and returns when the passes have finished. */
+int hm_render_pretrain(hm_render* render, int passes, void* stream);
 /* Frames the renderer keeps in flight (the resolved frames_in_flight). */
 int hm_render_frames_in_flight(const hm_render* render);
 /* Makes `stream` wait for every frame in flight (no host synchronisation). */

@@ -198,3 +198,27 @@ def test_read_async_matches_read(R):
     for k in range(3):
         r2.frame()
     assert np.array_equal(sums[2].numpy() * (1.0 / 3), r2.read(R.IMAGE_FINAL))
+
+
+def test_scene_sample_training_lowers_cache_loss_and_error(R):
+    """hm_render_pretrain (the reference's initial training on scene samples)
+    trains the cache before the first frame: the training loss drops and the
+    first frames come out closer to a converged PT reference."""
+    cfg = small_cfg(R, 3000, 128)
+    s = R.Scene(cfg)
+    pt = R.Renderer(s, R.PT)
+    for _ in range(256):
+        pt.frame()
+    ref = pt.read(R.IMAGE_FINAL)
+    errs, losses = [], []
+    for passes in (0, 64):
+        r = R.Renderer(s, R.MSNN, beta=1, train_records=4096, train=True)
+        r.pretrain(passes)
+        losses.append(r.stats().last_loss)
+        for _ in range(4):
+            r.frame()
+        img = r.read(R.IMAGE_FINAL)
+        assert np.isfinite(img).all()
+        errs.append(R.relmse(img, ref))
+        r.close()
+    assert errs[1] < errs[0], errs

@@ -17,13 +17,13 @@
 
 namespace hm {
 
-int launch_camera(const SceneDev& s, const FrameParams& fp, const PathState& ps, int* queue, int* count,
-                  cudaStream_t st);
-int launch_shade(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
+int launch_camera(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, int* queue,
+                  int* count, cudaStream_t st);
+int launch_shade(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, const FrameBufs& fb,
                  const int* queue, const int* count, int* keep, int grid, cudaStream_t st);
-int launch_finalize(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
-                    cudaStream_t st);
-int launch_compose(const SceneDev& s, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st);
+int launch_finalize(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps,
+                    const FrameBufs& fb, cudaStream_t st);
+int launch_compose(int P, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st);
 
 // ---- persistent traversal with warp-aggregated dynamic ray fetching
 // Ray sources: extension rays (one per queued path), shadow rays (two slots
@@ -33,6 +33,7 @@ struct ExtendRays {
   const int* queue;
   const int* count;
   HM_D int n() const { return *count; }
+  HM_D int path(int i) const { return queue[i]; }
   HM_D bool ray(int i, f3* o, f3* d) const {
     const int pid = queue[i];
     const float4 a = ps.ray_o[pid], b = ps.ray_d[pid];
@@ -51,6 +52,7 @@ struct ShadowRays {
   const int* count;
   uint8_t* vis;  // [P][2]: 1 = unoccluded
   HM_D int n() const { return 2 * *count; }
+  HM_D int path(int i) const { return queue[i >> 1]; }
   HM_D bool ray(int i, f3* o, f3* d) const {
     const int pid = queue[i >> 1];
     if (!(ps.flags[pid] & F_DL)) return false;
@@ -71,6 +73,7 @@ struct BatchRays {
   float tmin, tmax;
   float4* out;
   HM_D int n() const { return (int)count; }
+  HM_D int path(int i) const { return i; }
   HM_D bool ray(int i, f3* o, f3* d) const {
     *o = mk(org[3 * i], org[3 * i + 1], org[3 * i + 2]);
     *d = mk(dir[3 * i], dir[3 * i + 1], dir[3 * i + 2]);
@@ -84,8 +87,11 @@ constexpr int kMaxRounds = 1 << 22;   // per-warp round cap (~6k rounds per warp
 
 // COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
 // cnt[0..2] (an untimed instrumentation pass; timed frames use COUNT = false).
-template <class Src, bool ANY_HIT, bool COUNT>
-__global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev s, float tmin, float tmax,
+// MULTI: the rays belong to the scenes of a batch (b.path_scene of the ray's
+// path selects the tree each lane walks).
+template <class Src, bool ANY_HIT, bool COUNT, bool MULTI>
+__global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __grid_constant__ SceneDev s0,
+                                                               Batch b, float tmin, float tmax,
                                                                int* __restrict__ fetch, int* err,
                                                                unsigned long long* cnt) {
   const unsigned FULL = 0xffffffffu;
@@ -94,6 +100,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
   if (n <= 0) return;  // an empty bounce: no ray-fetch atomics at all
   int2 stack[kStack];
   TravState t;
+  const SceneDev* sp = &s0;
   TraceCount tc{0, 0};
   uint32_t rays = 0;
   int cur = -1;
@@ -113,6 +120,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
         if (my < n) {
           f3 o, d;
           if (src.ray(my, &o, &d)) {
+            if (MULTI) sp = &b.scenes[b.path_scene[src.path(my)]].s;
             trav_init(t, o, d, tmin, tmax);
             cur = my;
             if (COUNT) ++rays;
@@ -137,11 +145,11 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
       if (needm == 0) break;
       const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.pend >= 0);
       if (parked != 0 && __popc(needm) <= kStragglers) break;
-      if (need) trav_inner_step<COUNT>(s, t, stack, err, &tc);
+      if (need) trav_inner_step<COUNT>(*sp, t, stack, err, &tc);
     }
     // leaf phase: the parked curve / triangle tests run together
     if (cur >= 0) {
-      const bool done = trav_leaf<ANY_HIT, COUNT>(s, t, &tc);
+      const bool done = trav_leaf<ANY_HIT, COUNT>(*sp, t, &tc);
       if (done || trav_finished(t)) {
         src.write(cur, t.h);
         cur = -1;
@@ -156,12 +164,23 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, SceneDev
 }
 
 template <class Src, bool ANY_HIT>
-static int launch_persistent(const Src& src, const SceneDev& s, float tmin, float tmax, int* fetch, int* err,
-                             unsigned long long* cnt, bool counting, int max_blocks, cudaStream_t st) {
-  if (counting)
-    persistent_trace_kernel<Src, ANY_HIT, true><<<max_blocks, 128, 0, st>>>(src, s, tmin, tmax, fetch, err, cnt);
-  else
-    persistent_trace_kernel<Src, ANY_HIT, false><<<max_blocks, 128, 0, st>>>(src, s, tmin, tmax, fetch, err, cnt);
+static int launch_persistent(const Src& src, const SceneDev& s, const Batch& b, float tmin, float tmax, int* fetch,
+                             int* err, unsigned long long* cnt, bool counting, int max_blocks, cudaStream_t st) {
+  if (b.scenes) {
+    if (counting)
+      persistent_trace_kernel<Src, ANY_HIT, true, true><<<max_blocks, 128, 0, st>>>(src, s, b, tmin, tmax, fetch,
+                                                                                    err, cnt);
+    else
+      persistent_trace_kernel<Src, ANY_HIT, false, true><<<max_blocks, 128, 0, st>>>(src, s, b, tmin, tmax, fetch,
+                                                                                     err, cnt);
+  } else {
+    if (counting)
+      persistent_trace_kernel<Src, ANY_HIT, true, false><<<max_blocks, 128, 0, st>>>(src, s, b, tmin, tmax, fetch,
+                                                                                     err, cnt);
+    else
+      persistent_trace_kernel<Src, ANY_HIT, false, false><<<max_blocks, 128, 0, st>>>(src, s, b, tmin, tmax, fetch,
+                                                                                      err, cnt);
+  }
   HM_CHECK_LAUNCH("persistent_trace_kernel");
   return HM_OK;
 }
@@ -171,7 +190,8 @@ static int persistent_blocks() {
   int dev = 0, sms = 152, per_sm = 4;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_trace_kernel<Src, ANY_HIT, false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, persistent_trace_kernel<Src, ANY_HIT, false, false>, 128,
+                                                0);
   return sms * std::max(1, per_sm);
 }
 
@@ -340,6 +360,13 @@ struct Render {
   bool train = true;
   uint32_t seed = 0;
   hm_mlp* mlp = nullptr;
+  // batch of scenes (hm_render_create_batch): the frame's paths are the
+  // scenes' pixels one scene after another; batch.scenes == nullptr otherwise
+  std::vector<Scene*> bscenes;
+  std::vector<int> bbeta;  // BETA - 1 per scene
+  std::vector<BatchScene> bhost;
+  Batch batch{nullptr, nullptr, 0};
+  int max_path_v2 = 0;
   float4* d_samples = nullptr;  // scene-sample training pass: points on the hair
   int n_samples = 0;
   int pretrain_passes = 0;
@@ -452,6 +479,17 @@ static int render_setup(Render* r, const hm_render_options* o) {
   Scene* s = r->scene;
   if (int st = s->ensure_built()) return st;
   r->P = s->width * s->height;
+  r->max_path_v2 = s->path_v2;
+  if (!r->bscenes.empty()) {
+    int64_t total = 0;
+    for (Scene* b : r->bscenes) {
+      if (int st = b->ensure_built()) return st;
+      total += (int64_t)b->width * b->height;
+      r->max_path_v2 = std::max(r->max_path_v2, b->path_v2);
+    }
+    if (total > INT32_MAX / 4) return hm_set_error("hm_render_create_batch: too many pixels"), HM_ECAPACITY;
+    r->P = (int)total;
+  }
   const int P = r->P;
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = r->alloc(&r->acc_pt, (size_t)P * 3);
@@ -470,7 +508,7 @@ static int render_setup(Render* r, const hm_render_options* o) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
-  r->fetch_slots = 2 * (s->path_v2 + 2);
+  r->fetch_slots = 2 * (r->max_path_v2 + 2);
   r->blocks_extend = persistent_blocks<ExtendRays, false>();
   r->blocks_shadow = persistent_blocks<ShadowRays, true>();
   if (r->mode == MODE_MSNN) {
@@ -478,6 +516,39 @@ static int render_setup(Render* r, const hm_render_options* o) {
     // everyNth = frameSize / numTrainRecords (integer division, render_hair_msnn.cu:106), at least 1
     r->every_nth = std::max(1, P / r->n_train);
     r->n_train = std::min(r->n_train, (P + r->every_nth - 1) / r->every_nth);
+  }
+  if (!r->bscenes.empty()) {
+    // one shared cache: every scene gives one training record per every_nth
+    // of its pixels, records stored scene after scene
+    int pix = 0, rec = 0;
+    r->bhost.clear();
+    for (size_t k = 0; k < r->bscenes.size(); ++k) {
+      Scene* b = r->bscenes[k];
+      BatchScene bs{};
+      bs.s = b->dev();
+      bs.pix_off = pix;
+      bs.n_pix = b->width * b->height;
+      bs.every_nth = r->every_nth;
+      bs.n_train = r->mode == MODE_MSNN ? (bs.n_pix + r->every_nth - 1) / r->every_nth : 0;
+      bs.train_off = rec;
+      bs.beta = r->bbeta[k];
+      pix += bs.n_pix;
+      rec += bs.n_train;
+      r->bhost.push_back(bs);
+    }
+    if (r->mode == MODE_MSNN) r->n_train = rec;
+    std::vector<int> owner(P);
+    for (size_t k = 0; k < r->bhost.size(); ++k)
+      std::fill(owner.begin() + r->bhost[k].pix_off, owner.begin() + r->bhost[k].pix_off + r->bhost[k].n_pix, (int)k);
+    BatchScene* d_bs = nullptr;
+    int* d_owner = nullptr;
+    e = r->alloc(&d_bs, r->bhost.size());
+    if (e == cudaSuccess) e = r->alloc(&d_owner, (size_t)P);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d_bs, r->bhost.data(), r->bhost.size() * sizeof(BatchScene), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d_owner, owner.data(), (size_t)P * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return hm_cuda_status(e, "batch tables");
+    r->batch = Batch{d_bs, d_owner, P};
   }
   if (r->depth <= 0) {
     // default: up to 6 frames in flight (the measured optimum at 512x512),
@@ -559,25 +630,25 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   if (counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
   cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
   mark(S_CAMERA);
-  if (int e = launch_camera(sd, fp, sl.ps, q_cur, c_cur, st)) return e;
+  if (int e = launch_camera(sd, fp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
   const int grid = r->sm_count * 8;
   const int nblocks = (r->P + kScanBlock - 1) / kScanBlock;
   int count = r->P;
   int bounces = 0;
   int64_t ext_rays = 0;
   const FrameBufs fb = sl.fb;
-  for (int it = 0; it <= s->path_v2 && count > 0; ++it) {
+  for (int it = 0; it <= r->max_path_v2 && count > 0; ++it) {
     cur_bounce = it;
     paths_at.push_back(count);
     mark(S_EXTEND);
-    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, 0.f, 1e30f,
+    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, r->batch, 0.f, 1e30f,
                                                      sl.fetch + 2 * it, sl.err, r->d_cnt, counting,
                                                      r->blocks_extend, st))
       return e;
     mark(S_SHADE);
-    if (int e = launch_shade(sd, fp, sl.ps, fb, q_cur, c_cur, sl.keep, grid, st)) return e;
+    if (int e = launch_shade(sd, fp, r->batch, sl.ps, fb, q_cur, c_cur, sl.keep, grid, st)) return e;
     mark(S_SHADOW);
-    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, 0.f, 1e30f,
+    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, r->batch, 0.f, 1e30f,
                                                     sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, counting,
                                                     r->blocks_shadow, st))
       return e;
@@ -610,12 +681,12 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     if (r->have_compose_ev) cudaStreamWaitEvent(st, r->ev_compose, 0);
     if (r->have_read_ev) cudaStreamWaitEvent(st, r->ev_read, 0);
     mark(S_FINALIZE);
-    if (int e = launch_finalize(sd, fp, sl.ps, fb, st)) return e;
+    if (int e = launch_finalize(sd, fp, r->batch, sl.ps, fb, st)) return e;
     cudaEventRecord(r->ev_compose, st);
     r->have_compose_ev = true;
   } else {
     mark(S_FINALIZE);
-    if (int e = launch_finalize(sd, fp, sl.ps, fb, st)) return e;
+    if (int e = launch_finalize(sd, fp, r->batch, sl.ps, fb, st)) return e;
     // cache step: after the previous frame's inference (weights and workspace)
     if (r->have_mlp_ev) cudaStreamWaitEvent(st, r->ev_mlp, 0);
     mark(S_TRAIN);
@@ -630,7 +701,7 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     if (r->have_compose_ev) cudaStreamWaitEvent(st, r->ev_compose, 0);
     if (r->have_read_ev) cudaStreamWaitEvent(st, r->ev_read, 0);
     mark(S_COMPOSE);
-    if (int e = launch_compose(sd, fp, fb, st)) return e;
+    if (int e = launch_compose(r->P, fp, fb, st)) return e;
     cudaEventRecord(r->ev_compose, st);
     r->have_compose_ev = true;
     hm_mlp_desc md;
@@ -683,16 +754,10 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
 
 using namespace hm;
 
-extern "C" hm_render* hm_render_create(hm_scene* scene, const hm_render_options* opt, int* status) {
-  int dummy;
-  if (!status) status = &dummy;
-  if (!scene) {
-    *status = HM_EINVAL;
-    hm_set_error("hm_render_create: NULL scene");
-    return nullptr;
-  }
+static hm_render* render_create(Scene* first, const std::vector<Scene*>& batch, const int* betas,
+                                const hm_render_options* opt, int* status) {
   Render* r = new Render();
-  r->scene = (Scene*)scene;
+  r->scene = first;
   if (opt) {
     r->mode = opt->mode;
     r->beta_knob = opt->beta;
@@ -702,26 +767,72 @@ extern "C" hm_render* hm_render_create(hm_scene* scene, const hm_render_options*
   } else {
     r->train = r->scene->cache_train;
   }
-  if (r->mode != MODE_PT && r->mode != MODE_MSNN) {
-    delete r;
-    *status = HM_EINVAL;
-    hm_set_error("hm_render_create: unknown mode");
-    return nullptr;
-  }
-  if (r->beta_knob < 1) {
-    delete r;
-    *status = HM_EINVAL;
-    hm_set_error("hm_render_create: BETA must be >= 1 (internal beta = BETA - 1)");
-    return nullptr;
-  }
-  int st = render_setup(r, opt);
-  if (st != HM_OK) {
+  auto fail = [&](int st, const char* msg) -> hm_render* {
     delete r;
     *status = st;
+    if (msg) hm_set_error("%s", msg);
     return nullptr;
+  };
+  if (r->mode != MODE_PT && r->mode != MODE_MSNN) return fail(HM_EINVAL, "hm_render_create: unknown mode");
+  // internal beta = BETA - 1 (render_hair_msnn.cu:1170); BETA = 0 stops the
+  // short path at the first bounce
+  if (r->beta_knob < 0) return fail(HM_EINVAL, "hm_render_create: BETA must be >= 0 (internal beta = BETA - 1)");
+  if (!batch.empty()) {
+    r->bscenes = batch;
+    for (size_t k = 0; k < batch.size(); ++k) {
+      const int bk = betas ? betas[k] : r->beta_knob;
+      if (bk < 0) return fail(HM_EINVAL, "hm_render_create_batch: BETA must be >= 0");
+      r->bbeta.push_back(bk - 1);
+    }
   }
+  int st = render_setup(r, opt);
+  if (st != HM_OK) return fail(st, nullptr);
   *status = HM_OK;
   return (hm_render*)r;
+}
+
+extern "C" hm_render* hm_render_create(hm_scene* scene, const hm_render_options* opt, int* status) {
+  int dummy;
+  if (!status) status = &dummy;
+  if (!scene) {
+    *status = HM_EINVAL;
+    hm_set_error("hm_render_create: NULL scene");
+    return nullptr;
+  }
+  return render_create((Scene*)scene, {}, nullptr, opt, status);
+}
+
+extern "C" hm_render* hm_render_create_batch(hm_scene* const* scenes, const int* betas, int n_scenes,
+                                             const hm_render_options* opt, int* status) {
+  int dummy;
+  if (!status) status = &dummy;
+  if (!scenes || n_scenes < 1) {
+    *status = HM_EINVAL;
+    hm_set_error("hm_render_create_batch: no scenes");
+    return nullptr;
+  }
+  std::vector<Scene*> v;
+  for (int k = 0; k < n_scenes; ++k) {
+    if (!scenes[k]) {
+      *status = HM_EINVAL;
+      hm_set_error("hm_render_create_batch: NULL scene %d", k);
+      return nullptr;
+    }
+    v.push_back((Scene*)scenes[k]);
+  }
+  return render_create(v[0], v, betas, opt, status);
+}
+
+extern "C" int hm_render_batch_scene(const hm_render* h, int scene, int* pixel_offset, int* width, int* height) {
+  const Render* r = (const Render*)h;
+  if (!r) return hm_set_error("hm_render_batch_scene: NULL"), HM_EINVAL;
+  const int n = r->bscenes.empty() ? 1 : (int)r->bscenes.size();
+  if (scene < 0 || scene >= n) return hm_set_error("hm_render_batch_scene: scene %d of %d", scene, n), HM_EINVAL;
+  const Scene* sc = r->bscenes.empty() ? r->scene : r->bscenes[scene];
+  if (pixel_offset) *pixel_offset = r->bscenes.empty() ? 0 : r->bhost[scene].pix_off;
+  if (width) *width = sc->width;
+  if (height) *height = sc->height;
+  return HM_OK;
 }
 
 extern "C" void hm_render_destroy(hm_render* h) { delete (Render*)h; }
@@ -827,6 +938,7 @@ static int build_scene_samples(Render* r) {
 // the reference's accumId during initial training.
 static int render_pretrain(Render* r, int passes, cudaStream_t user) {
   if (r->mode != MODE_MSNN) return hm_set_error("hm_render_pretrain: HairMSNN renderers only"), HM_EINVAL;
+  if (!r->bscenes.empty()) return hm_set_error("hm_render_pretrain: not available for batches"), HM_EUNSUPPORTED;
   if (int e = render_sync(r)) return e;
   if (!r->d_samples)
     if (int e = build_scene_samples(r)) return e;
@@ -847,14 +959,15 @@ static int render_pretrain(Render* r, int passes, cudaStream_t user) {
     int* c_cur = sl.counts;
     int* c_next = sl.counts + 1;
     cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
-    if (int e = launch_camera(sd, fp, sl.ps, q_cur, c_cur, st)) return e;
+    const Batch nob{nullptr, nullptr, 0};
+    if (int e = launch_camera(sd, fp, nob, sl.ps, q_cur, c_cur, st)) return e;
     for (int it = 0; it <= s->path_v2; ++it) {
-      if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, 0.f, 1e30f,
+      if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, nob, 0.f, 1e30f,
                                                        sl.fetch + 2 * it, sl.err, r->d_cnt, false,
                                                        r->blocks_extend, st))
         return e;
-      if (int e = launch_shade(sd, fp, sl.ps, sl.fb, q_cur, c_cur, sl.keep, grid, st)) return e;
-      if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, 0.f, 1e30f,
+      if (int e = launch_shade(sd, fp, nob, sl.ps, sl.fb, q_cur, c_cur, sl.keep, grid, st)) return e;
+      if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, nob, 0.f, 1e30f,
                                                       sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, false,
                                                       r->blocks_shadow, st))
         return e;
@@ -868,7 +981,7 @@ static int render_pretrain(Render* r, int passes, cudaStream_t user) {
       std::swap(q_cur, q_next);
       std::swap(c_cur, c_next);
     }
-    if (int e = launch_finalize(sd, fp, sl.ps, sl.fb, st)) return e;
+    if (int e = launch_finalize(sd, fp, nob, sl.ps, sl.fb, st)) return e;
     if (r->have_mlp_ev) cudaStreamWaitEvent(st, r->ev_mlp, 0);
     if (int e = hm_mlp_training_step(r->mlp, sl.fb.nn_train_in, sl.fb.nn_train_out, r->n_train, sl.d_loss, st))
       return e;
@@ -982,9 +1095,10 @@ extern "C" int hm_trace_rays(const hm_scene* h, const float* d_org, const float*
   if (e != cudaSuccess) return hm_cuda_status(e, "hm_trace_rays");
   cudaMemsetAsync(err, 0, 2 * sizeof(int), (cudaStream_t)stream);
   BatchRays src{d_org, d_dir, n, tmin, tmax, (float4*)d_hits};
-  int st = any_hit ? launch_persistent<BatchRays, true>(src, s->dev(), tmin, tmax, err + 1, err, nullptr, false,
+  const Batch nob{nullptr, nullptr, 0};
+  int st = any_hit ? launch_persistent<BatchRays, true>(src, s->dev(), nob, tmin, tmax, err + 1, err, nullptr, false,
                                                         persistent_blocks<BatchRays, true>(), (cudaStream_t)stream)
-                   : launch_persistent<BatchRays, false>(src, s->dev(), tmin, tmax, err + 1, err, nullptr, false,
+                   : launch_persistent<BatchRays, false>(src, s->dev(), nob, tmin, tmax, err + 1, err, nullptr, false,
                                                          persistent_blocks<BatchRays, false>(), (cudaStream_t)stream);
   if (st != HM_OK) {
     cudaFree(err);

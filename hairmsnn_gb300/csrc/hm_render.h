@@ -53,6 +53,35 @@ struct FrameParams {
   uint32_t sample_key;    // permutation of the samples for this pass
 };
 
+// Several scenes in one frame (a batch): the frame's paths, training
+// records and accumulators are the scenes' ranges one after another, and
+// every path knows its scene.  Single-scene frames pass scenes == nullptr.
+struct BatchScene {
+  SceneDev s;
+  int pix_off, n_pix;                 // paths [pix_off, pix_off + n_pix)
+  int train_off, n_train, every_nth;  // training records of this scene
+  int beta;                           // BETA - 1
+};
+struct Batch {
+  const BatchScene* scenes;  // device array
+  const int* path_scene;     // scene of every path
+  int n_paths;
+};
+
+// The scene and the per-scene knobs of one path.
+struct PathCtx {
+  const SceneDev* s;
+  int local;       // pixel index inside its scene
+  int train_base;  // first training record of its scene
+  int every_nth, n_train, beta;
+};
+template <bool MULTI>
+HM_D PathCtx path_ctx(const SceneDev& s, const FrameParams& fp, const Batch& b, int pid) {
+  if (!MULTI) return PathCtx{&s, pid, 0, fp.every_nth, fp.n_train, fp.beta};
+  const BatchScene& bs = b.scenes[b.path_scene[pid]];
+  return PathCtx{&bs.s, pid - bs.pix_off, bs.train_off, bs.every_nth, bs.n_train, bs.beta};
+}
+
 struct FrameBufs {
   float* nn_frame_in;   // [P][in_ch]
   float* nn_frame_out;  // [P][3]

@@ -25,9 +25,10 @@ HM_D void st3(float4* p, int i, f3 v, float w = 0.f) { p[i] = make_float4(v.x, v
 // Camera rays of one frame, or (fp.pretrain) the rays of the scene-sample
 // training pass: record r aims from the camera at sample perm(r) (the
 // reference's sceneIndices[trOfs], a shuffled index, hair_msnn.cu:222-233).
-__global__ void __launch_bounds__(256) camera_kernel(SceneDev s, FrameParams fp, PathState ps, int* queue,
-                                                     int* count) {
-  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
+template <bool MULTI>
+__global__ void __launch_bounds__(256) camera_kernel(const __grid_constant__ SceneDev s0, FrameParams fp, Batch b,
+                                                     PathState ps, int* queue, int* count) {
+  const int P = fp.pretrain ? fp.n_train : (MULTI ? b.n_paths : s0.width * s0.height);
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid == 0) *count = P;
   if (pid >= P) return;
@@ -37,8 +38,8 @@ __global__ void __launch_bounds__(256) camera_kernel(SceneDev s, FrameParams fp,
     ps.rng[pid] = rng_seed(fp.frame_seed, (uint32_t)pid);
     ps.flags[pid] = F_TRAIN;
     ps.bounce[pid] = 0;
-    st3(ps.ray_o, pid, s.cam_pos);
-    st3(ps.ray_d, pid, normalize(mk(sp.x, sp.y, sp.z) - s.cam_pos));
+    st3(ps.ray_o, pid, s0.cam_pos);
+    st3(ps.ray_d, pid, normalize(mk(sp.x, sp.y, sp.z) - s0.cam_pos));
     st3(ps.beta, pid, splat(1.f));
     st3(ps.beta_s, pid, splat(1.f));
     st3(ps.col, pid, splat(0.f));
@@ -46,14 +47,16 @@ __global__ void __launch_bounds__(256) camera_kernel(SceneDev s, FrameParams fp,
     queue[pid] = pid;
     return;
   }
-  const int x = pid % s.width, y = pid / s.width;
-  uint32_t rng = rng_seed(fp.frame_seed, (uint32_t)pid);
+  const PathCtx c = path_ctx<MULTI>(s0, fp, b, pid);
+  const SceneDev& s = *c.s;
+  const int x = c.local % s.width, y = c.local / s.width;
+  uint32_t rng = rng_seed(fp.frame_seed, (uint32_t)c.local);
   uint32_t flags = 0;
   if (fp.mode == MODE_MSNN) {
-    const int tr = pid / fp.every_nth;
-    if (tr < fp.n_train) {
-      const uint32_t pick = feistel_perm((uint32_t)tr, (uint32_t)fp.n_train, (uint32_t)fp.accum_id) % fp.every_nth;
-      if ((uint32_t)(pid % fp.every_nth) == pick) flags |= F_TRAIN;
+    const int tr = c.local / c.every_nth;
+    if (tr < c.n_train) {
+      const uint32_t pick = feistel_perm((uint32_t)tr, (uint32_t)c.n_train, (uint32_t)fp.accum_id) % c.every_nth;
+      if ((uint32_t)(c.local % c.every_nth) == pick) flags |= F_TRAIN;
     }
   }
   const float ox = lcg_next(rng), oy = lcg_next(rng);
@@ -79,14 +82,18 @@ HM_D void write_cache_input(float* dst, int in_ch, f3 p, f3 wo, f3 t) {
 }
 
 // Shades every path of `queue`; keep[i] = 1 if path queue[i] continues.
-__global__ void __launch_bounds__(128) shade_kernel(SceneDev s, FrameParams fp, PathState ps, FrameBufs fb,
-                                                    const int* __restrict__ queue, const int* __restrict__ count,
-                                                    int* __restrict__ keep) {
+template <bool MULTI>
+__global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ SceneDev s0, FrameParams fp, Batch b,
+                                                    PathState ps, FrameBufs fb, const int* __restrict__ queue,
+                                                    const int* __restrict__ count, int* __restrict__ keep) {
   const int n = *count;
-  const int v2_stop = s.path_v2 - 1;  // hair_msnn.cu:201 / path_tracing.cu:54
-  const int v1_stop = s.path_v1 - 1;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int pid = queue[i];
+    const PathCtx c = path_ctx<MULTI>(s0, fp, b, pid);
+    const SceneDev& s = *c.s;
+    const int v2_stop = s.path_v2 - 1;  // hair_msnn.cu:201 / path_tracing.cu:54
+    const int v1_stop = s.path_v1 - 1;
+    const int rec = c.train_base + c.local / c.every_nth;  // training record of a training path
     uint32_t flags = ps.flags[pid];
     const int k = ps.bounce[pid];
     const float4 h = ps.hit[pid];
@@ -100,8 +107,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneDev s, FrameParams fp, 
       if (fp.mode == MODE_MSNN) {
         write_cache_input(fb.nn_frame_in + (size_t)pid * fp.in_ch, fp.in_ch, splat(0.f), -1.f * rd, splat(0.f));
         if (train)
-          write_cache_input(fb.nn_train_in + (size_t)(pid / fp.every_nth) * fp.in_ch, fp.in_ch, splat(0.f),
-                            -1.f * rd, splat(0.f));
+          write_cache_input(fb.nn_train_in + (size_t)rec * fp.in_ch, fp.in_ch, splat(0.f), -1.f * rd, splat(0.f));
       }
       ps.flags[pid] = flags;
       keep[i] = 0;
@@ -118,7 +124,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneDev s, FrameParams fp, 
         const f3 pn = v.p / s.scene_scale;
         write_cache_input(fb.nn_frame_in + (size_t)pid * fp.in_ch, fp.in_ch, pn, v.wo, v.t);
         if (train)
-          write_cache_input(fb.nn_train_in + (size_t)(pid / fp.every_nth) * fp.in_ch, fp.in_ch, pn, v.wo, v.t);
+          write_cache_input(fb.nn_train_in + (size_t)rec * fp.in_ch, fp.in_ch, pn, v.wo, v.t);
       }
     }
     uint32_t rng = ps.rng[pid];
@@ -146,7 +152,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneDev s, FrameParams fp, 
       if (fp.mode == MODE_MSNN && train) {
         const float qs = fmaxf(0.05f, 1.f - luminance(beta_s));
         const float eps = lcg_next(rng);
-        if (eps < qs || k > fp.beta) beta_s = splat(0.f);
+        if (eps < qs || k > c.beta) beta_s = splat(0.f);
         if (eps < q) {
           done = true;
         } else {
@@ -155,7 +161,7 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneDev s, FrameParams fp, 
         }
       } else if (fp.mode == MODE_MSNN) {
         const float eps = lcg_next(rng);
-        if (eps < q || k > fp.beta) done = true;
+        if (eps < q || k > c.beta) done = true;
         else beta = beta / (1.f - q);
       } else {
         const float eps = lcg_next(rng);
@@ -185,8 +191,10 @@ __global__ void __launch_bounds__(128) shade_kernel(SceneDev s, FrameParams fp, 
 HM_D bool anynan(f3 c) { return isnan(c.x) || isnan(c.y) || isnan(c.z); }
 HM_D bool anyinf(f3 c) { return isinf(c.x) || isinf(c.y) || isinf(c.z); }
 
-__global__ void __launch_bounds__(256) finalize_kernel(SceneDev s, FrameParams fp, PathState ps, FrameBufs fb) {
-  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
+template <bool MULTI>
+__global__ void __launch_bounds__(256) finalize_kernel(const __grid_constant__ SceneDev s0, FrameParams fp, Batch b,
+                                                       PathState ps, FrameBufs fb) {
+  const int P = fp.pretrain ? fp.n_train : (MULTI ? b.n_paths : s0.width * s0.height);
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid >= P) return;
   const uint32_t flags = ps.flags[pid];
@@ -210,7 +218,8 @@ __global__ void __launch_bounds__(256) finalize_kernel(SceneDev s, FrameParams f
     if (anyinf(c)) c = splat(1e5f);
     if (anynan(sc)) sc = splat(0.01f);
     if (anyinf(sc)) sc = splat(1e5f);
-    float* t = fb.nn_train_out + (size_t)(pid / fp.every_nth) * 3;
+    const PathCtx pc = path_ctx<MULTI>(s0, fp, b, pid);
+    float* t = fb.nn_train_out + (size_t)(pc.train_base + pc.local / pc.every_nth) * 3;
     t[0] = c.x - sc.x;
     t[1] = c.y - sc.y;
     t[2] = c.z - sc.z;
@@ -221,8 +230,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(SceneDev s, FrameParams f
   fb.gbuf[pid] = make_float4(color.x, color.y, color.z, w);
 }
 
-__global__ void __launch_bounds__(256) compose_kernel(SceneDev s, FrameParams fp, FrameBufs fb) {
-  const int P = s.width * s.height;
+__global__ void __launch_bounds__(256) compose_kernel(int P, FrameParams fp, FrameBufs fb) {
   const int pid = blockIdx.x * blockDim.x + threadIdx.x;
   if (pid >= P) return;
   const float4 g = fb.gbuf[pid];
@@ -250,32 +258,40 @@ __global__ void __launch_bounds__(256) compose_kernel(SceneDev s, FrameParams fp
   }
 }
 
-int launch_camera(const SceneDev& s, const FrameParams& fp, const PathState& ps, int* queue, int* count,
-                  cudaStream_t st) {
-  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
-  camera_kernel<<<(P + 255) / 256, 256, 0, st>>>(s, fp, ps, queue, count);
+int launch_camera(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, int* queue,
+                  int* count, cudaStream_t st) {
+  const int P = fp.pretrain ? fp.n_train : (b.scenes ? b.n_paths : s.width * s.height);
+  if (b.scenes)
+    camera_kernel<true><<<(P + 255) / 256, 256, 0, st>>>(s, fp, b, ps, queue, count);
+  else
+    camera_kernel<false><<<(P + 255) / 256, 256, 0, st>>>(s, fp, b, ps, queue, count);
   HM_CHECK_LAUNCH("camera_kernel");
   return HM_OK;
 }
 
-int launch_shade(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
+int launch_shade(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, const FrameBufs& fb,
                  const int* queue, const int* count, int* keep, int grid, cudaStream_t st) {
-  shade_kernel<<<grid, 128, 0, st>>>(s, fp, ps, fb, queue, count, keep);
+  if (b.scenes)
+    shade_kernel<true><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep);
+  else
+    shade_kernel<false><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep);
   HM_CHECK_LAUNCH("shade_kernel");
   return HM_OK;
 }
 
-int launch_finalize(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
-                    cudaStream_t st) {
-  const int P = fp.pretrain ? fp.n_train : s.width * s.height;
-  finalize_kernel<<<(P + 255) / 256, 256, 0, st>>>(s, fp, ps, fb);
+int launch_finalize(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps,
+                    const FrameBufs& fb, cudaStream_t st) {
+  const int P = fp.pretrain ? fp.n_train : (b.scenes ? b.n_paths : s.width * s.height);
+  if (b.scenes)
+    finalize_kernel<true><<<(P + 255) / 256, 256, 0, st>>>(s, fp, b, ps, fb);
+  else
+    finalize_kernel<false><<<(P + 255) / 256, 256, 0, st>>>(s, fp, b, ps, fb);
   HM_CHECK_LAUNCH("finalize_kernel");
   return HM_OK;
 }
 
-int launch_compose(const SceneDev& s, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st) {
-  const int P = s.width * s.height;
-  compose_kernel<<<(P + 255) / 256, 256, 0, st>>>(s, fp, fb);
+int launch_compose(int P, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st) {
+  compose_kernel<<<(P + 255) / 256, 256, 0, st>>>(P, fp, fb);
   HM_CHECK_LAUNCH("compose_kernel");
   return HM_OK;
 }

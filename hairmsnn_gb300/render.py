@@ -91,6 +91,9 @@ def _declare():
     L.hm_render_wait.argtypes = [vp, vp]
     L.hm_render_frames_in_flight.argtypes = [vp]
     L.hm_render_pretrain.argtypes = [vp, i32, vp]
+    L.hm_render_create_batch.restype = vp
+    L.hm_render_create_batch.argtypes = [P(vp), P(i32), i32, P(hm_render_options), P(i32)]
+    L.hm_render_batch_scene.argtypes = [vp, i32, P(i32), P(i32), P(i32)]
     L.hm_render_read_async.argtypes = [vp, i32, vp, vp]
     L.hm_render_reset.argtypes = [vp]
     L.hm_render_read.argtypes = [vp, i32, vp]
@@ -247,6 +250,44 @@ class Renderer:
         host = np.zeros(count, np.float32)
         check(lib().hm_copy_to_host(host.ctypes.data_as(ctypes.c_void_p), p, count * 4))
         return host.reshape(-1, width)
+
+
+class BatchRenderer(Renderer):
+    """Many scenes rendered as one (hm_render_create_batch): one frame() takes
+    one sample per pixel of every scene; one cache network serves them all.
+    read_scene(k) returns scene k's image."""
+
+    def __init__(self, scenes, mode=MSNN, betas=None, train_records=16384, train=True, precision=0, seed=0,
+                 cache_config=None, frames_in_flight=0):
+        _declare()
+        self.scenes = list(scenes)
+        n = len(self.scenes)
+        o = hm_render_options(mode, int(betas[0]) if betas is not None else 1, train_records, 1 if train else 0,
+                              precision, seed, cache_config.encode() if cache_config else None, frames_in_flight)
+        arr = (ctypes.c_void_p * n)(*[sc._h.value for sc in self.scenes])
+        b = (ctypes.c_int * n)(*[int(x) for x in betas]) if betas is not None else None
+        st = ctypes.c_int(0)
+        h = lib().hm_render_create_batch(arr, b, n, ctypes.byref(o), ctypes.byref(st))
+        if not h:
+            check(st.value)
+        self._h = ctypes.c_void_p(h)
+        self.mode = mode
+        self.layout = []
+        for k in range(n):
+            off, w, hh = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+            check(lib().hm_render_batch_scene(self._h, k, ctypes.byref(off), ctypes.byref(w), ctypes.byref(hh)))
+            self.layout.append((off.value, w.value, hh.value))
+        self.pixels = sum(w * hh for _, w, hh in self.layout)
+        self.width, self.height = self.pixels, 1
+
+    def read(self, which=IMAGE_FINAL):
+        img = np.zeros((self.pixels, 3), np.float64)
+        check(lib().hm_render_read(self._h, which, img.ctypes.data_as(ctypes.c_void_p)))
+        return img
+
+    def read_scene(self, k, which=IMAGE_FINAL):
+        off, w, h = self.layout[k]
+        return self.read(which)[off:off + w * h].reshape(h, w, 3)
 
 
 def relmse(img, ref, eps=1e-2):

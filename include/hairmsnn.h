@@ -270,7 +270,7 @@ enum hm_image { HM_IMAGE_FINAL = 0, HM_IMAGE_SHORT = 1, HM_IMAGE_CACHE = 2 };
 
 typedef struct hm_render_options {
   int mode;                      /* hm_render_mode */
-  int beta;                      /* BETA >= 1 */
+  int beta;                      /* BETA >= 0 (internal beta = BETA - 1) */
   int train_records;             /* per frame; 0 = 16384 (render_hair_msnn.h:127-129) */
   int train;                     /* online cache training on/off (tcnn.init_train) */
   int cache_precision;           /* HM_PREC_* */
@@ -300,6 +300,17 @@ void hm_render_destroy(hm_render* render);
  * reused, or by hm_render_read / _get_stats / _reset, which synchronise).
  * With instrumentation on, frames run one at a time. */
 int hm_render_frame(hm_render* render, void* stream);
+/* Many scenes rendered as one (no reference counterpart; the batched-render
+ * configuration): every frame takes one sample per pixel of every scene, the
+ * paths of all scenes share the same kernel launches (each path knows its
+ * scene and walks that scene's tree), and one cache network is trained on
+ * and queried for all of them.  betas: per-scene BETA (NULL: options->beta).
+ * Images are stored scene after scene: read them with hm_render_read
+ * ([total pixels][3]) and slice with hm_render_batch_scene, which gives a
+ * scene's first pixel and size (single-scene renderers: scene 0). */
+hm_render* hm_render_create_batch(hm_scene* const* scenes, const int* betas, int n_scenes,
+                                  const hm_render_options* options, int* status);
+int hm_render_batch_scene(const hm_render* render, int scene, int* pixel_offset, int* width, int* height);
 /* Scene-sample training of the cache before rendering: the reference's
  * initial training (render_hair_msnn.cu:641-650: genTrainingData + train for
  * one second of wall time, TRAIN_DATA_GEN pass hair_msnn.cu:222-233) as an

@@ -361,6 +361,9 @@ def make_workload(name, torch):
         return VertexWorkload(torch)
     if name == "precision":
         return PrecisionWorkload(torch)
+    if name == "batch":
+        from hairmsnn_gb300 import render as _r
+        return _r.BatchBenchWorkload(torch)
     if name == "quality":
         from hairmsnn_gb300 import render as _r
         return _r.RenderQualityWorkload(torch)
@@ -449,7 +452,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "render"),
-                    choices=["render", "vertex", "precision", "quality"])
+                    choices=["render", "vertex", "precision", "quality", "batch"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)

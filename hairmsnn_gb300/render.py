@@ -592,6 +592,83 @@ class RenderQualityWorkload(RenderBenchWorkload):
         return c
 
 
+def batch_scene_configs(n=64, seed=0):
+    """The batched-render workload's scenes (seeded): square images of side
+    128, 256, 512 or 1024; log-uniform 2k-50k curly strands (helix radius
+    2-8 mm, pitch 5-20 mm, 48-128 control points, 20 cm long); BETA uniform
+    in 0..10; sigma_a uniform in [0.02, 0.5]^3.  Returns (configs, betas)."""
+    rng = np.random.default_rng(seed)
+    cfgs, betas = [], []
+    for k in range(n):
+        side = int(rng.choice([128, 256, 512, 1024]))
+        strands = int(np.exp(rng.uniform(np.log(2000), np.log(50000))))
+        cps = int(rng.integers(48, 129))
+        cfg = straight_hair_scene(side, side, strands=strands, control_points=cps, seed=1000 + k)
+        p = cfg["hair"]["procedural"]
+        p["type"] = "curly"
+        p["helix_radius"] = float(rng.uniform(0.02, 0.08))   # scene unit = 10 cm
+        p["helix_pitch"] = float(rng.uniform(0.05, 0.2))
+        cfg["hair"]["sigma_a"] = [float(x) for x in rng.uniform(0.02, 0.5, 3)]
+        cfgs.append(cfg)
+        betas.append(int(rng.integers(0, 11)))
+    return cfgs, betas
+
+
+class BatchBenchWorkload(RenderBenchWorkload):
+    """bench.py workload: one frame (1 spp) of each of 64 uneven scenes,
+    rendered as one batch with one shared FP32 cache network (width 64)."""
+
+    name = "batch"
+    metric = "paths/s (64 concurrent HairMSNN scenes, 128^2..1024^2, 2k-50k curly strands, one shared cache)"
+    unit = "paths/s"
+
+    def __init__(self, torch, n_scenes=64, train_records=1 << 16):
+        import time
+        self.torch = torch
+        self.train_records = train_records
+        t0 = time.perf_counter()
+        cfgs, self.betas = batch_scene_configs(n_scenes)
+        self.scenes = [Scene(c) for c in cfgs]
+        for sc in self.scenes:
+            sc.build()
+        self.setup_s = time.perf_counter() - t0
+        self.r = BatchRenderer(self.scenes, MSNN, betas=self.betas, train_records=train_records, train=True)
+        self.P = self.r.pixels
+        self.h2d_bytes = 0
+        self.d2h_bytes = self.P * 3 * 8
+        self.stage_ms = []
+        self.launches = []
+        self.read_stream = torch.cuda.Stream()
+        self.host_sums = [torch.empty((self.P, 3), dtype=torch.float64, pin_memory=True) for _ in range(2)]
+        self.n_scenes = n_scenes
+        infos = [sc.info() for sc in self.scenes]
+        self.stats_scenes = {"pixels": self.P, "segments": int(sum(i.n_segments for i in infos)),
+                             "strands": int(sum(i.n_strands for i in infos))}
+
+    def e2e_region(self, steps):
+        import time
+        torch = self.torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for k in range(steps):
+            self.r.frame()
+            self.r.read_async(self.host_sums[k & 1], IMAGE_FINAL, stream=self.read_stream)
+        torch.cuda.synchronize()
+        return 1e3 * (time.perf_counter() - t0) / steps
+
+    def config(self):
+        return {"workload": f"batch: {self.n_scenes} scenes (seeded), sides 128/256/512/1024, log-uniform 2k-50k "
+                            "curly strands (helix r 2-8 mm, pitch 5-20 mm, 48-128 CPs), BETA 0..10, sigma_a "
+                            "U[0.02,0.5]^3, one shared FP32 cache (HashGrid/OneBlob MLP 64x2), 2^16 records/frame",
+                **self.stats_scenes, "frames_in_flight": self.r.depth(), "scene_setup_s": round(self.setup_s, 1),
+                "l2": "inputs larger than L2 (path state of tens of millions of paths); no flush kernel",
+                "parallelism": "replicas"}
+
+    def cpu_baseline(self, threads, budget_s=20.0):
+        return {"value": None, "unit": self.unit, "cores": threads, "kind": "port",
+                "sample": "not run for the batch workload (see the render workload's CPU baseline)"}
+
+
 def _default_cache_config():
     return {
         "loss": {"otype": "RelativeL2Luminance"},

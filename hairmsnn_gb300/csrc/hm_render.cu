@@ -382,7 +382,9 @@ struct Render {
   int last_bounces = 0;
   int sm_count = 152;
   int fetch_slots = 0;
-  int blocks_extend = 0, blocks_shadow = 0;
+  int blocks_extend = 0, blocks_shadow = 0;  // persistent traversal grids
+  int blocks_extend_max = 0, blocks_shadow_max = 0;
+  int shade_blocks_per_sm = 8;                // shading grid = SMs x this
   int last_error = 0;
   // instrumentation (synchronous frames)
   bool timing = false, counting = false;
@@ -509,8 +511,8 @@ static int render_setup(Render* r, const hm_render_options* o) {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
   r->fetch_slots = 2 * (r->max_path_v2 + 2);
-  r->blocks_extend = persistent_blocks<ExtendRays, false>();
-  r->blocks_shadow = persistent_blocks<ShadowRays, true>();
+  r->blocks_extend = r->blocks_extend_max = persistent_blocks<ExtendRays, false>();
+  r->blocks_shadow = r->blocks_shadow_max = persistent_blocks<ShadowRays, true>();
   if (r->mode == MODE_MSNN) {
     r->n_train = o && o->train_records > 0 ? o->train_records : 16384;
     // everyNth = frameSize / numTrainRecords (integer division, render_hair_msnn.cu:106), at least 1
@@ -631,7 +633,7 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
   mark(S_CAMERA);
   if (int e = launch_camera(sd, fp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
-  const int grid = r->sm_count * 8;
+  const int grid = r->sm_count * r->shade_blocks_per_sm;
   const int nblocks = (r->P + kScanBlock - 1) / kScanBlock;
   int count = r->P;
   int bounces = 0;
@@ -864,6 +866,97 @@ extern "C" int hm_render_read_async(hm_render* h, int which, double* host_dst, v
   if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_read_async");
   r->have_read_ev = true;
   return HM_OK;
+}
+
+// ---- launch-shape autotuner
+// Times pipelined frames for candidate launch shapes and keeps the fastest:
+// the persistent traversal grids (resident blocks per SM, extension and
+// shadow rays tuned together, then each alone) and the shading grid.  These
+// shapes do not change any result (every ray and path is computed alone), and
+// the tuning frames neither train the cache nor stay in the image: training
+// is paused and the renderer is reset afterwards, so a tuned renderer renders
+// exactly what an untuned one does.
+static int render_autotune(Render* r, int frames, cudaStream_t user, hm_render_tuning* out) {
+  if (int e = render_sync(r)) return e;
+  const bool train = r->train;
+  r->train = false;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  auto time_frames = [&](float* ms) -> int {
+    cudaEventRecord(a, user);
+    for (int k = 0; k < frames; ++k)
+      if (int e = render_frame(r, user, false)) return e;
+    for (auto& sl : r->slots)
+      if (sl.in_flight) cudaStreamWaitEvent(user, sl.done, 0);
+    cudaEventRecord(b, user);
+    cudaError_t e = cudaEventSynchronize(b);
+    if (e != cudaSuccess) return hm_cuda_status(e, "autotune");
+    cudaEventElapsedTime(ms, a, b);
+    return render_sync(r);
+  };
+  int status = HM_OK;
+  float warm = 0.f;
+  status = time_frames(&warm);  // warm-up at the current shapes
+  const int sms = r->sm_count;
+  const int ext_max = r->blocks_extend_max / sms, sh_max = r->blocks_shadow_max / sms;
+  auto tune = [&](int* ext_per_sm, int* sh_per_sm, bool both, bool ext_only) {
+    float best = 1e30f;
+    int best_e = *ext_per_sm, best_s = *sh_per_sm;
+    const int hi = std::max(ext_max, sh_max);
+    for (int c = 2; c <= hi && status == HM_OK; ++c) {
+      const int ce = both || ext_only ? std::min(c, ext_max) : *ext_per_sm;
+      const int cs = both || !ext_only ? std::min(c, sh_max) : *sh_per_sm;
+      r->blocks_extend = ce * sms;
+      r->blocks_shadow = cs * sms;
+      float ms = 0.f;
+      status = time_frames(&ms);
+      if (ms < best) {
+        best = ms;
+        best_e = ce;
+        best_s = cs;
+      }
+    }
+    *ext_per_sm = best_e;
+    *sh_per_sm = best_s;
+    r->blocks_extend = best_e * sms;
+    r->blocks_shadow = best_s * sms;
+    return best;
+  };
+  int e_per_sm = ext_max, s_per_sm = sh_max;
+  tune(&e_per_sm, &s_per_sm, true, false);
+  tune(&e_per_sm, &s_per_sm, false, true);
+  float best_ms = tune(&e_per_sm, &s_per_sm, false, false);
+  int best_grid = r->shade_blocks_per_sm;
+  for (int g : {4, 8, 16}) {
+    if (status != HM_OK) break;
+    r->shade_blocks_per_sm = g;
+    float ms = 0.f;
+    status = time_frames(&ms);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_grid = g;
+    }
+  }
+  r->shade_blocks_per_sm = best_grid;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  r->train = train;
+  // forget the tuning frames
+  r->accum_id = 0;
+  if (out) {
+    out->extend_blocks_per_sm = e_per_sm;
+    out->shadow_blocks_per_sm = s_per_sm;
+    out->shade_blocks_per_sm = best_grid;
+    out->ms_per_frame = best_ms / (float)std::max(1, frames);
+  }
+  return status;
+}
+
+extern "C" int hm_render_autotune(hm_render* h, int frames, void* stream, hm_render_tuning* out) {
+  Render* r = (Render*)h;
+  if (!r || frames < 1) return hm_set_error("hm_render_autotune: bad arguments"), HM_EINVAL;
+  return render_autotune(r, frames, (cudaStream_t)stream, out);
 }
 
 extern "C" int hm_render_frames_in_flight(const hm_render* h) {

@@ -40,6 +40,11 @@ class hm_render_options(ctypes.Structure):
                 ("cache_config_json", ctypes.c_char_p), ("frames_in_flight", ctypes.c_int)]
 
 
+class hm_render_tuning(ctypes.Structure):
+    _fields_ = [("extend_blocks_per_sm", ctypes.c_int), ("shadow_blocks_per_sm", ctypes.c_int),
+                ("shade_blocks_per_sm", ctypes.c_int), ("ms_per_frame", ctypes.c_float)]
+
+
 class hm_render_stats(ctypes.Structure):
     _fields_ = [("frames", ctypes.c_int), ("pixels", ctypes.c_int), ("extension_rays", ctypes.c_int64),
                 ("last_bounces", ctypes.c_int), ("train_records", ctypes.c_int), ("every_nth", ctypes.c_int),
@@ -94,6 +99,7 @@ def _declare():
     L.hm_render_create_batch.restype = vp
     L.hm_render_create_batch.argtypes = [P(vp), P(i32), i32, P(hm_render_options), P(i32)]
     L.hm_render_batch_scene.argtypes = [vp, i32, P(i32), P(i32), P(i32)]
+    L.hm_render_autotune.argtypes = [vp, i32, vp, P(hm_render_tuning)]
     L.hm_render_read_async.argtypes = [vp, i32, vp, vp]
     L.hm_render_reset.argtypes = [vp]
     L.hm_render_read.argtypes = [vp, i32, vp]
@@ -197,6 +203,12 @@ class Renderer:
     def frame(self, stream=None):
         """Enqueue one frame (asynchronous; see hm_render_frame)."""
         check(lib().hm_render_frame(self._h, _stream(stream)))
+
+    def autotune(self, frames=4, stream=None):
+        """Pick the fastest launch shapes (see hm_render_autotune); returns them."""
+        t = hm_render_tuning()
+        check(lib().hm_render_autotune(self._h, int(frames), _stream(stream), ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in t._fields_}
 
     def pretrain(self, passes, stream=None):
         """Scene-sample training of the cache (see hm_render_pretrain)."""
@@ -343,6 +355,7 @@ class RenderBenchWorkload:
         self.scene.build()
         self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True,
                           frames_in_flight=frames_in_flight)
+        self.tuning = self.r.autotune(frames=6)
         self.P = width * height
         self.h2d_bytes = 0
         self.d2h_bytes = self.P * 3 * 8
@@ -466,6 +479,7 @@ class RenderBenchWorkload:
                       "several frames in flight, past the 129 MB L2 (scene: 4-wide BVH 40 MB + curves 10 MB); "
                       "no flush kernel",
                 "frames_in_flight": self.r.depth(),
+                "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
                 "parallelism": "replicas"}
 
     def cpu_baseline(self, threads, budget_s=20.0):
@@ -633,6 +647,7 @@ class BatchBenchWorkload(RenderBenchWorkload):
             sc.build()
         self.setup_s = time.perf_counter() - t0
         self.r = BatchRenderer(self.scenes, MSNN, betas=self.betas, train_records=train_records, train=True)
+        self.tuning = self.r.autotune(frames=1)
         self.P = self.r.pixels
         self.h2d_bytes = 0
         self.d2h_bytes = self.P * 3 * 8
@@ -661,6 +676,7 @@ class BatchBenchWorkload(RenderBenchWorkload):
                             "curly strands (helix r 2-8 mm, pitch 5-20 mm, 48-128 CPs), BETA 0..10, sigma_a "
                             "U[0.02,0.5]^3, one shared FP32 cache (HashGrid/OneBlob MLP 64x2), 2^16 records/frame",
                 **self.stats_scenes, "frames_in_flight": self.r.depth(), "scene_setup_s": round(self.setup_s, 1),
+                "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
                 "l2": "inputs larger than L2 (path state of tens of millions of paths); no flush kernel",
                 "parallelism": "replicas"}
 

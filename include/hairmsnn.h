@@ -320,6 +320,17 @@ int hm_render_batch_scene(const hm_render* render, int scene, int* pixel_offset,
  * takes one training step.  HairMSNN renderers only; waits for frames in
  * flight and returns when the passes have finished. */
 int hm_render_pretrain(hm_render* render, int passes, void* stream);
+/* Launch-shape autotuner (no reference counterpart): times `frames`
+ * pipelined frames per candidate and keeps the fastest persistent-traversal
+ * grids (resident blocks per SM) and shading grid.  The shapes change no
+ * result; the tuning frames do not train the cache and are dropped from the
+ * image (the renderer is reset), so a tuned renderer renders bit for bit
+ * what an untuned one does.  `out` (may be NULL) receives the choice. */
+typedef struct hm_render_tuning {
+  int extend_blocks_per_sm, shadow_blocks_per_sm, shade_blocks_per_sm;
+  float ms_per_frame; /* best time per frame seen while tuning */
+} hm_render_tuning;
+int hm_render_autotune(hm_render* render, int frames, void* stream, hm_render_tuning* out);
 /* Frames the renderer keeps in flight (the resolved frames_in_flight). */
 int hm_render_frames_in_flight(const hm_render* render);
 /* Makes `stream` wait for every frame in flight (no host synchronisation). */

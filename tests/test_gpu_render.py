@@ -222,3 +222,22 @@ def test_scene_sample_training_lowers_cache_loss_and_error(R):
         errs.append(R.relmse(img, ref))
         r.close()
     assert errs[1] < errs[0], errs
+
+
+def test_autotuned_renderer_renders_the_same_image(R):
+    """The autotuner only changes launch shapes; its frames neither train the
+    cache nor stay in the image."""
+    cfg = small_cfg(R, 800, 64)
+    imgs = []
+    for tune in (False, True):
+        s = R.Scene(cfg)
+        r = R.Renderer(s, R.MSNN, beta=2, train_records=1024, train=True, seed=9)
+        if tune:
+            t = r.autotune(frames=2)
+            assert 2 <= t["extend_blocks_per_sm"] and t["shade_blocks_per_sm"] in (4, 8, 16)
+        for _ in range(4):
+            r.frame()
+        imgs.append([r.read(w) for w in (R.IMAGE_FINAL, R.IMAGE_SHORT, R.IMAGE_CACHE)])
+        r.close()
+    for a, b in zip(*imgs):
+        assert np.array_equal(a, b)

@@ -413,24 +413,6 @@ __global__ void __launch_bounds__(256) mlp_fwd_kernel(const float* __restrict__ 
   }
 }
 
-// Loss gradient of one query (tcnn semantics, averaged over n * out_ch).
-HM_D void loss_grad(int loss, const float* pred, const float* tgt, int out_ch, float inv_total,
-                    float* grad, float* value) {
-  float lum2 = 0.f;
-  if (loss == LOSS_REL_L2_LUM) {
-    float lum = 0.299f * pred[0] + 0.587f * pred[1] + 0.114f * pred[2];
-    lum2 = lum * lum + 0.01f;
-  }
-  float v = 0.f;
-  for (int o = 0; o < out_ch; ++o) {
-    float diff = pred[o] - tgt[o];
-    float den = loss == LOSS_L2 ? 1.f : (loss == LOSS_REL_L2 ? pred[o] * pred[o] + 0.01f : lum2);
-    v += diff * diff / den * inv_total;
-    grad[o] = 2.f * diff / den * inv_total;
-  }
-  *value = v;
-}
-
 // Fused backward of one 64-query tile.  Inputs: X (encoded), acts (h_1..h_L),
 // pred [n][16], target [n][out_ch].  Outputs: dZ of every layer
 // (dz [L+1][n][16 or W]: index L is dOut), per-block loss partials, and dX
@@ -648,6 +630,11 @@ struct Mlp {
   int64_t params_version = 1, packed_version = 0;
   int* tc_err_host = nullptr;  // host-mapped timeout flag of the kernel
   int* tc_err_dev = nullptr;
+  // FP16 / BF16 handles also train on the tensor cores; FP16 gradients carry
+  // a static loss scale of 128 (BF16: 1), divided out in the optimizer step
+  TcTrainBufs tcb;
+  float loss_scale = 1.f;
+  bool tc_train = false;
 };
 
 }  // namespace hm
@@ -816,6 +803,8 @@ extern "C" hm_mlp* hm_mlp_create(const char* config_json, int in_ch, int out_ch,
       int st = tc_pack_alloc(m->cfg.d, precision, &m->tc);
       if (st != HM_OK) e = cudaErrorMemoryAllocation;
     }
+    m->tc_train = tc_trainable(m->cfg.d, precision);
+    m->loss_scale = precision == HM_PREC_FP16 ? 128.f : 1.f;
   }
   if (e != cudaSuccess) {
     *status = hm_cuda_status(e, "hm_mlp_create");
@@ -849,6 +838,7 @@ extern "C" void hm_mlp_destroy(hm_mlp* h) {
   cudaFree(m->loss_dev);
   cudaFree(m->grid_acc);
   tc_pack_free(&m->tc);
+  tc_train_free(&m->tcb);
   if (m->tc_err_host) cudaFreeHost(m->tc_err_host);
   delete m;
 }
@@ -891,6 +881,8 @@ extern "C" int hm_mlp_get_gradients(const hm_mlp* h, float* host_out) {
   const Mlp* m = (const Mlp*)h;
   if (!m || !host_out) return hm_set_error("hm_mlp_get_gradients: NULL"), HM_EINVAL;
   cudaError_t e = cudaMemcpy(host_out, m->grads, m->n_params * sizeof(float), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && m->tc_train && m->loss_scale != 1.f)  // undo the FP16 loss scale
+    for (int64_t i = 0; i < m->n_params; ++i) host_out[i] /= m->loss_scale;
   return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_mlp_get_gradients");
 }
 
@@ -906,6 +898,15 @@ extern "C" int hm_mlp_reset(hm_mlp* h) {
   m->lr = m->cfg.adam.lr;
   m->params_version += 1;
   return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_mlp_reset");
+}
+
+// A bounded tensor-core wait that expired in an earlier call is reported here.
+static int tc_prepare(Mlp* m) {
+  if (*(volatile int*)m->tc_err_host) {
+    *m->tc_err_host = 0;
+    return hm_set_error("mlp: a tensor-core wait expired in an earlier call"), HM_ETIMEOUT;
+  }
+  return HM_OK;
 }
 
 // Inference on the tensor cores (FP16 / BF16 / E4M3 operands, FP32
@@ -951,13 +952,31 @@ extern "C" int hm_mlp_forward(hm_mlp* h, const float* d_in, float* d_out, int64_
   if (int s = check_io("hm_mlp_forward", m, d_in, d_in, n)) return s;
   if (n == 0) return HM_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  if (int s = ensure_ws(m, n)) return s;
-  if (int s = encode(m, d_in, n, st)) return s;
-  if (int s = dispatch_fwd(m, m->X, m->pred, 16, m->acts, n, st)) return s;
+  const float* pred = nullptr;
+  if (m->tc_train) {
+    if (int s = tc_prepare(m)) return s;
+    if (n > m->tcb.cap) {
+      const int64_t cap = std::max<int64_t>((n + 127) / 128 * 128, 1024);
+      if (int s = tc_train_alloc(m->cfg.d, cap, m->cfg.d.n_enc_params > 0, &m->tcb)) return s;
+    }
+    if (m->packed_version != m->params_version) {
+      if (int s = tc_pack(m->cfg.d, m->params, m->tc, st)) return s;
+      m->packed_version = m->params_version;
+    }
+    if (int s = tc_train_forward(m->cfg.d, m->tc, m->params + m->cfg.d.n_net_params, d_in, n, m->tcb, m->tc_err_dev,
+                                 st))
+      return s;
+    pred = m->tcb.pred;
+  } else {
+    if (int s = ensure_ws(m, n)) return s;
+    if (int s = encode(m, d_in, n, st)) return s;
+    if (int s = dispatch_fwd(m, m->X, m->pred, 16, m->acts, n, st)) return s;
+    pred = m->pred;
+  }
   m->last_n = n;
   m->last_in = d_in;
   if (d_out) {
-    cudaError_t e = cudaMemcpy2DAsync(d_out, m->cfg.d.out_ch * sizeof(float), m->pred, 16 * sizeof(float),
+    cudaError_t e = cudaMemcpy2DAsync(d_out, m->cfg.d.out_ch * sizeof(float), pred, 16 * sizeof(float),
                                       m->cfg.d.out_ch * sizeof(float), n, cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) return hm_cuda_status(e, "hm_mlp_forward copy");
   }
@@ -974,6 +993,29 @@ extern "C" int hm_mlp_backward(hm_mlp* h, const float* d_target, int64_t n, floa
   cudaStream_t st = (cudaStream_t)stream;
   const MlpDims& d = m->cfg.d;
   if (int s = set_dims_symbol(m, st)) return s;
+  if (m->tc_train) {
+    if (int s = tc_prepare(m)) return s;
+    if (int s = tc_backward(d, m->tc, m->tcb, d_target, m->cfg.loss, m->loss_scale, n, m->loss_dev, m->grads,
+                            &m->dw_part, &m->dw_part_cap, m->tc_err_dev, st))
+      return s;
+    if (d.n_enc_params > 0) {
+      if (!m->grid_acc) {
+        cudaError_t e = cudaMalloc(&m->grid_acc, d.n_enc_params * sizeof(long long));
+        if (e != cudaSuccess) return hm_cuda_status(e, "grid grad accumulator");
+      }
+      cudaError_t e = cudaMemsetAsync(m->grid_acc, 0, d.n_enc_params * sizeof(long long), st);
+      if (e != cudaSuccess) return hm_cuda_status(e, "grid grad clear");
+      grid_bwd_kernel<<<(int)((n + 255) / 256), 256, 0, st>>>(m->last_in, m->tcb.dX, m->grid_acc, n);
+      HM_CHECK_LAUNCH("grid_bwd_kernel");
+      grid_fix_to_float_kernel<<<1024, 256, 0, st>>>(m->grid_acc, m->grads + d.n_net_params, d.n_enc_params);
+      HM_CHECK_LAUNCH("grid_fix_to_float_kernel");
+    }
+    if (d_loss) {
+      cudaError_t e = cudaMemcpyAsync(d_loss, m->loss_dev, sizeof(float), cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) return hm_cuda_status(e, "loss copy");
+    }
+    return HM_OK;
+  }
   if (int s = dispatch_bwd(m, d_target, n, st)) return s;
   // weight gradients, split over the batch in fixed chunks
   const int64_t chunk = 1024;
@@ -1047,7 +1089,7 @@ extern "C" int hm_mlp_training_step(hm_mlp* h, const float* d_in, const float* d
   if (int s = hm_mlp_forward(h, d_in, nullptr, n, stream)) return s;
   if (n == 0) return HM_OK;
   if (int s = hm_mlp_backward(h, d_target, n, d_loss, stream)) return s;
-  return hm_mlp_optimizer_step(h, 1.f, stream);
+  return hm_mlp_optimizer_step(h, ((Mlp*)h)->loss_scale, stream);
 }
 
 // trainer->loss(ctx) (render_hair_msnn.cu:691): the last loss, synchronously.

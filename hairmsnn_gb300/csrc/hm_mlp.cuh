@@ -112,6 +112,24 @@ HM_D uint32_t grid_index(const EncSeg& s, int l, uint32_t x, uint32_t y, uint32_
 }
 
 
+// Loss gradient of one query (tcnn semantics, averaged over n * out_ch).
+HM_D void loss_grad(int loss, const float* pred, const float* tgt, int out_ch, float inv_total,
+                    float* grad, float* value) {
+  float lum2 = 0.f;
+  if (loss == LOSS_REL_L2_LUM) {
+    float lum = 0.299f * pred[0] + 0.587f * pred[1] + 0.114f * pred[2];
+    lum2 = lum * lum + 0.01f;
+  }
+  float v = 0.f;
+  for (int o = 0; o < out_ch; ++o) {
+    float diff = pred[o] - tgt[o];
+    float den = loss == LOSS_L2 ? 1.f : (loss == LOSS_REL_L2 ? pred[o] * pred[o] + 0.01f : lum2);
+    v += diff * diff / den * inv_total;
+    grad[o] = 2.f * diff / den * inv_total;
+  }
+  *value = v;
+}
+
 // ---- tensor-core (tcgen05) forward for HM_PREC_FP16 / BF16 / FP8_E4M3
 // Weights are repacked from the FP32 master copy into the operand layout of
 // the MMA (K-major, 8-row x 16-byte core matrices) whenever they change.
@@ -125,6 +143,23 @@ struct TcPack {
   int64_t bytes = 0;
   uint8_t* blob = nullptr;  // device
   float* scales = nullptr;  // device [16]: 1/weight scale per layer; [15]: hash-grid amax
+  // training (FP16 / BF16 only): the transposed matrices W_l^T as B operands
+  // of the backward pass (rows = layer inputs, K = layer outputs)
+  int NT[16], KT[16];
+  int64_t boff_t[16];
+  int64_t bytes_t = 0;
+  uint8_t* blob_t = nullptr;
+};
+
+// Device buffers of a tensor-core training step (batch capacity rows).
+struct TcTrainBufs {
+  uint16_t* x16 = nullptr;   // [cap][K0] encoded inputs as rounded for layer 0
+  uint16_t* h16 = nullptr;   // [L][cap][W] hidden activations
+  uint16_t* dz16 = nullptr;  // [L+1][cap][max(W,16)] loss-scaled dZ per layer
+  float* pred = nullptr;     // [cap][16]
+  float* dX = nullptr;       // [cap][in_pad] loss-scaled input gradient (hash grids only)
+  float* loss_part = nullptr;
+  int64_t cap = 0;
 };
 
 // Whether the tensor-core path covers this network at this precision.
@@ -137,5 +172,17 @@ void tc_pack_free(TcPack* pk);
 // out [n][out_stride] (the first out_ch columns written).
 int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
                int out_stride, int64_t n, int* err_flag, cudaStream_t st);
+// Training on the tensor cores (FP16 / BF16): forward keeping the operands,
+// backward (loss gradient scaled by loss_scale, dgrad chain, dX when the
+// encoding has parameters), weight gradients as per-chunk partials reduced
+// in a fixed order into grads (still scaled by loss_scale).
+bool tc_trainable(const MlpDims& d, int precision);
+int tc_train_alloc(const MlpDims& d, int64_t cap, bool need_dx, TcTrainBufs* b);
+void tc_train_free(TcTrainBufs* b);
+int tc_train_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, int64_t n,
+                     const TcTrainBufs& b, int* err_flag, cudaStream_t st);
+int tc_backward(const MlpDims& d, const TcPack& pk, const TcTrainBufs& b, const float* target, int loss,
+                float loss_scale, int64_t n, float* loss_out, float* grads, float** dw_part, int64_t* dw_cap,
+                int* err_flag, cudaStream_t st);
 
 }  // namespace hm

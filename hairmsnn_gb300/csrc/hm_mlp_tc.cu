@@ -33,6 +33,8 @@
 #include <cuda_fp16.h>
 #include <cuda_fp8.h>
 
+#include <string.h>
+
 #include <algorithm>
 #include <string>
 
@@ -166,6 +168,7 @@ struct RowPacker {
   uint8_t* A;
   int row;
   float scale;
+  uint8_t* mirror = nullptr;  // training: the row's operand bytes also go here
   HM_D RowPacker(uint8_t* a, int r, int first_group, float sc) : group(first_group), A(a), row(r), scale(sc) {}
   HM_D void push(float v) {
     constexpr int SH = PREC == TC_E4M3 ? 8 : 16;
@@ -182,6 +185,7 @@ struct RowPacker {
     w3 = (w3 >> SH) | (h << (32 - SH));
     if (++cnt == kPer) {
       *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, group * 16)) = make_uint4(w0, w1, w2, w3);
+      if (mirror) *reinterpret_cast<uint4*>(mirror + group * 16) = make_uint4(w0, w1, w2, w3);
       ++group;
       cnt = 0;
     }
@@ -332,13 +336,17 @@ struct TcArgs {
   int* err;  // host-mapped
   int a_bytes;
   int ncols;
+  // training forward (STORE): operands kept for the backward pass
+  uint16_t* x16;  // [n][K0]
+  uint16_t* h16;  // [L][n][W]
+  float* pred;    // [n][16]
 };
 
 // 256 threads: thread (warp w, lane i) owns row 32 * (w % 4) + i of the tile
 // (tensor-memory lanes are split by warp quadrant) and half h = w / 4 of the
 // work on that row: every other 16-byte feature group when encoding, and
 // accumulator columns [h * W/2, (h + 1) * W/2) in the epilogues.
-template <int PREC, int W>
+template <int PREC, int W, bool STORE>
 __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_constant__ TcArgs p) {
   constexpr bool F8 = PREC == TC_E4M3;
   constexpr int EB = F8 ? 1 : 2;       // bytes per element
@@ -421,6 +429,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
         const int G = kn / CK, gsplit = (G + 1) >> 1;
         const int g0 = half ? gsplit : 0, g1 = half ? G : gsplit;
         RowPacker<PREC> pk(A, row, g0, row_scale);
+        if (STORE && valid) pk.mirror = reinterpret_cast<uint8_t*>(p.x16 + q * K0 + kc);
         if (valid) {
           enc_range<PREC>(d, xin, p.enc_params, kc + g0 * CK, kc + g1 * CK, pk);
         } else {
@@ -469,6 +478,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
           for (int w2 = 0; w2 < 4; ++w2) word[w2] = pack2<PREC>(v[g * 8 + 2 * w2], v[g * 8 + 2 * w2 + 1]);
           *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, (half * HW + g * 8) * 2)) =
               make_uint4(word[0], word[1], word[2], word[3]);
+          if (STORE && valid)
+            *reinterpret_cast<uint4*>(p.h16 + ((int64_t)(l - 1) * p.n + q) * W + half * HW + g * 8) =
+                make_uint4(word[0], word[1], word[2], word[3]);
         }
       }
       tc_fence_before();
@@ -482,8 +494,14 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
       float t[16];
       tmem_ld16(row_taddr, t);
       const float sc = row_inv * w_inv(L);
-      if (valid)
-        for (int o = 0; o < d.out_ch && o < p.out_stride; ++o) p.out[q * p.out_stride + o] = t[o] * sc;
+      if (valid) {
+        if (STORE) {
+#pragma unroll
+          for (int o = 0; o < 16; ++o) p.pred[q * 16 + o] = t[o] * sc;
+        } else {
+          for (int o = 0; o < d.out_ch && o < p.out_stride; ++o) p.out[q * p.out_stride + o] = t[o] * sc;
+        }
+      }
     }
     tc_fence_before();
     __syncthreads();
@@ -547,6 +565,21 @@ __global__ void tc_pack_kernel(MlpDims d, const float* __restrict__ params, int 
   }
 }
 
+// W_l^T for the backward pass: element (n = input, k = output) of layer l.
+template <int PREC>
+__global__ void tc_pack_t_kernel(MlpDims d, const float* __restrict__ params, int layer, int NT, int KT,
+                                 int64_t boff, uint8_t* __restrict__ blob) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= (int64_t)NT * KT) return;
+  const int n = (int)(i / KT), k = (int)(i % KT);
+  const int fan_in = layer == 0 ? d.in_pad : d.width;
+  const float w = n < fan_in ? params[d.layer_off[layer] + (int64_t)k * fan_in + n] : 0.f;
+  if (PREC == TC_BF16)
+    *reinterpret_cast<__nv_bfloat16*>(blob + boff + op_offset(NT, n, 2 * k)) = __float2bfloat16_rn(w);
+  else
+    *reinterpret_cast<__half*>(blob + boff + op_offset(NT, n, 2 * k)) = __float2half_rn(w);
+}
+
 // ------------------------------------------------------------------ host API
 static int tc_kinst(int precision) { return precision == HM_PREC_FP8_E4M3 ? 32 : 16; }
 static int round_up(int x, int m) { return (x + m - 1) / m * m; }
@@ -597,6 +630,17 @@ int tc_pack_alloc(const MlpDims& d, int precision, TcPack* pk) {
   pk->bytes = off;
   cudaError_t e = cudaMalloc(&pk->blob, (size_t)off);
   if (e == cudaSuccess) e = cudaMalloc(&pk->scales, 16 * sizeof(float));
+  if (e == cudaSuccess && tc_trainable(d, precision)) {
+    int64_t ot = 0;
+    for (int l = 0; l < pk->n_layers; ++l) {
+      pk->NT[l] = pk->K[l];  // the layer's inputs
+      pk->KT[l] = pk->N[l];  // the layer's outputs
+      pk->boff_t[l] = ot;
+      ot += (int64_t)pk->NT[l] * pk->KT[l] * 2;
+    }
+    pk->bytes_t = ot;
+    e = cudaMalloc(&pk->blob_t, (size_t)ot);
+  }
   if (e != cudaSuccess) return hm_cuda_status(e, "tensor-core weight blob");
   cudaMemset(pk->scales, 0, 16 * sizeof(float));
   return HM_OK;
@@ -605,8 +649,10 @@ int tc_pack_alloc(const MlpDims& d, int precision, TcPack* pk) {
 void tc_pack_free(TcPack* pk) {
   cudaFree(pk->blob);
   cudaFree(pk->scales);
+  cudaFree(pk->blob_t);
   pk->blob = nullptr;
   pk->scales = nullptr;
+  pk->blob_t = nullptr;
 }
 
 int tc_pack(const MlpDims& d, const float* params, TcPack& pk, cudaStream_t st) {
@@ -624,13 +670,22 @@ int tc_pack(const MlpDims& d, const float* params, TcPack& pk, cudaStream_t st) 
     else
       tc_pack_kernel<TC_FP16><<<blocks, 256, 0, st>>>(d, params, l, pk.N[l], pk.K[l], pk.boff[l], pk.scales, pk.blob);
     HM_CHECK_LAUNCH("tc_pack_kernel");
+    if (pk.blob_t) {
+      const int64_t ct = (int64_t)pk.NT[l] * pk.KT[l];
+      const int bt = (int)((ct + 255) / 256);
+      if (pk.precision == HM_PREC_BF16)
+        tc_pack_t_kernel<TC_BF16><<<bt, 256, 0, st>>>(d, params, l, pk.NT[l], pk.KT[l], pk.boff_t[l], pk.blob_t);
+      else
+        tc_pack_t_kernel<TC_FP16><<<bt, 256, 0, st>>>(d, params, l, pk.NT[l], pk.KT[l], pk.boff_t[l], pk.blob_t);
+      HM_CHECK_LAUNCH("tc_pack_t_kernel");
+    }
   }
   return HM_OK;
 }
 
-template <int PREC, int W>
+template <int PREC, int W, bool STORE = false>
 static int tc_launch(const TcArgs& a, size_t smem, cudaStream_t st) {
-  auto kern = mlp_tc_fwd_kernel<PREC, W>;
+  auto kern = mlp_tc_fwd_kernel<PREC, W, STORE>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, (int)cudaSharedmemCarveoutMaxShared);
@@ -652,10 +707,10 @@ static int tc_launch(const TcArgs& a, size_t smem, cudaStream_t st) {
   return HM_OK;
 }
 
-int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
-               int out_stride, int64_t n, int* err_flag, cudaStream_t st) {
-  if (n <= 0) return HM_OK;
-  TcArgs a;
+static int tc_args(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
+                   int out_stride, int64_t n, int* err_flag, TcArgs* ap, size_t* smem_out) {
+  TcArgs& a = *ap;
+  memset(&a, 0, sizeof(a));
   a.d = d;
   a.blob = pk.blob;
   a.blob_bytes = pk.bytes;
@@ -675,7 +730,7 @@ int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, cons
   int ncols = 32;
   while (ncols < std::max(d.width, 16)) ncols *= 2;
   a.ncols = ncols;
-  // shared memory: A tile + weights (+ guard band when it fits) + barrier
+  // shared memory: A tile + weights + barrier
   const int eb = pk.elem_bytes;
   const int64_t wbytes = (pk.bytes + 127) & ~(int64_t)127;
   const int64_t misc = 1152;  // barrier, tensor-memory address, E4M3 row maxima
@@ -692,7 +747,16 @@ int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, cons
   if (total(kc0) > kTcSmemMax) return hm_set_error("mlp: tensor-core tile does not fit"), HM_EUNSUPPORTED;
   a.kc0 = kc0;
   a.a_bytes = (int)a_bytes_for(kc0);
-  const size_t smem = (size_t)(a.a_bytes + wbytes + misc);
+  *smem_out = (size_t)(a.a_bytes + wbytes + misc);
+  return HM_OK;
+}
+
+int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
+               int out_stride, int64_t n, int* err_flag, cudaStream_t st) {
+  if (n <= 0) return HM_OK;
+  TcArgs a;
+  size_t smem = 0;
+  if (int e = tc_args(d, pk, enc_params, in, out, out_stride, n, err_flag, &a, &smem)) return e;
   const int W = d.width;
   switch (pk.precision) {
     case HM_PREC_BF16:
@@ -705,6 +769,466 @@ int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, cons
       return W == 32 ? tc_launch<TC_E4M3, 32>(a, smem, st) : W == 64 ? tc_launch<TC_E4M3, 64>(a, smem, st)
              : tc_launch<TC_E4M3, 128>(a, smem, st);
   }
+}
+
+// =================================================================== training
+bool tc_trainable(const MlpDims& d, int precision) {
+  return (precision == HM_PREC_FP16 || precision == HM_PREC_BF16) && d.width >= 16;
+}
+
+int tc_train_alloc(const MlpDims& d, int64_t cap, bool need_dx, TcTrainBufs* b) {
+  tc_train_free(b);
+  const int L = d.n_hidden;
+  const int wz = std::max(d.width, 16);
+  cudaError_t e = cudaMalloc(&b->x16, (size_t)cap * d.in_pad * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&b->h16, (size_t)L * cap * d.width * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&b->dz16, (size_t)(L + 1) * cap * wz * 2);
+  if (e == cudaSuccess) e = cudaMalloc(&b->pred, (size_t)cap * 16 * sizeof(float));
+  if (e == cudaSuccess && need_dx) e = cudaMalloc(&b->dX, (size_t)cap * d.in_pad * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&b->loss_part, 4096 * sizeof(float));
+  if (e != cudaSuccess) {
+    tc_train_free(b);
+    return hm_cuda_status(e, "tensor-core training buffers");
+  }
+  b->cap = cap;
+  return HM_OK;
+}
+
+void tc_train_free(TcTrainBufs* b) {
+  cudaFree(b->x16);
+  cudaFree(b->h16);
+  cudaFree(b->dz16);
+  cudaFree(b->pred);
+  cudaFree(b->dX);
+  cudaFree(b->loss_part);
+  *b = TcTrainBufs{};
+}
+
+int tc_train_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, int64_t n,
+                     const TcTrainBufs& b, int* err_flag, cudaStream_t st) {
+  if (n <= 0) return HM_OK;
+  TcArgs a;
+  size_t smem = 0;
+  if (int e = tc_args(d, pk, enc_params, in, nullptr, 16, n, err_flag, &a, &smem)) return e;
+  a.x16 = b.x16;
+  a.h16 = b.h16;
+  a.pred = b.pred;
+  const int W = d.width;
+  if (pk.precision == HM_PREC_BF16)
+    return W == 16 ? tc_launch<TC_BF16, 16, true>(a, smem, st) : W == 32 ? tc_launch<TC_BF16, 32, true>(a, smem, st)
+           : W == 64 ? tc_launch<TC_BF16, 64, true>(a, smem, st) : tc_launch<TC_BF16, 128, true>(a, smem, st);
+  return W == 16 ? tc_launch<TC_FP16, 16, true>(a, smem, st) : W == 32 ? tc_launch<TC_FP16, 32, true>(a, smem, st)
+         : W == 64 ? tc_launch<TC_FP16, 64, true>(a, smem, st) : tc_launch<TC_FP16, 128, true>(a, smem, st);
+}
+
+// ---- backward: loss gradient and the dgrad chain, one 128-row tile at a time
+// dZ_{L+1} = loss gradient x loss_scale (16 columns); for j = L .. 1:
+// dH_j = dZ_{j+1} W_j (A = dZ_{j+1}, B = W_j^T, accumulator in tensor memory),
+// dZ_j = dH_j where h_j > 0; and dX = dZ_1 W_0 when the encoding has
+// parameters.  Every dZ is rounded to the operand type, kept in shared memory
+// as the next A operand and written out for the weight gradients.
+struct TcBwdArgs {
+  MlpDims d;
+  const uint8_t* blob_t;
+  int64_t blob_bytes;
+  int64_t boff_t[16];
+  int NT[16], KT[16];
+  int L;
+  const uint16_t* h16;
+  uint16_t* dz16;
+  const float* pred;
+  const float* target;
+  float* dX;
+  float* loss_part;
+  int loss;
+  float inv_total, loss_scale;
+  int64_t n;
+  int* err;
+  int a_bytes;
+  int ncols;
+  int wz;  // row pitch of dz16 (max(W, 16))
+};
+
+template <int PREC, int W>
+__global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_bwd_kernel(const __grid_constant__ TcBwdArgs p) {
+  constexpr int FMT = PREC == TC_BF16 ? 1 : 0;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* A = smem;
+  uint8_t* Wt = smem + p.a_bytes;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(Wt + ((p.blob_bytes + 127) & ~(int64_t)127));
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 1);
+  float* red = reinterpret_cast<float*>(holder + 4);  // [256] loss partials
+
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = ((warp & 3) << 5) | (tid & 31);
+  const int half = warp >> 2;
+  const MlpDims& d = p.d;
+  const int L = p.L;
+  for (int64_t i = tid; i < p.blob_bytes / 16; i += kTcThreads)
+    reinterpret_cast<uint4*>(Wt)[i] = __ldg(reinterpret_cast<const uint4*>(p.blob_t) + i);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(holder, p.ncols);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *holder;
+  const uint32_t row_taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const uint32_t a_base = smem_u32(A), w_base = smem_u32(Wt);
+  const uint32_t a_lbo = 16 * kTcRows;
+  uint32_t phase = 0;
+  bool failed = false;
+  float loss_acc = 0.f;
+
+  auto run = [&](int j, int k_count) -> bool {  // MMAs of dH_j = dZ_{j+1} W_j
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t idesc = tc_idesc(kTcRows, p.NT[j], FMT);
+      const uint32_t b_lbo = 16 * p.NT[j];
+      const uint32_t b_base = w_base + (uint32_t)p.boff_t[j];
+      for (int ks = 0; ks < k_count / 16; ++ks) {
+        const uint64_t ad = tc_sdesc(a_base + (uint32_t)ks * 2 * a_lbo, a_lbo, 128);
+        const uint64_t bd = tc_sdesc(b_base + (uint32_t)ks * 2 * b_lbo, b_lbo, 128);
+        tc_mma<false>(tmem, ad, bd, idesc, ks > 0 ? 1u : 0u);
+      }
+      tc_commit(bar);
+    }
+    const bool ok = mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    const bool bad = __syncthreads_or(!ok);
+    tc_fence_after();
+    return !bad;
+  };
+
+  const int64_t n_tiles = (p.n + kTcRows - 1) / kTcRows;
+  for (int64_t tile = blockIdx.x; tile < n_tiles && !failed; tile += gridDim.x) {
+    const int64_t q = tile * kTcRows + row;
+    const bool valid = q < p.n;
+    // ---- loss gradient (half 0 of each row): dZ_{L+1}, 16 columns
+    if (half == 0) {
+      float g[16], pr[16];
+#pragma unroll
+      for (int o = 0; o < 16; ++o) {
+        g[o] = 0.f;
+        pr[o] = valid ? p.pred[q * 16 + o] : 0.f;
+      }
+      if (valid) {
+        float tg[16];
+        for (int o = 0; o < d.out_ch; ++o) tg[o] = __ldg(p.target + q * d.out_ch + o);
+        float v = 0.f;
+        loss_grad(p.loss, pr, tg, d.out_ch, p.inv_total, g, &v);
+        loss_acc += v;
+      }
+      uint32_t word[8];
+#pragma unroll
+      for (int w2 = 0; w2 < 8; ++w2) word[w2] = pack2<PREC>(g[2 * w2] * p.loss_scale, g[2 * w2 + 1] * p.loss_scale);
+      *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, 0)) = make_uint4(word[0], word[1], word[2], word[3]);
+      *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, 16)) = make_uint4(word[4], word[5], word[6], word[7]);
+      if (valid) {
+        uint4* dst = reinterpret_cast<uint4*>(p.dz16 + ((int64_t)L * p.n + q) * p.wz);
+        dst[0] = make_uint4(word[0], word[1], word[2], word[3]);
+        dst[1] = make_uint4(word[4], word[5], word[6], word[7]);
+      }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    int kk = 16;  // K of the next MMA: columns of the dZ in A
+    for (int j = L; j >= 0 && !failed; --j) {
+      if (j == 0 && !p.dX) break;
+      if (!run(j, kk)) {
+        failed = true;
+        break;
+      }
+      const int nt = p.NT[j];  // inputs of layer j: W (j >= 1) or K0 (j == 0)
+      if (j == 0) {
+        // dX (loss-scaled, FP32) for the hash-grid backward
+        for (int c = half * 16; c < nt; c += 32) {
+          float t[16];
+          tmem_ld16(row_taddr + c, t);
+          if (valid)
+            for (int e = 0; e < 16 && c + e < d.in_pad; ++e) p.dX[q * d.in_pad + c + e] = t[e];
+        }
+      } else {
+        constexpr int HW = W / 2;
+        const uint16_t* hrow = p.h16 + ((int64_t)(j - 1) * p.n + (valid ? q : 0)) * W + half * HW;
+#pragma unroll
+        for (int c = 0; c < HW / 16; ++c) {
+          float t[16];
+          tmem_ld16(row_taddr + half * HW + c * 16, t);
+          uint4 hv[2];
+          hv[0] = valid ? __ldg(reinterpret_cast<const uint4*>(hrow + c * 16)) : make_uint4(0, 0, 0, 0);
+          hv[1] = valid ? __ldg(reinterpret_cast<const uint4*>(hrow + c * 16 + 8)) : make_uint4(0, 0, 0, 0);
+          const uint16_t* hs = reinterpret_cast<const uint16_t*>(hv);
+          uint32_t word[8];
+#pragma unroll
+          for (int w2 = 0; w2 < 8; ++w2) {
+            const float a0 = hs[2 * w2] != 0 && !(hs[2 * w2] & 0x8000) ? t[2 * w2] : 0.f;
+            const float a1 = hs[2 * w2 + 1] != 0 && !(hs[2 * w2 + 1] & 0x8000) ? t[2 * w2 + 1] : 0.f;
+            word[w2] = pack2<PREC>(a0, a1);
+          }
+          const int col = half * HW + c * 16;
+          *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, col * 2)) =
+              make_uint4(word[0], word[1], word[2], word[3]);
+          *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, col * 2 + 16)) =
+              make_uint4(word[4], word[5], word[6], word[7]);
+          if (valid) {
+            uint4* dst = reinterpret_cast<uint4*>(p.dz16 + ((int64_t)(j - 1) * p.n + q) * p.wz + col);
+            dst[0] = make_uint4(word[0], word[1], word[2], word[3]);
+            dst[1] = make_uint4(word[4], word[5], word[6], word[7]);
+          }
+        }
+        kk = W;
+      }
+      tc_fence_before();
+      fence_proxy_async_smem();
+      __syncthreads();
+    }
+  }
+  // per-CTA loss partial, fixed order
+  red[tid] = loss_acc;
+  __syncthreads();
+  if (tid == 0) {
+    float s = 0.f;
+    for (int i = 0; i < kTcThreads; ++i) s += red[i];
+    p.loss_part[blockIdx.x] = s;
+  }
+  if (failed && tid == 0) atomicOr(p.err, 1);
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, p.ncols);
+}
+
+// ---- weight gradients of one layer: dW[o][i] = sum over rows dZ[row][o] h[row][i]
+// The batch is split in fixed chunks; a CTA accumulates its chunk in tensor
+// memory (A = dZ^T: the layer's outputs padded to 128 rows, B = h^T, K = the
+// 128 rows of a tile) and writes an FP32 partial [outputs][inputs].
+struct TcWgradArgs {
+  const uint16_t* dz;  // [n][dz_pitch], columns = outputs
+  int dz_pitch;
+  const uint16_t* h;   // [n][h_pitch], columns = inputs
+  int h_pitch;
+  int n_out, n_in;     // n_in: multiple of 16, <= 256
+  int64_t n;
+  int64_t chunk;
+  float* part;         // [splits][n_out][n_in]
+  int* err;
+  int ncols;
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_wgrad_kernel(const __grid_constant__ TcWgradArgs p) {
+  constexpr int FMT = PREC == TC_BF16 ? 1 : 0;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* A = smem;                        // [128 outputs][128 rows]
+  uint8_t* B = smem + kTcRows * kTcRows * 2;  // [n_in][128 rows]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(B + (size_t)p.n_in * kTcRows * 2);
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  // A rows beyond the layer's outputs stay zero
+  for (int i = tid; i < kTcRows * kTcRows * 2 / 16; i += kTcThreads)
+    reinterpret_cast<uint4*>(A)[i] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(holder, p.ncols);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *holder;
+  const uint32_t a_base = smem_u32(A), b_base = smem_u32(B);
+  const uint32_t a_lbo = 16 * kTcRows, b_lbo = 16 * p.n_in;
+  uint32_t phase = 0;
+  bool failed = false;
+  const int64_t r0 = blockIdx.x * p.chunk, r1 = min(p.n, r0 + p.chunk);
+  bool first = true;
+  for (int64_t t0 = r0; t0 < r1 && !failed; t0 += kTcRows) {
+    // transpose the tile's rows into A (dZ^T) and B (h^T): element (feature f,
+    // row k) at op_offset(rows_of_operand, f, 2k)
+    const int k = tid >> 1, hf = tid & 1;
+    const int64_t q = t0 + k;
+    const bool valid = q < r1;
+    for (int f = hf; f < p.n_out; f += 2) {
+      const uint16_t v = valid ? p.dz[q * p.dz_pitch + f] : (uint16_t)0;
+      *reinterpret_cast<uint16_t*>(A + op_offset(kTcRows, f, 2 * k)) = v;
+    }
+    for (int f = hf; f < p.n_in; f += 2) {
+      const uint16_t v = valid ? p.h[q * p.h_pitch + f] : (uint16_t)0;
+      *reinterpret_cast<uint16_t*>(B + op_offset(p.n_in, f, 2 * k)) = v;
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t idesc = tc_idesc(kTcRows, p.n_in, FMT);
+      for (int ks = 0; ks < kTcRows / 16; ++ks) {
+        const uint64_t ad = tc_sdesc(a_base + (uint32_t)ks * 2 * a_lbo, a_lbo, 128);
+        const uint64_t bd = tc_sdesc(b_base + (uint32_t)ks * 2 * b_lbo, b_lbo, 128);
+        tc_mma<false>(tmem, ad, bd, idesc, (!first || ks > 0) ? 1u : 0u);
+      }
+      tc_commit(bar);
+    }
+    const bool ok = mbar_wait_bounded(bar, phase);
+    phase ^= 1u;
+    if (__syncthreads_or(!ok)) failed = true;
+    tc_fence_after();
+    first = false;
+  }
+  // epilogue: row o of the accumulator (tensor-memory lane o) -> part
+  if (!failed && !first && warp < 4) {
+    const int o = tid;  // lanes 0..127 by warp quadrant
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    float* dst = p.part + ((int64_t)blockIdx.x * p.n_out + o) * p.n_in;
+    for (int c = 0; c < p.n_in; c += 16) {
+      float t[16];
+      tmem_ld16(taddr + c, t);
+      if (o < p.n_out)
+#pragma unroll
+        for (int e = 0; e < 16; ++e) dst[c + e] = t[e];
+    }
+  } else if (!failed && first && warp < 4 && tid < p.n_out) {
+    float* dst = p.part + ((int64_t)blockIdx.x * p.n_out + tid) * p.n_in;
+    for (int c = 0; c < p.n_in; ++c) dst[c] = 0.f;
+  }
+  if (failed && tid == 0) atomicOr(p.err, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, p.ncols);
+}
+
+__global__ void tc_reduce_kernel(const float* __restrict__ part, int splits, int64_t mn, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < mn; i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int k = 0; k < splits; ++k) s += part[(int64_t)k * mn + i];
+    out[i] = s;
+  }
+}
+
+__global__ void tc_loss_reduce_kernel(const float* __restrict__ part, int nb, float* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    float s = 0.f;
+    for (int i = 0; i < nb; ++i) s += part[i];
+    *out = s;
+  }
+}
+
+template <int PREC, int W>
+static int tc_bwd_launch(const TcBwdArgs& a, size_t smem, cudaStream_t st, int* blocks_out) {
+  auto kern = mlp_tc_bwd_kernel<PREC, W>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return hm_cuda_status(e, "mlp_tc_bwd_kernel smem");
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t tiles = (a.n + kTcRows - 1) / kTcRows;
+  const int blocks = (int)std::min<int64_t>(std::min<int64_t>(tiles, sms), 4096);
+  kern<<<blocks, kTcThreads, smem, st>>>(a);
+  HM_CHECK_LAUNCH("mlp_tc_bwd_kernel");
+  *blocks_out = blocks;
+  return HM_OK;
+}
+
+int tc_backward(const MlpDims& d, const TcPack& pk, const TcTrainBufs& b, const float* target, int loss,
+                float loss_scale, int64_t n, float* loss_out, float* grads, float** dw_part, int64_t* dw_cap,
+                int* err_flag, cudaStream_t st) {
+  if (n <= 0) return HM_OK;
+  const int L = d.n_hidden;
+  const int W = d.width;
+  TcBwdArgs a;
+  memset(&a, 0, sizeof(a));
+  a.d = d;
+  a.blob_t = pk.blob_t;
+  // layer 0's transposed block (dX) is only loaded when the encoding needs it
+  const bool need_dx = b.dX != nullptr;
+  a.blob_bytes = need_dx ? pk.bytes_t : pk.bytes_t;
+  for (int l = 0; l < 16; ++l) {
+    a.boff_t[l] = l < pk.n_layers ? pk.boff_t[l] : 0;
+    a.NT[l] = l < pk.n_layers ? pk.NT[l] : 0;
+    a.KT[l] = l < pk.n_layers ? pk.KT[l] : 0;
+  }
+  a.L = L;
+  a.h16 = b.h16;
+  a.dz16 = b.dz16;
+  a.pred = b.pred;
+  a.target = target;
+  a.dX = b.dX;
+  a.loss_part = b.loss_part;
+  a.loss = loss;
+  a.inv_total = 1.f / ((float)n * (float)d.out_ch);
+  a.loss_scale = loss_scale;
+  a.n = n;
+  a.err = err_flag;
+  a.wz = std::max(W, 16);
+  int ncols = 32;
+  while (ncols < std::max(W, need_dx ? pk.NT[0] : 16)) ncols *= 2;
+  a.ncols = ncols;
+  a.a_bytes = kTcRows * std::max(W, 16) * 2;
+  const size_t smem = (size_t)a.a_bytes + ((pk.bytes_t + 127) & ~(int64_t)127) + 64 + 1024 + 64;
+  if (smem > (size_t)kTcSmemMax) return hm_set_error("mlp: backward tile does not fit"), HM_EUNSUPPORTED;
+  int blocks = 0;
+  int s = HM_OK;
+  if (pk.precision == HM_PREC_BF16)
+    s = W == 16 ? tc_bwd_launch<TC_BF16, 16>(a, smem, st, &blocks) : W == 32 ? tc_bwd_launch<TC_BF16, 32>(a, smem, st, &blocks)
+        : W == 64 ? tc_bwd_launch<TC_BF16, 64>(a, smem, st, &blocks) : tc_bwd_launch<TC_BF16, 128>(a, smem, st, &blocks);
+  else
+    s = W == 16 ? tc_bwd_launch<TC_FP16, 16>(a, smem, st, &blocks) : W == 32 ? tc_bwd_launch<TC_FP16, 32>(a, smem, st, &blocks)
+        : W == 64 ? tc_bwd_launch<TC_FP16, 64>(a, smem, st, &blocks) : tc_bwd_launch<TC_FP16, 128>(a, smem, st, &blocks);
+  if (s) return s;
+  tc_loss_reduce_kernel<<<1, 32, 0, st>>>(b.loss_part, blocks, loss_out);
+  HM_CHECK_LAUNCH("tc_loss_reduce_kernel");
+  // weight gradients
+  const int64_t chunk = 2048;
+  const int splits = (int)((n + chunk - 1) / chunk);
+  int64_t need = 0;
+  for (int l = 0; l <= L; ++l) need = std::max<int64_t>(need, (int64_t)splits * pk.N[l] * pk.K[l]);
+  if (need > *dw_cap) {
+    cudaFree(*dw_part);
+    *dw_part = nullptr;
+    cudaError_t e = cudaMalloc(dw_part, need * sizeof(float));
+    if (e != cudaSuccess) return hm_cuda_status(e, "tensor-core dW partials");
+    *dw_cap = need;
+  }
+  for (int l = 0; l <= L; ++l) {
+    TcWgradArgs g;
+    g.n_out = pk.N[l];
+    g.n_in = pk.K[l];
+    g.dz = b.dz16 + (int64_t)l * n * std::max(W, 16);
+    g.dz_pitch = std::max(W, 16);
+    g.h = l == 0 ? b.x16 : b.h16 + (int64_t)(l - 1) * n * W;
+    g.h_pitch = l == 0 ? pk.K[0] : W;
+    g.n = n;
+    g.chunk = chunk;
+    g.part = *dw_part;
+    g.err = err_flag;
+    int nc = 32;
+    while (nc < g.n_in) nc *= 2;
+    g.ncols = nc;
+    const size_t sm = (size_t)kTcRows * kTcRows * 2 + (size_t)g.n_in * kTcRows * 2 + 64;
+    if (pk.precision == HM_PREC_BF16) {
+      cudaFuncSetAttribute(mlp_tc_wgrad_kernel<TC_BF16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      mlp_tc_wgrad_kernel<TC_BF16><<<splits, kTcThreads, sm, st>>>(g);
+    } else {
+      cudaFuncSetAttribute(mlp_tc_wgrad_kernel<TC_FP16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      mlp_tc_wgrad_kernel<TC_FP16><<<splits, kTcThreads, sm, st>>>(g);
+    }
+    HM_CHECK_LAUNCH("mlp_tc_wgrad_kernel");
+    // the layer's weights are [out][in_l] with in_l = fan_in (<= K[l]); the
+    // partial rows are K[l] wide, the parameters fan_in wide
+    const int fan_in = l == 0 ? d.in_pad : W;
+    const int64_t mn = (int64_t)pk.N[l] * pk.K[l];
+    if (fan_in == pk.K[l]) {
+      tc_reduce_kernel<<<256, 256, 0, st>>>(*dw_part, splits, mn, grads + d.layer_off[l]);
+      HM_CHECK_LAUNCH("tc_reduce_kernel");
+    } else {
+      return hm_set_error("mlp: padded K in training"), HM_EUNSUPPORTED;
+    }
+  }
+  return HM_OK;
 }
 
 }  // namespace hm

@@ -93,6 +93,7 @@ def lib():
     L.hm_mlp_inference.argtypes = [vp, vp, vp, i64, vp]
     L.hm_mlp_forward.argtypes = [vp, vp, vp, i64, vp]
     L.hm_mlp_backward.argtypes = [vp, vp, i64, vp, vp]
+    L.hm_mlp_backward_output_grad.argtypes = [vp, vp, i64, vp]
     L.hm_mlp_optimizer_step.argtypes = [vp, ctypes.c_float, vp]
     L.hm_mlp_training_step.argtypes = [vp, vp, vp, i64, vp, vp]
     L.hm_mlp_last_loss.argtypes = [vp, P(ctypes.c_float)]

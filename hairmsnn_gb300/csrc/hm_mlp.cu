@@ -698,14 +698,14 @@ static int launch_fwd(Mlp* m, const float* X, float* out, int out_stride, float*
 }
 
 template <int W>
-static int launch_bwd(Mlp* m, const float* target, int64_t n, cudaStream_t st) {
+static int launch_bwd(Mlp* m, const float* target, int loss, int64_t n, cudaStream_t st) {
   size_t sm = bwd_smem(m->cfg.d);
   cudaFuncSetAttribute(mlp_bwd_kernel<W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   int blocks = (int)((n + BM - 1) / BM);
   float inv_total = 1.f / ((float)n * (float)m->cfg.d.out_ch);
   mlp_bwd_kernel<W><<<blocks, 256, sm, st>>>(m->params, m->acts, m->pred, target, m->dz,
                                              m->cfg.d.n_enc_params > 0 ? m->dX : nullptr,
-                                             m->loss_part, m->cfg.loss, inv_total, n);
+                                             m->loss_part, loss, inv_total, n);
   HM_CHECK_LAUNCH("mlp_bwd_kernel");
   loss_reduce_kernel<<<1, 32, 0, st>>>(m->loss_part, blocks, m->loss_dev);
   HM_CHECK_LAUNCH("loss_reduce_kernel");
@@ -720,12 +720,12 @@ static int dispatch_fwd(Mlp* m, const float* X, float* out, int out_stride, floa
     default: return launch_fwd<128>(m, X, out, out_stride, acts, n, st);
   }
 }
-static int dispatch_bwd(Mlp* m, const float* target, int64_t n, cudaStream_t st) {
+static int dispatch_bwd(Mlp* m, const float* target, int loss, int64_t n, cudaStream_t st) {
   switch (m->cfg.d.width) {
-    case 16: return launch_bwd<16>(m, target, n, st);
-    case 32: return launch_bwd<32>(m, target, n, st);
-    case 64: return launch_bwd<64>(m, target, n, st);
-    default: return launch_bwd<128>(m, target, n, st);
+    case 16: return launch_bwd<16>(m, target, loss, n, st);
+    case 32: return launch_bwd<32>(m, target, loss, n, st);
+    case 64: return launch_bwd<64>(m, target, loss, n, st);
+    default: return launch_bwd<128>(m, target, loss, n, st);
   }
 }
 
@@ -983,19 +983,19 @@ extern "C" int hm_mlp_forward(hm_mlp* h, const float* d_in, float* d_out, int64_
   return HM_OK;
 }
 
-// Backward of the last forward against d_target [n][out_ch]: fills the
-// parameter gradients and the loss (device scalar; d_loss may be NULL).
-extern "C" int hm_mlp_backward(hm_mlp* h, const float* d_target, int64_t n, float* d_loss, void* stream) {
-  Mlp* m = (Mlp*)h;
-  if (int s = check_io("hm_mlp_backward", m, d_target, d_target, n)) return s;
+// Backward of the last forward against d_target [n][out_ch] under `loss`
+// (LOSS_OUTPUT_GRAD: d_target is dL/d(output)): fills the parameter
+// gradients and the loss (device scalar; d_loss may be NULL).
+static int mlp_backward(Mlp* m, const char* who, const float* d_target, int loss, int64_t n, float* d_loss,
+                        cudaStream_t st) {
+  if (int s = check_io(who, m, d_target, d_target, n)) return s;
   if (n == 0) return HM_OK;
-  if (n != m->last_n) return hm_set_error("hm_mlp_backward: batch differs from the last forward"), HM_EINVAL;
-  cudaStream_t st = (cudaStream_t)stream;
+  if (n != m->last_n) return hm_set_error("%s: batch differs from the last forward", who), HM_EINVAL;
   const MlpDims& d = m->cfg.d;
   if (int s = set_dims_symbol(m, st)) return s;
   if (m->tc_train) {
     if (int s = tc_prepare(m)) return s;
-    if (int s = tc_backward(d, m->tc, m->tcb, d_target, m->cfg.loss, m->loss_scale, n, m->loss_dev, m->grads,
+    if (int s = tc_backward(d, m->tc, m->tcb, d_target, loss, m->loss_scale, n, m->loss_dev, m->grads,
                             &m->dw_part, &m->dw_part_cap, m->tc_err_dev, st))
       return s;
     if (d.n_enc_params > 0) {
@@ -1016,7 +1016,7 @@ extern "C" int hm_mlp_backward(hm_mlp* h, const float* d_target, int64_t n, floa
     }
     return HM_OK;
   }
-  if (int s = dispatch_bwd(m, d_target, n, st)) return s;
+  if (int s = dispatch_bwd(m, d_target, loss, n, st)) return s;
   // weight gradients, split over the batch in fixed chunks
   const int64_t chunk = 1024;
   const int splits = (int)((n + chunk - 1) / chunk);
@@ -1061,6 +1061,20 @@ extern "C" int hm_mlp_backward(hm_mlp* h, const float* d_target, int64_t n, floa
     if (e != cudaSuccess) return hm_cuda_status(e, "loss copy");
   }
   return HM_OK;
+}
+
+extern "C" int hm_mlp_backward(hm_mlp* h, const float* d_target, int64_t n, float* d_loss, void* stream) {
+  Mlp* m = (Mlp*)h;
+  if (!m) return hm_set_error("hm_mlp_backward: NULL"), HM_EINVAL;
+  return mlp_backward(m, "hm_mlp_backward", d_target, m->cfg.loss, n, d_loss, (cudaStream_t)stream);
+}
+
+// tcnn's backward with a given dL/d(output) [n][out_ch] (no loss).
+extern "C" int hm_mlp_backward_output_grad(hm_mlp* h, const float* d_dloss_doutput, int64_t n, void* stream) {
+  Mlp* m = (Mlp*)h;
+  if (!m) return hm_set_error("hm_mlp_backward_output_grad: NULL"), HM_EINVAL;
+  return mlp_backward(m, "hm_mlp_backward_output_grad", d_dloss_doutput, LOSS_OUTPUT_GRAD, n, nullptr,
+                      (cudaStream_t)stream);
 }
 
 // One optimizer step on the current gradients: ExponentialDecay wrapping

@@ -26,7 +26,9 @@
 namespace hm {
 
 enum EncType { ENC_IDENTITY = 0, ENC_FREQUENCY = 1, ENC_ONEBLOB = 2, ENC_HASHGRID = 3 };
-enum LossType { LOSS_L2 = 0, LOSS_REL_L2 = 1, LOSS_REL_L2_LUM = 2 };
+// LOSS_OUTPUT_GRAD: the "target" is dL/d(output) itself (tcnn's backward
+// with dL_doutput), used as the output gradient unscaled.
+enum LossType { LOSS_L2 = 0, LOSS_REL_L2 = 1, LOSS_REL_L2_LUM = 2, LOSS_OUTPUT_GRAD = 3 };
 enum Activation { ACT_NONE = 0, ACT_RELU = 1 };
 
 constexpr int kMaxSegs = 8;
@@ -115,6 +117,11 @@ HM_D uint32_t grid_index(const EncSeg& s, int l, uint32_t x, uint32_t y, uint32_
 // Loss gradient of one query (tcnn semantics, averaged over n * out_ch).
 HM_D void loss_grad(int loss, const float* pred, const float* tgt, int out_ch, float inv_total,
                     float* grad, float* value) {
+  if (loss == LOSS_OUTPUT_GRAD) {
+    for (int o = 0; o < out_ch; ++o) grad[o] = tgt[o];
+    *value = 0.f;
+    return;
+  }
   float lum2 = 0.f;
   if (loss == LOSS_REL_L2_LUM) {
     float lum = 0.299f * pred[0] + 0.587f * pred[1] + 0.114f * pred[2];

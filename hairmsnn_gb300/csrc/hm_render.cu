@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "hm_hair_grad.cuh"
 #include "hm_mlp.cuh"
 #include "hm_render.h"
 #include "hm_trace.cuh"
@@ -20,7 +21,11 @@ namespace hm {
 int launch_camera(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, int* queue,
                   int* count, cudaStream_t st);
 int launch_shade(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, const FrameBufs& fb,
-                 const int* queue, const int* count, int* keep, int grid, cudaStream_t st);
+                 const int* queue, const int* count, int* keep, int grid, cudaStream_t st,
+                 const DiffParams* dp = nullptr);
+int launch_group_dual(const SceneDev& s, void* out, int n, cudaStream_t st);
+size_t group_dual_bytes();
+int launch_replay_cache_grad(int P, const PathState& ps, const DiffParams& dp, float* dy, cudaStream_t st);
 int launch_finalize(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps,
                     const FrameBufs& fb, cudaStream_t st);
 int launch_compose(int P, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st);
@@ -198,27 +203,48 @@ static int persistent_blocks() {
 // Resolves the pending direct-lighting samples of each queued path: visible
 // sum, NaN check (directLighting, optix_common.cuh:296-308), weighted add to
 // the path radiance.  Explicitly rounded operations: no contraction.
+// REPLAY: the stashed gradient terms of the visible samples join the path's
+// gradient sums (none when the sum was a NaN and was dropped).
+template <bool REPLAY>
 __global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const int* __restrict__ queue,
                                                              const int* __restrict__ count,
-                                                             const uint8_t* __restrict__ vis) {
+                                                             const uint8_t* __restrict__ vis, DiffParams dp) {
   const int n = *count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int pid = queue[i];
     const uint32_t flags = ps.flags[pid];
     if (!(flags & F_DL)) continue;
     float c0x = 0.f, c0y = 0.f, c0z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
+    bool use0 = false, use1 = false;
     if (ps.sh_o0[pid].w != 0.f && vis[2 * pid]) {
       const float4 c = ps.sh_c0[pid];
       c0x = c.x; c0y = c.y; c0z = c.z;
+      use0 = true;
     }
     if (ps.sh_o1[pid].w != 0.f && vis[2 * pid + 1]) {
       const float4 c = ps.sh_c1[pid];
       c1x = c.x; c1y = c.y; c1z = c.z;
+      use1 = true;
     }
     float sx = __fadd_rn(0.f, __fadd_rn(c0x, c1x));
     float sy = __fadd_rn(0.f, __fadd_rn(c0y, c1y));
     float sz = __fadd_rn(0.f, __fadd_rn(c0z, c1z));
-    if (isnan(sx) || isnan(sy) || isnan(sz)) sx = sy = sz = 0.f;
+    if (isnan(sx) || isnan(sy) || isnan(sz)) {
+      sx = sy = sz = 0.f;
+      use0 = use1 = false;
+    }
+    if constexpr (REPLAY) {
+      if (use0 || use1) {
+        const size_t P = (size_t)dp.P;
+        const int g = __float_as_int(dp.stash[2 * kNd * P + pid]);
+        float* acc = dp.gacc + (size_t)g * kNd * P + pid;
+#pragma unroll
+        for (int k = 0; k < kNd; ++k) {
+          const float a = (use0 ? dp.stash[k * P + pid] : 0.f) + (use1 ? dp.stash[(kNd + k) * P + pid] : 0.f);
+          acc[k * P] += a;
+        }
+      }
+    }
     const float4 w = ps.dl_w[pid];
     float4 c = ps.col[pid];
     c.x = __fadd_rn(c.x, __fmul_rn(w.x, sx));
@@ -234,6 +260,36 @@ __global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const
       ps.col_s[pid] = cs;
     }
     ps.flags[pid] = flags & ~F_DL;
+  }
+}
+
+// ---- path-replay gradient sums (fixed order: results do not depend on timing)
+// Block b sums paths [b * per, (b + 1) * per) of every row in FP64.
+__global__ void __launch_bounds__(256) grad_block_sum_kernel(const float* __restrict__ gacc, int P, int rows,
+                                                             double* __restrict__ partial) {
+  __shared__ double red[256];
+  const int per = (P + gridDim.x - 1) / gridDim.x;
+  const int lo = blockIdx.x * per, hi = min(P, lo + per);
+  for (int row = 0; row < rows; ++row) {
+    double a = 0.0;
+    for (int i = lo + threadIdx.x; i < hi; i += 256) a += (double)gacc[(size_t)row * P + i];
+    red[threadIdx.x] = a;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[(size_t)blockIdx.x * rows + row] = red[0];
+    __syncthreads();
+  }
+}
+// out[row] = sum over n_parts parts (in order) of part[part][row]
+__global__ void grad_parts_sum_kernel(const double* __restrict__ part, int n_parts, int rows,
+                                      double* __restrict__ out) {
+  for (int row = threadIdx.x; row < rows; row += blockDim.x) {
+    double a = 0.0;
+    for (int b = 0; b < n_parts; ++b) a += part[(size_t)b * rows + row];
+    out[row] = a;
   }
 }
 
@@ -347,7 +403,14 @@ struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
   bool in_flight = false;
+  // path replay (allocated by the first differentiable forward)
+  float* gacc = nullptr;       // [groups * 6][P]
+  int gacc_rows = 0;
+  float* stash = nullptr;      // [13][P]
+  double* partial = nullptr;   // [kGradBlocks][groups * 6]
 };
+
+constexpr int kGradBlocks = 304;  // blocks of the per-frame gradient sum
 
 struct Render {
   Scene* scene = nullptr;
@@ -370,6 +433,21 @@ struct Render {
   float4* d_samples = nullptr;  // scene-sample training pass: points on the hair
   int n_samples = 0;
   int pretrain_passes = 0;
+  // differentiable rendering (hm_render_diff_forward / _backward)
+  bool diff_fwd = false;          // frames being enqueued belong to a differentiable forward
+  int diff_frames = 0;            // frames of the last differentiable forward
+  int diff_groups = 0;            // material groups it was rendered with
+  int diff_material_version = 0;  // the scene's materials it was rendered with
+  bool diff_detached = false;     // ... with evaluation materials (no backward)
+  int64_t diff_cap_frames = 0;    // capacity of the per-frame buffers
+  float4* diff_col = nullptr;     // [frames][P] path radiance
+  float* diff_in = nullptr;       // [frames][P][in_ch] cache inputs (replay)
+  float* diff_dy = nullptr;       // [frames][P][3] dL/d(cache output)
+  double* diff_gframe = nullptr;  // [frames][groups * 6]
+  double* diff_gsum = nullptr;    // [groups * 6]
+  double* h_gsum = nullptr;       // pinned copy
+  void* diff_dual = nullptr;      // [kMaxStrandGroups] HairConstsD
+  HairConsts* diff_eval = nullptr;  // [kMaxStrandGroups] evaluation materials (detached renders)
   int P = 0;
   int depth = 0;  // 0: chosen from the frame size in render_setup
   std::vector<Slot> slots;
@@ -398,9 +476,12 @@ struct Render {
       if (s.st) cudaStreamDestroy(s.st);
       if (s.done) cudaEventDestroy(s.done);
       if (s.h_err) cudaFreeHost(s.h_err);
+      for (void* p : {(void*)s.gacc, (void*)s.stash, (void*)s.partial, (void*)s.ps.beta_d}) cudaFree(p);
     }
     for (void* p : allocs) cudaFree(p);
     if (d_samples) cudaFree(d_samples);
+    for (void* p : {(void*)diff_col, (void*)diff_in, (void*)diff_dy, (void*)diff_gframe}) cudaFree(p);
+    if (h_gsum) cudaFreeHost(h_gsum);
     if (h_count) cudaFreeHost(h_count);
     if (mlp) hm_mlp_destroy(mlp);
     for (auto e : ev) cudaEventDestroy(e);
@@ -598,6 +679,16 @@ static int render_sync(Render* r) {
   return status;
 }
 
+// Bounce rounds a frame enqueues: path_v2 + 1, or, for HairMSNN frames
+// without training pixels, the short paths' BETA + 1 vertices (at least 2):
+// vertex k > beta = BETA - 1 always ends the path.
+static int bounce_rounds(const Render* r, const FrameParams& fp) {
+  const int full = r->max_path_v2 + 1;
+  if (fp.mode == MODE_MSNN && fp.no_train && r->bscenes.empty())
+    return std::min(full, std::max(2, r->beta_knob + 1));
+  return full;
+}
+
 // Enqueues one frame.  sync_bounces: read the queue length after every
 // bounce (instrumented frames: per-stage events, early exit); otherwise the
 // whole frame is enqueued without a host round trip.
@@ -611,6 +702,13 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   cudaStreamWaitEvent(st, r->ev_submit, 0);
   FrameParams fp{r->mode, r->beta_knob - 1, r->accum_id, r->accum_id + 10007, r->every_nth, r->n_train, r->in_ch,
                  0, nullptr, 0, 0u};
+  FrameBufs fb = sl.fb;
+  if (!r->diff_fwd) r->diff_frames = 0;  // a plain frame ends the replayable forward
+  if (r->diff_fwd) {  // a frame of a differentiable forward
+    fp.no_train = 1;
+    fp.eval_hc = r->diff_detached ? r->diff_eval : nullptr;
+    fb.col_out = r->diff_col + (size_t)r->accum_id * r->P;
+  }
   int* q_cur = sl.q_a;
   int* q_next = sl.q_b;
   int* c_cur = sl.counts;
@@ -638,8 +736,8 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   int count = r->P;
   int bounces = 0;
   int64_t ext_rays = 0;
-  const FrameBufs fb = sl.fb;
-  for (int it = 0; it <= r->max_path_v2 && count > 0; ++it) {
+  const int rounds = bounce_rounds(r, fp);
+  for (int it = 0; it < rounds && count > 0; ++it) {
     cur_bounce = it;
     paths_at.push_back(count);
     mark(S_EXTEND);
@@ -654,7 +752,7 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
                                                     sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, counting,
                                                     r->blocks_shadow, st))
       return e;
-    shadow_resolve_kernel<<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis);
+    shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{});
     HM_CHECK_LAUNCH("shadow_resolve_kernel");
     mark(S_COMPACT);
     scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
@@ -692,7 +790,7 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     // cache step: after the previous frame's inference (weights and workspace)
     if (r->have_mlp_ev) cudaStreamWaitEvent(st, r->ev_mlp, 0);
     mark(S_TRAIN);
-    if (r->train) {
+    if (r->train && !r->diff_fwd) {
       if (int e = hm_mlp_training_step(r->mlp, fb.nn_train_in, fb.nn_train_out, r->n_train, sl.d_loss, st))
         return e;
     }
@@ -709,7 +807,7 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     hm_mlp_desc md;
     hm_mlp_info(r->mlp, &md);
     const bool grid_enc = md.n_params > md.n_network_params;
-    launches += (r->train ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 2 : 0) + 1 : 0) + 2 + 1;
+    launches += (r->train && !r->diff_fwd ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 2 : 0) + 1 : 0) + 2 + 1;
   }
   mark(S_END);
   cudaMemcpyAsync(sl.h_err, sl.err, sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -1064,7 +1162,7 @@ static int render_pretrain(Render* r, int passes, cudaStream_t user) {
                                                       sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, false,
                                                       r->blocks_shadow, st))
         return e;
-      shadow_resolve_kernel<<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis);
+      shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{});
       scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
                                                                                     nblocks);
       scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
@@ -1092,6 +1190,185 @@ extern "C" int hm_render_pretrain(hm_render* h, int passes, void* stream) {
   if (!r || passes < 0) return hm_set_error("hm_render_pretrain: bad arguments"), HM_EINVAL;
   if (passes == 0) return HM_OK;
   return render_pretrain(r, passes, (cudaStream_t)stream);
+}
+
+// ---- differentiable rendering: detached forward frames and path replay
+// Buffers for `frames` frames with `groups` materials (grown on demand).
+static int diff_setup(Render* r, int frames, int groups) {
+  const int64_t P = r->P;
+  const int rows = groups * kNd;
+  cudaError_t e = cudaSuccess;
+  if (frames > r->diff_cap_frames) {
+    for (void* p : {(void*)r->diff_col, (void*)r->diff_in, (void*)r->diff_dy, (void*)r->diff_gframe}) cudaFree(p);
+    r->diff_col = nullptr;
+    r->diff_in = r->diff_dy = nullptr;
+    r->diff_gframe = nullptr;
+    r->diff_cap_frames = 0;
+    e = cudaMalloc(&r->diff_col, (size_t)frames * P * sizeof(float4));
+    if (e == cudaSuccess && r->mode == MODE_MSNN)
+      e = cudaMalloc(&r->diff_in, (size_t)frames * P * r->in_ch * sizeof(float));
+    if (e == cudaSuccess && r->mode == MODE_MSNN) e = cudaMalloc(&r->diff_dy, (size_t)frames * P * 3 * sizeof(float));
+    if (e == cudaSuccess)
+      e = cudaMalloc(&r->diff_gframe, (size_t)frames * kMaxStrandGroups * kNd * sizeof(double));
+    if (e != cudaSuccess) return hm_cuda_status(e, "differentiable render buffers");
+    r->diff_cap_frames = frames;
+  }
+  if (!r->diff_gsum) {
+    if (e == cudaSuccess) e = r->alloc(&r->diff_gsum, kMaxStrandGroups * kNd);
+    if (e == cudaSuccess) e = cudaMallocHost(&r->h_gsum, kMaxStrandGroups * kNd * sizeof(double));
+    if (e == cudaSuccess) e = r->alloc((char**)&r->diff_dual, kMaxStrandGroups * group_dual_bytes());
+    if (e == cudaSuccess) e = r->alloc(&r->diff_eval, kMaxStrandGroups);
+    if (e != cudaSuccess) return hm_cuda_status(e, "differentiable render tables");
+  }
+  for (auto& sl : r->slots) {
+    if (!sl.stash) {
+      if (e == cudaSuccess) e = cudaMalloc(&sl.stash, (size_t)(2 * kNd + 1) * P * sizeof(float));
+      if (e == cudaSuccess) e = cudaMalloc(&sl.partial, (size_t)kGradBlocks * kMaxStrandGroups * kNd * sizeof(double));
+      if (e == cudaSuccess) e = cudaMalloc(&sl.ps.beta_d, (size_t)P * sizeof(float4));
+    }
+    if (e == cudaSuccess && sl.gacc_rows < rows) {
+      cudaFree(sl.gacc);
+      sl.gacc = nullptr;
+      sl.gacc_rows = 0;
+      e = cudaMalloc(&sl.gacc, (size_t)rows * P * sizeof(float));
+      if (e == cudaSuccess) sl.gacc_rows = rows;
+    }
+    if (e != cudaSuccess) return hm_cuda_status(e, "replay slot buffers");
+  }
+  return HM_OK;
+}
+
+static int diff_forward(Render* r, int frames, const hm_hair_params* eval, int n_eval, cudaStream_t user) {
+  if (!r->bscenes.empty()) return hm_set_error("hm_render_diff_forward: single-scene renders only"), HM_EUNSUPPORTED;
+  if (frames < 1) return hm_set_error("hm_render_diff_forward: frames < 1"), HM_EINVAL;
+  const int groups = r->scene->n_groups();
+  if (eval && n_eval != groups)
+    return hm_set_error("hm_render_diff_forward: %d evaluation materials for %d groups", n_eval, groups), HM_EINVAL;
+  if (int e = render_sync(r)) return e;
+  if (int e = diff_setup(r, frames, groups)) return e;
+  if (eval) {
+    std::vector<HairConsts> hc(groups);
+    for (int g = 0; g < groups; ++g) hc[g] = hair_consts_from_params(eval[g]);
+    cudaError_t e = cudaMemcpy(r->diff_eval, hc.data(), groups * sizeof(HairConsts), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return hm_cuda_status(e, "evaluation materials");
+  }
+  r->accum_id = 0;
+  r->diff_frames = 0;
+  r->diff_groups = groups;
+  r->diff_material_version = r->scene->material_version;
+  r->diff_detached = eval != nullptr;
+  r->diff_fwd = true;
+  int st = HM_OK;
+  for (int f = 0; f < frames && st == HM_OK; ++f) st = render_frame(r, user, false);
+  r->diff_fwd = false;
+  if (st == HM_OK) r->diff_frames = frames;
+  return st;
+}
+
+// Replays frame f of the last differentiable forward on its own slot.
+static int replay_frame(Render* r, int f, const float* adjoint) {
+  Scene* s = r->scene;
+  const SceneDev sd = s->dev();
+  Slot& sl = r->slots[f % r->depth];
+  if (int e = slot_finish(r, sl)) return e;
+  const cudaStream_t st = sl.st;
+  FrameParams fp{r->mode, r->beta_knob - 1, f, f + 10007, r->every_nth, r->n_train, r->in_ch, 0, nullptr, 0, 0u};
+  fp.no_train = 1;
+  FrameBufs fb = sl.fb;
+  if (r->mode == MODE_MSNN) fb.nn_frame_in = r->diff_in + (size_t)f * r->P * r->in_ch;
+  const int rows = r->diff_groups * kNd;
+  const DiffParams dp{r->diff_col + (size_t)f * r->P, adjoint, 1.f / (float)r->diff_frames, sl.gacc, sl.stash,
+                      (const HairConstsD*)r->diff_dual, r->P};
+  cudaMemsetAsync(sl.gacc, 0, (size_t)rows * r->P * sizeof(float), st);
+  cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
+  int* q_cur = sl.q_a;
+  int* q_next = sl.q_b;
+  int* c_cur = sl.counts;
+  int* c_next = sl.counts + 1;
+  if (int e = launch_camera(sd, fp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
+  const int grid = r->sm_count * r->shade_blocks_per_sm;
+  const int nblocks = (r->P + kScanBlock - 1) / kScanBlock;
+  const int rounds = bounce_rounds(r, fp);
+  for (int it = 0; it < rounds; ++it) {
+    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, r->batch, 0.f, 1e30f,
+                                                     sl.fetch + 2 * it, sl.err, r->d_cnt, false, r->blocks_extend,
+                                                     st))
+      return e;
+    if (int e = launch_shade(sd, fp, r->batch, sl.ps, fb, q_cur, c_cur, sl.keep, grid, st, &dp)) return e;
+    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, r->batch, 0.f, 1e30f,
+                                                    sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, false,
+                                                    r->blocks_shadow, st))
+      return e;
+    shadow_resolve_kernel<true><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, dp);
+    scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
+                                                                                  nblocks);
+    scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
+    scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, q_cur, c_cur, sl.block_sums,
+                                                                              q_next, nblocks);
+    HM_CHECK_LAUNCH("replay bounce");
+    std::swap(q_cur, q_next);
+    std::swap(c_cur, c_next);
+  }
+  if (r->mode == MODE_MSNN)
+    if (int e = launch_replay_cache_grad(r->P, sl.ps, dp, r->diff_dy + (size_t)f * r->P * 3, st)) return e;
+  grad_block_sum_kernel<<<kGradBlocks, 256, 0, st>>>(sl.gacc, r->P, rows, sl.partial);
+  grad_parts_sum_kernel<<<1, 384, 0, st>>>(sl.partial, kGradBlocks, rows, r->diff_gframe + (size_t)f * rows);
+  HM_CHECK_LAUNCH("replay gradient sums");
+  cudaMemcpyAsync(sl.h_err, sl.err, sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(sl.done, st);
+  sl.in_flight = true;
+  return HM_OK;
+}
+
+static int diff_backward(Render* r, const float* adjoint, double* host_grad, int n_grad, cudaStream_t user) {
+  if (r->diff_frames <= 0) return hm_set_error("hm_render_diff_backward: no differentiable forward to replay"), HM_EINVAL;
+  if (r->diff_detached)
+    return hm_set_error("hm_render_diff_backward: the last forward was detached (evaluation materials)"), HM_EINVAL;
+  if (r->scene->n_groups() != r->diff_groups || r->scene->material_version != r->diff_material_version)
+    return hm_set_error("hm_render_diff_backward: the scene's materials changed since the forward"), HM_EINVAL;
+  if (r->accum_id != r->diff_frames)
+    return hm_set_error("hm_render_diff_backward: frames were rendered after the differentiable forward"), HM_EINVAL;
+  const int rows = r->diff_groups * kNd;
+  if (n_grad < rows) return hm_set_error("hm_render_diff_backward: %d gradient slots for %d", n_grad, rows), HM_ECAPACITY;
+  if (int e = render_sync(r)) return e;
+  const cudaStream_t st0 = r->slots[0].st;
+  cudaEventRecord(r->ev_submit, user);
+  for (auto& sl : r->slots) cudaStreamWaitEvent(sl.st, r->ev_submit, 0);
+  if (int e = launch_group_dual(r->scene->dev(), r->diff_dual, r->diff_groups, st0)) return e;
+  cudaEventRecord(r->ev_mlp, st0);
+  for (auto& sl : r->slots) cudaStreamWaitEvent(sl.st, r->ev_mlp, 0);
+  for (int f = 0; f < r->diff_frames; ++f)
+    if (int e = replay_frame(r, f, adjoint)) return e;
+  if (int e = render_sync(r)) return e;
+  grad_parts_sum_kernel<<<1, 384, 0, st0>>>(r->diff_gframe, r->diff_frames, rows, r->diff_gsum);
+  HM_CHECK_LAUNCH("replay gradient total");
+  if (r->mode == MODE_MSNN) {
+    // dL/dW: the cache's backward over every replayed frame's queries at once
+    const int64_t n = (int64_t)r->diff_frames * r->P;
+    if (int e = hm_mlp_forward(r->mlp, r->diff_in, nullptr, n, st0)) return e;
+    if (int e = hm_mlp_backward_output_grad(r->mlp, r->diff_dy, n, st0)) return e;
+  }
+  cudaError_t e = cudaMemcpyAsync(r->h_gsum, r->diff_gsum, rows * sizeof(double), cudaMemcpyDeviceToHost, st0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st0);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_diff_backward");
+  memcpy(host_grad, r->h_gsum, rows * sizeof(double));
+  cudaEventRecord(r->ev_submit, st0);
+  cudaStreamWaitEvent((cudaStream_t)user, r->ev_submit, 0);
+  return HM_OK;
+}
+
+extern "C" int hm_render_diff_forward(hm_render* h, int frames, const hm_hair_params* eval_materials, int n_materials,
+                                      void* stream) {
+  Render* r = (Render*)h;
+  if (!r) return hm_set_error("hm_render_diff_forward: NULL"), HM_EINVAL;
+  return diff_forward(r, frames, eval_materials, n_materials, (cudaStream_t)stream);
+}
+
+extern "C" int hm_render_diff_backward(hm_render* h, const float* d_adjoint, double* host_grad, int n_grad,
+                                       void* stream) {
+  Render* r = (Render*)h;
+  if (!r || !d_adjoint || !host_grad) return hm_set_error("hm_render_diff_backward: NULL"), HM_EINVAL;
+  return diff_backward(r, d_adjoint, host_grad, n_grad, (cudaStream_t)stream);
 }
 
 extern "C" int hm_render_reset(hm_render* h) {

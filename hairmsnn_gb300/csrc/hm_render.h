@@ -34,6 +34,7 @@ struct PathState {
   float4* sh_c1;
   float4* dl_w;   // weight of the visible direct-lighting sum in col
   float4* dl_ws;  // ... in col_s
+  float4* beta_d; // detached renders: throughput of the sampling material (Russian roulette)
 };
 
 struct FrameParams {
@@ -51,6 +52,28 @@ struct FrameParams {
   const float4* samples;  // points on the hair curves (xyz)
   int n_samples;
   uint32_t sample_key;    // permutation of the samples for this pass
+  // differentiable renders: no training pixels (every pixel a short path +
+  // cache query), and, for a detached render, the materials (one per strand
+  // group) of the hair BSDF values; sampling, pdfs, MIS weights and Russian
+  // roulette keep the scene's materials
+  int no_train;
+  const HairConsts* eval_hc;
+};
+
+// Path replay (Vicini et al. 2021, "Path Replay Backpropagation"): a frame
+// of a differentiable render re-traced with the same random numbers, every
+// hair vertex adding adjoint-weighted material derivatives of the path's
+// radiance; the radiance still to come after a vertex is the path's total
+// (kept from its forward frame) minus what the replay has gathered so far.
+struct HairConstsD;
+struct DiffParams {
+  const float4* col_total;       // [P] radiance of each path in the forward frame
+  const float* adjoint;          // [P][3] dLoss/dImage
+  float adj_scale;               // 1 / frames (the image is their mean)
+  float* gacc;                   // [n_groups * 6][P] per-path gradient sums
+  float* stash;                  // [13][P] gradient terms waiting for shadow rays; [12]: group
+  const HairConstsD* group_dual; // [n_groups] materials with their partials
+  int P;
 };
 
 // Several scenes in one frame (a batch): the frame's paths, training
@@ -91,6 +114,7 @@ struct FrameBufs {
   double* acc_pt;       // [P][3] running sums (FP64)
   double* acc_nn;
   double* acc_final;
+  float4* col_out;      // differentiable renders: each path's radiance (NULL otherwise)
 };
 
 // Training-pixel choice: the reference shuffles a table of 0..R-1 each frame

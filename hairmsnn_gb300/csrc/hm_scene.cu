@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cmath>
 #include <fstream>
 #include <sstream>
 
@@ -72,6 +73,7 @@ static void gen_hair(const HairGen& g, f3 head_r, Scene* s) {
     float jitter = 0.15f * (lcg_next(st) - 0.5f);
     float hphase = 2.f * kPi * lcg_next(st);
     int first = (int)s->cp.size();
+    s->strand_seg.push_back((int)s->seg.size());
     for (int i = 0; i < g.cps; ++i) {
       f3 q = p;
       if (g.type == "curly") {
@@ -95,6 +97,7 @@ static void gen_hair(const HairGen& g, f3 head_r, Scene* s) {
     }
     for (int i = 0; i + 3 < g.cps; ++i) s->seg.push_back(first + i);
   }
+  s->strand_seg.push_back((int)s->seg.size());
 }
 
 // ------------------------------------------------------------ .hair files
@@ -155,6 +158,7 @@ static int load_hair_file(const std::string& path, Scene* s, f3* raw_lo, f3* raw
   int left = -1;
   s->cp.clear();
   s->seg.clear();
+  s->strand_seg.clear();
   for (int64_t i = 0; i < (int64_t)n_points; ++i) {
     const f3 p = point(i);
     const float w = width(i);
@@ -170,6 +174,7 @@ static int load_hair_file(const std::string& path, Scene* s, f3* raw_lo, f3* raw
       first = true;
     }
     if (first) {
+      s->strand_seg.push_back((int)s->seg.size());
       const f3 q = p + (p - point(i + 1));
       s->cp.push_back(make_float4(q.x, q.y, q.z, 0.2f * w));
       s->seg.push_back((int)s->cp.size() - 1);
@@ -187,6 +192,8 @@ static int load_hair_file(const std::string& path, Scene* s, f3* raw_lo, f3* raw
   // last control points: drop them
   while (!s->seg.empty() && s->seg.back() + 3 >= (int)s->cp.size()) s->seg.pop_back();
   s->n_strands = (int)strand;
+  s->strand_seg.push_back((int)s->seg.size());
+  for (int& o : s->strand_seg) o = std::min(o, (int)s->seg.size());
   if (s->seg.empty()) return hm_set_error("scene: %s has no complete segment", path.c_str()), HM_EPARSE;
   *raw_lo = lo;
   *raw_hi = hi;
@@ -472,6 +479,59 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
     s->hair.gain_tt = (float)hair.number_or("Gain TT", 1.0);
     s->hair.gain_trt = (float)hair.number_or("Gain TRT", 1.0);
     s->hair.gain_trrt = (float)hair.number_or("Gain TRRT", 1.0);
+    // ---- strand groups (no reference counterpart): per-group materials
+    if (hair.has("groups")) {
+      const Json& gj = hair["groups"];
+      const int count = (int)gj.number_or("count", 1);
+      if (count < 1 || count > kMaxStrandGroups) throw JsonError("scene: hair.groups.count out of range");
+      const std::string how = gj.string_or("assign", "azimuth");
+      if (how != "azimuth" && how != "index") throw JsonError("scene: hair.groups.assign must be azimuth or index");
+      std::vector<int> grp(s->n_strands, 0);
+      if (how == "index") {
+        for (int k = 0; k < s->n_strands; ++k) grp[k] = k % count;
+      } else {
+        // azimuth of each strand's root (its second control point) around the
+        // mean root, split into `count` equal wedges
+        std::vector<f3> root(s->n_strands);
+        double cx = 0.0, cy = 0.0;
+        for (int k = 0; k < s->n_strands; ++k) {
+          const int a = s->strand_seg[k];
+          const int cpi = a < (int)s->seg.size() ? s->seg[a] + 1 : 0;
+          const float4 c = s->cp.empty() ? make_float4(0, 0, 0, 0) : s->cp[std::min(cpi, (int)s->cp.size() - 1)];
+          root[k] = mk(c.x, c.y, c.z);
+          cx += c.x;
+          cy += c.y;
+        }
+        cx /= std::max(1, s->n_strands);
+        cy /= std::max(1, s->n_strands);
+        for (int k = 0; k < s->n_strands; ++k) {
+          const double ang = std::atan2((double)root[k].y - cy, (double)root[k].x - cx) + 3.141592653589793;
+          grp[k] = std::min(count - 1, (int)(ang / (2.0 * 3.141592653589793) * count));
+        }
+      }
+      std::vector<hm_hair_params> mats(count, s->hair);
+      const Json& mj = gj["materials"];
+      if (mj.is_array()) {
+        if ((int)mj.size() > count) throw JsonError("scene: more hair.groups.materials than groups");
+        for (size_t g = 0; g < mj.size(); ++g) {
+          const Json& m = mj[g];
+          hm_hair_params& p = mats[g];
+          if (m["sigma_a"].is_array()) {
+            f3 sa = f3_of(m["sigma_a"], mk(p.sigma_a[0], p.sigma_a[1], p.sigma_a[2]));
+            p.sigma_a[0] = sa.x; p.sigma_a[1] = sa.y; p.sigma_a[2] = sa.z;
+          }
+          p.beta_m = (float)m.number_or("beta_m", p.beta_m);
+          p.beta_n = (float)m.number_or("beta_n", p.beta_n);
+          if (m.has("alpha")) p.alpha = 3.14159f * (float)m["alpha"].as_number() / 180.f;
+          p.gain_r = (float)m.number_or("Gain R", p.gain_r);
+          p.gain_tt = (float)m.number_or("Gain TT", p.gain_tt);
+          p.gain_trt = (float)m.number_or("Gain TRT", p.gain_trt);
+          p.gain_trrt = (float)m.number_or("Gain TRRT", p.gain_trrt);
+        }
+      }
+      s->strand_group = grp;
+      s->group_mats = mats;
+    }
     // ---- lights
     const Json& lights = j["lights"];
     if (lights.has("sky")) {
@@ -577,6 +637,56 @@ Scene::~Scene() {
   cudaFree(d_cp); cudaFree(d_seg); cudaFree(d_vtx); cudaFree(d_nrm); cudaFree(d_tri);
   cudaFree(d_env); cudaFree(d_cpdf); cudaFree(d_ccdf); cudaFree(d_mpdf); cudaFree(d_mcdf);
   cudaFree(d_dlights); cudaFree(d_nodes); cudaFree(d_prim_of_leaf); cudaFree(d_wnodes);
+  cudaFree(d_seg_group); cudaFree(d_group_hc); cudaFree(d_group_raw);
+}
+
+// Strand groups: every segment takes its strand's group.
+int Scene::set_strand_groups(const int* groups, int n, int ng) {
+  if (n != n_strands) return hm_set_error("strand groups: %d entries for %d strands", n, n_strands), HM_EINVAL;
+  if (ng < 1 || ng > kMaxStrandGroups) return hm_set_error("strand groups: 1..%d groups", kMaxStrandGroups), HM_EINVAL;
+  for (int k = 0; k < n; ++k)
+    if (groups[k] < 0 || groups[k] >= ng) return hm_set_error("strand groups: group %d of strand %d", groups[k], k), HM_EINVAL;
+  strand_group.assign(groups, groups + n);
+  if ((int)group_mats.size() != ng) group_mats.assign(ng, hair);
+  ++material_version;
+  return built ? upload_groups() : HM_OK;
+}
+
+int Scene::set_group_materials(const hm_hair_params* m, int n) {
+  if (group_mats.empty()) {
+    if (n != 1) return hm_set_error("group materials: the scene has one material"), HM_EINVAL;
+    hair = m[0];
+    ++material_version;
+    return HM_OK;
+  }
+  if (n != (int)group_mats.size())
+    return hm_set_error("group materials: %d given for %d groups", n, (int)group_mats.size()), HM_EINVAL;
+  group_mats.assign(m, m + n);
+  ++material_version;
+  return built ? upload_groups() : HM_OK;
+}
+
+// Device tables of the groups.  Frames in flight may read them: wait first.
+int Scene::upload_groups() {
+  if (group_mats.empty()) return HM_OK;
+  cudaError_t e = cudaDeviceSynchronize();
+  const int ng = (int)group_mats.size();
+  if (e == cudaSuccess && !d_seg_group) e = cudaMalloc(&d_seg_group, std::max<size_t>(1, seg.size()));
+  if (e == cudaSuccess && !d_group_hc) e = cudaMalloc(&d_group_hc, kMaxStrandGroups * sizeof(HairConsts));
+  if (e == cudaSuccess && !d_group_raw) e = cudaMalloc(&d_group_raw, kMaxStrandGroups * sizeof(hm_hair_params));
+  if (e != cudaSuccess) return hm_cuda_status(e, "strand group tables");
+  seg_group_host.assign(seg.size(), 0);
+  if (!strand_group.empty())
+    for (int k = 0; k < n_strands; ++k)
+      for (int i = strand_seg[k]; i < strand_seg[k + 1]; ++i) seg_group_host[i] = strand_group[k];
+  std::vector<uint8_t> sg(seg_group_host.begin(), seg_group_host.end());
+  std::vector<HairConsts> hc(ng);
+  for (int g = 0; g < ng; ++g) hc[g] = hair_consts_from_params(group_mats[g]);
+  if (!sg.empty()) e = cudaMemcpy(d_seg_group, sg.data(), sg.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_group_hc, hc.data(), ng * sizeof(HairConsts), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(d_group_raw, group_mats.data(), ng * sizeof(hm_hair_params), cudaMemcpyHostToDevice);
+  return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "strand group upload");
 }
 
 SceneDev Scene::dev() const {
@@ -623,6 +733,13 @@ SceneDev Scene::dev() const {
   d.cam_du = ddu;
   d.cam_dv = ddv;
   d.hair = hair_consts_from_params(hair);
+  d.hair_raw = hair;
+  if (!group_mats.empty() && d_seg_group) {
+    d.seg_group = d_seg_group;
+    d.group_hc = d_group_hc;
+    d.group_raw = d_group_raw;
+    d.n_groups = (int)group_mats.size();
+  }
   d.mis = mis;
   d.width = width;
   d.height = height;
@@ -640,6 +757,7 @@ namespace hm {
 int Scene::ensure_built() {
   if (built) return HM_OK;
   int st = upload();
+  if (st == HM_OK) st = upload_groups();
   if (st == HM_OK) st = build_bvh(0);
   if (st == HM_OK) {
     cudaError_t e = cudaDeviceSynchronize();
@@ -684,6 +802,7 @@ extern "C" int hm_scene_info(const hm_scene* h, hm_scene_desc* out) {
   out->n_triangles = (int)s->tri.size();
   out->n_bvh_nodes = s->n_nodes;
   out->n_bvh_wide_nodes = s->n_wnodes;
+  out->n_groups = s->group_mats.empty() ? 0 : (int)s->group_mats.size();
   out->width = s->width;
   out->height = s->height;
   out->spp = s->spp;
@@ -731,6 +850,9 @@ extern "C" int64_t hm_scene_export_size(const hm_scene* h, int which) {
     case HM_SCENE_BVH_WIDE_NODES: return (int64_t)s->n_wnodes * 128;
     case HM_SCENE_CAMERA: return 12 * 4;
     case HM_SCENE_MATERIALS: return 16 * 4;
+    case HM_SCENE_STRAND_GROUPS: return (int64_t)s->strand_group.size() * 4;
+    case HM_SCENE_GROUP_MATERIALS: return (int64_t)s->group_mats.size() * (int64_t)sizeof(hm_hair_params);
+    case HM_SCENE_SEGMENT_GROUPS: return s->group_mats.empty() ? 0 : (int64_t)s->seg.size() * 4;
     default: return -1;
   }
 }
@@ -750,6 +872,16 @@ extern "C" int hm_scene_export(const hm_scene* h, int which, void* out, int64_t 
     case HM_SCENE_ENV_MPDF: return export_vec(s->mpdf, out, cap);
     case HM_SCENE_ENV_MCDF: return export_vec(s->mcdf, out, cap);
     case HM_SCENE_DIR_LIGHTS: return export_vec(s->dlights, out, cap);
+    case HM_SCENE_STRAND_GROUPS: return export_vec(s->strand_group, out, cap);
+    case HM_SCENE_GROUP_MATERIALS: return export_vec(s->group_mats, out, cap);
+    case HM_SCENE_SEGMENT_GROUPS: {
+      if (s->group_mats.empty()) return HM_OK;
+      std::vector<int> sg(s->seg.size(), 0);
+      if (!s->strand_group.empty())
+        for (int k = 0; k < s->n_strands; ++k)
+          for (int i = s->strand_seg[k]; i < s->strand_seg[k + 1]; ++i) sg[i] = s->strand_group[k];
+      return export_vec(sg, out, cap);
+    }
     case HM_SCENE_BVH_NODES:
     case HM_SCENE_BVH_LEAVES:
     case HM_SCENE_BVH_WIDE_NODES: {
@@ -782,4 +914,16 @@ extern "C" int hm_scene_export(const hm_scene* h, int which, void* out, int64_t 
     default:
       return hm_set_error("hm_scene_export: unknown array %d", which), HM_EINVAL;
   }
+}
+
+extern "C" int hm_scene_set_strand_groups(hm_scene* h, const int32_t* groups, int n_strands, int n_groups) {
+  Scene* s = (Scene*)h;
+  if (!s || (!groups && n_strands)) return hm_set_error("hm_scene_set_strand_groups: NULL"), HM_EINVAL;
+  return s->set_strand_groups(groups, n_strands, n_groups);
+}
+
+extern "C" int hm_scene_set_group_materials(hm_scene* h, const hm_hair_params* materials, int n_groups) {
+  Scene* s = (Scene*)h;
+  if (!s || !materials) return hm_set_error("hm_scene_set_group_materials: NULL"), HM_EINVAL;
+  return s->set_group_materials(materials, n_groups);
 }

@@ -18,6 +18,8 @@ HM_D int3 ldi3(const int3* p) {
   return make_int3(__ldg(q), __ldg(q + 1), __ldg(q + 2));
 }
 
+constexpr int kMaxStrandGroups = 64;  // materials per scene (group ids are bytes)
+
 // Device view of the scene, passed to every render kernel by value.
 struct SceneDev {
   // hair: cubic B-spline segments over control points (x, y, z, radius)
@@ -58,6 +60,13 @@ struct SceneDev {
   f3 cam_pos, cam_d00, cam_du, cam_dv;
   // material, integrator
   HairConsts hair;
+  hm_hair_params hair_raw;  // the parameters `hair` was made from
+  // strand groups: segment -> group, per-group material (n_groups == 0:
+  // every segment uses `hair`)
+  const uint8_t* seg_group;
+  const HairConsts* group_hc;
+  const hm_hair_params* group_raw;
+  int n_groups;
   int mis;
   int width, height;
   int path_v1, path_v2;
@@ -69,6 +78,12 @@ struct Scene {
   std::vector<float4> cp;
   std::vector<int> seg;
   int n_strands = 0;
+  std::vector<int> strand_seg;  // first segment of every strand (n_strands + 1 entries)
+  // strand groups (empty: one material, `hair`)
+  std::vector<int> strand_group;
+  std::vector<hm_hair_params> group_mats;
+  std::vector<int> seg_group_host;  // group of every segment (derived)
+  int material_version = 0;          // bumped by every change of groups or materials
   std::vector<float3> vtx, nrm;
   std::vector<int3> tri;
   f3 diffuse{0.5f, 0.5f, 0.5f};
@@ -105,6 +120,9 @@ struct Scene {
   int n_nodes = 0;
   float4* d_wnodes = nullptr;
   int n_wnodes = 0;
+  uint8_t* d_seg_group = nullptr;
+  HairConsts* d_group_hc = nullptr;
+  hm_hair_params* d_group_raw = nullptr;
   bool built = false;
 
   ~Scene();
@@ -113,6 +131,10 @@ struct Scene {
   int build_bvh(cudaStream_t st);
   SceneDev dev() const;
   int n_prims() const { return (int)seg.size() + (int)tri.size(); }
+  int n_groups() const { return group_mats.empty() ? 1 : (int)group_mats.size(); }
+  int set_strand_groups(const int* groups, int n, int n_groups);
+  int set_group_materials(const hm_hair_params* m, int n);
+  int upload_groups();
 };
 
 int scene_from_json(const char* text, const char* base_dir, Scene* s);

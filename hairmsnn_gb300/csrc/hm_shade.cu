@@ -11,6 +11,7 @@
 //                    reference's NaN/Inf scrubbing (hair_msnn.cu:242-312)
 //   compose_kernel   RENDER pass: short path + cache on hair pixels, FP64
 //                    accumulation (hair_msnn.cu:314-356; utils.cuh:13-35 for PT)
+#include "hm_hair_grad.cuh"
 #include "hm_render.h"
 #include "hm_shading.cuh"
 
@@ -52,7 +53,7 @@ __global__ void __launch_bounds__(256) camera_kernel(const __grid_constant__ Sce
   const int x = c.local % s.width, y = c.local / s.width;
   uint32_t rng = rng_seed(fp.frame_seed, (uint32_t)c.local);
   uint32_t flags = 0;
-  if (fp.mode == MODE_MSNN) {
+  if (fp.mode == MODE_MSNN && !fp.no_train) {
     const int tr = c.local / c.every_nth;
     if (tr < c.n_train) {
       const uint32_t pick = feistel_perm((uint32_t)tr, (uint32_t)c.n_train, (uint32_t)fp.accum_id) % c.every_nth;
@@ -71,6 +72,7 @@ __global__ void __launch_bounds__(256) camera_kernel(const __grid_constant__ Sce
   st3(ps.beta_s, pid, splat(1.f));
   st3(ps.col, pid, splat(0.f));
   st3(ps.col_s, pid, splat(0.f));
+  if (fp.eval_hc) st3(ps.beta_d, pid, splat(1.f));
   queue[pid] = pid;
 }
 
@@ -81,11 +83,70 @@ HM_D void write_cache_input(float* dst, int in_ch, f3 p, f3 wo, f3 t) {
   for (int c = 9; c < in_ch; ++c) dst[c] = 0.f;
 }
 
+HM_D float comp(f3 v, int c) { return c == 0 ? v.x : (c == 1 ? v.y : v.z); }
+
+// Path-replay terms of one hair vertex (material derivatives, adjoint A,
+// throughput bw at the vertex, R = the path's total radiance minus what it
+// gathered before the vertex).
+//  * Its own direct lighting: a sample's contribution c = f * (emitted
+//    radiance, MIS weight, 1 / pdf), with f the BSDF value at the sample's
+//    direction; the weight and the pdf are held fixed (detached sampling),
+//    so d c = c * (d f) / f.  E[k] gets A . (bw * d c_k), counted only if
+//    the shadow ray finds the light.
+//  * The continuation: the throughput factor f / pdf of the sampled
+//    direction scales all the radiance gathered after the vertex, R minus
+//    this vertex's own direct lighting, so T gets A . ((d f) / f * R) and
+//    E[k] loses A . ((d f) / f * bw * c_k), the part of R that is the
+//    sample's (if visible).
+// Non-finite terms (a NaN path, f = 0) are left out.
+HM_D void replay_vertex(const HairConstsD& hcd, const Vertex& v, f3 A, f3 bw, f3 R, const ShadowSample ss[2],
+                        bool dl, bool cont, f3 wl_next, float E[2][kNd], float T[kNd]) {
+  const float h = dot(v.fr.r1, v.n);
+#pragma unroll
+  for (int i = 0; i < kNd; ++i) {
+    E[0][i] = 0.f;
+    E[1][i] = 0.f;
+    T[i] = 0.f;
+  }
+  for (int k = 0; k < 2; ++k) {
+    if (!dl || !ss[k].valid) continue;
+    const HairEvalD e = hair_eval_dual(v.wo_local, ss[k].wl, h, hcd);
+    for (int c = 0; c < 3; ++c) {
+      const float f = e.f[c].v;
+      const float w = comp(A, c) * comp(bw, c) * comp(ss[k].c, c) / f;
+      if (f == 0.f || !isfinite(w)) continue;
+#pragma unroll
+      for (int i = 0; i < kNd; ++i) E[k][i] += w * e.f[c].d[i];
+    }
+  }
+  if (!cont) return;
+  const HairEvalD e = hair_eval_dual(v.wo_local, wl_next, h, hcd);
+  for (int c = 0; c < 3; ++c) {
+    const float f = e.f[c].v;
+    if (f == 0.f) continue;
+    const float a = comp(A, c) / f;
+    const float t = a * comp(R, c);
+    const float u0 = dl && ss[0].valid ? a * comp(bw, c) * comp(ss[0].c, c) : 0.f;
+    const float u1 = dl && ss[1].valid ? a * comp(bw, c) * comp(ss[1].c, c) : 0.f;
+    if (!isfinite(t) || !isfinite(u0) || !isfinite(u1)) continue;
+#pragma unroll
+    for (int i = 0; i < kNd; ++i) {
+      const float d = e.f[c].d[i];
+      T[i] += t * d;
+      E[0][i] -= u0 * d;
+      E[1][i] -= u1 * d;
+    }
+  }
+}
+
 // Shades every path of `queue`; keep[i] = 1 if path queue[i] continues.
-template <bool MULTI>
+// REPLAY: the same shading (same random numbers, same results) plus the
+// path-replay terms of each hair vertex (single-scene frames).
+template <bool MULTI, bool REPLAY>
 __global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ SceneDev s0, FrameParams fp, Batch b,
                                                     PathState ps, FrameBufs fb, const int* __restrict__ queue,
-                                                    const int* __restrict__ count, int* __restrict__ keep) {
+                                                    const int* __restrict__ count, int* __restrict__ keep,
+                                                    DiffParams dp) {
   const int n = *count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int pid = queue[i];
@@ -117,7 +178,8 @@ __global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ Scen
       keep[i] = 0;
       continue;
     }
-    const Vertex v = setup_vertex(s, ro, rd, h);
+    Vertex v = setup_vertex(s, ro, rd, h);
+    if (fp.eval_hc && !v.surface) v.hc_eval = fp.eval_hc + v.group;
     if (k == 0) {
       flags |= F_PRIM_HIT | (v.surface ? F_PRIM_SURF : 0u);
       if (fp.mode == MODE_MSNN) {
@@ -130,10 +192,15 @@ __global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ Scen
     uint32_t rng = ps.rng[pid];
     f3 beta = ld3(ps.beta, pid);
     f3 beta_s = ld3(ps.beta_s, pid);
+    // detached renders: Russian roulette on the sampling material's throughput
+    const bool detached = fp.eval_hc != nullptr;
+    f3 beta_d = detached ? ld3(ps.beta_d, pid) : beta;
+    const f3 beta_v = beta;  // throughput at the vertex
     // ---- direct lighting at this vertex
     const bool do_dl = fp.mode == MODE_MSNN || (k == 0 ? v1_stop == 0 : k >= v1_stop);
+    ShadowSample ss[2];
+    ss[0].valid = ss[1].valid = 0;
     if (do_dl) {
-      ShadowSample ss[2];
       direct_lighting(s, v, rng, ss);
       st3(ps.sh_o0, pid, ss[0].o, ss[0].valid ? 1.f : 0.f);
       st3(ps.sh_d0, pid, ss[0].d);
@@ -159,29 +226,59 @@ __global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ Scen
           beta = beta / (1.f - q);
           if (beta_s.x != 0.f || beta_s.y != 0.f || beta_s.z != 0.f) beta_s = beta_s / (1.f - qs);
         }
-      } else if (fp.mode == MODE_MSNN) {
-        const float eps = lcg_next(rng);
-        if (eps < q || k > c.beta) done = true;
-        else beta = beta / (1.f - q);
       } else {
+        const float qd = detached ? fmaxf(0.05f, 1.f - luminance(beta_d)) : q;
         const float eps = lcg_next(rng);
-        if (eps < q) done = true;
-        else beta = beta / (1.f - q);
+        if (eps < qd || (fp.mode == MODE_MSNN && k > c.beta)) {
+          done = true;
+        } else {
+          beta = beta / (1.f - qd);
+          if (detached) beta_d = beta_d / (1.f - qd);
+        }
       }
     }
     // ---- next vertex
+    bool cont = false;
+    f3 wl_next = splat(0.f);
     if (!done && k + 1 <= v2_stop) {
-      f3 o, d;
-      const f3 mul = next_vertex(s, v, rng, &o, &d);
+      f3 o, d, mul_s;
+      bool mul_nan = false;
+      const f3 mul = next_vertex(s, v, rng, &o, &d, &mul_s, &wl_next, &mul_nan);
       beta = beta * mul;
       beta_s = beta_s * mul;
+      if (detached) beta_d = beta_d * mul_s;
       st3(ps.ray_o, pid, o);
       st3(ps.ray_d, pid, d);
       ps.bounce[pid] = k + 1;
       k_keep = 1;
+      cont = !mul_nan;
+    }
+    if constexpr (REPLAY) {
+      float E[2][kNd], T[kNd];
+      if (!v.surface) {
+        const float* ad = dp.adjoint + 3 * (size_t)c.local;
+        const f3 A = dp.adj_scale * mk(ad[0], ad[1], ad[2]);
+        const f3 R = ld3(dp.col_total, pid) - ld3(ps.col, pid);
+        replay_vertex(dp.group_dual[v.group], v, A, beta_v, R, ss, do_dl, cont, wl_next, E, T);
+        float* g = dp.gacc + (size_t)v.group * kNd * dp.P + pid;
+#pragma unroll
+        for (int i = 0; i < kNd; ++i) g[(size_t)i * dp.P] += T[i];
+      } else {
+#pragma unroll
+        for (int i = 0; i < kNd; ++i) E[0][i] = E[1][i] = 0.f;
+      }
+      if (do_dl) {
+#pragma unroll
+        for (int i = 0; i < kNd; ++i) {
+          dp.stash[(size_t)i * dp.P + pid] = E[0][i];
+          dp.stash[(size_t)(kNd + i) * dp.P + pid] = E[1][i];
+        }
+        dp.stash[(size_t)(2 * kNd) * dp.P + pid] = __int_as_float(v.group);
+      }
     }
     st3(ps.beta, pid, beta);
     st3(ps.beta_s, pid, beta_s);
+    if (detached) st3(ps.beta_d, pid, beta_d);
     ps.rng[pid] = rng;
     ps.flags[pid] = flags;
     keep[i] = k_keep;
@@ -200,6 +297,7 @@ __global__ void __launch_bounds__(256) finalize_kernel(const __grid_constant__ S
   const uint32_t flags = ps.flags[pid];
   const bool hit = flags & F_PRIM_HIT;
   f3 color = ld3(ps.col, pid);
+  if (fb.col_out) fb.col_out[pid] = ps.col[pid];  // differentiable renders: the path's radiance
   if (fp.mode == MODE_PT) {
     // writePixel (utils.cuh:13-35), FP64 accumulation
     if (anynan(color)) color = splat(0.f);
@@ -270,12 +368,49 @@ int launch_camera(const SceneDev& s, const FrameParams& fp, const Batch& b, cons
 }
 
 int launch_shade(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps, const FrameBufs& fb,
-                 const int* queue, const int* count, int* keep, int grid, cudaStream_t st) {
-  if (b.scenes)
-    shade_kernel<true><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep);
-  else
-    shade_kernel<false><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep);
+                 const int* queue, const int* count, int* keep, int grid, cudaStream_t st, const DiffParams* dp) {
+  if (dp) {
+    if (b.scenes) return hm_set_error("path replay: single-scene renders only"), HM_EINVAL;
+    shade_kernel<false, true><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep, *dp);
+  } else if (b.scenes) {
+    shade_kernel<true, false><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep, DiffParams{});
+  } else {
+    shade_kernel<false, false><<<grid, 128, 0, st>>>(s, fp, b, ps, fb, queue, count, keep, DiffParams{});
+  }
   HM_CHECK_LAUNCH("shade_kernel");
+  return HM_OK;
+}
+
+// Materials with their partials, one per strand group (the scene's own
+// material when it has no groups).
+__global__ void group_dual_kernel(const __grid_constant__ SceneDev s, HairConstsD* out, int n) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n) return;
+  const hm_hair_params& m = s.n_groups ? s.group_raw[g] : s.hair_raw;
+  const float gain[4] = {m.gain_r, m.gain_tt, m.gain_trt, m.gain_trrt};
+  out[g] = hair_consts_dual(m.sigma_a, m.beta_m, m.beta_n, m.alpha, gain);
+}
+
+int launch_group_dual(const SceneDev& s, void* out, int n, cudaStream_t st) {
+  group_dual_kernel<<<1, 64, 0, st>>>(s, (HairConstsD*)out, n);
+  HM_CHECK_LAUNCH("group_dual_kernel");
+  return HM_OK;
+}
+size_t group_dual_bytes() { return sizeof(HairConstsD); }
+
+// dL/d(cache output) of a replayed frame: the adjoint of the pixels whose
+// image took the cache (hair at the primary hit), 0 elsewhere.
+__global__ void __launch_bounds__(256) replay_cache_grad_kernel(int P, PathState ps, DiffParams dp, float* dy) {
+  const int pid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pid >= P) return;
+  const uint32_t flags = ps.flags[pid];
+  const bool nn = (flags & F_PRIM_HIT) && !(flags & F_PRIM_SURF);
+  for (int c = 0; c < 3; ++c) dy[3 * (size_t)pid + c] = nn ? dp.adj_scale * dp.adjoint[3 * (size_t)pid + c] : 0.f;
+}
+
+int launch_replay_cache_grad(int P, const PathState& ps, const DiffParams& dp, float* dy, cudaStream_t st) {
+  replay_cache_grad_kernel<<<(P + 255) / 256, 256, 0, st>>>(P, ps, dp, dy);
+  HM_CHECK_LAUNCH("replay_cache_grad_kernel");
   return HM_OK;
 }
 

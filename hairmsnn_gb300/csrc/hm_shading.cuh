@@ -256,6 +256,9 @@ struct Vertex {
   f3 wo_local;
   int surface;
   float radius;
+  int group;                  // strand group (0 for the surface)
+  const HairConsts* hc;       // material that samples and weighs (pdfs, MIS)
+  const HairConsts* hc_eval;  // material of the BSDF values (== hc but in detached renders)
 };
 
 // hairCH (optix_common.cuh:558-599) with computeCurveIntersection
@@ -284,6 +287,8 @@ HM_D Vertex setup_vertex(const SceneDev& s, f3 ro, f3 rd, const float4 hit) {
     v.fr.r1 = Y;
     v.fr.r2 = Z;
     v.surface = 0;
+    v.group = s.seg_group ? (int)__ldg(s.seg_group + prim) : 0;
+    v.hc = s.n_groups ? s.group_hc + v.group : &s.hair;
   } else {
     const int3 tv = ldi3(s.tri + (prim - s.n_seg));
     const float bu = hit.z, bv = hit.w;
@@ -295,7 +300,10 @@ HM_D Vertex setup_vertex(const SceneDev& s, f3 ro, f3 rd, const float4 hit) {
     v.t = v.fr.r0;
     v.radius = 0.f;
     v.surface = 1;
+    v.group = 0;
+    v.hc = &s.hair;
   }
+  v.hc_eval = v.hc;
   v.wo_local = normalize(to_local(v.fr, v.wo));
   return v;
 }
@@ -304,6 +312,7 @@ HM_D Vertex setup_vertex(const SceneDev& s, f3 ro, f3 rd, const float4 hit) {
 struct ShadowSample {
   f3 c;       // contribution if visible
   f3 o, d;    // shadow ray
+  f3 wl;      // its direction in the vertex frame
   int valid;  // 0: no ray, contributes nothing
 };
 
@@ -311,8 +320,9 @@ HM_D f3 bsdf_eval_vertex(const SceneDev& s, const Vertex& v, f3 wi_local, float*
   if (!v.surface) {
     f3 n_local = v.n;  // unused by the eval; h is taken from the frame
     (void)n_local;
-    HairEval e = hair_eval(v.wo_local, wi_local, dot(v.fr.r1, v.n), s.hair);
+    HairEval e = hair_eval(v.wo_local, wi_local, dot(v.fr.r1, v.n), *v.hc);
     *pdf = e.pdf;
+    if (v.hc_eval != v.hc) return hair_eval(v.wo_local, wi_local, dot(v.fr.r1, v.n), *v.hc_eval).f;
     return e.f;
   }
   f3 f = frostbite_ggx(v.wo_local, wi_local, s.diffuse, s.alpha);
@@ -354,6 +364,7 @@ HM_D ShadowSample sample_lights(const SceneDev& s, const Vertex& v, f3* p, uint3
   }
   out.o = *p + 1e-3f * nd;
   out.d = wi;
+  out.wl = wi_local;
   out.valid = 1;
   f3 bsdf = bsdf_eval_vertex(s, v, wi_local, &bsdfPdf, true);
   if (s.mis && !*is_delta)
@@ -373,9 +384,10 @@ HM_D ShadowSample sample_bsdf(const SceneDev& s, const Vertex& v, f3* p, uint32_
   f3 bsdf, wi_local;
   if (!v.surface) {
     float r2 = lcg_next(rng), r3 = lcg_next(rng);
-    HairEval e = hair_sample(v.wo_local, dot(v.fr.r1, v.n), r0, r1, r2, r3, s.hair, &wi_local);
+    HairEval e = hair_sample(v.wo_local, dot(v.fr.r1, v.n), r0, r1, r2, r3, *v.hc, &wi_local);
     bsdf = e.f;
     bsdfPdf = e.pdf;
+    if (v.hc_eval != v.hc) bsdf = hair_eval(v.wo_local, wi_local, dot(v.fr.r1, v.n), *v.hc_eval).f;
   } else {
     wi_local = sample_ggx(r0, r1, s.alpha, v.wo_local, &bsdfPdf);
     bsdf = frostbite_ggx(v.wo_local, wi_local, s.diffuse, s.alpha);
@@ -390,6 +402,7 @@ HM_D ShadowSample sample_bsdf(const SceneDev& s, const Vertex& v, f3* p, uint32_
   }
   out.o = *p + 1e-3f * nd;
   out.d = wi;
+  out.wl = wi_local;
   out.valid = 1;
   f3 emit = env_radiance(s, wi);
   float lightPdf = env_pdf(s, wi) * 1.f / (float)s.n_total_lights;
@@ -413,18 +426,25 @@ HM_D void direct_lighting(const SceneDev& s, const Vertex& v, uint32_t& rng, Sha
 
 // msnnNextPathVertex / nextPathVertex (hair_msnn.cu:18-65,
 // optix_common.cuh:311-360): sample, throughput factor, extension ray.
-HM_D f3 next_vertex(const SceneDev& s, const Vertex& v, uint32_t& rng, f3* ro, f3* rd) {
+// Detached renders (v.hc_eval != v.hc) also give the factor of the sampling
+// material in *mul_s; *wl receives the sampled direction in the vertex frame
+// and *mul_nan whether the factor was a NaN replaced by 1.
+HM_D f3 next_vertex(const SceneDev& s, const Vertex& v, uint32_t& rng, f3* ro, f3* rd, f3* mul_s = nullptr,
+                    f3* wl = nullptr, bool* mul_nan = nullptr) {
   float r0 = lcg_next(rng), r1 = lcg_next(rng);
   float pdf = 1.f;
-  f3 bsdf, wi_local;
+  f3 bsdf, wi_local, bsdf_s;
   if (!v.surface) {
     float r2 = lcg_next(rng), r3 = lcg_next(rng);
-    HairEval e = hair_sample(v.wo_local, dot(v.fr.r1, v.n), r0, r1, r2, r3, s.hair, &wi_local);
+    HairEval e = hair_sample(v.wo_local, dot(v.fr.r1, v.n), r0, r1, r2, r3, *v.hc, &wi_local);
     bsdf = e.f;
     pdf = e.pdf;
+    bsdf_s = bsdf;
+    if (v.hc_eval != v.hc) bsdf = hair_eval(v.wo_local, wi_local, dot(v.fr.r1, v.n), *v.hc_eval).f;
   } else {
     wi_local = sample_ggx(r0, r1, s.alpha, v.wo_local, &pdf);
     bsdf = frostbite_ggx(v.wo_local, wi_local, s.diffuse, s.alpha);
+    bsdf_s = bsdf;
   }
   const f3 wi = normalize(to_world(v.fr, wi_local));
   const bool lower = dot(wi, v.n) < 0.f;
@@ -435,7 +455,17 @@ HM_D f3 next_vertex(const SceneDev& s, const Vertex& v, uint32_t& rng, f3* ro, f
     p = p + 2.f * v.radius * nd;
   }
   f3 mul = pdf == 0.f ? bsdf : bsdf / pdf;
-  if (isnan(mul.x) || isnan(mul.y) || isnan(mul.z)) mul = splat(1.f);
+  const bool is_nan = isnan(mul.x) || isnan(mul.y) || isnan(mul.z);
+  if (is_nan) mul = splat(1.f);
+  if (mul_s) {
+    *mul_s = mul;
+    if (v.hc_eval != v.hc) {
+      *mul_s = pdf == 0.f ? bsdf_s : bsdf_s / pdf;
+      if (isnan(mul_s->x) || isnan(mul_s->y) || isnan(mul_s->z)) *mul_s = splat(1.f);
+    }
+  }
+  if (wl) *wl = wi_local;
+  if (mul_nan) *mul_nan = is_nan;
   *ro = p + 1e-3f * nd;
   *rd = wi;  // -si.wo
   return mul;

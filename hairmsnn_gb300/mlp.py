@@ -62,9 +62,23 @@ class TinyMLP:
         self._h = ctypes.c_void_p(h)
         self.training_loss = 0.0
 
+    @classmethod
+    def wrap(cls, handle):
+        """A view of a network owned elsewhere (e.g. a renderer's cache)."""
+        if not handle:
+            raise ValueError("no network")
+        net = cls.__new__(cls)
+        net._h = ctypes.c_void_p(handle)
+        net._borrowed = True
+        net.training_loss = 0.0
+        d = net.info()
+        net.input_ch, net.output_ch = d.in_ch, d.out_ch
+        return net
+
     def close(self):
         if getattr(self, "_h", None):
-            lib().hm_mlp_destroy(self._h)
+            if not getattr(self, "_borrowed", False):
+                lib().hm_mlp_destroy(self._h)
             self._h = None
 
     def __del__(self):
@@ -104,6 +118,10 @@ class TinyMLP:
         loss = torch.zeros(1, dtype=torch.float32, device=d_target.device)
         check(lib().hm_mlp_backward(self._h, _vp(d_target), d_target.shape[0], _vp(loss), _stream(stream)))
         return loss
+
+    def backward_output_grad(self, d_dy, stream=None):
+        """Backward of the last forward with dL/d(output) given ([n, out_ch])."""
+        check(lib().hm_mlp_backward_output_grad(self._h, _vp(d_dy), d_dy.shape[0], _stream(stream)))
 
     def optimizer_step(self, loss_scale=1.0, stream=None):
         check(lib().hm_mlp_optimizer_step(self._h, float(loss_scale), _stream(stream)))

@@ -16,12 +16,13 @@ from ._ffi import check, lib
 
 HM_SCENE = dict(control_points=0, segments=1, vertices=2, normals=3, triangles=4, env=5, env_cpdf=6,
                 env_ccdf=7, env_mpdf=8, env_mcdf=9, dir_lights=10, bvh_nodes=11, bvh_leaves=12, camera=13,
-                materials=14, bvh_wide_nodes=15)
+                materials=14, bvh_wide_nodes=15, strand_groups=16, group_materials=17, segment_groups=18)
 DTYPES = dict(control_points=(np.float32, 4), segments=(np.int32, 1), vertices=(np.float32, 3),
               normals=(np.float32, 3), triangles=(np.int32, 3), env=(np.float32, 4), env_cpdf=(np.float32, 1),
               env_ccdf=(np.float32, 1), env_mpdf=(np.float32, 1), env_mcdf=(np.float32, 1),
               dir_lights=(np.float32, 6), bvh_nodes=(np.float32, 16), bvh_leaves=(np.int32, 1),
-              camera=(np.float32, 12), materials=(np.float32, 16), bvh_wide_nodes=(np.float32, 32))
+              camera=(np.float32, 12), materials=(np.float32, 16), bvh_wide_nodes=(np.float32, 32),
+              strand_groups=(np.int32, 1), group_materials=(np.float32, 10), segment_groups=(np.int32, 1))
 PT, MSNN = 0, 1
 IMAGE_FINAL, IMAGE_SHORT, IMAGE_CACHE = 0, 1, 2
 
@@ -31,7 +32,8 @@ class hm_scene_desc(ctypes.Structure):
         "n_strands", "n_control_points", "n_segments", "n_vertices", "n_triangles", "n_bvh_nodes", "width",
         "height", "spp", "path_v1", "path_v2", "env_width", "env_height", "n_dir_lights", "mis", "env_pdf",
         "has_env", "shading_catrom")] + [("scene_scale", ctypes.c_float), ("bounds_min", ctypes.c_float * 3),
-                       ("bounds_max", ctypes.c_float * 3), ("n_bvh_wide_nodes", ctypes.c_int)]
+                       ("bounds_max", ctypes.c_float * 3), ("n_bvh_wide_nodes", ctypes.c_int),
+                       ("n_groups", ctypes.c_int)]
 
 
 class hm_render_options(ctypes.Structure):
@@ -110,6 +112,10 @@ def _declare():
     L.hm_copy_to_host.argtypes = [vp, vp, i64]
     L.hm_render_set_instrumentation.argtypes = [vp, i32, i32]
     L.hm_render_get_timings.argtypes = [vp, P(hm_render_timings)]
+    L.hm_scene_set_strand_groups.argtypes = [vp, P(i32), i32, i32]
+    L.hm_scene_set_group_materials.argtypes = [vp, vp, i32]
+    L.hm_render_diff_forward.argtypes = [vp, i32, vp, i32, vp]
+    L.hm_render_diff_backward.argtypes = [vp, vp, P(ctypes.c_double), i32, vp]
     _declared = True
 
 
@@ -160,6 +166,25 @@ class Scene:
             check(lib().hm_scene_export(self._h, which, out.ctypes.data_as(ctypes.c_void_p), nbytes))
         return out.reshape(-1, width) if width > 1 else out
 
+    def set_strand_groups(self, groups, n_groups):
+        """Group of every strand (int array [n_strands]); see hm_scene_set_strand_groups."""
+        g = np.ascontiguousarray(groups, np.int32)
+        check(lib().hm_scene_set_strand_groups(self._h, g.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), len(g),
+                                               int(n_groups)))
+
+    def set_group_materials(self, materials):
+        """materials [n_groups, 10]: sigma_a rgb, beta_m, beta_n, alpha (rad), gains R, TT, TRT, TRRT."""
+        arr = hair_params_array(materials)
+        check(lib().hm_scene_set_group_materials(self._h, arr, len(arr)))
+
+    def group_materials(self):
+        """[n_groups, 10] (the scene's material alone when it has no groups)."""
+        m = self.export("group_materials")
+        if len(m):
+            return m
+        x = self.export("materials")[0]
+        return x[:10].reshape(1, 10).copy()
+
     def trace(self, org, dirs, tmin=0.0, tmax=1e30, any_hit=False, stream=None):
         """org, dirs: CUDA float32 [n, 3] -> hits [n, 4] (t, prim bits, u, v)."""
         import torch
@@ -169,6 +194,16 @@ class Scene:
                                   tmin, tmax, 1 if any_hit else 0, ctypes.c_void_p(hits.data_ptr()),
                                   _stream(stream)))
         return hits
+
+
+def hair_params_array(materials):
+    """ctypes array of hm_hair_params from rows of 10 floats."""
+    from ._ffi import hm_hair_params
+    m = np.asarray(materials, np.float64).reshape(-1, 10)
+    arr = (hm_hair_params * len(m))()
+    for i, row in enumerate(m):
+        arr[i] = hm_hair_params.from_array(row)
+    return arr
 
 
 class Renderer:
@@ -249,6 +284,32 @@ class Renderer:
         t = hm_render_timings()
         check(lib().hm_render_get_timings(self._h, ctypes.byref(t)))
         return t
+
+    def diff_forward(self, frames, eval_materials=None, stream=None):
+        """Differentiable forward: `frames` frames with the cache frozen (see
+        hm_render_diff_forward); eval_materials [n_groups, 10] makes it a
+        detached render.  The image is read() afterwards."""
+        arr, n = (hair_params_array(eval_materials), 0) if eval_materials is not None else (None, 0)
+        if arr is not None:
+            n = len(arr)
+        check(lib().hm_render_diff_forward(self._h, int(frames), arr, n, _stream(stream)))
+
+    def diff_backward(self, adjoint, stream=None):
+        """Path replay for dL/dImage `adjoint` (CUDA float32 [H, W, 3]):
+        returns dL/d(material) [n_groups, 6] (sigma_a rgb, beta_m, beta_n,
+        alpha); the cache's gradients hold dL/dW afterwards."""
+        a = adjoint.contiguous()
+        assert a.dtype.is_floating_point and a.element_size() == 4 and a.is_cuda
+        n = 6 * 64
+        out = (ctypes.c_double * n)()
+        check(lib().hm_render_diff_backward(self._h, ctypes.c_void_p(a.data_ptr()), out, n, _stream(stream)))
+        g = max(1, self.scene.info().n_groups)
+        return np.array(out[:6 * g], np.float64).reshape(g, 6)
+
+    def cache(self):
+        """The render's cache network as a TinyMLP view (not owned)."""
+        from .mlp import TinyMLP
+        return TinyMLP.wrap(lib().hm_render_cache(self._h))
 
     def buffer(self, which):
         """Host copy of a device buffer of the last frame (see hm_render_buffer):

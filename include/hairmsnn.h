@@ -165,6 +165,11 @@ int hm_mlp_inference_noalloc(hm_mlp* mlp, const float* d_in, float* d_out, int64
  * (may be NULL), optimizer_step applies ExponentialDecay(Adam). */
 int hm_mlp_forward(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, void* stream);
 int hm_mlp_backward(hm_mlp* mlp, const float* d_target, int64_t n, float* d_loss, void* stream);
+/* The backward of the last forward with a given dL/d(output) [n][out_ch]
+ * instead of a loss (tcnn's Network::backward with dL_doutput; used to
+ * carry image gradients into the cache weights).  Gradients as for
+ * hm_mlp_backward; the loss is not computed. */
+int hm_mlp_backward_output_grad(hm_mlp* mlp, const float* d_dloss_doutput, int64_t n, void* stream);
 int hm_mlp_optimizer_step(hm_mlp* mlp, float loss_scale, void* stream);
 int hm_mlp_training_step(hm_mlp* mlp, const float* d_in, const float* d_target, int64_t n,
                          float* d_loss, void* stream);
@@ -211,6 +216,7 @@ typedef struct hm_scene_desc {
   float scene_scale;
   float bounds_min[3], bounds_max[3];
   int n_bvh_wide_nodes; /* 4-wide nodes traversed by the kernels (0 before the build) */
+  int n_groups;         /* strand groups with their own material (0: one material) */
 } hm_scene_desc;
 
 enum hm_scene_array {
@@ -229,9 +235,12 @@ enum hm_scene_array {
   HM_SCENE_BVH_LEAVES = 12,    /* int32 primitive of each leaf slot */
   HM_SCENE_CAMERA = 13,        /* pos, dir_00, dir_du, dir_dv (12 floats) */
   HM_SCENE_MATERIALS = 14,     /* 16 floats: hair params, diffuse, alpha, env scale/rotation */
-  HM_SCENE_BVH_WIDE_NODES = 15 /* 128 bytes each: lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
-                                  child[4] (>= 0 wide node, < 0 leaf ~slot) + 16 bytes of padding;
-                                  empty slots hold the box [+inf, +inf] */
+  HM_SCENE_BVH_WIDE_NODES = 15, /* 128 bytes each: lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
+                                   child[4] (>= 0 wide node, < 0 leaf ~slot) + 16 bytes of padding;
+                                   empty slots hold the box [+inf, +inf] */
+  HM_SCENE_STRAND_GROUPS = 16,   /* int32 group of each strand (empty: one material) */
+  HM_SCENE_GROUP_MATERIALS = 17, /* hm_hair_params of each group */
+  HM_SCENE_SEGMENT_GROUPS = 18   /* int32 group of each segment (empty: one material) */
 };
 
 /* Host-only: parses and generates (no device work). */
@@ -244,6 +253,17 @@ int hm_scene_info(const hm_scene* scene, hm_scene_desc* out);
 /* Host copy of one scene array (bytes: hm_scene_export_size). */
 int64_t hm_scene_export_size(const hm_scene* scene, int which);
 int hm_scene_export(const hm_scene* scene, int which, void* host_out, int64_t capacity_bytes);
+/* Strand groups (no reference counterpart: the reference has one hair
+ * material per scene, copied into every hit by hairCH, optix_common.cuh
+ * :585-593).  Every strand gets a group in [0, n_groups), n_groups <= 64,
+ * and every group its own material; a new grouping starts with every group
+ * at the scene's material.  The scene JSON can give the same with
+ * hair.groups = {count, assign: "azimuth" | "index", materials: [...]}.
+ * hm_scene_set_group_materials replaces the groups' materials (n_groups = 1
+ * on an ungrouped scene replaces the scene's material); it waits for the
+ * device, so frames in flight finish with the old materials. */
+int hm_scene_set_strand_groups(hm_scene* scene, const int32_t* strand_group, int n_strands, int n_groups);
+int hm_scene_set_group_materials(hm_scene* scene, const hm_hair_params* materials, int n_groups);
 
 /* Closest-hit (any_hit = 0) or any-hit traversal of n rays: d_org, d_dir
  * [n][3]; d_hits [n][4] = (t, primitive id as int bits (-1 miss), u, v):
@@ -365,6 +385,37 @@ hm_mlp* hm_render_cache(hm_render* render);
 /* Device buffers of the last frame: 0 cache inputs [P][12], 1 cache outputs
  * [P][3], 2 training inputs [R][12], 3 training targets [R][3], 4 G-buffer. */
 int hm_render_buffer(hm_render* render, int which, void** dptr, int64_t* count);
+
+/* ------------------------------------------------------------------------
+ * Differentiable rendering by path replay (no reference counterpart; the
+ * differentiable appearance-fit configuration).  Single-scene renderers.
+ *
+ * hm_render_diff_forward restarts accumulation and enqueues `frames` frames
+ * (one sample per pixel each) with the cache frozen: no training pixels and
+ * no training step, so in HairMSNN mode every hair pixel is its short path
+ * plus the cache at the primary hit.  The image is then
+ * hm_render_read(HM_IMAGE_FINAL), the mean of the frames.  Each path's
+ * radiance is kept (16 bytes per path and frame) for the replay.
+ *   eval_materials (may be NULL): a detached render for finite differences:
+ *   the hair BSDF values come from these materials (one per strand group),
+ *   while directions, pdfs, MIS weights and Russian roulette keep the
+ *   scene's; such a forward cannot be replayed.
+ *
+ * hm_render_diff_backward replays the paths of the last forward with the
+ * same random numbers and returns dL/d(material) for d_adjoint = dL/dImage
+ * ([H][W][3] FP32 on the device, the layout of hm_render_read):
+ * host_grad[g * 6 + k] (FP64), k = sigma_a r, g, b, beta_m, beta_n, alpha
+ * (radians), for every strand group g (one group on an ungrouped scene);
+ * n_grad >= 6 * groups.  The sampling is detached (the sampled directions,
+ * pdfs and MIS weights are held fixed; Path Replay Backpropagation, Vicini
+ * et al. 2021): the result is the exact derivative of the detached render
+ * and an unbiased estimate of the derivative of the expected image.  In
+ * HairMSNN mode the cache network's parameter gradients
+ * (hm_mlp_get_gradients on hm_render_cache) receive dL/d(weights).
+ * Synchronises. */
+int hm_render_diff_forward(hm_render* render, int frames, const hm_hair_params* eval_materials, int n_materials,
+                           void* stream);
+int hm_render_diff_backward(hm_render* render, const float* d_adjoint, double* host_grad, int n_grad, void* stream);
 
 #ifdef __cplusplus
 }

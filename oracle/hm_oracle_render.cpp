@@ -46,6 +46,10 @@ struct OScene {
   V3 cam_pos, cam_d00, cam_du, cam_dv;
   float hp[10];
   HairShading hs;
+  // strand groups: group of every segment and the groups' materials (empty:
+  // every segment uses hs)
+  std::vector<int> seg_group;
+  std::vector<HairShading> ghs;
   V3 diffuse;
   float alpha;  // clamp(alpha,.01,1)^2
   float env_scale = 1.f, env_rot = 0.f;
@@ -378,7 +382,10 @@ struct SI {
   V3 Le, p, wo, wi, wo_local, wi_local, n, t;
   V3 to_local[3], to_world[3];
   float radius = 0.f;
+  int group = 0;  // strand group of a hair hit
 };
+
+const HairShading& hair_of(const OScene& s, const SI& si) { return s.ghs.empty() ? s.hs : s.ghs[si.group]; }
 
 float tex_nearest(const std::vector<float>& t, int w, int h, float u, float v) {
   int x = std::min(std::max((int)floorf(u * (float)w), 0), w - 1);
@@ -493,6 +500,7 @@ void trace_radiance(const OScene& s, V3 o, V3 d, SI& si) {
     return;
   }
   if (h.prim < s.n_seg()) {  // hairCH
+    si.group = s.seg_group.empty() ? 0 : s.seg_group[h.prim];
     const float* q = &s.cp[4 * s.seg[h.prim]];
     V4 cps[4];
     for (int i = 0; i < 4; ++i) cps[i] = V4(q[4 * i], q[4 * i + 1], q[4 * i + 2], q[4 * i + 3]);
@@ -537,7 +545,7 @@ void trace_radiance(const OScene& s, V3 o, V3 d, SI& si) {
 bool visible(const OScene& s, V3 o, V3 d) { return trace(s, o, d, 0.f, 1e30f, true).prim < 0; }
 
 V3 hair_f(const OScene& s, const SI& si, float* pdf) {
-  return disney_hair(si.wo_local, si.wi_local, dot(si.to_local[1], si.n), s.hs, pdf);
+  return disney_hair(si.wo_local, si.wi_local, dot(si.to_local[1], si.n), hair_of(s, si), pdf);
 }
 
 V3 sample_lights(const OScene& s, SI& si, uint32_t& rng, bool& is_delta) {  // sampleLights
@@ -593,7 +601,7 @@ V3 sample_bsdf(const OScene& s, SI& si, uint32_t& rng) {  // sampleBSDF
     r[2] = lcg_randomf(rng);
     r[3] = lcg_randomf(rng);
     V3 wil;
-    bsdf = sample_disney_hair(si.wo_local, dot(si.to_local[1], si.n), r, s.hs, &wil, &bsdf_pdf, nullptr);
+    bsdf = sample_disney_hair(si.wo_local, dot(si.to_local[1], si.n), r, hair_of(s, si), &wil, &bsdf_pdf, nullptr);
     si.wi_local = wil;
     si.wi = normalize(apply_mat(si.to_world, si.wi_local));
   } else {
@@ -646,7 +654,7 @@ V3 next_vertex(const OScene& s, SI& si, uint32_t& rng) {  // msnnNextPathVertex 
     r[2] = lcg_randomf(rng);
     r[3] = lcg_randomf(rng);
     V3 wil;
-    next_bsdf = sample_disney_hair(si.wo_local, dot(si.to_local[1], si.n), r, s.hs, &wil, &next_pdf, nullptr);
+    next_bsdf = sample_disney_hair(si.wo_local, dot(si.to_local[1], si.n), r, hair_of(s, si), &wil, &next_pdf, nullptr);
     si.wi_local = wil;
     si.wi = normalize(apply_mat(si.to_world, si.wi_local));
   } else {
@@ -792,6 +800,14 @@ void* hmo_scene_new(const float* cp, int n_cp, const int* seg, int n_seg, const 
 }
 
 void hmo_scene_free(void* h) { delete (OScene*)h; }
+
+// Strand groups: group of every segment, each group's 10 material floats.
+void hmo_scene_set_groups(void* h, const int* seg_group, int n_seg, const float* mats10, int n_groups) {
+  OScene* s = (OScene*)h;
+  s->seg_group.assign(seg_group, seg_group + n_seg);
+  s->ghs.clear();
+  for (int g = 0; g < n_groups; ++g) s->ghs.push_back(setup_hair_shading(mats10 + 10 * g));
+}
 
 int hmo_bvh_sizes(void* h, int* n_nodes, int* n_leaves) {
   OScene* s = (OScene*)h;

@@ -121,6 +121,8 @@ def _declare_render(L):
     L.hmo_trace_rays.argtypes = [vp, F32P, F32P, i32, f32, f32, i32, F32P]
     L.hmo_render_pixels.restype = None
     L.hmo_render_pixels.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, F32P, F32P, F32P, I32P, i32]
+    L.hmo_scene_set_groups.restype = None
+    L.hmo_scene_set_groups.argtypes = [vp, I32P, i32, F32P, i32]
     L._render_declared = True
 
 
@@ -159,7 +161,17 @@ class OracleScene:
         settings = dict(width=i.width, height=i.height, path_v1=i.path_v1, path_v2=i.path_v2, mis=i.mis,
                         env_pdf=i.env_pdf, has_env=i.has_env, catrom=i.shading_catrom, env_w=i.env_width,
                         env_h=i.env_height)
-        return cls(arrays, settings, i.scene_scale)
+        o = cls(arrays, settings, i.scene_scale)
+        if i.n_groups > 0:
+            o.set_groups(scene.export("segment_groups"), scene.export("group_materials"))
+        return o
+
+    def set_groups(self, seg_group, materials):
+        """Strand groups: group of every segment, [n_groups, 10] materials."""
+        sg = np.ascontiguousarray(seg_group, np.int32)
+        m = f32(np.asarray(materials).reshape(-1, 10))
+        self._keep["groups"] = (sg, m)
+        lib().hmo_scene_set_groups(self.h, sg, len(sg), m.ravel(), len(m))
 
     def __del__(self):
         try:

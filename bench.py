@@ -364,6 +364,9 @@ def make_workload(name, torch):
     if name == "batch":
         from hairmsnn_gb300 import render as _r
         return _r.BatchBenchWorkload(torch)
+    if name == "diff":
+        from hairmsnn_gb300 import render as _r
+        return _r.DiffBenchWorkload(torch)
     if name == "quality":
         from hairmsnn_gb300 import render as _r
         return _r.RenderQualityWorkload(torch)
@@ -452,7 +455,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "render"),
-                    choices=["render", "vertex", "precision", "quality", "batch"])
+                    choices=["render", "vertex", "precision", "quality", "batch", "diff"])
+    ap.add_argument("--fit-steps", type=int, default=200,
+                    help="diff workload: Adam steps of the sigma_a recovery reported after the timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -539,6 +544,12 @@ def main():
                     "h2d_bytes_per_step": wl.h2d_bytes, "d2h_bytes_per_step": wl.d2h_bytes},
             "gpu_launches": launches,
             "roofline": roof, "clocks": clocks}
+    if hasattr(wl, "paths_per_step"):
+        line["paths_per_s"] = round(wl.paths_per_step() * ws / (ms * 1e-3), 1)
+    if hasattr(wl, "fit") and args.fit_steps > 0:
+        err = wl.fit(args.fit_steps)
+        line["fit"] = {"adam_steps": args.fit_steps, "sigma_a_rel_error_max": round(float(err.max()), 5),
+                       "sigma_a_rel_error_mean": round(float(err.mean()), 5), "start": "sigma_a x 0.5 or 1.5"}
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = wl.cpu_baseline(host_threads())
     print(json.dumps(line), flush=True)

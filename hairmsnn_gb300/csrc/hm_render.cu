@@ -1259,7 +1259,7 @@ static int diff_forward(Render* r, int frames, const hm_hair_params* eval, int n
   r->diff_detached = eval != nullptr;
   r->diff_fwd = true;
   int st = HM_OK;
-  for (int f = 0; f < frames && st == HM_OK; ++f) st = render_frame(r, user, false);
+  for (int f = 0; f < frames && st == HM_OK; ++f) st = render_frame(r, user, r->timing || r->counting);
   r->diff_fwd = false;
   if (st == HM_OK) r->diff_frames = frames;
   return st;
@@ -1448,6 +1448,9 @@ extern "C" int hm_render_buffer(hm_render* h, int which, void** dptr, int64_t* c
     case 2: *dptr = fb.nn_train_in; if (count) *count = (int64_t)r->n_train * r->in_ch; break;
     case 3: *dptr = fb.nn_train_out; if (count) *count = (int64_t)r->n_train * 3; break;
     case 4: *dptr = fb.gbuf; if (count) *count = (int64_t)r->P; break;
+    case 5: *dptr = r->acc_final; if (count) *count = (int64_t)r->P * 3; break;
+    case 6: *dptr = r->acc_pt; if (count) *count = (int64_t)r->P * 3; break;
+    case 7: *dptr = r->acc_nn; if (count) *count = (int64_t)r->P * 3; break;
     default: return HM_EINVAL;
   }
   return HM_OK;

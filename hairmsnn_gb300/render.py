@@ -311,6 +311,20 @@ class Renderer:
         from .mlp import TinyMLP
         return TinyMLP.wrap(lib().hm_render_cache(self._h))
 
+    def device_sums(self, which=5):
+        """Zero-copy torch view ([H, W, 3] float64, on the device) of the FP64
+        running sums: 5 final image, 6 short paths, 7 cache (divide by the
+        frame count; valid while the renderer lives)."""
+        import torch
+        p = ctypes.c_void_p()
+        n = ctypes.c_int64()
+        check(lib().hm_render_buffer(self._h, which, ctypes.byref(p), ctypes.byref(n)))
+
+        class _Dev:
+            __cuda_array_interface__ = {"shape": (self.height, self.width, 3), "typestr": "<f8",
+                                        "data": (p.value, False), "version": 2, "strides": None}
+        return torch.as_tensor(_Dev(), device="cuda")
+
     def buffer(self, which):
         """Host copy of a device buffer of the last frame (see hm_render_buffer):
         0 cache inputs [P,12], 1 cache outputs [P,3], 2 training inputs [R,12],
@@ -393,11 +407,12 @@ def straight_hair_scene(width=512, height=512, strands=10000, control_points=64,
 RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
 NODE_BYTES = 128              # one 4-wide BVH node: four child boxes + child codes
 PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
-# DRAM bytes per extension ray of the extension traversal kernel, from ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum) over every launch of two
-# 256x256 frames of this scene: 395.3 MB for about 2 x 137k rays.  ncu runs
-# each launch with cold caches, so this is an upper bound for warm frames.
-EXTEND_DRAM_BYTES_PER_RAY = 1440
+# DRAM bytes per extension ray of the extension traversal kernel (4-wide
+# BVH), from ncu (dram__bytes_read.sum + dram__bytes_write.sum) of the first
+# launch of a 256x256 frame of this scene: 28.0 MB for its 65,536 camera
+# rays.  ncu runs each launch with cold caches, so this is an upper bound
+# for warm frames.
+EXTEND_DRAM_BYTES_PER_RAY = 427
 
 
 class RenderBenchWorkload:
@@ -758,3 +773,233 @@ def _default_cache_config():
             {"n_dims_to_encode": 6, "otype": "OneBlob", "n_bins": 4}, {"otype": "Identity"}]},
         "network": {"otype": "FullyFusedMLP", "activation": "ReLU", "output_activation": "None",
                     "n_neurons": 64, "n_hidden_layers": 2}}
+
+
+# ----------------------------------------------------- differentiable rendering
+def diff_materials(n, seed=0):
+    """Seeded strand-group materials [n, 10]: sigma_a U[0.08, 0.5]^3,
+    beta_m U[0.6, 0.75] (every lobe's M_p on its direct branch), beta_n
+    U[0.3, 0.6], alpha U[1, 4] degrees (in radians), gains 1."""
+    rng = np.random.default_rng(seed)
+    m = np.zeros((n, 10), np.float32)
+    m[:, 0:3] = rng.uniform(0.08, 0.5, (n, 3))
+    m[:, 3] = rng.uniform(0.6, 0.75, n)
+    m[:, 4] = rng.uniform(0.3, 0.6, n)
+    m[:, 5] = np.deg2rad(rng.uniform(1.0, 4.0, n))
+    m[:, 6:10] = 1.0
+    return m
+
+
+def curly_hair_diff_scene(width=256, height=256, strands=20000, control_points=96, groups=4, seed=7):
+    """The differentiable-fit workload's scene: 20k curly strands (helix
+    radius 5 mm, pitch 10 mm, 96 B-spline control points, 20 cm), head,
+    sky + directional light, split by root azimuth into `groups` strand
+    groups with seeded materials.  Returns (config, materials)."""
+    cfg = straight_hair_scene(width, height, strands=strands, control_points=control_points, seed=seed)
+    p = cfg["hair"]["procedural"]
+    p["type"] = "curly"
+    p["helix_radius"] = 0.05
+    p["helix_pitch"] = 0.1
+    mats = diff_materials(groups, seed)
+    cfg["hair"]["groups"] = {"count": groups, "assign": "azimuth", "materials": [
+        {"sigma_a": [float(x) for x in r[0:3]], "beta_m": float(r[3]), "beta_n": float(r[4]),
+         "alpha": float(np.rad2deg(r[5]))} for r in mats]}
+    return cfg, mats
+
+
+class DiffBenchWorkload:
+    """bench.py workload: one gradient evaluation per step of the
+    differentiable appearance fit.  A step renders 64 frames (1 spp each) of
+    20k curly strands at 256x256, HairMSNN with BETA=2 and the cache frozen
+    (hm_render_diff_forward), forms the L2 image loss against a target
+    rendered at the true materials, and replays the paths
+    (hm_render_diff_backward) for dL/d(sigma_a, beta_m, beta_n, alpha) of 4
+    strand groups and dL/dW of the cache.  The target is rendered once with
+    the same frame seeds; the materials start with sigma_a 50% off."""
+
+    name = "diff"
+    metric = ("gradient evaluations/s (path replay: dL/d(material) of 4 strand groups + dL/dW, 20k curly strands, "
+              "256x256, 64 spp, BETA=2)")
+    unit = "gradient evaluations/s"
+
+    def __init__(self, torch, width=256, height=256, spp=64, strands=20000, groups=4, pretrain_passes=64):
+        self.torch = torch
+        self.width, self.height, self.spp, self.groups = width, height, spp, groups
+        self.cfg, self.truth = curly_hair_diff_scene(width, height, strands=strands, groups=groups)
+        self.scene = Scene(self.cfg)
+        self.scene.build()
+        self.scene.set_group_materials(self.truth)
+        self.r = Renderer(self.scene, MSNN, beta=2, train_records=1 << 14, train=True)
+        self.tuning = self.r.autotune(frames=4)
+        self.r.pretrain(pretrain_passes)
+        self.P = width * height
+        self.n = self.P * 3
+        self.r.diff_forward(spp)
+        self.target = (self.r.device_sums(5) / spp).clone()
+        self.target_host = self.target.cpu().numpy()
+        self.start = self.truth.copy()
+        self.start[:, 0:3] *= np.where(np.random.default_rng(11).random((groups, 3)) < 0.5, 0.5, 1.5)
+        self.scene.set_group_materials(self.start)
+        self.h2d_bytes = self.P * 3 * 4
+        self.d2h_bytes = self.P * 3 * 8 + groups * 6 * 8
+        self.launches = []
+        self.adj_host = torch.empty((height, width, 3), dtype=torch.float32, pin_memory=True)
+        self.adj_dev = torch.empty((height, width, 3), dtype=torch.float32, device="cuda")
+
+    def gradient(self):
+        """One gradient evaluation on the device: forward, adjoint, replay."""
+        self.r.diff_forward(self.spp)
+        img = self.r.device_sums(5) / self.spp
+        adj = ((2.0 / self.n) * (img - self.target)).float()
+        return self.r.diff_backward(adj)
+
+    def step(self, events=None):
+        self.last_grad = self.gradient()
+
+    def timed_region(self, steps, flush):
+        """CUDA events on the submitting stream around `steps` evaluations;
+        every evaluation streams 64 frames of path state (about 20 MB per
+        frame at 256x256, several in flight) and 4.2M cache queries through
+        the backward, far past the 129 MB L2: no flush kernel."""
+        torch = self.torch
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(steps):
+            self.step()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / steps
+
+    def e2e_region(self, steps):
+        """Through the public API with host buffers: forward, image read to the
+        host (FP64), adjoint on the host, copied in from pinned memory,
+        replay returning the gradients to the host."""
+        import time
+        torch = self.torch
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            self.r.diff_forward(self.spp)
+            img = self.r.read()
+            self.adj_host.numpy()[...] = (2.0 / self.n) * (img - self.target_host)
+            self.adj_dev.copy_(self.adj_host, non_blocking=True)
+            self.last_grad = self.r.diff_backward(self.adj_dev)
+        torch.cuda.synchronize()
+        return 1e3 * (time.perf_counter() - t0) / steps
+
+    @property
+    def kernels_per_step(self):
+        # forward frames (bounce loop, cache inference, compose) + replay frames
+        # (bounce loop, cache adjoint, two gradient sums) + group duals, total,
+        # cache forward + backward
+        rounds = 3  # BETA + 1 vertices at BETA = 2
+        md = self.r.cache().info()
+        # cache forward (encode, layers) + backward (fused dgrad, loss sum,
+        # per-layer weight-gradient partials and reduction, hash-grid scatter
+        # and conversion)
+        mlp = 2 + 2 + 2 * (md.n_hidden_layers + 1) + 2
+        fwd = 1 + 7 * rounds + 1 + 2 + 1
+        rep = 1 + 7 * rounds + 3
+        return self.spp * (fwd + rep) + 2 + mlp
+
+    def units_per_step(self):
+        return 1
+
+    def paths_per_step(self):
+        return 2 * self.P * self.spp
+
+    def fit(self, steps=200, lr=0.05):
+        """Adam on log(sigma_a) of every group from the +-50% start; returns
+        the final relative error per component (the other materials fixed)."""
+        torch = self.torch
+        x = torch.tensor(np.log(self.start[:, 0:3].astype(np.float64)), requires_grad=True)
+        opt = torch.optim.Adam([x], lr=lr)
+        for _ in range(steps):
+            m = self.truth.copy()
+            m[:, 0:3] = np.exp(x.detach().numpy())
+            self.scene.set_group_materials(m)
+            g = self.gradient()
+            opt.zero_grad()
+            x.grad = torch.from_numpy(g[:, 0:3] * m[:, 0:3])
+            opt.step()
+        self.scene.set_group_materials(self.start)
+        got = np.exp(x.detach().numpy())
+        return np.abs(got - self.truth[:, 0:3]) / self.truth[:, 0:3]
+
+    def roofline(self, seg_ms, pk):
+        """Traversal of the forward frames (instrumented, one frame at a time)
+        and the split of an evaluation into forward, replay and cache backward."""
+        torch = self.torch
+        self.r.instrument(timing=True, counting=False)
+        self.r.diff_forward(4)
+        t = self.r.timings().as_dict()
+        self.r.instrument(timing=True, counting=True)
+        self.r.diff_forward(1)
+        c = self.r.timings()
+        self.r.instrument(timing=False, counting=False)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        ev[0].record()
+        self.r.diff_forward(self.spp)
+        ev[1].record()
+        img = self.r.device_sums(5) / self.spp
+        self.r.diff_backward(((2.0 / self.n) * (img - self.target)).float())
+        ev[2].record()
+        torch.cuda.synchronize()
+        dominant = "extend_ms" if t["extend_ms"] >= t["shadow_ms"] else "shadow_ms"
+        if dominant == "extend_ms":
+            rays, nodes, prims = c.extension_rays, c.extend_nodes, c.extend_prims
+        else:
+            rays, nodes, prims = c.shadow_rays, c.shadow_nodes, c.shadow_prims
+        alg = rays * RAY_RECORD_BYTES + nodes * NODE_BYTES + prims * PRIM_BYTES
+        ach = alg / (t[dominant] * 1e-3) / 1e9
+        return {"kernel": dominant.replace("_ms", "_kernel") + " (forward frames)", "bound": "hbm",
+                "achieved": round(ach, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(ach / pk["hbm_gbs"], 4), "traffic": None,
+                "evaluation_split_ms": {"forward_64_frames": round(ev[0].elapsed_time(ev[1]), 3),
+                                        "replay_and_cache_backward": round(ev[1].elapsed_time(ev[2]), 3)},
+                "stage_ms_per_forward_frame": {k: round(t[k], 4) for k in ("extend_ms", "shade_ms", "shadow_ms",
+                                                                           "compact_ms", "infer_ms")},
+                "rays_per_forward_frame": {"extension": int(c.extension_rays), "shadow": int(c.shadow_rays)},
+                "algorithmic_bytes_per_frame": int(alg),
+                "note": ("algorithmic bytes = rays x 48 B + 4-wide BVH nodes visited x 128 B + primitives tested "
+                         "x 64 B, counted in an untimed forward frame; the replay re-traces the same rays. "
+                         "Peak " + pk["source"])}
+
+    def config(self):
+        return {"workload": "diff: 20k curly procedural strands x 96 B-spline CPs (helix r 5 mm, pitch 10 mm), "
+                            "20k-tri head, sky + directional light, 256x256, 64 spp per evaluation, HairMSNN BETA=2, "
+                            "cache FP32 (frozen, 64 scene-sample training passes), 4 azimuthal strand groups; "
+                            "L2 image loss against a target at the true materials (same frame seeds)",
+                "pixels": self.P, "spp": self.spp, "groups": self.groups,
+                "paths_per_evaluation": self.paths_per_step(),
+                "l2": "inputs larger than L2: 64 frames of path state and 4.2M cache queries per evaluation",
+                "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
+                "parallelism": "replicas"}
+
+    def cpu_baseline(self, threads, budget_s=20.0):
+        """The reference has no gradient path.  Baseline: central finite
+        differences on the host, the way to differentiate it as it is: one
+        gradient of 4 groups x 6 parameters = 49 forward renders of 256x256 x
+        64 spp, each timed as the oracle's reference-structured integrator
+        (rayGenCam / msnnPathTrace G-buffer pass) on a bounded pixel sample."""
+        import time
+        from oracle import pyoracle as po
+        o = po.OracleScene.from_library(self.scene)
+        n = 4096
+        t0 = time.perf_counter()
+        done = 0
+        p0 = (self.height // 2) * self.width
+        while True:
+            o.render_pixels(1, beta=2, accum_id=done // self.P, every_nth=self.P, n_train=0, p0=p0, n=n,
+                            threads=threads)
+            done += n
+            p0 = (p0 + n) % (self.P - n)
+            if time.perf_counter() - t0 > budget_s:
+                break
+        rate = done / (time.perf_counter() - t0)
+        renders = 2 * self.groups * 6 + 1
+        value = rate / (self.P * self.spp * renders)
+        return {"value": value, "unit": self.unit, "cores": threads, "kind": "port",
+                "sample": f"{done} pixels (1 spp) of the oracle's forward integrator on {threads} threads "
+                          f"({rate:.0f} paths/s); a finite-difference gradient = {renders} renders of "
+                          f"{self.P} pixels x {self.spp} spp; cache not included"}

@@ -383,7 +383,9 @@ int hm_render_get_timings(const hm_render* render, hm_render_timings* out);
 /* The render's cache network (owned by the render; NULL in PT mode). */
 hm_mlp* hm_render_cache(hm_render* render);
 /* Device buffers of the last frame: 0 cache inputs [P][12], 1 cache outputs
- * [P][3], 2 training inputs [R][12], 3 training targets [R][3], 4 G-buffer. */
+ * [P][3], 2 training inputs [R][12], 3 training targets [R][3], 4 G-buffer;
+ * and the FP64 running sums [P][3] of the frames accumulated so far (divide
+ * by the frame count): 5 final image, 6 short paths, 7 cache. */
 int hm_render_buffer(hm_render* render, int which, void** dptr, int64_t* count);
 
 /* ------------------------------------------------------------------------

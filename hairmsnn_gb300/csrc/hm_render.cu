@@ -403,6 +403,11 @@ struct Slot {
   cudaStream_t st = nullptr;
   cudaEvent_t done = nullptr;
   bool in_flight = false;
+  // the frame's path tracing (camera + bounce rounds) as a CUDA graph,
+  // replayed every frame of this slot; the frame number comes from d_frame
+  int* d_frame = nullptr;
+  cudaGraphExec_t trace_exec = nullptr;
+  int64_t trace_key[10] = {};
   // path replay (allocated by the first differentiable forward)
   float* gacc = nullptr;       // [groups * 6][P]
   int gacc_rows = 0;
@@ -421,6 +426,7 @@ struct Render {
   int every_nth = 1;
   int in_ch = 12;
   bool train = true;
+  bool graphs = true;  // replay each slot's path tracing as a CUDA graph
   uint32_t seed = 0;
   hm_mlp* mlp = nullptr;
   // batch of scenes (hm_render_create_batch): the frame's paths are the
@@ -477,6 +483,7 @@ struct Render {
       if (s.done) cudaEventDestroy(s.done);
       if (s.h_err) cudaFreeHost(s.h_err);
       for (void* p : {(void*)s.gacc, (void*)s.stash, (void*)s.partial, (void*)s.ps.beta_d}) cudaFree(p);
+      if (s.trace_exec) cudaGraphExecDestroy(s.trace_exec);
     }
     for (void* p : allocs) cudaFree(p);
     if (d_samples) cudaFree(d_samples);
@@ -536,6 +543,7 @@ static cudaError_t slot_alloc(Render* r, Slot& sl) {
   if (e == cudaSuccess) e = r->alloc(&sl.fetch, r->fetch_slots);
   if (e == cudaSuccess) e = r->alloc(&sl.vis, (size_t)P * 2);
   if (e == cudaSuccess) e = r->alloc(&sl.d_loss, 1);
+  if (e == cudaSuccess) e = r->alloc(&sl.d_frame, 1);
   if (e == cudaSuccess) e = cudaMallocHost(&sl.h_err, sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
@@ -689,6 +697,8 @@ static int bounce_rounds(const Render* r, const FrameParams& fp) {
   return full;
 }
 
+__global__ void set_frame_kernel(int* d_frame, int v) { *d_frame = v; }
+
 // Enqueues one frame.  sync_bounces: read the queue length after every
 // bounce (instrumented frames: per-stage events, early exit); otherwise the
 // whole frame is enqueued without a host round trip.
@@ -709,10 +719,6 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     fp.eval_hc = r->diff_detached ? r->diff_eval : nullptr;
     fb.col_out = r->diff_col + (size_t)r->accum_id * r->P;
   }
-  int* q_cur = sl.q_a;
-  int* q_next = sl.q_b;
-  int* c_cur = sl.counts;
-  int* c_next = sl.counts + 1;
   // instrumentation: event pairs per stage (timing) / work counters (counting)
   size_t ne = 0;
   int cur_bounce = -1;
@@ -728,49 +734,92 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   enum { S_CAMERA, S_EXTEND, S_SHADE, S_SHADOW, S_COMPACT, S_FINALIZE, S_TRAIN, S_INFER, S_COMPOSE, S_END };
   const bool counting = r->counting && sync_bounces;
   if (counting) cudaMemsetAsync(r->d_cnt, 0, 8 * sizeof(unsigned long long), st);
-  cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
-  mark(S_CAMERA);
-  if (int e = launch_camera(sd, fp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
   const int grid = r->sm_count * r->shade_blocks_per_sm;
   const int nblocks = (r->P + kScanBlock - 1) / kScanBlock;
   int count = r->P;
   int bounces = 0;
   int64_t ext_rays = 0;
   const int rounds = bounce_rounds(r, fp);
-  for (int it = 0; it < rounds && count > 0; ++it) {
-    cur_bounce = it;
-    paths_at.push_back(count);
-    mark(S_EXTEND);
-    if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, r->batch, 0.f, 1e30f,
-                                                     sl.fetch + 2 * it, sl.err, r->d_cnt, counting,
-                                                     r->blocks_extend, st))
-      return e;
-    mark(S_SHADE);
-    if (int e = launch_shade(sd, fp, r->batch, sl.ps, fb, q_cur, c_cur, sl.keep, grid, st)) return e;
-    mark(S_SHADOW);
-    if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, r->batch, 0.f, 1e30f,
-                                                    sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, counting,
-                                                    r->blocks_shadow, st))
-      return e;
-    shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{});
-    HM_CHECK_LAUNCH("shadow_resolve_kernel");
-    mark(S_COMPACT);
-    scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
-                                                                                  nblocks);
-    scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
-    scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, q_cur, c_cur, sl.block_sums,
-                                                                              q_next, nblocks);
-    HM_CHECK_LAUNCH("compaction");
-    if (sync_bounces) {
-      ext_rays += count;
-      cudaError_t e = cudaMemcpyAsync(r->h_count, c_next, sizeof(int), cudaMemcpyDeviceToHost, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) return hm_cuda_status(e, "bounce count");
-      count = *r->h_count;
+  FrameBufs fb_trace = fb;
+  fb_trace.col_out = nullptr;  // finalize's; keeps the traced launches identical across frames
+  // camera + bounce rounds (extend -> shade -> shadow -> resolve -> compact)
+  auto trace = [&](const FrameParams& tfp) -> int {
+    int* q_cur = sl.q_a;
+    int* q_next = sl.q_b;
+    int* c_cur = sl.counts;
+    int* c_next = sl.counts + 1;
+    cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
+    mark(S_CAMERA);
+    if (int e = launch_camera(sd, tfp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
+    bounces = 0;
+    for (int it = 0; it < rounds && count > 0; ++it) {
+      cur_bounce = it;
+      paths_at.push_back(count);
+      mark(S_EXTEND);
+      if (int e = launch_persistent<ExtendRays, false>(ExtendRays{sl.ps, q_cur, c_cur}, sd, r->batch, 0.f, 1e30f,
+                                                       sl.fetch + 2 * it, sl.err, r->d_cnt, counting,
+                                                       r->blocks_extend, st))
+        return e;
+      mark(S_SHADE);
+      if (int e = launch_shade(sd, tfp, r->batch, sl.ps, fb_trace, q_cur, c_cur, sl.keep, grid, st)) return e;
+      mark(S_SHADOW);
+      if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, r->batch, 0.f,
+                                                      1e30f, sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, counting,
+                                                      r->blocks_shadow, st))
+        return e;
+      shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{});
+      HM_CHECK_LAUNCH("shadow_resolve_kernel");
+      mark(S_COMPACT);
+      scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
+                                                                                    nblocks);
+      scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
+      scatter_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, q_cur, c_cur,
+                                                                                sl.block_sums, q_next, nblocks);
+      HM_CHECK_LAUNCH("compaction");
+      if (sync_bounces) {
+        ext_rays += count;
+        cudaError_t e = cudaMemcpyAsync(r->h_count, c_next, sizeof(int), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return hm_cuda_status(e, "bounce count");
+        count = *r->h_count;
+      }
+      std::swap(q_cur, q_next);
+      std::swap(c_cur, c_next);
+      ++bounces;
     }
-    std::swap(q_cur, q_next);
-    std::swap(c_cur, c_next);
-    ++bounces;
+    return HM_OK;
+  };
+  if (r->graphs && !sync_bounces) {
+    // the same launches as a graph per slot, captured once and replayed;
+    // the camera kernel reads the frame number from the slot's d_frame
+    set_frame_kernel<<<1, 1, 0, st>>>(sl.d_frame, r->accum_id);
+    HM_CHECK_LAUNCH("set_frame_kernel");
+    FrameParams tfp = fp;
+    tfp.d_frame = sl.d_frame;
+    const int64_t key[10] = {rounds, r->blocks_extend, r->blocks_shadow, grid, s->material_version, tfp.no_train,
+                             (int64_t)(uintptr_t)tfp.eval_hc, (int64_t)(uintptr_t)sl.ps.beta_d, r->mode, 1};
+    if (!sl.trace_exec || memcmp(key, sl.trace_key, sizeof(key)) != 0) {
+      if (sl.trace_exec) cudaGraphExecDestroy(sl.trace_exec);
+      sl.trace_exec = nullptr;
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed);
+      if (e != cudaSuccess) return hm_cuda_status(e, "trace graph capture");
+      const int te = trace(tfp);
+      e = cudaStreamEndCapture(st, &g);
+      if (te != HM_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return te != HM_OK ? te : hm_cuda_status(e, "trace graph capture");
+      }
+      e = cudaGraphInstantiate(&sl.trace_exec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return hm_cuda_status(e, "trace graph instantiate");
+      memcpy(sl.trace_key, key, sizeof(key));
+    }
+    cudaError_t e = cudaGraphLaunch(sl.trace_exec, st);
+    if (e != cudaSuccess) return hm_cuda_status(e, "trace graph launch");
+    bounces = rounds;
+  } else {
+    if (int e = trace(fp)) return e;
   }
   r->rays_extend += ext_rays;
   r->last_bounces = bounces;
@@ -1055,6 +1104,14 @@ extern "C" int hm_render_autotune(hm_render* h, int frames, void* stream, hm_ren
   Render* r = (Render*)h;
   if (!r || frames < 1) return hm_set_error("hm_render_autotune: bad arguments"), HM_EINVAL;
   return render_autotune(r, frames, (cudaStream_t)stream, out);
+}
+
+extern "C" int hm_render_set_graphs(hm_render* h, int on) {
+  Render* r = (Render*)h;
+  if (!r) return hm_set_error("hm_render_set_graphs: NULL"), HM_EINVAL;
+  if (int e = render_sync(r)) return e;
+  r->graphs = on != 0;
+  return HM_OK;
 }
 
 extern "C" int hm_render_frames_in_flight(const hm_render* h) {

@@ -58,6 +58,8 @@ struct FrameParams {
   // roulette keep the scene's materials
   int no_train;
   const HairConsts* eval_hc;
+  // frames replayed from a CUDA graph read the frame number (accum_id) here
+  const int* d_frame;
 };
 
 // Path replay (Vicini et al. 2021, "Path Replay Backpropagation"): a frame

@@ -51,12 +51,13 @@ __global__ void __launch_bounds__(256) camera_kernel(const __grid_constant__ Sce
   const PathCtx c = path_ctx<MULTI>(s0, fp, b, pid);
   const SceneDev& s = *c.s;
   const int x = c.local % s.width, y = c.local / s.width;
-  uint32_t rng = rng_seed(fp.frame_seed, (uint32_t)c.local);
+  const int accum_id = fp.d_frame ? *fp.d_frame : fp.accum_id;
+  uint32_t rng = rng_seed(fp.d_frame ? accum_id + 10007 : fp.frame_seed, (uint32_t)c.local);
   uint32_t flags = 0;
   if (fp.mode == MODE_MSNN && !fp.no_train) {
     const int tr = c.local / c.every_nth;
     if (tr < c.n_train) {
-      const uint32_t pick = feistel_perm((uint32_t)tr, (uint32_t)c.n_train, (uint32_t)fp.accum_id) % c.every_nth;
+      const uint32_t pick = feistel_perm((uint32_t)tr, (uint32_t)c.n_train, (uint32_t)accum_id) % c.every_nth;
       if ((uint32_t)(c.local % c.every_nth) == pick) flags |= F_TRAIN;
     }
   }

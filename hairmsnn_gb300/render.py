@@ -115,6 +115,7 @@ def _declare():
     L.hm_scene_set_strand_groups.argtypes = [vp, P(i32), i32, i32]
     L.hm_scene_set_group_materials.argtypes = [vp, vp, i32]
     L.hm_render_diff_forward.argtypes = [vp, i32, vp, i32, vp]
+    L.hm_render_set_graphs.argtypes = [vp, i32]
     L.hm_render_diff_backward.argtypes = [vp, vp, P(ctypes.c_double), i32, vp]
     _declared = True
 
@@ -248,6 +249,11 @@ class Renderer:
     def pretrain(self, passes, stream=None):
         """Scene-sample training of the cache (see hm_render_pretrain)."""
         check(lib().hm_render_pretrain(self._h, int(passes), _stream(stream)))
+
+    def set_graphs(self, on=True):
+        """Replay each frame's path tracing as a CUDA graph (default) or launch
+        its kernels one by one (see hm_render_set_graphs)."""
+        check(lib().hm_render_set_graphs(self._h, 1 if on else 0))
 
     def depth(self):
         """Frames in flight (hm_render_options.frames_in_flight as resolved)."""

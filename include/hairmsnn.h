@@ -351,6 +351,14 @@ typedef struct hm_render_tuning {
   float ms_per_frame; /* best time per frame seen while tuning */
 } hm_render_tuning;
 int hm_render_autotune(hm_render* render, int frames, void* stream, hm_render_tuning* out);
+/* Launch mode (no reference counterpart).  on (the default): each frame's
+ * path tracing (camera and every bounce round: extend, shade, shadow,
+ * resolve, compact) is one CUDA graph per frame slot, captured on first use
+ * and replayed every frame with the frame number read from device memory;
+ * recaptured when launch shapes or materials change.  off: the same kernels
+ * launched one by one.  Images are bit-identical either way; instrumented
+ * frames always launch one by one. */
+int hm_render_set_graphs(hm_render* render, int on);
 /* Frames the renderer keeps in flight (the resolved frames_in_flight). */
 int hm_render_frames_in_flight(const hm_render* render);
 /* Makes `stream` wait for every frame in flight (no host synchronisation). */

@@ -161,14 +161,18 @@ def test_online_training_reduces_cache_loss(R):
 
 @pytest.mark.parametrize("mode", ["pt", "msnn"])
 def test_pipelined_frames_match_serial_frames_bitwise(R, mode):
-    """Frames in flight on separate streams (1, 3, 5 slots; with and without
-    per-bounce synchronisation) give the same accumulated images bit for bit."""
+    """Frames in flight on separate streams (1, 3, 5 slots; path tracing
+    replayed from per-slot CUDA graphs or launched kernel by kernel; with and
+    without per-bounce synchronisation) give the same accumulated images bit
+    for bit."""
     cfg = small_cfg(R, 800, 64)
     m = R.PT if mode == "pt" else R.MSNN
     results = []
-    for depth, sync in ((1, False), (3, False), (5, False), (3, True)):
+    for depth, sync, graphs in ((1, False, True), (3, False, True), (5, False, True), (3, False, False),
+                                (3, True, True)):
         s = R.Scene(cfg)
         r = R.Renderer(s, m, beta=2, train_records=1024, train=True, seed=5, frames_in_flight=depth)
+        r.set_graphs(graphs)
         if sync:
             r.instrument(timing=True)
         for _ in range(7):

@@ -1,7 +1,7 @@
 """Command line: the reference's `render_hair_msnn [scene.json] [BETA]`
 (render_hair_msnn.cu:1146-1175) without the viewer.
 
-  python -m hairmsnn_gb300 render [scene.json] [BETA] [--frames N] [--mode msnn|pt]
+  python -m hairmsnn_gb300 render [scene.json] [BETA] [--frames N] [--mode msnn|pt|nrc]
                                   [--width W --height H] [--out image.pfm] [--stats out.json]
 
   python -m hairmsnn_gb300 infer [--config c1_cache_w64.json] [--precision fp16]
@@ -122,7 +122,8 @@ def main(argv=None):
     r.add_argument("scene", nargs="?", default=None)
     r.add_argument("beta", nargs="?", type=int, default=1)
     r.add_argument("--frames", type=int, default=None, help="default: integrator.spp")
-    r.add_argument("--mode", choices=["msnn", "pt"], default="msnn")
+    r.add_argument("--mode", choices=["msnn", "pt", "nrc"], default="msnn",
+                   help="nrc: the reference's neural-radiance-caching comparison renderer (render_nrc.cu)")
     r.add_argument("--width", type=int, default=None)
     r.add_argument("--height", type=int, default=None)
     r.add_argument("--strands", type=int, default=None, help="built-in scene only")
@@ -152,8 +153,10 @@ def main(argv=None):
     if a.height:
         cfg.setdefault("integrator", {})["height"] = a.height
     scene = render.Scene(cfg, base)
-    rd = render.Renderer(scene, render.MSNN if a.mode == "msnn" else render.PT, beta=a.beta,
-                         train_records=a.train_records, train=cfg.get("tcnn", {}).get("init_train", True))
+    mode = {"msnn": render.MSNN, "pt": render.PT, "nrc": render.NRC}[a.mode]
+    records = a.train_records if (a.mode != "nrc" or a.train_records != 16384) else 65536
+    rd = render.Renderer(scene, mode, beta=a.beta, train_records=records,
+                         train=cfg.get("tcnn", {}).get("init_train", True))
     rd.instrument(timing=True)
     frames = a.frames if a.frames is not None else scene.info().spp
     log = []

@@ -32,6 +32,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3"
 PER_FILE_FLAGS = {
     "hm_bsdf.cu": ["-fmad=false"],
     "hm_shade.cu": ["-fmad=false"],
+    "hm_nrc.cu": ["-fmad=false"],
 }
 
 

@@ -26,6 +26,13 @@ int launch_shade(const SceneDev& s, const FrameParams& fp, const Batch& b, const
 int launch_group_dual(const SceneDev& s, void* out, int n, cudaStream_t st);
 size_t group_dual_bytes();
 int launch_replay_cache_grad(int P, const PathState& ps, const DiffParams& dp, float* dy, cudaStream_t st);
+int launch_nrc_camera(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
+                      const NrcBufs& nb, int* queue, int* count, cudaStream_t st);
+int launch_nrc_shade(const SceneDev& s, const FrameParams& fp, const PathState& ps, const FrameBufs& fb,
+                     const NrcBufs& nb, const int* queue, const int* count, int* keep, int grid, cudaStream_t st);
+int launch_nrc_finalize(int P, const PathState& ps, const FrameBufs& fb, float4* col_out, cudaStream_t st);
+int launch_nrc_compose(int P, int n_pix, const FrameParams& fp, const FrameBufs& fb, const NrcBufs& nb,
+                       cudaStream_t st);
 int launch_finalize(const SceneDev& s, const FrameParams& fp, const Batch& b, const PathState& ps,
                     const FrameBufs& fb, cudaStream_t st);
 int launch_compose(int P, const FrameParams& fp, const FrameBufs& fb, cudaStream_t st);
@@ -205,10 +212,14 @@ static int persistent_blocks() {
 // the path radiance.  Explicitly rounded operations: no contraction.
 // REPLAY: the stashed gradient terms of the visible samples join the path's
 // gradient sums (none when the sum was a NaN and was dropped).
+// rec_idx / rec (NRC frames, else NULL): the visible sum is also the
+// vertex's direct light in the training pixel's train buffer.
 template <bool REPLAY>
 __global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const int* __restrict__ queue,
                                                              const int* __restrict__ count,
-                                                             const uint8_t* __restrict__ vis, DiffParams dp) {
+                                                             const uint8_t* __restrict__ vis, DiffParams dp,
+                                                             const int* __restrict__ rec_idx = nullptr,
+                                                             float4* __restrict__ rec = nullptr) {
   const int n = *count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int pid = queue[i];
@@ -233,6 +244,10 @@ __global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const
       sx = sy = sz = 0.f;
       use0 = use1 = false;
     }
+    if (rec_idx) {
+      const int ri = rec_idx[pid];
+      if (ri >= 0) rec[(size_t)ri * kNrcRecordF4 + 3] = make_float4(sx, sy, sz, 0.f);
+    }
     if constexpr (REPLAY) {
       if (use0 || use1) {
         const size_t P = (size_t)dp.P;
@@ -251,7 +266,7 @@ __global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const
     c.y = __fadd_rn(c.y, __fmul_rn(w.y, sy));
     c.z = __fadd_rn(c.z, __fmul_rn(w.z, sz));
     ps.col[pid] = c;
-    if (flags & F_TRAIN) {
+    if ((flags & F_TRAIN) && !rec_idx) {
       const float4 ws = ps.dl_ws[pid];
       float4 cs = ps.col_s[pid];
       cs.x = __fadd_rn(cs.x, __fmul_rn(ws.x, sx));
@@ -408,6 +423,7 @@ struct Slot {
   int* d_frame = nullptr;
   cudaGraphExec_t trace_exec = nullptr;
   int64_t trace_key[10] = {};
+  NrcBufs nrc{};  // NRC renderers
   // path replay (allocated by the first differentiable forward)
   float* gacc = nullptr;       // [groups * 6][P]
   int gacc_rows = 0;
@@ -422,9 +438,12 @@ struct Render {
   int mode = MODE_MSNN;
   int beta_knob = 1;
   int accum_id = 0;
-  int n_train = 16384;
+  int n_train = 16384;  // training records per frame (NRC: training pixels)
   int every_nth = 1;
   int in_ch = 12;
+  int nn_rows = 0;        // cache queries per frame (NRC: pixels + training suffixes)
+  int nrc_records = 0;    // NRC: training records per frame (numTrainingRecords)
+  float nrc_c = 0.01f;
   bool train = true;
   bool graphs = true;  // replay each slot's path tracing as a CUDA graph
   uint32_t seed = 0;
@@ -554,14 +573,31 @@ static cudaError_t slot_alloc(Render* r, Slot& sl) {
   sl.fb.acc_pt = r->acc_pt;
   sl.fb.acc_nn = r->acc_nn;
   sl.fb.acc_final = r->acc_final;
-  if (r->mode == MODE_MSNN) {
-    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_frame_in, (size_t)P * r->in_ch);
-    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_frame_out, (size_t)P * 3);
-    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_train_in, (size_t)r->n_train * r->in_ch);
-    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_train_out, (size_t)r->n_train * 3);
+  if (r->mode == MODE_MSNN || r->mode == MODE_NRC) {
+    const int64_t recs = r->mode == MODE_NRC ? r->nrc_records : r->n_train;
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_frame_in, (size_t)r->nn_rows * r->in_ch);
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_frame_out, (size_t)r->nn_rows * 3);
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_train_in, (size_t)recs * r->in_ch);
+    if (e == cudaSuccess) e = r->alloc(&sl.fb.nn_train_out, (size_t)recs * 3);
     if (e != cudaSuccess) return e;
-    cudaMemset(sl.fb.nn_train_in, 0, (size_t)r->n_train * r->in_ch * sizeof(float));
-    cudaMemset(sl.fb.nn_train_out, 0, (size_t)r->n_train * 3 * sizeof(float));
+    cudaMemset(sl.fb.nn_frame_in, 0, (size_t)r->nn_rows * r->in_ch * sizeof(float));
+    cudaMemset(sl.fb.nn_train_in, 0, (size_t)recs * r->in_ch * sizeof(float));
+    cudaMemset(sl.fb.nn_train_out, 0, (size_t)recs * 3 * sizeof(float));
+  }
+  if (r->mode == MODE_NRC) {
+    NrcBufs& nb = sl.nrc;
+    const int R = r->n_train;
+    if (e == cudaSuccess) e = r->alloc(&nb.prev, (size_t)P);
+    if (e == cudaSuccess) e = r->alloc(&nb.spread, (size_t)P);
+    if (e == cudaSuccess) e = r->alloc(&nb.gbeta, (size_t)P);
+    if (e == cudaSuccess) e = r->alloc(&nb.dl_rec, (size_t)P);
+    if (e == cudaSuccess) e = r->alloc(&nb.rec, (size_t)R * kNrcMaxBounces * kNrcRecordF4);
+    if (e == cudaSuccess) e = r->alloc(&nb.tinfo, (size_t)R);
+    if (e != cudaSuccess) return e;
+    cudaMemset(nb.rec, 0, (size_t)R * kNrcMaxBounces * kNrcRecordF4 * sizeof(float4));
+    cudaMemset(nb.tinfo, 0, (size_t)R * sizeof(int4));
+    nb.c = r->nrc_c;
+    nb.all_unbiased = 0;
   }
   return e;
 }
@@ -599,14 +635,28 @@ static int render_setup(Render* r, const hm_render_options* o) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
-  r->fetch_slots = 2 * (r->max_path_v2 + 2);
+  r->fetch_slots = 2 * (std::max(r->max_path_v2, kNrcMaxBounces) + 2);
   r->blocks_extend = r->blocks_extend_max = persistent_blocks<ExtendRays, false>();
   r->blocks_shadow = r->blocks_shadow_max = persistent_blocks<ShadowRays, true>();
+  r->nn_rows = P;
   if (r->mode == MODE_MSNN) {
     r->n_train = o && o->train_records > 0 ? o->train_records : 16384;
     // everyNth = frameSize / numTrainRecords (integer division, render_hair_msnn.cu:106), at least 1
     r->every_nth = std::max(1, P / r->n_train);
     r->n_train = std::min(r->n_train, (P + r->every_nth - 1) / r->every_nth);
+  } else if (r->mode == MODE_NRC) {
+    // render_nrc.cu:124-146: numTrainingPixels = numTrainingRecords / MAX_BOUNCES,
+    // everyNth = frameSize / numTrainingPixels; the cache queries are the
+    // frame's pixels plus one per training suffix; cache inputs are 9
+    // channels (render_nrc.h:123)
+    r->nrc_records = o && o->train_records > 0 ? o->train_records : 65536;
+    r->n_train = std::max(1, r->nrc_records / kNrcMaxBounces);
+    r->every_nth = std::max(1, P / r->n_train);
+    r->n_train = std::min(r->n_train, (P + r->every_nth - 1) / r->every_nth);
+    r->nrc_records = std::max(r->nrc_records, r->n_train * kNrcMaxBounces);
+    r->in_ch = 9;
+    r->nn_rows = P + r->n_train;
+    if (o && o->nrc_c > 0.f) r->nrc_c = o->nrc_c;
   }
   if (!r->bscenes.empty()) {
     // one shared cache: every scene gives one training record per every_nth
@@ -652,7 +702,7 @@ static int render_setup(Render* r, const hm_render_options* o) {
     e = slot_alloc(r, sl);
     if (e != cudaSuccess) return hm_cuda_status(e, "render frame slot");
   }
-  if (r->mode == MODE_MSNN) {
+  if (r->mode == MODE_MSNN || r->mode == MODE_NRC) {
     std::string cfg = o && o->cache_config_json ? o->cache_config_json
                                                 : (s->cache_config.empty() ? kDefaultCacheConfig : s->cache_config);
     int st = 0;
@@ -691,6 +741,7 @@ static int render_sync(Render* r) {
 // without training pixels, the short paths' BETA + 1 vertices (at least 2):
 // vertex k > beta = BETA - 1 always ends the path.
 static int bounce_rounds(const Render* r, const FrameParams& fp) {
+  if (fp.mode == MODE_NRC) return kNrcMaxBounces;  // the 40th vertex ends every path
   const int full = r->max_path_v2 + 1;
   if (fp.mode == MODE_MSNN && fp.no_train && r->bscenes.empty())
     return std::min(full, std::max(2, r->beta_knob + 1));
@@ -750,7 +801,11 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     int* c_next = sl.counts + 1;
     cudaMemsetAsync(sl.fetch, 0, r->fetch_slots * sizeof(int), st);
     mark(S_CAMERA);
-    if (int e = launch_camera(sd, tfp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
+    if (tfp.mode == MODE_NRC) {
+      if (int e = launch_nrc_camera(sd, tfp, sl.ps, fb_trace, sl.nrc, q_cur, c_cur, st)) return e;
+    } else {
+      if (int e = launch_camera(sd, tfp, r->batch, sl.ps, q_cur, c_cur, st)) return e;
+    }
     bounces = 0;
     for (int it = 0; it < rounds && count > 0; ++it) {
       cur_bounce = it;
@@ -761,13 +816,19 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
                                                        r->blocks_extend, st))
         return e;
       mark(S_SHADE);
-      if (int e = launch_shade(sd, tfp, r->batch, sl.ps, fb_trace, q_cur, c_cur, sl.keep, grid, st)) return e;
+      if (tfp.mode == MODE_NRC) {
+        if (int e = launch_nrc_shade(sd, tfp, sl.ps, fb_trace, sl.nrc, q_cur, c_cur, sl.keep, grid, st)) return e;
+      } else {
+        if (int e = launch_shade(sd, tfp, r->batch, sl.ps, fb_trace, q_cur, c_cur, sl.keep, grid, st)) return e;
+      }
       mark(S_SHADOW);
       if (int e = launch_persistent<ShadowRays, true>(ShadowRays{sl.ps, q_cur, c_cur, sl.vis}, sd, r->batch, 0.f,
                                                       1e30f, sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, counting,
                                                       r->blocks_shadow, st))
         return e;
-      shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{});
+      shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{},
+                                                         tfp.mode == MODE_NRC ? sl.nrc.dl_rec : nullptr,
+                                                         sl.nrc.rec);
       HM_CHECK_LAUNCH("shadow_resolve_kernel");
       mark(S_COMPACT);
       scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
@@ -825,7 +886,32 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   r->last_bounces = bounces;
   cur_bounce = -1;
   int launches = 1 + 7 * bounces + 1;
-  if (r->mode == MODE_PT) {
+  if (r->mode == MODE_NRC) {
+    // G_BUFFER done; then inference, RENDER pass (compose + training data),
+    // training step (render_nrc.cu:651-681)
+    mark(S_FINALIZE);
+    if (int e = launch_nrc_finalize(r->P, sl.ps, fb, nullptr, st)) return e;
+    if (r->have_mlp_ev) cudaStreamWaitEvent(st, r->ev_mlp, 0);
+    mark(S_INFER);
+    if (int e = hm_mlp_inference(r->mlp, fb.nn_frame_in, fb.nn_frame_out, r->nn_rows, st)) return e;
+    if (r->have_compose_ev) cudaStreamWaitEvent(st, r->ev_compose, 0);
+    if (r->have_read_ev) cudaStreamWaitEvent(st, r->ev_read, 0);
+    mark(S_COMPOSE);
+    if (int e = launch_nrc_compose(r->P, r->n_train, fp, fb, sl.nrc, st)) return e;
+    cudaEventRecord(r->ev_compose, st);
+    r->have_compose_ev = true;
+    mark(S_TRAIN);
+    if (r->train) {
+      if (int e = hm_mlp_training_step(r->mlp, fb.nn_train_in, fb.nn_train_out, r->nrc_records, sl.d_loss, st))
+        return e;
+    }
+    cudaEventRecord(r->ev_mlp, st);
+    r->have_mlp_ev = true;
+    hm_mlp_desc md;
+    hm_mlp_info(r->mlp, &md);
+    const bool grid_enc = md.n_params > md.n_network_params;
+    launches += (r->train ? 4 + 2 * (md.n_hidden_layers + 1) + (grid_enc ? 2 : 0) + 1 : 0) + 2 + 2;
+  } else if (r->mode == MODE_PT) {
     // writePixel accumulates: frames in order, after any pending read-back
     if (r->have_compose_ev) cudaStreamWaitEvent(st, r->ev_compose, 0);
     if (r->have_read_ev) cudaStreamWaitEvent(st, r->ev_read, 0);
@@ -922,7 +1008,10 @@ static hm_render* render_create(Scene* first, const std::vector<Scene*>& batch, 
     if (msg) hm_set_error("%s", msg);
     return nullptr;
   };
-  if (r->mode != MODE_PT && r->mode != MODE_MSNN) return fail(HM_EINVAL, "hm_render_create: unknown mode");
+  if (r->mode != MODE_PT && r->mode != MODE_MSNN && r->mode != MODE_NRC)
+    return fail(HM_EINVAL, "hm_render_create: unknown mode");
+  if (r->mode == MODE_NRC && !batch.empty())
+    return fail(HM_EUNSUPPORTED, "hm_render_create_batch: NRC renders single scenes");
   // internal beta = BETA - 1 (render_hair_msnn.cu:1170); BETA = 0 stops the
   // short path at the first bounce
   if (r->beta_knob < 0) return fail(HM_EINVAL, "hm_render_create: BETA must be >= 0 (internal beta = BETA - 1)");
@@ -1004,8 +1093,8 @@ extern "C" int hm_render_read_async(hm_render* h, int which, double* host_dst, v
                       : which == HM_IMAGE_SHORT ? r->acc_pt
                       : which == HM_IMAGE_CACHE ? r->acc_nn : nullptr;
   if (!src) return hm_set_error("hm_render_read_async: unknown image %d", which), HM_EINVAL;
-  if (r->mode == MODE_PT && which != HM_IMAGE_FINAL)
-    return hm_set_error("hm_render_read_async: PT renders have only the final image"), HM_EINVAL;
+  if (r->mode != MODE_MSNN && which != HM_IMAGE_FINAL)
+    return hm_set_error("hm_render_read_async: PT and NRC renders have only the final image"), HM_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
   if (r->have_compose_ev) cudaStreamWaitEvent(s, r->ev_compose, 0);
   cudaError_t e = cudaMemcpyAsync(host_dst, src, (size_t)r->P * 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -1297,6 +1386,7 @@ static int diff_setup(Render* r, int frames, int groups) {
 
 static int diff_forward(Render* r, int frames, const hm_hair_params* eval, int n_eval, cudaStream_t user) {
   if (!r->bscenes.empty()) return hm_set_error("hm_render_diff_forward: single-scene renders only"), HM_EUNSUPPORTED;
+  if (r->mode == MODE_NRC) return hm_set_error("hm_render_diff_forward: HairMSNN and PT renders only"), HM_EUNSUPPORTED;
   if (frames < 1) return hm_set_error("hm_render_diff_forward: frames < 1"), HM_EINVAL;
   const int groups = r->scene->n_groups();
   if (eval && n_eval != groups)
@@ -1444,7 +1534,8 @@ extern "C" int hm_render_read(hm_render* h, int which, double* host_rgb) {
                       : which == HM_IMAGE_SHORT ? r->acc_pt
                       : which == HM_IMAGE_CACHE ? r->acc_nn : nullptr;
   if (!src) return hm_set_error("hm_render_read: unknown image %d", which), HM_EINVAL;
-  if (r->mode == MODE_PT && which != HM_IMAGE_FINAL) return hm_set_error("hm_render_read: PT renders have only the final image"), HM_EINVAL;
+  if (r->mode != MODE_MSNN && which != HM_IMAGE_FINAL)
+    return hm_set_error("hm_render_read: PT and NRC renders have only the final image"), HM_EINVAL;
   const size_t n = (size_t)r->P * 3;
   cudaError_t e = cudaMemcpy(host_rgb, src, n * sizeof(double), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_read");
@@ -1461,7 +1552,7 @@ extern "C" int hm_render_get_stats(const hm_render* h, hm_render_stats* out) {
   out->pixels = r->P;
   out->extension_rays = r->rays_extend;
   out->last_bounces = r->last_bounces;
-  out->train_records = r->mode == MODE_MSNN ? r->n_train : 0;
+  out->train_records = r->mode == MODE_MSNN ? r->n_train : (r->mode == MODE_NRC ? r->nrc_records : 0);
   out->every_nth = r->every_nth;
   float loss = 0.f;
   if (r->mlp && r->train && r->accum_id > 0)
@@ -1500,14 +1591,26 @@ extern "C" int hm_render_buffer(hm_render* h, int which, void** dptr, int64_t* c
   if (int st = render_sync(r)) return st;
   const FrameBufs& fb = r->slots[r->accum_id > 0 ? (r->accum_id - 1) % r->depth : 0].fb;
   switch (which) {
-    case 0: *dptr = fb.nn_frame_in; if (count) *count = (int64_t)r->P * r->in_ch; break;
-    case 1: *dptr = fb.nn_frame_out; if (count) *count = (int64_t)r->P * 3; break;
-    case 2: *dptr = fb.nn_train_in; if (count) *count = (int64_t)r->n_train * r->in_ch; break;
-    case 3: *dptr = fb.nn_train_out; if (count) *count = (int64_t)r->n_train * 3; break;
+    case 0: *dptr = fb.nn_frame_in; if (count) *count = (int64_t)r->nn_rows * r->in_ch; break;
+    case 1: *dptr = fb.nn_frame_out; if (count) *count = (int64_t)r->nn_rows * 3; break;
+    case 2: *dptr = fb.nn_train_in;
+      if (count) *count = (int64_t)(r->mode == MODE_NRC ? r->nrc_records : r->n_train) * r->in_ch;
+      break;
+    case 3: *dptr = fb.nn_train_out;
+      if (count) *count = (int64_t)(r->mode == MODE_NRC ? r->nrc_records : r->n_train) * 3;
+      break;
     case 4: *dptr = fb.gbuf; if (count) *count = (int64_t)r->P; break;
     case 5: *dptr = r->acc_final; if (count) *count = (int64_t)r->P * 3; break;
     case 6: *dptr = r->acc_pt; if (count) *count = (int64_t)r->P * 3; break;
     case 7: *dptr = r->acc_nn; if (count) *count = (int64_t)r->P * 3; break;
+    case 8: case 9: case 10: {
+      if (r->mode != MODE_NRC) return hm_set_error("hm_render_buffer: NRC buffers of a non-NRC renderer"), HM_EINVAL;
+      const NrcBufs& nb = r->slots[r->accum_id > 0 ? (r->accum_id - 1) % r->depth : 0].nrc;
+      if (which == 8) { *dptr = nb.gbeta; if (count) *count = (int64_t)r->P; }
+      if (which == 9) { *dptr = nb.rec; if (count) *count = (int64_t)r->n_train * kNrcMaxBounces * kNrcRecordF4; }
+      if (which == 10) { *dptr = nb.tinfo; if (count) *count = (int64_t)r->n_train; }
+      break;
+    }
     default: return HM_EINVAL;
   }
   return HM_OK;

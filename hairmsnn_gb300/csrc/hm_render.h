@@ -9,10 +9,30 @@ enum PathFlags : uint32_t {
   F_TRAIN = 1u,     // pixel produces a training record this frame
   F_DL = 2u,        // shadow rays of the current vertex are pending
   F_PRIM_HIT = 4u,  // primary ray hit something
-  F_PRIM_SURF = 8u  // ... and it was the head surface
+  F_PRIM_SURF = 8u, // ... and it was the head surface
+  // NRC (nrc.cu:136-310)
+  F_NRC_SUFFIX = 16u,    // a training pixel past its cache query (isTrainingSuffix)
+  F_NRC_UNBIASED = 32u,  // training pixel traced to the end (every 16th)
+  F_NRC_RECALC = 64u,    // a0 of the suffix is taken at the next vertex
+  F_NRC_NOSPREAD = 128u, // unbiased suffix past its cache query: no spread test (c = 1e30)
+  F_NRC_GSNAP = 256u     // the G-buffer was written when the path took the cache
 };
 
-enum RenderMode { MODE_PT = 0, MODE_MSNN = 1 };
+enum RenderMode { MODE_PT = 0, MODE_MSNN = 1, MODE_NRC = 2 };
+
+// NRC buffers of one frame slot.
+constexpr int kNrcMaxBounces = 40;  // MAX_BOUNCES (nrc.cuh:13)
+constexpr int kNrcRecordF4 = 5;     // per vertex: position / scale, wo, n, direct light, throughput factor
+struct NrcBufs {
+  float4* prev;    // [P] previous vertex and the pdf of the direction sampled there
+  float4* spread;  // [P] accumulated spread, a0
+  float4* gbeta;   // [P] throughput at the cache query (0: no query)
+  int* dl_rec;     // [P] train record of the pending direct light (-1: none)
+  float4* rec;     // [R][40][5] train buffer (TrainBuffer, nrc.cuh:29-40)
+  int4* tinfo;     // [R] bounces, suffix ended at a cache query, unbiased, primary hit
+  float c;         // spread threshold multiplier (render_nrc.h:132)
+  int all_unbiased;
+};
 
 // Structure-of-arrays path state, one slot per pixel (capacity W*H).
 struct PathState {

@@ -427,10 +427,11 @@ HM_D void direct_lighting(const SceneDev& s, const Vertex& v, uint32_t& rng, Sha
 // msnnNextPathVertex / nextPathVertex (hair_msnn.cu:18-65,
 // optix_common.cuh:311-360): sample, throughput factor, extension ray.
 // Detached renders (v.hc_eval != v.hc) also give the factor of the sampling
-// material in *mul_s; *wl receives the sampled direction in the vertex frame
-// and *mul_nan whether the factor was a NaN replaced by 1.
+// material in *mul_s; *wl receives the sampled direction in the vertex frame,
+// *mul_nan whether the factor was a NaN replaced by 1 and *pdf_out the pdf
+// of the sampled direction (nextPathVertexNRC's return value).
 HM_D f3 next_vertex(const SceneDev& s, const Vertex& v, uint32_t& rng, f3* ro, f3* rd, f3* mul_s = nullptr,
-                    f3* wl = nullptr, bool* mul_nan = nullptr) {
+                    f3* wl = nullptr, bool* mul_nan = nullptr, float* pdf_out = nullptr) {
   float r0 = lcg_next(rng), r1 = lcg_next(rng);
   float pdf = 1.f;
   f3 bsdf, wi_local, bsdf_s;
@@ -466,6 +467,7 @@ HM_D f3 next_vertex(const SceneDev& s, const Vertex& v, uint32_t& rng, f3* ro, f
   }
   if (wl) *wl = wi_local;
   if (mul_nan) *mul_nan = is_nan;
+  if (pdf_out) *pdf_out = pdf;
   *ro = p + 1e-3f * nd;
   *rd = wi;  // -si.wo
   return mul;

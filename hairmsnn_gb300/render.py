@@ -23,7 +23,7 @@ DTYPES = dict(control_points=(np.float32, 4), segments=(np.int32, 1), vertices=(
               dir_lights=(np.float32, 6), bvh_nodes=(np.float32, 16), bvh_leaves=(np.int32, 1),
               camera=(np.float32, 12), materials=(np.float32, 16), bvh_wide_nodes=(np.float32, 32),
               strand_groups=(np.int32, 1), group_materials=(np.float32, 10), segment_groups=(np.int32, 1))
-PT, MSNN = 0, 1
+PT, MSNN, NRC = 0, 1, 2
 IMAGE_FINAL, IMAGE_SHORT, IMAGE_CACHE = 0, 1, 2
 
 
@@ -39,7 +39,8 @@ class hm_scene_desc(ctypes.Structure):
 class hm_render_options(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int), ("beta", ctypes.c_int), ("train_records", ctypes.c_int),
                 ("train", ctypes.c_int), ("cache_precision", ctypes.c_int), ("seed", ctypes.c_uint32),
-                ("cache_config_json", ctypes.c_char_p), ("frames_in_flight", ctypes.c_int)]
+                ("cache_config_json", ctypes.c_char_p), ("frames_in_flight", ctypes.c_int),
+                ("nrc_c", ctypes.c_float)]
 
 
 class hm_render_tuning(ctypes.Structure):
@@ -211,11 +212,13 @@ class Renderer:
     """One frame() = one sample per pixel of HairMSNN (mode=MSNN) or plain PT."""
 
     def __init__(self, scene, mode=MSNN, beta=1, train_records=16384, train=True, precision=0, seed=0,
-                 cache_config=None, frames_in_flight=0):
+                 cache_config=None, frames_in_flight=0, nrc_c=0.0):
         _declare()
         self.scene = scene
+        if mode == NRC and train_records == 16384:
+            train_records = 65536  # the NRC renderer's numTrainingRecords
         o = hm_render_options(mode, beta, train_records, 1 if train else 0, precision, seed,
-                              cache_config.encode() if cache_config else None, frames_in_flight)
+                              cache_config.encode() if cache_config else None, frames_in_flight, nrc_c)
         st = ctypes.c_int(0)
         h = lib().hm_render_create(scene._h, ctypes.byref(o), ctypes.byref(st))
         if not h:
@@ -338,9 +341,10 @@ class Renderer:
         p = ctypes.c_void_p()
         n = ctypes.c_int64()
         check(lib().hm_render_buffer(self._h, which, ctypes.byref(p), ctypes.byref(n)))
-        width = {0: 12, 1: 3, 2: 12, 3: 3, 4: 4}[which]
-        count = n.value * (4 if which == 4 else 1)
-        host = np.zeros(count, np.float32)
+        in_ch = 9 if self.mode == NRC else 12
+        width = {0: in_ch, 1: 3, 2: in_ch, 3: 3, 4: 4, 8: 4, 9: 20, 10: 4}[which]
+        count = n.value * (4 if which in (4, 8, 9, 10) else 1)
+        host = np.zeros(count, np.int32 if which == 10 else np.float32)
         check(lib().hm_copy_to_host(host.ctypes.data_as(ctypes.c_void_p), p, count * 4))
         return host.reshape(-1, width)
 

@@ -285,19 +285,26 @@ int hm_trace_rays(const hm_scene* scene, const float* d_org, const float* d_dir,
  * ---------------------------------------------------------------------- */
 typedef struct hm_render hm_render;
 
-enum hm_render_mode { HM_MODE_PT = 0, HM_MODE_MSNN = 1 };
+/* HM_MODE_NRC: the reference's comparison renderer, neural radiance caching
+ * (RenderWindowNRC, render_nrc.cu:640-701, cuda/nrc.cu): each path stops
+ * where its spread passes c * a0 and takes the cache there; one pixel in
+ * every everyNth traces a training suffix and gives one record per vertex
+ * (train_records default 65536 = 1638 pixels x 40 vertices); the cache takes
+ * 9 inputs (position, wo, n).  Single scenes; the final image only. */
+enum hm_render_mode { HM_MODE_PT = 0, HM_MODE_MSNN = 1, HM_MODE_NRC = 2 };
 enum hm_image { HM_IMAGE_FINAL = 0, HM_IMAGE_SHORT = 1, HM_IMAGE_CACHE = 2 };
 
 typedef struct hm_render_options {
   int mode;                      /* hm_render_mode */
   int beta;                      /* BETA >= 0 (internal beta = BETA - 1) */
-  int train_records;             /* per frame; 0 = 16384 (render_hair_msnn.h:127-129) */
+  int train_records;             /* per frame; 0 = 16384 (render_hair_msnn.h:127-129), NRC 65536 */
   int train;                     /* online cache training on/off (tcnn.init_train) */
   int cache_precision;           /* HM_PREC_* */
   uint32_t seed;                 /* cache initialisation */
   const char* cache_config_json; /* NULL: the scene's tcnn.config, else the built-in one */
   int frames_in_flight;          /* frames pipelined on their own streams (1..8); 0: up to 6,
                                     fewer when their path state would pass ~2 GB */
+  float nrc_c;                   /* NRC spread threshold multiplier c (0: 0.01, render_nrc.h:132) */
 } hm_render_options;
 
 typedef struct hm_render_stats {
@@ -393,7 +400,12 @@ hm_mlp* hm_render_cache(hm_render* render);
 /* Device buffers of the last frame: 0 cache inputs [P][12], 1 cache outputs
  * [P][3], 2 training inputs [R][12], 3 training targets [R][3], 4 G-buffer;
  * and the FP64 running sums [P][3] of the frames accumulated so far (divide
- * by the frame count): 5 final image, 6 short paths, 7 cache. */
+ * by the frame count): 5 final image, 6 short paths, 7 cache.  NRC renders
+ * (9 input channels; rows [P, P + T) of 0/1 are the T training pixels'
+ * suffix queries): 8 throughput at each pixel's cache query (float4 [P]),
+ * 9 train buffer (float4 [T][40][5]: position / scale, wo, n, direct light,
+ * throughput factor), 10 per training pixel (int4: bounces, suffix ended at
+ * a query, unbiased, primary hit). */
 int hm_render_buffer(hm_render* render, int which, void** dptr, int64_t* count);
 
 /* ------------------------------------------------------------------------

@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <thread>
+#include <memory>
 #include <vector>
 
 #include "hm_oracle_math.h"
@@ -644,7 +645,7 @@ V3 direct_lighting(const OScene& s, SI si, uint32_t& rng) {  // directLighting
   return final_color;
 }
 
-V3 next_vertex(const OScene& s, SI& si, uint32_t& rng) {  // msnnNextPathVertex / nextPathVertex
+V3 next_vertex(const OScene& s, SI& si, uint32_t& rng, float* pdf_out = nullptr) {  // msnnNextPathVertex / nextPathVertex
   float r0 = lcg_randomf(rng);
   float r1 = lcg_randomf(rng);
   float next_pdf = 1.f;
@@ -672,8 +673,90 @@ V3 next_vertex(const OScene& s, SI& si, uint32_t& rng) {  // msnnNextPathVertex 
   }
   V3 mul = next_pdf == 0.f ? next_bsdf : next_bsdf / next_pdf;
   if (isnan(mul.x) || isnan(mul.y) || isnan(mul.z)) mul = V3(1.f);
+  if (pdf_out) *pdf_out = next_pdf;  // nextPathVertexNRC returns it (nrc.cu:17-66)
   trace_radiance(s, si.p + 1e-3f * nd, -si.wo, si);
   return mul;
+}
+
+// nrcTracePaths (cuda/nrc.cu:136-310) in the reference's loop, with
+// nrcSpread (utils.cuh:86-90).  Outputs of one pixel: the G-buffer
+// (radiance, beta), its cache query row, and for a training pixel the train
+// buffer (TrainBuffer, nrc.cuh:29-40) and the suffix's query row.
+constexpr int kNrcMaxBounces = 40;
+struct NrcOut {
+  V3 rad, beta;
+  float query[9];
+  float suffix_query[9];
+  float rec[kNrcMaxBounces][15];  // vert, wo, n, vertRadiance, vertBeta
+  int bounces = 0, thit = 0;
+};
+
+float nrc_spread(V3 x1, V3 x2, float abscos, float pdf) {
+  float l = length(x2 - x1);
+  return sqrtf(l * l / pdf / abscos);
+}
+
+void nrc_query_row(const OScene& s, const SI& si, float* row) {
+  V3 p = si.p / s.scene_scale;
+  float r[9] = {p.x, p.y, p.z, si.wo.x, si.wo.y, si.wo.z, si.n.x, si.n.y, si.n.z};
+  memcpy(row, r, sizeof(r));
+}
+
+void nrc_trace_paths(const OScene& s, SI si, uint32_t& rng, bool training, bool unbiased, float c, NrcOut& o) {
+  bool suffix = false, recalc = false;
+  float l0 = length(si.p - s.cam_pos);
+  float a0 = l0 * l0 / (4.f * 3.1415926f) / fabsf(si.wo_local.z);
+  V3 prev_point(0.f);
+  float spread = 0.f;
+  V3 final_color(0.f), beta(1.f);
+  for (int bounce = 0; bounce < kNrcMaxBounces; bounce++) {
+    V3 direct = direct_lighting(s, si, rng);
+    final_color = final_color + beta * direct;
+    V3 prev_wo = si.wo, prev_n = si.n;
+    prev_point = si.p;
+    float prev_pdf = 1.f;
+    V3 this_beta = next_vertex(s, si, rng, &prev_pdf);
+    beta = beta * this_beta;
+    if (training) {
+      if (recalc) {
+        float l = length(si.p - prev_point);
+        a0 = l * l / (4.f * 3.1415926f) / fabsf(si.wo_local.z);
+        recalc = false;
+      }
+      V3 q = prev_point / s.scene_scale;
+      float r[15] = {q.x, q.y, q.z, prev_wo.x, prev_wo.y, prev_wo.z, prev_n.x, prev_n.y, prev_n.z,
+                     direct.x, direct.y, direct.z, this_beta.x, this_beta.y, this_beta.z};
+      memcpy(o.rec[bounce], r, sizeof(r));
+    }
+    spread = spread + nrc_spread(si.p, prev_point, fabsf(si.wo_local.z), prev_pdf);
+    bool cond = spread * spread > c * a0;
+    if (!si.hit || bounce == kNrcMaxBounces - 1) {
+      if (!suffix) {
+        o.rad = final_color;
+        o.beta = V3(0.f);
+      }
+      o.bounces = bounce;
+      o.thit = 0;
+      break;
+    } else if (cond && !suffix) {
+      o.rad = final_color;
+      o.beta = beta;
+      nrc_query_row(s, si, o.query);
+      if (training) {
+        suffix = true;
+        recalc = true;
+        spread = 0.f;
+      } else {
+        break;
+      }
+    } else if (cond && suffix) {
+      nrc_query_row(s, si, o.suffix_query);
+      o.bounces = bounce;
+      o.thit = 1;
+      if (!unbiased) break;
+      c = 1e30f;
+    }
+  }
 }
 
 V3 msnn_path_trace(const OScene& s, SI si, uint32_t& rng, int v2_stop, int beta_int) {
@@ -800,6 +883,67 @@ void* hmo_scene_new(const float* cp, int n_cp, const int* seg, int n_seg, const 
 }
 
 void hmo_scene_free(void* h) { delete (OScene*)h; }
+
+// One frame of the NRC G_BUFFER pass (rayGenCam, nrc.cu:312-356) for pixels
+// [p0, p0 + np): gbuf [np][7] = radiance, beta, hit; query / suffix_query
+// [np][9]; records [np][40][15]; tinfo [np][4] = bounces, suffix ended at a
+// query, unbiased, training pixel.
+void hmo_render_nrc(void* h, int accum_id, int every_nth, int n_train, float c, int p0, int np, float* gbuf,
+                    float* query, float* suffix_query, float* records, int* tinfo, int threads) {
+  OScene* s = (OScene*)h;
+  auto work = [&](int b, int e) {
+    for (int pid = b; pid < e; ++pid) {
+      const int x = pid % s->width, y = pid / s->width;
+      uint32_t rng = get_rng(accum_id + 10007, (uint32_t)x, (uint32_t)y, (uint32_t)s->width, (uint32_t)s->height);
+      bool training = false;
+      const int tr = pid / every_nth;
+      if (tr < n_train) {
+        uint32_t pick = feistel_perm((uint32_t)tr, (uint32_t)n_train, (uint32_t)accum_id) % every_nth;
+        training = (uint32_t)(pid % every_nth) == pick;
+      }
+      const bool unbiased = training && tr % 16 == 0;
+      float ox = lcg_randomf(rng);
+      float oy = lcg_randomf(rng);
+      float su = ((float)x + ox) / (float)s->width, sv = ((float)y + oy) / (float)s->height;
+      V3 dir = normalize(s->cam_d00 + su * s->cam_du + sv * s->cam_dv);
+      SI si;
+      si.hit = false;
+      si.wo = -1.f * dir;
+      si.wi = dir;
+      trace_radiance(*s, s->cam_pos, dir, si);
+      std::unique_ptr<NrcOut> o(new NrcOut());
+      memset(o->query, 0, sizeof(o->query));
+      memset(o->suffix_query, 0, sizeof(o->suffix_query));
+      memset(o->rec, 0, sizeof(o->rec));
+      bool hit = si.hit && !(si.surface && si.wo_local.z < 0.f);
+      if (!hit) {
+        o->rad = si.hit ? V3(0.f) : si.Le;
+        o->beta = V3(0.f);
+      } else {
+        nrc_trace_paths(*s, si, rng, training, unbiased, c, *o);
+      }
+      const int i = pid - p0;
+      float g[7] = {o->rad.x, o->rad.y, o->rad.z, o->beta.x, o->beta.y, o->beta.z, hit ? 1.f : 0.f};
+      memcpy(gbuf + 7 * (size_t)i, g, sizeof(g));
+      memcpy(query + 9 * (size_t)i, o->query, sizeof(o->query));
+      memcpy(suffix_query + 9 * (size_t)i, o->suffix_query, sizeof(o->suffix_query));
+      memcpy(records + (size_t)i * kNrcMaxBounces * 15, o->rec, sizeof(o->rec));
+      int t[4] = {o->bounces, o->thit, unbiased ? 1 : 0, training ? 1 : 0};
+      memcpy(tinfo + 4 * (size_t)i, t, sizeof(t));
+    }
+  };
+  if (threads <= 1) {
+    work(p0, p0 + np);
+    return;
+  }
+  std::vector<std::thread> pool;
+  int chunk = (np + threads - 1) / threads;
+  for (int k = 0; k < threads; ++k) {
+    int b = p0 + k * chunk, e = std::min(p0 + np, b + chunk);
+    if (b < e) pool.emplace_back(work, b, e);
+  }
+  for (auto& t : pool) t.join();
+}
 
 // Strand groups: group of every segment, each group's 10 material floats.
 void hmo_scene_set_groups(void* h, const int* seg_group, int n_seg, const float* mats10, int n_groups) {

@@ -121,6 +121,8 @@ def _declare_render(L):
     L.hmo_trace_rays.argtypes = [vp, F32P, F32P, i32, f32, f32, i32, F32P]
     L.hmo_render_pixels.restype = None
     L.hmo_render_pixels.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, F32P, F32P, F32P, I32P, i32]
+    L.hmo_render_nrc.restype = None
+    L.hmo_render_nrc.argtypes = [vp, i32, i32, i32, f32, i32, i32, F32P, F32P, F32P, F32P, I32P, i32]
     L.hmo_scene_set_groups.restype = None
     L.hmo_scene_set_groups.argtypes = [vp, I32P, i32, F32P, i32]
     L._render_declared = True
@@ -204,6 +206,23 @@ class OracleScene:
         lib().hmo_render_pixels(self.h, mode, beta, accum_id, every_nth, n_train, p0, n, color, nn_in, train, flags,
                                 threads)
         return color, nn_in, train, flags
+
+
+def _render_nrc(self, accum_id=0, every_nth=1, n_train=0, c=0.01, p0=0, n=None, threads=8):
+    """One frame of the NRC G_BUFFER pass for pixels [p0, p0+n): dict of
+    gbuf [n,7] (radiance, beta, hit), query [n,9], suffix_query [n,9],
+    records [n,40,15] (vert, wo, n, direct light, factor), tinfo [n,4]
+    (bounces, suffix ended at a query, unbiased, training pixel)."""
+    n = self.width * self.height - p0 if n is None else n
+    out = dict(gbuf=np.zeros((n, 7), np.float32), query=np.zeros((n, 9), np.float32),
+               suffix_query=np.zeros((n, 9), np.float32), records=np.zeros((n, 40, 15), np.float32),
+               tinfo=np.zeros((n, 4), np.int32))
+    lib().hmo_render_nrc(self.h, accum_id, every_nth, n_train, c, p0, n, out["gbuf"], out["query"],
+                         out["suffix_query"], out["records"], out["tinfo"], threads)
+    return out
+
+
+OracleScene.render_nrc = _render_nrc
 
 
 def wide_collapse(nodes):

@@ -603,8 +603,9 @@ class RenderBenchWorkload:
 
 
 class RenderQualityWorkload(RenderBenchWorkload):
-    """HairMSNN (BETA=1, online cache training) against plain path tracing on
-    the render workload's scene: relMSE of each at 16 spp against a
+    """HairMSNN (BETA=1, online cache training) against plain path tracing and
+    the reference's NRC comparison renderer (online training, 65536 records
+    per frame) on the render workload's scene: relMSE of each at 16 spp against a
     converged PT reference of the same scene, their frame times, and the PT
     sample count (and time) needed to reach HairMSNN's relMSE, assuming PT's
     relMSE falls as 1/spp (it is unbiased).  The reference uses frames
@@ -666,6 +667,12 @@ class RenderQualityWorkload(RenderBenchWorkload):
         t_pre = self._timed_frames(ms, spp)
         e_pre = relmse(ms.read(IMAGE_FINAL), ref)
         ms.close()
+        # the reference's comparison renderer: NRC with online training
+        # (65536 records per frame, c = 0.01), same frames
+        nrc = Renderer(self.scene, NRC, train=True, frames_in_flight=self.frames_in_flight)
+        nrc_ms = self._timed_frames(nrc, spp)
+        e_nrc = relmse(nrc.read(IMAGE_FINAL), ref)
+        nrc.close()
         e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
         eq_spp = spp * e_pt / e_ms
         return {"spp": spp, "reference_spp": self.ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
@@ -673,6 +680,10 @@ class RenderQualityWorkload(RenderBenchWorkload):
                          "paths_per_s": round(self.P / (ms_ms * 1e-3), 1)},
                 "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
                        "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
+                "nrc": {"relmse": round(e_nrc, 6), "ms_per_frame": round(nrc_ms, 3),
+                        "paths_per_s": round(self.P / (nrc_ms * 1e-3), 1),
+                        "pt_spp_for_same_relmse": round(spp * e_pt / e_nrc, 2),
+                        "speedup_at_equal_relmse": round((spp * e_pt / e_nrc) * pt_ms / (spp * nrc_ms), 3)},
                 "msnn_by_cache_precision": by_prec,
                 "msnn_after_scene_sample_training": {
                     "passes": self.pretrain_passes, "training_ms": round(pre_ms, 1), "relmse": round(e_pre, 6),

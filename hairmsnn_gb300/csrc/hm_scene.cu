@@ -12,6 +12,7 @@
 #include <fstream>
 #include <sstream>
 
+#include "hm_exr.h"
 #include "hm_json.h"
 #include "hm_scene.h"
 
@@ -545,8 +546,21 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
       s->env_scale = (float)sk.number_or("scale", 1.0);
       s->env_rot_phi = (float)sk.number_or("rotation", 0.0);
     } else if (lights.has("environment")) {
-      hm_set_error("scene: EXR environment maps are not supported; use lights.sky");
-      return HM_EUNSUPPORTED;
+      // parseScene (scene.cpp:234-253): {"exr": path, "scale": s, "rotation": r}
+      const Json& ev = lights["environment"];
+      const std::string path = join_path(base, ev["exr"].as_string());
+      std::string data, err;
+      if (!read_file(path, &data)) {
+        hm_set_error("scene: cannot read environment map %s", path.c_str());
+        return HM_EINVAL;
+      }
+      if (int st = exr_load_rgba(data, &s->env, &s->env_w, &s->env_h, &err)) {
+        hm_set_error("scene: %s: %s", path.c_str(), err.c_str());
+        return st;
+      }
+      s->has_env = true;
+      s->env_scale = (float)ev["scale"].as_number();
+      s->env_rot_phi = (float)ev.number_or("rotation", 0.0);
     }
     if (lights["directional"].is_array()) {
       for (size_t i = 0; i < lights["directional"].size(); ++i) {

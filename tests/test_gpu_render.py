@@ -109,6 +109,28 @@ def test_pt_frame_matches_oracle_integrator(R):
     assert abs(img.mean() - col.mean()) <= 0.02 * col.mean()
 
 
+def test_pt_frame_with_exr_environment_matches_oracle(R, tmp_path):
+    """The same comparison with the sky replaced by an OpenEXR environment
+    map (ZIP-compressed, half floats) read from a file."""
+    from test_exr_env import write_exr
+    h, w = 64, 128
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    sky = {c: (0.4 + 0.6 * np.exp(-((x - 40 - 10 * i) ** 2 + (y - 20) ** 2) / 60.0) + 0.2 * (y < 32))
+           .astype(np.float32) for i, c in enumerate("RGB")}
+    write_exr(tmp_path / "env.exr", sky, "zip", half=True)
+    cfg = small_cfg(R, 1500, 64)
+    cfg["lights"] = {"environment": {"exr": "env.exr", "scale": 1.0, "rotation": 0.3}}
+    s = R.Scene(cfg, str(tmp_path))
+    assert s.info().env_width == w
+    r = R.Renderer(s, R.PT)
+    r.frame()
+    img = r.read(R.IMAGE_FINAL).reshape(-1, 3)
+    col, _, _, _ = po.OracleScene.from_library(s).render_pixels(0)
+    frac = frame_compare(img, col.astype(np.float64))
+    assert frac >= 0.95, frac
+    assert abs(img.mean() - col.mean()) <= 0.02 * col.mean()
+
+
 def test_msnn_gbuffer_matches_oracle_integrator(R):
     res = 64
     cfg = small_cfg(R, 1500, res)

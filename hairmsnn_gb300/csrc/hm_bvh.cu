@@ -33,13 +33,32 @@ struct Aabb {
   float lo[3], hi[3];
 };
 
+// One de Casteljau halving of a cubic Bezier (4 points x (x, y, z, r)):
+// the left (right = 0) or right half, explicitly rounded.
+HM_D void bezier_half(float w[4][4], int right) {
+  for (int k = 0; k < 4; ++k) {
+    const float m01 = __fmul_rn(__fadd_rn(w[0][k], w[1][k]), 0.5f);
+    const float m12 = __fmul_rn(__fadd_rn(w[1][k], w[2][k]), 0.5f);
+    const float m23 = __fmul_rn(__fadd_rn(w[2][k], w[3][k]), 0.5f);
+    const float m012 = __fmul_rn(__fadd_rn(m01, m12), 0.5f);
+    const float m123 = __fmul_rn(__fadd_rn(m12, m23), 0.5f);
+    const float m = __fmul_rn(__fadd_rn(m012, m123), 0.5f);
+    if (right) {
+      w[0][k] = m; w[1][k] = m123; w[2][k] = m23;
+    } else {
+      w[1][k] = m01; w[2][k] = m012; w[3][k] = m;
+    }
+  }
+}
+
 HM_D Aabb prim_aabb(const SceneDev& s, int p) {
   Aabb b;
-  if (p < s.n_seg) {
-    // hull of the segment's Bezier control points (the curve lies inside
-    // it), grown by their largest radius; the B-spline control polygon
-    // spans three segments and gave boxes about three times too long
-    const float4* c = s.cp + s.seg[p];
+  if (p < s.n_hprim) {
+    // hull of the Bezier control points of the segment's part (the curve
+    // lies inside it), grown by their largest radius; the B-spline control
+    // polygon spans three segments and gave boxes about three times too long
+    const int part = p / s.n_seg;
+    const float4* c = s.cp + s.seg[p - part * s.n_seg];
     float4 q[4] = {c[0], c[1], c[2], c[3]};
     float w[4][4];
     for (int k = 0; k < 4; ++k) {
@@ -49,13 +68,15 @@ HM_D Aabb prim_aabb(const SceneDev& s, int p) {
       w[2][k] = __fmul_rn(__fadd_rn(q1, __fmul_rn(2.f, q2)), 1.f / 3.f);
       w[3][k] = __fmul_rn(__fadd_rn(__fadd_rn(q1, __fmul_rn(4.f, q2)), q3), 1.f / 6.f);
     }
+    // part j of 2^L: halve L times, the bits of j from the top choosing the side
+    for (int bit = s.seg_split >> 1; bit > 0; bit >>= 1) bezier_half(w, part & bit);
     const float r = fmaxf(fmaxf(w[0][3], w[1][3]), fmaxf(w[2][3], w[3][3]));
     for (int k = 0; k < 3; ++k) {
       b.lo[k] = __fsub_rn(fminf(fminf(w[0][k], w[1][k]), fminf(w[2][k], w[3][k])), r);
       b.hi[k] = __fadd_rn(fmaxf(fmaxf(w[0][k], w[1][k]), fmaxf(w[2][k], w[3][k])), r);
     }
   } else {
-    int3 t = s.tri[p - s.n_seg];
+    int3 t = s.tri[p - s.n_hprim];
     float3 a = s.vtx[t.x], bb = s.vtx[t.y], c = s.vtx[t.z];
     b.lo[0] = fminf(fminf(a.x, bb.x), c.x);
     b.lo[1] = fminf(fminf(a.y, bb.y), c.y);

@@ -584,6 +584,12 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
     s->image_output = in.string_or("image_output", "");
     s->stats_output = in.string_or("stats_output", "");
     s->shading_catrom = in.bool_or("shade_catmull_rom", false) ? 1 : 0;
+    // BVH leaves per segment (no reference counterpart: OptiX builds its own
+    // curve hierarchy); 2 halves the curve tests per ray (measured 5.2 -> 3.5
+    // per extension ray, 10% faster frames) for twice the leaves
+    s->seg_split = (int)in.number_or("segment_splits", 2);
+    if (s->seg_split != 1 && s->seg_split != 2 && s->seg_split != 4)
+      throw JsonError("scene: integrator.segment_splits must be 1, 2 or 4");
     if (s->width <= 0 || s->height <= 0 || (int64_t)s->width * s->height > 2048 * 2048 ||
         ((int64_t)s->width * s->height) % 128 != 0)
       throw JsonError("scene: image size must be at most 2K x 2K and a multiple of 128 pixels");
@@ -708,6 +714,8 @@ SceneDev Scene::dev() const {
   d.cp = d_cp;
   d.seg = d_seg;
   d.n_seg = (int)seg.size();
+  d.seg_split = seg_split;
+  d.n_hprim = d.n_seg * seg_split;
   d.shading_catrom = shading_catrom;
   d.vtx = d_vtx;
   d.nrm = d_nrm;
@@ -817,6 +825,7 @@ extern "C" int hm_scene_info(const hm_scene* h, hm_scene_desc* out) {
   out->n_bvh_nodes = s->n_nodes;
   out->n_bvh_wide_nodes = s->n_wnodes;
   out->n_groups = s->group_mats.empty() ? 0 : (int)s->group_mats.size();
+  out->segment_splits = s->seg_split;
   out->width = s->width;
   out->height = s->height;
   out->spp = s->spp;

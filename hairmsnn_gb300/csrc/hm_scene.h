@@ -26,6 +26,10 @@ struct SceneDev {
   const float4* cp;
   const int* seg;  // first control point of each segment
   int n_seg;
+  // BVH leaves per segment: segment k's part j (its u range [j, j+1) / split)
+  // is leaf primitive k + j * n_seg; triangles follow at n_hprim
+  int seg_split;
+  int n_hprim;  // n_seg * seg_split
   int shading_catrom;  // 1: shade with the Catmull-Rom interpretation (reference CH quirk)
   // head mesh
   const float3* vtx;
@@ -100,6 +104,7 @@ struct Scene {
   int width = 512, height = 512, spp = 16, path_v1 = 1, path_v2 = 40;
   bool mis = true;
   int shading_catrom = 0;
+  int seg_split = 2;  // BVH leaves per hair segment (1, 2 or 4)
   f3 bmin{1e30f, 1e30f, 1e30f}, bmax{-1e30f, -1e30f, -1e30f};
   float scene_scale = 1.f;
   std::string cache_config;  // tcnn JSON text (scene "tcnn.config")
@@ -130,7 +135,7 @@ struct Scene {
   int upload();
   int build_bvh(cudaStream_t st);
   SceneDev dev() const;
-  int n_prims() const { return (int)seg.size() + (int)tri.size(); }
+  int n_prims() const { return (int)seg.size() * seg_split + (int)tri.size(); }
   int n_groups() const { return group_mats.empty() ? 1 : (int)group_mats.size(); }
   int set_strand_groups(const int* groups, int n, int n_groups);
   int set_group_materials(const hm_hair_params* m, int n);

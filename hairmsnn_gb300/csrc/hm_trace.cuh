@@ -78,7 +78,10 @@ HM_D P4 lerp4(P4 a, P4 b, float t) {
   return P4{a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t, a.r + (b.r - a.r) * t};
 }
 
-HM_D bool curve_intersect(const SceneDev& s, int seg_idx, const Ray& r, float tmax, float* t_out, float* u_out) {
+// Part `part` of segment seg_idx (u in [part, part + 1) / s.seg_split); *u_out
+// is the u of the whole segment.
+HM_D bool curve_intersect(const SceneDev& s, int seg_idx, int part, const Ray& r, float tmax, float* t_out,
+                          float* u_out) {
   const float4* q = s.cp + __ldg(s.seg + seg_idx);
   const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2), q3 = __ldg(q + 3);
   // B-spline -> Bezier
@@ -96,7 +99,19 @@ HM_D bool curve_intersect(const SceneDev& s, int seg_idx, const Ray& r, float tm
     f3 p = mk(w.x, w.y, w.z) - r.o;
     return P4{dot(p, ax), dot(p, ay), dot(p, r.d), w.w};
   };
-  const P4 b0 = rs(w0), b1 = rs(w1), b2 = rs(w2), b3 = rs(w3);
+  P4 b0 = rs(w0), b1 = rs(w1), b2 = rs(w2), b3 = rs(w3);
+  for (int bit = s.seg_split >> 1; bit > 0; bit >>= 1) {  // de Casteljau halvings down to the part
+    auto mid = [](P4 a, P4 b) {
+      return P4{(a.x + b.x) * 0.5f, (a.y + b.y) * 0.5f, (a.z + b.z) * 0.5f, (a.r + b.r) * 0.5f};
+    };
+    const P4 m01 = mid(b0, b1), m12 = mid(b1, b2), m23 = mid(b2, b3), m012 = mid(m01, m12), m123 = mid(m12, m23);
+    const P4 m = mid(m012, m123);
+    if (part & bit) {
+      b0 = m; b1 = m123; b2 = m23;
+    } else {
+      b1 = m01; b2 = m012; b3 = m;
+    }
+  }
   const float rmax = fmaxf(fmaxf(b0.r, b1.r), fmaxf(b2.r, b3.r));
   // ray-space bounding rectangle of the control polygon (+ radius) must hold the ray
   if (fminf(fminf(b0.x, b1.x), fminf(b2.x, b3.x)) - rmax > 0.f ||
@@ -146,17 +161,23 @@ HM_D bool curve_intersect(const SceneDev& s, int seg_idx, const Ray& r, float tm
   }
   if (found) {
     *t_out = best_t;
-    *u_out = best_u;
+    *u_out = ((float)part + best_u) * (1.f / (float)s.seg_split);
   }
   return found;
 }
 
-HM_D bool prim_intersect(const SceneDev& s, int prim, const Ray& r, float tmax, float* t, float* u, float* v) {
-  if (prim < s.n_seg) {
+// A leaf primitive; *id is what the hit reports: the segment (< n_seg) or
+// n_seg + the triangle.
+HM_D bool prim_intersect(const SceneDev& s, int prim, const Ray& r, float tmax, float* t, float* u, float* v,
+                         int* id) {
+  if (prim < s.n_hprim) {
     *v = 0.f;
-    return curve_intersect(s, prim, r, tmax, t, u);
+    const int part = prim / s.n_seg;
+    *id = prim - part * s.n_seg;
+    return curve_intersect(s, *id, part, r, tmax, t, u);
   }
-  return tri_intersect(s, prim - s.n_seg, r, tmax, t, u, v);
+  *id = s.n_seg + (prim - s.n_hprim);
+  return tri_intersect(s, prim - s.n_hprim, r, tmax, t, u, v);
 }
 
 // Work counters of a traversal (COUNT instantiations only).
@@ -306,8 +327,9 @@ HM_D bool trav_leaf(const SceneDev& s, TravState& t, TraceCount* cnt) {
   t.pend = -1;
   if (COUNT) cnt->prims += 1;
   float th, u, v;
-  if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v)) {
-    t.h = Hit{th, prim, u, v};
+  int id;
+  if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v, &id)) {
+    t.h = Hit{th, id, u, v};
     if (ANY_HIT) return true;
   }
   return false;

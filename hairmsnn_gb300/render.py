@@ -33,7 +33,7 @@ class hm_scene_desc(ctypes.Structure):
         "height", "spp", "path_v1", "path_v2", "env_width", "env_height", "n_dir_lights", "mis", "env_pdf",
         "has_env", "shading_catrom")] + [("scene_scale", ctypes.c_float), ("bounds_min", ctypes.c_float * 3),
                        ("bounds_max", ctypes.c_float * 3), ("n_bvh_wide_nodes", ctypes.c_int),
-                       ("n_groups", ctypes.c_int)]
+                       ("n_groups", ctypes.c_int), ("segment_splits", ctypes.c_int)]
 
 
 class hm_render_options(ctypes.Structure):

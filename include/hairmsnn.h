@@ -217,6 +217,9 @@ typedef struct hm_scene_desc {
   float bounds_min[3], bounds_max[3];
   int n_bvh_wide_nodes; /* 4-wide nodes traversed by the kernels (0 before the build) */
   int n_groups;         /* strand groups with their own material (0: one material) */
+  int segment_splits;   /* BVH leaves per hair segment (integrator.segment_splits: 1, 2 (default), 4);
+                           HM_SCENE_BVH_LEAVES ids: segment k's part j is k + j * n_segments,
+                           triangle i is n_segments * segment_splits + i */
 } hm_scene_desc;
 
 enum hm_scene_array {

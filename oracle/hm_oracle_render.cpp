@@ -55,22 +55,39 @@ struct OScene {
   float alpha;  // clamp(alpha,.01,1)^2
   float env_scale = 1.f, env_rot = 0.f;
   int width = 0, height = 0, path_v1 = 1, path_v2 = 40, mis = 1, env_pdf = 1, has_env = 0, catrom = 0;
+  int seg_split = 1;  // BVH leaves per segment: part j of segment k is leaf primitive k + j * n_seg
   float scene_scale = 1.f;
   // BVH
   std::vector<float> nodes;  // [n_int][16]
   std::vector<int> leaf_prim;
   int n_seg() const { return (int)seg.size(); }
-  int n_prims() const { return (int)seg.size() + (int)tri.size() / 3; }
+  int n_hprim() const { return (int)seg.size() * seg_split; }
+  int n_prims() const { return n_hprim() + (int)tri.size() / 3; }
   int n_dl() const { return (int)dl.size() / 6; }
 };
 
 // ------------------------------------------------------------ BVH build
+// One de Casteljau halving (left or right half) of a cubic Bezier.
+void bezier_half(float w[4][4], int right) {
+  for (int k = 0; k < 4; ++k) {
+    const float m01 = (w[0][k] + w[1][k]) * 0.5f, m12 = (w[1][k] + w[2][k]) * 0.5f;
+    const float m23 = (w[2][k] + w[3][k]) * 0.5f;
+    const float m012 = (m01 + m12) * 0.5f, m123 = (m12 + m23) * 0.5f, m = (m012 + m123) * 0.5f;
+    if (right) {
+      w[0][k] = m; w[1][k] = m123; w[2][k] = m23;
+    } else {
+      w[1][k] = m01; w[2][k] = m012; w[3][k] = m;
+    }
+  }
+}
+
 Box prim_box(const OScene& s, int p) {
   Box b;
-  if (p < s.n_seg()) {
-    // hull of the Bezier control points of the segment, grown by their
-    // largest radius (same operation order as the device build)
-    const float* c = &s.cp[4 * s.seg[p]];
+  if (p < s.n_hprim()) {
+    // hull of the Bezier control points of the segment's part, grown by
+    // their largest radius (same operation order as the device build)
+    const int part = p / s.n_seg();
+    const float* c = &s.cp[4 * s.seg[p - part * s.n_seg()]];
     float w[4][4];
     for (int k = 0; k < 4; ++k) {
       const float q0 = c[k], q1 = c[4 + k], q2 = c[8 + k], q3 = c[12 + k];
@@ -79,13 +96,14 @@ Box prim_box(const OScene& s, int p) {
       w[2][k] = (q1 + 2.f * q2) * (1.f / 3.f);
       w[3][k] = ((q1 + 4.f * q2) + q3) * (1.f / 6.f);
     }
+    for (int bit = s.seg_split >> 1; bit > 0; bit >>= 1) bezier_half(w, part & bit);
     const float r = fmaxf(fmaxf(w[0][3], w[1][3]), fmaxf(w[2][3], w[3][3]));
     for (int k = 0; k < 3; ++k) {
       b.lo[k] = fminf(fminf(w[0][k], w[1][k]), fminf(w[2][k], w[3][k])) - r;
       b.hi[k] = fmaxf(fmaxf(w[0][k], w[1][k]), fmaxf(w[2][k], w[3][k])) + r;
     }
   } else {
-    const int* t = &s.tri[3 * (p - s.n_seg())];
+    const int* t = &s.tri[3 * (p - s.n_hprim())];
     const float *a = &s.vtx[3 * t[0]], *bb = &s.vtx[3 * t[1]], *c = &s.vtx[3 * t[2]];
     for (int k = 0; k < 3; ++k) {
       b.lo[k] = fminf(fminf(a[k], bb[k]), c[k]);
@@ -243,7 +261,7 @@ struct P4 {
   float x, y, z, r;
 };
 
-bool curve_hit(const OScene& s, int si, V3 o, V3 d, float tmin, float tmax, float* t_out, float* u_out) {
+bool curve_hit(const OScene& s, int si, int part, V3 o, V3 d, float tmin, float tmax, float* t_out, float* u_out) {
   const float* q = &s.cp[4 * s.seg[si]];
   float w[4][4];
   for (int c = 0; c < 4; ++c) {
@@ -261,6 +279,16 @@ bool curve_hit(const OScene& s, int si, V3 o, V3 d, float tmin, float tmax, floa
   for (int i = 0; i < 4; ++i) {
     V3 p = V3(w[i][0], w[i][1], w[i][2]) - o;
     b[i] = P4{dot(p, ax), dot(p, ay), dot(p, d), w[i][3]};
+  }
+  for (int bit = s.seg_split >> 1; bit > 0; bit >>= 1) {  // down to the part (de Casteljau halvings)
+    auto mid = [](P4 a, P4 c) { return P4{(a.x + c.x) * 0.5f, (a.y + c.y) * 0.5f, (a.z + c.z) * 0.5f, (a.r + c.r) * 0.5f}; };
+    P4 m01 = mid(b[0], b[1]), m12 = mid(b[1], b[2]), m23 = mid(b[2], b[3]);
+    P4 m012 = mid(m01, m12), m123 = mid(m12, m23), m = mid(m012, m123);
+    if (part & bit) {
+      b[0] = m; b[1] = m123; b[2] = m23;
+    } else {
+      b[1] = m01; b[2] = m012; b[3] = m;
+    }
   }
   float rmax = fmaxf(fmaxf(b[0].r, b[1].r), fmaxf(b[2].r, b[3].r));
   auto mn = [&](float P4::*f) { return fminf(fminf(b[0].*f, b[1].*f), fminf(b[2].*f, b[3].*f)); };
@@ -305,7 +333,7 @@ bool curve_hit(const OScene& s, int si, V3 o, V3 d, float tmin, float tmax, floa
   }
   if (found) {
     *t_out = best_t;
-    *u_out = best_u;
+    *u_out = ((float)part + best_u) * (1.f / (float)s.seg_split);
   }
   return found;
 }
@@ -327,12 +355,16 @@ OHit trace(const OScene& s, V3 o, V3 d, float tmin, float tmax, bool any) {
       (c == 0 ? *t0 : *t1) = tn <= tf ? tn : INFINITY;
     }
   };
-  auto prim_hit = [&](int prim, float* t, float* u, float* v) {
-    if (prim < s.n_seg()) {
+  // a leaf primitive; *id = the segment, or n_seg + the triangle
+  auto prim_hit = [&](int prim, float* t, float* u, float* v, int* id) {
+    if (prim < s.n_hprim()) {
       *v = 0.f;
-      return curve_hit(s, prim, o, d, tmin, h.t, t, u);
+      const int part = prim / s.n_seg();
+      *id = prim - part * s.n_seg();
+      return curve_hit(s, *id, part, o, d, tmin, h.t, t, u);
     }
-    return tri_hit(s, prim - s.n_seg(), o, d, tmin, h.t, t, u, v);
+    *id = s.n_seg() + (prim - s.n_hprim());
+    return tri_hit(s, prim - s.n_hprim(), o, d, tmin, h.t, t, u, v);
   };
   for (int guard = 0; guard < (1 << 22); ++guard) {
     const float* f = &s.nodes[16 * node];
@@ -343,8 +375,9 @@ OHit trace(const OScene& s, V3 o, V3 d, float tmin, float tmax, bool any) {
     memcpy(&c1, f + 13, 4);
     if (c0 < 0 && t0 < INFINITY) {
       float t, u, v;
-      if (prim_hit(s.leaf_prim[~c0], &t, &u, &v)) {
-        h = OHit{t, s.leaf_prim[~c0], u, v};
+      int id;
+      if (prim_hit(s.leaf_prim[~c0], &t, &u, &v, &id)) {
+        h = OHit{t, id, u, v};
         if (any) return h;
       }
       t0 = INFINITY;
@@ -352,8 +385,9 @@ OHit trace(const OScene& s, V3 o, V3 d, float tmin, float tmax, bool any) {
     }
     if (c1 < 0 && t1 < INFINITY) {
       float t, u, v;
-      if (prim_hit(s.leaf_prim[~c1], &t, &u, &v)) {
-        h = OHit{t, s.leaf_prim[~c1], u, v};
+      int id;
+      if (prim_hit(s.leaf_prim[~c1], &t, &u, &v, &id)) {
+        h = OHit{t, id, u, v};
         if (any) return h;
       }
       t1 = INFINITY;
@@ -841,7 +875,7 @@ extern "C" {
 void* hmo_scene_new(const float* cp, int n_cp, const int* seg, int n_seg, const float* vtx, const float* nrm, int n_vtx,
                     const int* tri, int n_tri, const float* env, int env_w, int env_h, const float* cpdf,
                     const float* ccdf, const float* mpdf, const float* mcdf, const float* dl, int n_dl,
-                    const float* camera12, const float* mat16, const int* settings8, float scene_scale) {
+                    const float* camera12, const float* mat16, const int* settings9, float scene_scale) {
   OScene* s = new OScene();
   s->cp.assign(cp, cp + 4 * (size_t)n_cp);
   s->seg.assign(seg, seg + n_seg);
@@ -869,14 +903,15 @@ void* hmo_scene_new(const float* cp, int n_cp, const int* seg, int n_seg, const 
   s->alpha = a * a;
   s->env_scale = mat16[14];
   s->env_rot = mat16[15];
-  s->width = settings8[0];
-  s->height = settings8[1];
-  s->path_v1 = settings8[2];
-  s->path_v2 = settings8[3];
-  s->mis = settings8[4];
-  s->env_pdf = settings8[5];
-  s->has_env = settings8[6];
-  s->catrom = settings8[7];
+  s->width = settings9[0];
+  s->height = settings9[1];
+  s->path_v1 = settings9[2];
+  s->path_v2 = settings9[3];
+  s->mis = settings9[4];
+  s->env_pdf = settings9[5];
+  s->has_env = settings9[6];
+  s->catrom = settings9[7];
+  s->seg_split = settings9[8];
   s->scene_scale = scene_scale;
   build_bvh(*s);
   return s;

@@ -140,7 +140,8 @@ class OracleScene:
         empty = np.zeros(4, np.float32)
         g = lambda k: a[k] if a[k].size else empty
         sets = np.array([settings["width"], settings["height"], settings["path_v1"], settings["path_v2"],
-                         settings["mis"], settings["env_pdf"], settings["has_env"], settings["catrom"]], np.int32)
+                         settings["mis"], settings["env_pdf"], settings["has_env"], settings["catrom"],
+                         settings.get("seg_split", 1)], np.int32)
         self.h = L.hmo_scene_new(
             a["control_points"].astype(np.float32).ravel(), len(a["control_points"]),
             a["segments"].astype(np.int32).ravel(), len(a["segments"]),
@@ -162,7 +163,7 @@ class OracleScene:
         i = scene.info()
         settings = dict(width=i.width, height=i.height, path_v1=i.path_v1, path_v2=i.path_v2, mis=i.mis,
                         env_pdf=i.env_pdf, has_env=i.has_env, catrom=i.shading_catrom, env_w=i.env_width,
-                        env_h=i.env_height)
+                        env_h=i.env_height, seg_split=i.segment_splits)
         o = cls(arrays, settings, i.scene_scale)
         if i.n_groups > 0:
             o.set_groups(scene.export("segment_groups"), scene.export("group_materials"))

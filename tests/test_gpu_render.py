@@ -1,7 +1,7 @@
 """GPU parity of the scene LBVH, traversal and wavefront integrator.
 
 * BVH: device node array == the oracle's host build, bit for bit; so is
-  the 4-wide collapse the kernels traverse.
+  the 4-wide collapse the kernels traverse (1, 2 or 4 leaves per segment).
 * Traversal: same closest primitive for >= 99.5% of rays; t within
   1e-4 relative where the primitive matches (the device contracts
   multiply-adds in traversal; the oracle does not).
@@ -33,9 +33,11 @@ def small_cfg(R, strands=400, res=64):
     return R.straight_hair_scene(res, res, strands=strands)
 
 
+@pytest.mark.parametrize("split", [1, 2, 4])
 @pytest.mark.parametrize("strands", [1, 400, 10000])
-def test_bvh_matches_host_build_bit_exact(R, strands):
+def test_bvh_matches_host_build_bit_exact(R, strands, split):
     cfg = small_cfg(R, strands)
+    cfg["integrator"]["segment_splits"] = split
     if strands == 1:
         cfg.pop("surface")
     s = R.Scene(cfg)
@@ -62,8 +64,12 @@ def camera_rays(o, cfg, res):
     return org, d
 
 
-def test_traversal_matches_oracle(R):
+@pytest.mark.parametrize("split", [1, 2])
+def test_traversal_matches_oracle(R, split):
+    """Hits report the segment (and its whole-segment u) whichever part of
+    it was the leaf."""
     cfg = small_cfg(R, 2000, 128)
+    cfg["integrator"]["segment_splits"] = split
     s = R.Scene(cfg)
     o = po.OracleScene.from_library(s)
     org, d = camera_rays(o, cfg, 128)

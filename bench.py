@@ -538,7 +538,8 @@ def main():
     roof = wl.roofline(seg_ms, pk)
     line = {"metric": wl.metric, "value": round(value, 2), "unit": wl.unit, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scene / queries)",
+            "vs_baseline": None, "dtype": getattr(wl, "dtype", "f32"),
+            "data": "synthetic (seeded procedural scene / queries)",
             "config": wl.config(),
             "e2e": {"value": round(wl.units_per_step() * ws / (e2e_ms * 1e-3), 2), "unit": wl.unit,
                     "h2d_bytes_per_step": wl.h2d_bytes, "d2h_bytes_per_step": wl.d2h_bytes},

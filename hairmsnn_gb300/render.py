@@ -426,11 +426,16 @@ EXTEND_DRAM_BYTES_PER_RAY = 427
 
 
 class RenderBenchWorkload:
-    """bench.py workload: one frame (1 spp) of the full HairMSNN render per step."""
+    """bench.py workload: one frame (1 spp) of the full HairMSNN render per
+    step, in the chosen form: FP16 cache network on the tensor cores
+    (training and inference), frames in flight, graph replay, autotuned
+    launch shapes, two BVH leaves per segment."""
 
     name = "render"
     metric = "paths/s (HairMSNN full wavefront render, 512x512, 1 spp/frame, online cache training 2^16/frame)"
     unit = "paths/s"
+    cache_precision = 1  # FP16 (tcgen05); its relMSE equals the FP32 cache's (quality workload)
+    dtype = "f32 (traversal, shading, FP64 sums); f16 cache MLP with f32 accumulation"
 
     def __init__(self, torch, width=512, height=512, train_records=1 << 16, frames_in_flight=0):
         self.torch = torch
@@ -440,7 +445,7 @@ class RenderBenchWorkload:
         self.scene = Scene(self.cfg)
         self.scene.build()
         self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True,
-                          frames_in_flight=frames_in_flight)
+                          precision=self.cache_precision, frames_in_flight=frames_in_flight)
         self.tuning = self.r.autotune(frames=6)
         self.P = width * height
         self.h2d_bytes = 0
@@ -471,7 +476,8 @@ class RenderBenchWorkload:
         self.r.wait()
         t1.record()
         torch.cuda.synchronize()
-        return t0.elapsed_time(t1) / steps
+        self.last_ms = t0.elapsed_time(t1) / steps
+        return self.last_ms
 
     @property
     def kernels_per_step(self):
@@ -522,6 +528,32 @@ class RenderBenchWorkload:
         self.r.instrument(timing=False, counting=False)
         return t
 
+    def plain_form(self, frames=20):
+        """The plain FP32 wavefront form on the same scene and GPU: FP32 cache,
+        one frame in flight, kernel-by-kernel launches, default launch
+        shapes, one BVH leaf per segment.  Pipelined frame time."""
+        torch = self.torch
+        cfg = dict(self.cfg)
+        cfg["integrator"] = dict(cfg["integrator"], segment_splits=1)
+        sc = Scene(cfg)
+        r = Renderer(sc, MSNN, beta=1, train_records=self.train_records, train=True, precision=0,
+                     frames_in_flight=1)
+        r.set_graphs(False)
+        for _ in range(3):
+            r.frame()
+        r.wait()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(frames):
+            r.frame()
+        r.wait()
+        t1.record()
+        torch.cuda.synchronize()
+        ms = t0.elapsed_time(t1) / frames
+        r.close()
+        sc.close()
+        return ms
+
     def roofline(self, seg_ms, pk):
         keys = ["extend_ms", "shade_ms", "shadow_ms", "compact_ms", "train_ms", "infer_ms", "compose_ms",
                 "camera_ms", "finalize_ms"]
@@ -554,12 +586,22 @@ class RenderBenchWorkload:
         else:
             out.update({"kernel": dominant, "bound": "tensor", "achieved": None, "peak": pk["bf16_tflops"],
                         "unit": "TFLOP/s", "frac": None, "traffic": None})
+        if type(self) is RenderBenchWorkload:
+            plain = self.plain_form()
+            chosen = self.last_ms if getattr(self, "last_ms", None) else None
+            out["plain_fp32_wavefront_form"] = {
+                "ms_per_frame": round(plain, 3), "paths_per_s": round(self.P / (plain * 1e-3), 1),
+                "chosen_form_speedup": round(plain / chosen, 3) if chosen else None,
+                "what": "FP32 cache, 1 frame in flight, kernel-by-kernel launches, default launch shapes, "
+                        "1 BVH leaf per segment; same scene and GPU"}
         return out
 
     def config(self):
-        return {"workload": "render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments), "
-                            "20k-tri head, Preetham sky T=3 + directional (3,3,3), 512x512, path_v1=1, path_v2=40, "
-                            "BETA=1, cache FP32 HashGrid/OneBlob MLP 64x2, 2^16 training records/frame",
+        return {"workload": "render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments, 2 BVH "
+                            "leaves each), 20k-tri head, Preetham sky T=3 + directional (3,3,3), 512x512, "
+                            "path_v1=1, path_v2=40, BETA=1, cache HashGrid/OneBlob MLP 64x2 in FP16 on tcgen05 "
+                            "(training and inference; FP32 master weights), 2^16 training records/frame",
+                "cache_precision": "fp16" if self.cache_precision == 1 else "fp32",
                 "pixels": self.P, "train_records": self.train_records,
                 "l2": "inputs larger than L2: each frame in flight streams its own ~90 MB path state, with "
                       "several frames in flight, past the 129 MB L2 (scene: 4-wide BVH 40 MB + curves 10 MB); "
@@ -728,6 +770,8 @@ def batch_scene_configs(n=64, seed=0):
 class BatchBenchWorkload(RenderBenchWorkload):
     """bench.py workload: one frame (1 spp) of each of 64 uneven scenes,
     rendered as one batch with one shared FP32 cache network (width 64)."""
+
+    dtype = "f32"
 
     name = "batch"
     metric = "paths/s (64 concurrent HairMSNN scenes, 128^2..1024^2, 2k-50k curly strands, one shared cache)"

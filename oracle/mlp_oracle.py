@@ -246,6 +246,20 @@ def backward(cfg, params, x, target):
     params = np.asarray(params, np.float64)
     out, hs = forward(cfg, params, x)
     loss, g = loss_and_grad(cfg, out, np.asarray(target, np.float64))
+    return loss, _backprop(cfg, params, x, hs, g)
+
+
+def backward_output_grad(cfg, params, x, dy):
+    """Parameter gradients for a given dL/d(output) [n, out_ch] (tcnn's
+    backward with dL_doutput; no loss)."""
+    params = np.asarray(params, np.float64)
+    out, hs = forward(cfg, params, x)
+    g = np.zeros_like(out)
+    g[:, :cfg.out_ch] = np.asarray(dy, np.float64)
+    return _backprop(cfg, params, x, hs, g)
+
+
+def _backprop(cfg, params, x, hs, g):
     Ws = weights(cfg, params)
     grads = np.zeros(cfg.n_params)
     dz = g
@@ -269,7 +283,7 @@ def backward(cfg, params, x, target):
             gcol = dX[:, s["out_off"] + l * F:s["out_off"] + (l + 1) * F]
             for idx, wt in _grid_corners(s, l, p):
                 np.add.at(tg, idx, wt[:, None] * gcol)
-    return loss, grads
+    return grads
 
 
 class Adam:

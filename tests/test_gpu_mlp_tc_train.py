@@ -103,3 +103,33 @@ def test_tensor_core_training_converges(mlpmod, prec):
         assert np.mean(losses[-5:]) < 0.5 * np.mean(losses[:5])
         finals[p] = np.mean(losses[-5:])
     assert finals[prec] <= 1.5 * finals["fp32"], finals
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("cfg,in_ch,gen", CASES[:2])
+def test_output_grad_backward_matches_oracle(mlpmod, cfg, in_ch, gen, prec):
+    """hm_mlp_backward_output_grad (tcnn's backward with dL_doutput) against
+    the FP64 oracle: FP32 within 1e-4, FP16 within 4e-2 and BF16 within
+    1.5e-1 (1.5x the loss-gradient bars: a random dL/d(output) is
+    uncorrelated with the outputs, so each weight's gradient is a sum with
+    more cancellation and its relative error is larger; layer 0 measured
+    2.7e-2 in FP16)."""
+    net = mlpmod.TinyMLP(cfg, in_ch, 3, precision=prec, seed=13)
+    oc = mo.Config(net.config_text, in_ch, 3)
+    if oc.n_enc_params:
+        p = net.params()
+        p[oc.n_net_params:] = np.random.default_rng(6).uniform(-0.5, 0.5, oc.n_enc_params)
+        net.set_params(p)
+    n = 4096 + 32
+    x = gen(n, seed=3)
+    dy = (np.random.default_rng(8).normal(size=(n, 3)) / n).astype(np.float32)
+    p0 = net.params().astype(np.float64)
+    net.forward(torch.from_numpy(x).cuda())
+    net.backward_output_grad(torch.from_numpy(dy).cuda())
+    ref = mo.backward_output_grad(oc, p0, x, dy)
+    g = net.gradients().astype(np.float64)
+    tg = 1e-4 if prec == "fp32" else 1.5 * TOL[prec][1]
+    for off, fo, fi in oc.layer_shapes:
+        assert rel_rms(g[off:off + fo * fi], ref[off:off + fo * fi]) <= tg, (off, prec)
+    if oc.n_enc_params:
+        assert rel_rms(g[oc.n_net_params:], ref[oc.n_net_params:]) <= tg

@@ -112,3 +112,26 @@ def test_oracle_gradients_match_finite_differences(enc):
         f = lambda o: np.sum((o[:, :3] - tgt) ** 2 / den) / (32 * 3)
         fd_frozen = (f(out1) - f(out2)) / (2 * eps)
         assert abs(fd_frozen - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd_frozen, g[i], fd)
+
+
+def test_oracle_output_grad_backward_matches_finite_differences():
+    """backward_output_grad: dW of <dy, output> (the cache adjoint of the
+    differentiable renderer) against central differences."""
+    enc = {"otype": "Composite", "nested": [{"otype": "HashGrid", "n_dims_to_encode": 3, "n_levels": 3,
+                                             "log2_hashmap_size": 6, "base_resolution": 2, "per_level_scale": 2.0},
+                                            {"otype": "OneBlob", "n_dims_to_encode": 2, "n_bins": 4},
+                                            {"otype": "Identity"}]}
+    cfg = mo.Config(tiny_cfg(enc), 6, 3)
+    rng = np.random.default_rng(2)
+    params = rng.normal(scale=0.3, size=cfg.n_params)
+    x = rng.uniform(0.05, 0.95, (24, 6)).astype(np.float32)
+    dy = rng.normal(size=(24, 3))
+    g = mo.backward_output_grad(cfg, params, x, dy)
+    f = lambda p: float(np.sum(mo.forward(cfg, p, x)[0][:, :3] * dy))
+    eps = 1e-6
+    for i in rng.choice(cfg.n_params, 60, replace=False):
+        p1, p2 = params.copy(), params.copy()
+        p1[i] += eps
+        p2[i] -= eps
+        fd = (f(p1) - f(p2)) / (2 * eps)
+        assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd, g[i])

@@ -7,6 +7,8 @@
   python -m hairmsnn_gb300 infer [--config c1_cache_w64.json] [--precision fp16]
                                  [--queries N] [--repeat R]
 
+  python -m hairmsnn_gb300 diff [--width W --height H --strands N --groups G --frames F]
+
 `infer` times cache-network inference on N synthetic hair-vertex queries
 (16-D: position, angles, h, sigma_a, beta) and prints the time per call.
 
@@ -115,6 +117,40 @@ def read_exr(path):
     return img[::-1].copy()
 
 
+def diff(a):
+    """Curly hair with strand groups (render.curly_hair_diff_scene): renders a
+    target at the groups' materials, moves sigma_a 50% off, renders again
+    (hm_render_diff_forward) and replays the paths (hm_render_diff_backward)
+    for dL/d(material) of the L2 image loss; prints the gradient and times."""
+    import numpy as np
+    import torch
+    from . import build, render
+    build.build()
+    cfg, mats = render.curly_hair_diff_scene(a.width, a.height, strands=a.strands,
+                                             control_points=a.control_points, groups=a.groups)
+    scene = render.Scene(cfg)
+    scene.set_group_materials(mats)
+    rd = render.Renderer(scene, render.MSNN, beta=a.beta, train=False)
+    rd.diff_forward(a.frames)
+    target = rd.device_sums(5).clone() / a.frames
+    off = mats.copy()
+    off[:, 0:3] *= 1.5
+    scene.set_group_materials(off)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rd.diff_forward(a.frames)
+    img = rd.device_sums(5) / a.frames
+    adj = (2.0 / img.numel()) * (img - target)
+    loss = float((adj * (img - target)).sum() / 2.0)
+    t1 = time.perf_counter()
+    g = rd.diff_backward(adj.float())
+    t2 = time.perf_counter()
+    print(json.dumps({"loss": loss, "forward_s": round(t1 - t0, 4), "backward_s": round(t2 - t1, 4),
+                      "grad_sigma_a": np.round(g[:, 0:3], 8).tolist(),
+                      "grad_beta_m_beta_n_alpha": np.round(g[:, 3:6], 8).tolist()}))
+    return 0
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m hairmsnn_gb300")
     sub = ap.add_subparsers(dest="cmd", required=True)
@@ -135,9 +171,19 @@ def main(argv=None):
     q.add_argument("--precision", choices=["fp32", "fp16", "bf16", "fp8"], default="fp16")
     q.add_argument("--queries", type=int, default=1 << 18)
     q.add_argument("--repeat", type=int, default=1)
+    d = sub.add_parser("diff", help="one gradient of the differentiable appearance fit")
+    d.add_argument("--width", type=int, default=256)
+    d.add_argument("--height", type=int, default=256)
+    d.add_argument("--strands", type=int, default=20000)
+    d.add_argument("--control-points", type=int, default=96)
+    d.add_argument("--groups", type=int, default=4)
+    d.add_argument("--frames", type=int, default=64)
+    d.add_argument("--beta", type=int, default=2)
     a = ap.parse_args(argv)
     if a.cmd == "infer":
         return infer(a)
+    if a.cmd == "diff":
+        return diff(a)
 
     from . import build, render
     build.build()

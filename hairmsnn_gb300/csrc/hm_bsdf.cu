@@ -49,7 +49,10 @@ HairConsts hair_consts_from_params(const hm_hair_params& p) {
 
 HM_D float ldg(const float* p) { return __ldg(p); }
 
-__global__ void __launch_bounds__(256) bsdf_eval_kernel(HairConsts hc, const float* __restrict__ wo,
+// Three 256-thread blocks per SM (at most 85 registers; the eval needs 79
+// without spilling): 37.5% occupancy instead of 25% at 92 registers, for a
+// kernel that waits on its transcendentals rather than on memory.
+__global__ void __launch_bounds__(256, 3) bsdf_eval_kernel(HairConsts hc, const float* __restrict__ wo,
                                                         const float* __restrict__ wi,
                                                         const float* __restrict__ t,
                                                         const float* __restrict__ h,
@@ -71,7 +74,7 @@ __global__ void __launch_bounds__(256) bsdf_eval_kernel(HairConsts hc, const flo
   }
 }
 
-__global__ void __launch_bounds__(256) bsdf_sample_kernel(HairConsts hc, const float* __restrict__ wo,
+__global__ void __launch_bounds__(256, 3) bsdf_sample_kernel(HairConsts hc, const float* __restrict__ wo,
                                                           const float* __restrict__ t,
                                                           const float* __restrict__ h,
                                                           const float* __restrict__ u,

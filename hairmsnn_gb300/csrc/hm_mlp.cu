@@ -633,6 +633,8 @@ struct Mlp {
   // FP16 / BF16 handles also train on the tensor cores; FP16 gradients carry
   // a static loss scale of 128 (BF16: 1), divided out in the optimizer step
   TcTrainBufs tcb;
+  uint8_t* tc_work = nullptr;  // tensor-core inference: encoded layer-0 operands
+  int64_t tc_work_cap = 0;
   float loss_scale = 1.f;
   bool tc_train = false;
 };
@@ -839,6 +841,7 @@ extern "C" void hm_mlp_destroy(hm_mlp* h) {
   cudaFree(m->grid_acc);
   tc_pack_free(&m->tc);
   tc_train_free(&m->tcb);
+  cudaFree(m->tc_work);
   if (m->tc_err_host) cudaFreeHost(m->tc_err_host);
   delete m;
 }
@@ -910,9 +913,11 @@ static int tc_prepare(Mlp* m) {
 }
 
 // Inference on the tensor cores (FP16 / BF16 / E4M3 operands, FP32
-// accumulation); encoding fused, no per-call allocation.  A bounded wait
-// that expired in an earlier call is reported here.
-static int tc_inference(Mlp* m, const float* d_in, float* d_out, int64_t n, cudaStream_t st) {
+// accumulation).  With allow_alloc the encoded operands go through a
+// workspace grown on demand (encode kernel, then the layers); without it
+// (hm_mlp_inference_noalloc) the encoding is fused into the layer kernel.  A
+// bounded wait that expired in an earlier call is reported here.
+static int tc_inference(Mlp* m, const float* d_in, float* d_out, int64_t n, cudaStream_t st, bool allow_alloc) {
   if (*(volatile int*)m->tc_err_host) {
     *m->tc_err_host = 0;
     return hm_set_error("mlp: a tensor-core wait expired in an earlier call"), HM_ETIMEOUT;
@@ -921,8 +926,19 @@ static int tc_inference(Mlp* m, const float* d_in, float* d_out, int64_t n, cuda
     if (int s = tc_pack(m->cfg.d, m->params, m->tc, st)) return s;
     m->packed_version = m->params_version;
   }
+  if (allow_alloc) {
+    const int64_t need = tc_encode_bytes(m->cfg.d, m->tc, n);
+    if (need > m->tc_work_cap) {
+      cudaFree(m->tc_work);
+      m->tc_work = nullptr;
+      m->tc_work_cap = 0;
+      cudaError_t e = cudaMalloc(&m->tc_work, (size_t)need);
+      if (e != cudaSuccess) return hm_cuda_status(e, "tensor-core encode workspace");
+      m->tc_work_cap = need;
+    }
+  }
   return tc_forward(m->cfg.d, m->tc, m->params + m->cfg.d.n_net_params, d_in, d_out, m->cfg.d.out_ch, n,
-                    m->tc_err_dev, st);
+                    m->tc_err_dev, st, allow_alloc ? m->tc_work : nullptr, allow_alloc ? m->tc_work_cap : 0);
 }
 
 static int check_io(const char* who, Mlp* m, const void* a, const void* b, int64_t n) {
@@ -940,7 +956,7 @@ extern "C" int hm_mlp_inference(hm_mlp* h, const float* d_in, float* d_out, int6
   if (int s = check_io("hm_mlp_inference", m, d_in, d_out, n)) return s;
   if (n == 0) return HM_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  if (m->precision != HM_PREC_FP32) return tc_inference(m, d_in, d_out, n, st);
+  if (m->precision != HM_PREC_FP32) return tc_inference(m, d_in, d_out, n, st, true);
   if (int s = ensure_ws(m, n)) return s;
   if (int s = encode(m, d_in, n, st)) return s;
   return dispatch_fwd(m, m->X, d_out, m->cfg.d.out_ch, nullptr, n, st);
@@ -1235,7 +1251,7 @@ extern "C" int hm_mlp_inference_noalloc(hm_mlp* h, const float* d_in, float* d_o
   Mlp* m = (Mlp*)h;
   if (int s = check_io("hm_mlp_inference_noalloc", m, d_in, d_out, n)) return s;
   if (n == 0) return HM_OK;
-  if (m->precision != HM_PREC_FP32) return tc_inference(m, d_in, d_out, n, (cudaStream_t)stream);
+  if (m->precision != HM_PREC_FP32) return tc_inference(m, d_in, d_out, n, (cudaStream_t)stream, false);
   const int64_t need = n * (int64_t)m->cfg.d.in_pad;
   if (need > kNoAllocScratchFloats)
     return hm_set_error("hm_mlp_inference_noalloc: %lld queries x %d encoded floats exceed the static scratch of "

@@ -176,9 +176,14 @@ int tc_pack_alloc(const MlpDims& d, int precision, TcPack* pk);
 int tc_pack(const MlpDims& d, const float* params, TcPack& pk, cudaStream_t st);
 void tc_pack_free(TcPack* pk);
 // Encoding + all layers of n queries on the tensor cores: in [n][in_ch],
-// out [n][out_stride] (the first out_ch columns written).
+// out [n][out_stride] (the first out_ch columns written).  With a workspace
+// of at least tc_encode_bytes the encoding runs first as its own kernel and
+// the layers load their input tiles by bulk copies; without one, the
+// encoding is fused into the layer kernel.
+int64_t tc_encode_bytes(const MlpDims& d, const TcPack& pk, int64_t n);
 int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
-               int out_stride, int64_t n, int* err_flag, cudaStream_t st);
+               int out_stride, int64_t n, int* err_flag, cudaStream_t st, uint8_t* work = nullptr,
+               int64_t work_bytes = 0);
 // Training on the tensor cores (FP16 / BF16): forward keeping the operands,
 // backward (loss gradient scaled by loss_scale, dgrad chain, dX when the
 // encoding has parameters), weight gradients as per-chunk partials reduced

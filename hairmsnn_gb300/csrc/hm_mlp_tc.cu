@@ -73,6 +73,20 @@ HM_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
   return false;
 }
 HM_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// The barrier's phase completes once `bytes` of asynchronous copies have
+// landed (and the one arrival of this call).
+HM_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+// One bulk copy global -> shared (16-byte aligned, a multiple of 16 bytes),
+// completing on `bar`.
+HM_D void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
 HM_D void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 HM_D void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -340,7 +354,42 @@ struct TcArgs {
   uint16_t* x16;  // [n][K0]
   uint16_t* h16;  // [L][n][W]
   float* pred;    // [n][16]
+  // inference with the encoding done beforehand by tc_encode_kernel: the
+  // layer-0 operand of tile t is the tile_bytes at a_pre + t * tile_bytes, in
+  // the MMA layout; E4M3 rows carry their activation scale in row_inv_pre
+  const uint8_t* a_pre;
+  const float* row_inv_pre;
+  int64_t tile_bytes;
 };
+
+// Encoding of every row into the layer-0 operand, in the MMA's shared-memory
+// layout one tile after another, so the forward kernel loads a tile (or a K
+// chunk of it) with one bulk copy.  One thread per row, 128 rows (one tile)
+// per block: the 32 rows of a warp write each 16-byte group as four 128-byte
+// runs.  Same arithmetic as the fused encoding (enc_range).
+template <int PREC>
+__global__ void __launch_bounds__(kTcRows) tc_encode_kernel(const __grid_constant__ TcArgs p, uint8_t* __restrict__ a_out,
+                                                            float* __restrict__ row_inv_out) {
+  const int row = threadIdx.x;
+  const int64_t tile = blockIdx.x;
+  const int64_t q = tile * kTcRows + row;
+  const bool valid = q < p.n;
+  const MlpDims& d = p.d;
+  const float* xin = p.in + (valid ? q : 0) * d.in_ch;
+  float row_scale = 1.f;
+  if (PREC == TC_E4M3) {
+    const float bound = valid ? enc_row_bound(d, xin, p.scales[15]) : 1.f;
+    row_scale = kE4M3Max / bound;
+    if (valid) row_inv_out[q] = bound / kE4M3Max;
+  }
+  RowPacker<PREC> pk(a_out + tile * p.tile_bytes, row, 0, row_scale);
+  const int K0 = p.K[0];
+  if (valid) {
+    enc_range<PREC>(d, xin, p.enc_params, 0, K0, pk);
+  } else {
+    for (int k = 0; k < K0; ++k) pk.push(0.f);
+  }
+}
 
 // 256 threads: thread (warp w, lane i) owns row 32 * (w % 4) + i of the tile
 // (tensor-memory lanes are split by warp quadrant) and half h = w / 4 of the
@@ -358,7 +407,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
   uint8_t* A = smem;
   uint8_t* Wt = smem + p.a_bytes;
   uint64_t* bar = reinterpret_cast<uint64_t*>(Wt + ((p.blob_bytes + 127) & ~(int64_t)127));
-  uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 1);
+  uint64_t* bar_a = bar + 1;  // bulk copies of pre-encoded operands
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bar + 2);
   float* amax_x = reinterpret_cast<float*>(holder + 4);  // [2][128] E4M3 row maxima
 
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -371,6 +421,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
     reinterpret_cast<uint4*>(Wt)[i] = __ldg(reinterpret_cast<const uint4*>(p.blob) + i);
   if (tid == 0) {
     mbar_init(bar, 1);
+    mbar_init(bar_a, 1);
     fence_mbar_init();
   }
   if (warp == 0) tmem_alloc(holder, p.ncols);
@@ -382,7 +433,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
   const uint32_t row_taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
   const uint32_t a_base = smem_u32(A), w_base = smem_u32(Wt);
   const uint32_t a_lbo = 16 * kTcRows;
-  uint32_t phase = 0;
+  uint32_t phase = 0, phase_a = 0;
   bool failed = false;
   auto w_inv = [&](int l) { return F8 ? __ldg(p.scales + l) : 1.f; };
   const float grid_amax = F8 ? p.scales[15] : 0.f;
@@ -401,7 +452,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
       }
       tc_commit(bar);
     }
-    const bool ok = mbar_wait_bounded(bar, phase);
+    // thread 0 (which committed) polls the barrier; the others sleep in the
+    // block barrier instead of spinning
+    const bool ok = threadIdx.x == 0 ? mbar_wait_bounded(bar, phase) : true;
     phase ^= 1u;
     const bool bad = __syncthreads_or(!ok);
     tc_fence_after();
@@ -416,15 +469,33 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
     float row_inv = 1.f;  // 1 / activation scale of this row of A
     float row_scale = 1.f;
     if (F8) {
-      const float bound = valid ? enc_row_bound(d, xin, grid_amax) : 1.f;
-      row_scale = kE4M3Max / bound;
-      row_inv = bound / kE4M3Max;
+      if (p.a_pre) {
+        row_inv = valid ? __ldg(p.row_inv_pre + q) : 1.f;
+      } else {
+        const float bound = valid ? enc_row_bound(d, xin, grid_amax) : 1.f;
+        row_scale = kE4M3Max / bound;
+        row_inv = bound / kE4M3Max;
+      }
     }
     // ---- layer 0, in K chunks
     const int K0 = p.K[0];
     for (int kc = 0; kc < K0 && !failed; kc += p.kc0) {
       const int kn = min(p.kc0, K0 - kc);
-      {
+      if (p.a_pre) {
+        // the chunk's K range is one contiguous run of the tile in the MMA layout
+        if (tid == 0) {
+          fence_proxy_async_smem();  // the previous tile's epilogue wrote A through the generic proxy
+          const uint32_t bytes = (uint32_t)(kn * EB * kTcRows);
+          mbar_arrive_expect_tx(bar_a, bytes);
+          bulk_copy_g2s(A, p.a_pre + tile * p.tile_bytes + (int64_t)kc * EB * kTcRows, bytes, bar_a);
+        }
+        const bool ok = tid == 0 ? mbar_wait_bounded(bar_a, phase_a) : true;
+        phase_a ^= 1u;
+        if (__syncthreads_or(!ok)) {
+          failed = true;
+          break;
+        }
+      } else {
         // the two halves of the row: groups [0, G/2) and [G/2, G) of the chunk
         const int G = kn / CK, gsplit = (G + 1) >> 1;
         const int g0 = half ? gsplit : 0, g1 = half ? G : gsplit;
@@ -435,9 +506,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
         } else {
           for (int k = g0 * CK; k < g1 * CK; ++k) pk.push(0.f);
         }
+        fence_proxy_async_smem();
+        __syncthreads();
       }
-      fence_proxy_async_smem();
-      __syncthreads();
       if (!run_layer(0, kc, kn, kc > 0)) failed = true;
     }
     // ---- hidden epilogues and the following layers
@@ -751,12 +822,35 @@ static int tc_args(const MlpDims& d, const TcPack& pk, const float* enc_params, 
   return HM_OK;
 }
 
+int64_t tc_encode_bytes(const MlpDims& d, const TcPack& pk, int64_t n) {
+  const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+  const int64_t tile_bytes = (int64_t)kTcRows * pk.K[0] * pk.elem_bytes;
+  return tiles * tile_bytes + (pk.precision == HM_PREC_FP8_E4M3 ? ((n * 4 + 255) & ~(int64_t)255) : 0);
+}
+
 int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
-               int out_stride, int64_t n, int* err_flag, cudaStream_t st) {
+               int out_stride, int64_t n, int* err_flag, cudaStream_t st, uint8_t* work, int64_t work_bytes) {
   if (n <= 0) return HM_OK;
   TcArgs a;
   size_t smem = 0;
   if (int e = tc_args(d, pk, enc_params, in, out, out_stride, n, err_flag, &a, &smem)) return e;
+  if (work && work_bytes >= tc_encode_bytes(d, pk, n)) {
+    // encode every row first (high occupancy, no tensor work), then the
+    // layers with the layer-0 operand loaded by bulk copies
+    const int64_t tiles = (n + kTcRows - 1) / kTcRows;
+    a.tile_bytes = (int64_t)kTcRows * pk.K[0] * pk.elem_bytes;
+    float* row_inv = pk.precision == HM_PREC_FP8_E4M3 ? reinterpret_cast<float*>(work + tiles * a.tile_bytes)
+                                                      : nullptr;
+    if (pk.precision == HM_PREC_BF16)
+      tc_encode_kernel<TC_BF16><<<(unsigned)tiles, kTcRows, 0, st>>>(a, work, row_inv);
+    else if (pk.precision == HM_PREC_FP16)
+      tc_encode_kernel<TC_FP16><<<(unsigned)tiles, kTcRows, 0, st>>>(a, work, row_inv);
+    else
+      tc_encode_kernel<TC_E4M3><<<(unsigned)tiles, kTcRows, 0, st>>>(a, work, row_inv);
+    HM_CHECK_LAUNCH("tc_encode_kernel");
+    a.a_pre = work;
+    a.row_inv_pre = row_inv;
+  }
   const int W = d.width;
   switch (pk.precision) {
     case HM_PREC_BF16:
@@ -896,7 +990,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_bwd_kernel(const __grid_
       }
       tc_commit(bar);
     }
-    const bool ok = mbar_wait_bounded(bar, phase);
+    // thread 0 (which committed) polls the barrier; the others sleep in the
+    // block barrier instead of spinning
+    const bool ok = threadIdx.x == 0 ? mbar_wait_bounded(bar, phase) : true;
     phase ^= 1u;
     const bool bad = __syncthreads_or(!ok);
     tc_fence_after();
@@ -1072,7 +1168,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_tc_wgrad_kernel(const __gri
       }
       tc_commit(bar);
     }
-    const bool ok = mbar_wait_bounded(bar, phase);
+    // thread 0 (which committed) polls the barrier; the others sleep in the
+    // block barrier instead of spinning
+    const bool ok = threadIdx.x == 0 ? mbar_wait_bounded(bar, phase) : true;
     phase ^= 1u;
     if (__syncthreads_or(!ok)) failed = true;
     tc_fence_after();

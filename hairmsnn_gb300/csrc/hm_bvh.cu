@@ -12,13 +12,14 @@
 //   4. karras_kernel       binary radix tree (Karras, HPG 2012)
 //   5. refit_kernel        bottom-up child AABBs, second arrival continues
 //   6. wide_gather_kernel / wide_link_kernel
-//                          collapse into 4-wide nodes, breadth first: the
-//                          wide node of binary node r holds r's children,
-//                          each internal child replaced by its own two
-//                          children; wide nodes are numbered level by level
-//                          in the order their parents list them (an
-//                          exclusive scan per level), so the array is the
-//                          same on every run and equals the host build
+//                          collapse into 8-wide nodes, breadth first: the
+//                          wide node of binary node r starts with r's
+//                          children and repeatedly opens its internal child
+//                          of largest surface area until it has 8; wide
+//                          nodes are numbered level by level in the order
+//                          their parents list them (an exclusive scan per
+//                          level), so the array is the same on every run
+//                          and equals the host build
 //
 // All float arithmetic uses explicitly rounded intrinsics (no contraction),
 // so the node array is bit-identical to a host build of the same algorithm.
@@ -246,7 +247,7 @@ __global__ void single_leaf_kernel(SceneDev s, float4* nodes, int* prim_of_leaf)
   prim_of_leaf[0] = 0;
 }
 
-// ---- 4-wide collapse
+// ---- 8-wide collapse
 HM_D void read_child(const float4* nodes, int node, int slot, float* lo, float* hi, int* code) {
   const float* f = reinterpret_cast<const float*>(nodes + 4 * (int64_t)node);
   for (int k = 0; k < 3; ++k) {
@@ -256,47 +257,59 @@ HM_D void read_child(const float4* nodes, int node, int slot, float* lo, float* 
   *code = __float_as_int(f[12 + slot]);
 }
 
-// One thread per wide node of the level (binary root roots[i]).  Writes the
-// boxes and leaf codes; internal children keep their binary index for now
+// Surface area / 2 of a box, explicitly rounded: the collapse's expansion order.
+HM_D float half_area(const float* lo, const float* hi) {
+  const float ex = __fsub_rn(hi[0], lo[0]), ey = __fsub_rn(hi[1], lo[1]), ez = __fsub_rn(hi[2], lo[2]);
+  return __fadd_rn(__fadd_rn(__fmul_rn(ex, ey), __fmul_rn(ey, ez)), __fmul_rn(ex, ez));
+}
+
+// One thread per wide node of the level (binary root roots[i]).  The node
+// starts with r's two children; while it has fewer than kWide, the internal
+// child with the largest surface area (the first of equals) is replaced by
+// its first child and its second child is appended.  Writes the boxes and
+// leaf codes; internal children keep their binary index for now
 // (wide_link_kernel renumbers them) and are counted in n_internal[i].
 __global__ void wide_gather_kernel(const float4* __restrict__ bnodes, const int* __restrict__ roots, int n, int wbase,
                                    float4* __restrict__ wnodes, int* __restrict__ n_internal) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int r = roots[i];
-  float lo[4][3], hi[4][3];
-  int code[4];
-  int k = 0, ni = 0;
+  float lo[kWide][3], hi[kWide][3], area[kWide];
+  int code[kWide];
   for (int slot = 0; slot < 2; ++slot) {
-    float l[3], h[3];
-    int c;
-    read_child(bnodes, r, slot, l, h, &c);
-    if (c < 0) {
-      for (int a = 0; a < 3; ++a) { lo[k][a] = l[a]; hi[k][a] = h[a]; }
-      code[k++] = c;
-    } else {
-      for (int s2 = 0; s2 < 2; ++s2) {
-        int c2;
-        read_child(bnodes, c, s2, lo[k], hi[k], &c2);
-        code[k++] = c2;
-        ni += c2 >= 0;
+    read_child(bnodes, r, slot, lo[slot], hi[slot], &code[slot]);
+    area[slot] = half_area(lo[slot], hi[slot]);
+  }
+  int k = 2;
+  while (k < kWide) {
+    int best = -1;
+    float ba = 0.f;
+    for (int j = 0; j < k; ++j)
+      if (code[j] >= 0 && (best < 0 || area[j] > ba)) {
+        best = j;
+        ba = area[j];
       }
+    if (best < 0) break;
+    const int c = code[best];
+    read_child(bnodes, c, 0, lo[best], hi[best], &code[best]);
+    area[best] = half_area(lo[best], hi[best]);
+    read_child(bnodes, c, 1, lo[k], hi[k], &code[k]);
+    area[k] = half_area(lo[k], hi[k]);
+    ++k;
+  }
+  int ni = 0;
+  for (int j = 0; j < k; ++j) ni += code[j] >= 0;
+  for (int j = k; j < kWide; ++j) {
+    for (int a = 0; a < 3; ++a) lo[j][a] = hi[j][a] = INFINITY;
+    code[j] = -1;
+  }
+  float* w = reinterpret_cast<float*>(wnodes + kWideF4 * (int64_t)(wbase + i));
+  for (int j = 0; j < kWide; ++j) {
+    for (int a = 0; a < 3; ++a) {
+      w[2 * a * kWide + j] = lo[j][a];
+      w[(2 * a + 1) * kWide + j] = hi[j][a];
     }
-  }
-  for (; k < 4; ++k) {
-    for (int a = 0; a < 3; ++a) lo[k][a] = hi[k][a] = INFINITY;
-    code[k] = -1;
-  }
-  float* w = reinterpret_cast<float*>(wnodes + 8 * (int64_t)(wbase + i));
-  for (int j = 0; j < 4; ++j) {
-    w[0 + j] = lo[j][0];
-    w[4 + j] = hi[j][0];
-    w[8 + j] = lo[j][1];
-    w[12 + j] = hi[j][1];
-    w[16 + j] = lo[j][2];
-    w[20 + j] = hi[j][2];
-    w[24 + j] = __int_as_float(code[j]);
-    w[28 + j] = 0.f;
+    w[6 * kWide + j] = __int_as_float(code[j]);
   }
   n_internal[i] = ni;
 }
@@ -307,9 +320,9 @@ __global__ void wide_link_kernel(const int* __restrict__ offs, int n, int wbase,
                                  int* __restrict__ next_roots) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int* child = reinterpret_cast<int*>(wnodes + 8 * (int64_t)(wbase + i) + 6);
+  int* child = reinterpret_cast<int*>(wnodes + kWideF4 * (int64_t)(wbase + i)) + 6 * kWide;
   int m = offs[i];
-  for (int j = 0; j < 4; ++j) {
+  for (int j = 0; j < kWide; ++j) {
     const int c = child[j];
     if (c >= 0) {
       next_roots[m] = c;
@@ -328,7 +341,7 @@ int build_wide(Scene& sc, cudaStream_t st) {
   void* tmp = nullptr;
   size_t tmp_bytes = 0;
   cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, cnt, offs, n_int + 1, st);
-  cudaError_t e = cudaMalloc(&sc.d_wnodes, (size_t)n_int * 8 * sizeof(float4));
+  cudaError_t e = cudaMalloc(&sc.d_wnodes, (size_t)n_int * kWideF4 * sizeof(float4));
   if (e == cudaSuccess) e = cudaMalloc(&ra, n_int * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&rb, n_int * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&cnt, (n_int + 1) * sizeof(int));
@@ -365,6 +378,23 @@ int build_wide(Scene& sc, cudaStream_t st) {
     sc.n_wnodes = wbase;
   }
   cudaFree(ra); cudaFree(rb); cudaFree(cnt); cudaFree(offs); cudaFree(tmp);
+  // the array was sized for the bound (one wide node per binary inner
+  // node); keep only what the tree uses
+  if (status == HM_OK && sc.n_wnodes < n_int) {
+    float4* exact = nullptr;
+    e = cudaMalloc(&exact, (size_t)sc.n_wnodes * kWideF4 * sizeof(float4));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(exact, sc.d_wnodes, (size_t)sc.n_wnodes * kWideF4 * sizeof(float4), cudaMemcpyDeviceToDevice,
+                          st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) {
+      cudaFree(sc.d_wnodes);
+      sc.d_wnodes = exact;
+    } else {
+      cudaFree(exact);
+      status = hm_cuda_status(e, "wide bvh compaction");
+    }
+  }
   return status;
 }
 

@@ -870,7 +870,7 @@ extern "C" int64_t hm_scene_export_size(const hm_scene* h, int which) {
     case HM_SCENE_DIR_LIGHTS: return (int64_t)s->dlights.size() * 4;
     case HM_SCENE_BVH_NODES: return (int64_t)s->n_nodes * 64;
     case HM_SCENE_BVH_LEAVES: return (int64_t)s->n_prims() * 4;
-    case HM_SCENE_BVH_WIDE_NODES: return (int64_t)s->n_wnodes * 128;
+    case HM_SCENE_BVH_WIDE_NODES: return (int64_t)s->n_wnodes * kWideNodeBytes;
     case HM_SCENE_CAMERA: return 12 * 4;
     case HM_SCENE_MATERIALS: return 16 * 4;
     case HM_SCENE_STRAND_GROUPS: return (int64_t)s->strand_group.size() * 4;
@@ -910,7 +910,7 @@ extern "C" int hm_scene_export(const hm_scene* h, int which, void* out, int64_t 
     case HM_SCENE_BVH_WIDE_NODES: {
       if (!s->built) return hm_set_error("hm_scene_export: call hm_scene_build first"), HM_EINVAL;
       int64_t bytes = which == HM_SCENE_BVH_NODES ? (int64_t)s->n_nodes * 64
-                      : which == HM_SCENE_BVH_LEAVES ? (int64_t)s->n_prims() * 4 : (int64_t)s->n_wnodes * 128;
+                      : which == HM_SCENE_BVH_LEAVES ? (int64_t)s->n_prims() * 4 : (int64_t)s->n_wnodes * kWideNodeBytes;
       if (cap < bytes) return hm_set_error("hm_scene_export: buffer too small"), HM_ECAPACITY;
       const void* src = which == HM_SCENE_BVH_NODES ? (const void*)s->d_nodes
                         : which == HM_SCENE_BVH_LEAVES ? (const void*)s->d_prim_of_leaf : (const void*)s->d_wnodes;

@@ -9,6 +9,10 @@
 
 namespace hm {
 
+constexpr int kWide = 8;                  // children per node of the traversed BVH
+constexpr int kWideF4 = 7 * kWide / 4;    // float4 per wide node (6 bounds + 1 code per child)
+constexpr int kWideNodeBytes = 16 * kWideF4;
+
 HM_D f3 ldf3(const float3* p) {
   const float* q = reinterpret_cast<const float*>(p);
   return mk(__ldg(q), __ldg(q + 1), __ldg(q + 2));
@@ -42,9 +46,10 @@ struct SceneDev {
   const float4* nodes;  // 4 float4 per node
   int n_nodes;
   const int* prim_of_leaf;  // leaf slot -> primitive id
-  // the same tree collapsed to 4-wide nodes (what the traversal walks):
-  // 8 float4 per node, lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
-  // child[4] (>= 0 wide node, < 0 leaf ~slot), padding
+  // the same tree collapsed to kWide-wide nodes (what the traversal walks):
+  // kWideF4 float4 per node, lo.x[8] hi.x[8] lo.y[8] hi.y[8] lo.z[8] hi.z[8]
+  // child[8] (>= 0 wide node, < 0 leaf ~slot; empty slots: code -1 and the
+  // box [+inf, +inf], which every ray misses)
   const float4* wnodes;
   int n_wnodes;
   // environment (lat-long, z up) and its sampling tables

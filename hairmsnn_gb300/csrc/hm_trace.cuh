@@ -2,11 +2,11 @@
 // round-cubic curve and triangle intersectors, which the reference reaches
 // through owl::traceRay in hair_msnn.cu:62 and optix_common.cuh:189,257).
 //
-// The kernels walk the LBVH collapsed to 4-wide nodes (128 B, 8 x float4:
-// lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] padding; child
-// >= 0 wide node, < 0 leaf slot ~i; empty slots hold a box that every ray
-// misses).  Children hit are visited nearest first; the others go on a
-// 96-entry stack with their entry distance.  A ray whose stack would
+// The kernels walk the LBVH collapsed to 8-wide nodes (224 B, 14 x float4:
+// lo.x[8] hi.x[8] lo.y[8] hi.y[8] lo.z[8] hi.z[8] child[8]; child >= 0 wide
+// node, < 0 leaf slot ~i; empty slots hold a box that every ray misses).
+// The nearest child hit is visited next; the others go on a 96-entry stack
+// with their entry distance, farthest first.  A ray whose stack would
 // overflow or whose visit count passes a fixed cap is reported through the
 // error word instead of looping or writing out of bounds.
 //
@@ -35,7 +35,7 @@ struct Hit {
 };
 
 enum { TRACE_ERR_STACK = 1, TRACE_ERR_STEPS = 2 };
-constexpr int kStack = 96;  // (child, distance) entries of the 4-wide traversal
+constexpr int kStack = 96;  // (child, distance) entries of the wide traversal
 constexpr int kMaxVisits = 1 << 20;
 
 
@@ -185,50 +185,52 @@ struct TraceCount {
   uint32_t nodes, prims;
 };
 
-// Slab test of the four children of wide node ni: entry distance per child
-// (INFINITY: missed or empty slot) and the child codes.
-HM_D void wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, float tmin, float tmax, float (&t)[4],
-                     int (&c)[4]) {
-  const float4* p = wn + 8 * (int64_t)ni;
-  const float4 lx = __ldg(p), hx = __ldg(p + 1), ly = __ldg(p + 2), hy = __ldg(p + 3), lz = __ldg(p + 4),
-               hz = __ldg(p + 5);
-  const int4 ch = __ldg(reinterpret_cast<const int4*>(p + 6));
-  const float alx[4] = {lx.x, lx.y, lx.z, lx.w}, ahx[4] = {hx.x, hx.y, hx.z, hx.w};
-  const float aly[4] = {ly.x, ly.y, ly.z, ly.w}, ahy[4] = {hy.x, hy.y, hy.z, hy.w};
-  const float alz[4] = {lz.x, lz.y, lz.z, lz.w}, ahz[4] = {hz.x, hz.y, hz.z, hz.w};
+// Slab test of the kWide children of wide node ni: entry distance per child
+// (INFINITY: missed or empty slot) and the child codes.  oct bit a is set
+// when the ray's direction is negative along axis a: the near plane of every
+// box is then its upper bound, so each slab needs one plane per side and no
+// min/max pairs (the near and far bound arrays are picked by address).
+HM_D void wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, int oct, float tmin, float tmax,
+                     float (&t)[kWide], int (&c)[kWide]) {
+  constexpr int G = kWide / 4;  // float4 per bound array
+  const float4* p = wn + kWideF4 * (int64_t)ni;
+  const int sx = oct & 1, sy = (oct >> 1) & 1, sz = (oct >> 2) & 1;
+  const float4* nxp = p + sx * G;
+  const float4* fxp = p + (1 - sx) * G;
+  const float4* nyp = p + (2 + sy) * G;
+  const float4* fyp = p + (3 - sy) * G;
+  const float4* nzp = p + (4 + sz) * G;
+  const float4* fzp = p + (5 - sz) * G;
+  const float nx = -o.x * inv.x, ny = -o.y * inv.y, nz = -o.z * inv.z;
 #pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const float tx0 = (alx[k] - o.x) * inv.x, tx1 = (ahx[k] - o.x) * inv.x;
-    const float ty0 = (aly[k] - o.y) * inv.y, ty1 = (ahy[k] - o.y) * inv.y;
-    const float tz0 = (alz[k] - o.z) * inv.z, tz1 = (ahz[k] - o.z) * inv.z;
-    const float tn = fmaxf(fmaxf(fminf(tx0, tx1), fminf(ty0, ty1)), fmaxf(fminf(tz0, tz1), tmin));
-    const float tf = fminf(fminf(fmaxf(tx0, tx1), fmaxf(ty0, ty1)), fminf(fmaxf(tz0, tz1), tmax));
-    t[k] = tn <= tf ? tn : INFINITY;
-  }
-  c[0] = ch.x;
-  c[1] = ch.y;
-  c[2] = ch.z;
-  c[3] = ch.w;
-}
-
-HM_D void cswap(float (&t)[4], int (&c)[4], int i, int j) {
-  if (t[j] < t[i]) {
-    const float tt = t[i];
-    t[i] = t[j];
-    t[j] = tt;
-    const int cc = c[i];
-    c[i] = c[j];
-    c[j] = cc;
+  for (int q = 0; q < G; ++q) {
+    const float4 a0 = __ldg(nxp + q), a1 = __ldg(fxp + q), b0 = __ldg(nyp + q), b1 = __ldg(fyp + q),
+                 c0 = __ldg(nzp + q), c1 = __ldg(fzp + q);
+    const int4 cv = __ldg(reinterpret_cast<const int4*>(p + 6 * G + q));
+    const float n_x[4] = {a0.x, a0.y, a0.z, a0.w}, f_x[4] = {a1.x, a1.y, a1.z, a1.w};
+    const float n_y[4] = {b0.x, b0.y, b0.z, b0.w}, f_y[4] = {b1.x, b1.y, b1.z, b1.w};
+    const float n_z[4] = {c0.x, c0.y, c0.z, c0.w}, f_z[4] = {c1.x, c1.y, c1.z, c1.w};
+    const int cc[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const float tn = fmaxf(fmaxf(fmaf(n_x[k], inv.x, nx), fmaf(n_y[k], inv.y, ny)),
+                             fmaxf(fmaf(n_z[k], inv.z, nz), tmin));
+      const float tf = fminf(fminf(fmaf(f_x[k], inv.x, nx), fmaf(f_y[k], inv.y, ny)),
+                             fminf(fmaf(f_z[k], inv.z, nz), tmax));
+      t[4 * q + k] = tn <= tf ? tn : INFINITY;
+      c[4 * q + k] = cc[k];
+    }
   }
 }
 
-// Resumable traversal of the 4-wide tree: one node visit per inner step, so
+// Resumable traversal of the wide tree: one node visit per inner step, so
 // a persistent kernel can hand a lane a new ray as soon as its previous ray
 // finishes (dynamic ray fetching, Aila & Laine, HPG 2009).  The stack holds
 // (child code, entry distance) pairs; entries beyond the closest hit found
 // so far are dropped when popped.
 struct TravState {
   f3 o, d, inv;
+  int oct;  // bit a: direction negative along axis a
   float tmin;
   Hit h;
   int node;
@@ -243,6 +245,7 @@ HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
   t.inv = mk(fabsf(d.x) > 1e-20f ? 1.f / d.x : copysignf(1e20f, d.x),
              fabsf(d.y) > 1e-20f ? 1.f / d.y : copysignf(1e20f, d.y),
              fabsf(d.z) > 1e-20f ? 1.f / d.z : copysignf(1e20f, d.z));
+  t.oct = (t.inv.x < 0.f ? 1 : 0) | (t.inv.y < 0.f ? 2 : 0) | (t.inv.z < 0.f ? 4 : 0);
   t.tmin = tmin;
   t.h = Hit{tmax, -1, 0.f, 0.f};
   t.node = 0;
@@ -287,35 +290,47 @@ HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err
       return;
     }
   }
-  float tt[4];
-  int cc[4];
-  wnode_test(s.wnodes, cur, t.o, t.inv, t.tmin, t.h.t, tt, cc);
+  float tt[kWide];
+  int cc[kWide];
+  wnode_test(s.wnodes, cur, t.o, t.inv, t.oct, t.tmin, t.h.t, tt, cc);
   if (COUNT) cnt->nodes += 1;
-  // ascending by entry distance (misses sort last)
-  cswap(tt, cc, 0, 1);
-  cswap(tt, cc, 2, 3);
-  cswap(tt, cc, 0, 2);
-  cswap(tt, cc, 1, 3);
-  cswap(tt, cc, 1, 2);
-  const int hits = (tt[0] < INFINITY) + (tt[1] < INFINITY) + (tt[2] < INFINITY) + (tt[3] < INFINITY);
-  if (hits == 0) {
+  unsigned m = 0;
+#pragma unroll
+  for (int k = 0; k < kWide; ++k) m |= (tt[k] < INFINITY ? 1u : 0u) << k;
+  if (m == 0) {
     t.node = -1;
     return;
   }
-  if (t.sp + hits - 1 > kStack) {
+  if (t.sp + __popc(m) - 1 > kStack) {
     atomicOr(err, TRACE_ERR_STACK);
     t.node = -1;
     t.sp = 0;
     return;
   }
+  // children hit but the nearest go on the stack farthest first (a ray hits
+  // one or two children of most nodes, so this loop is short)
+  while (m & (m - 1)) {
+    float tf = -1.f;
+    int cf = 0, kf = 0;
 #pragma unroll
-  for (int k = 3; k >= 1; --k)
-    if (k < hits) stack[t.sp++] = make_int2(cc[k], __float_as_int(tt[k]));
-  if (cc[0] < 0) {
-    t.pend = ~cc[0];
+    for (int k = 0; k < kWide; ++k)
+      if (((m >> k) & 1u) && tt[k] >= tf) {
+        tf = tt[k];
+        cf = cc[k];
+        kf = k;
+      }
+    stack[t.sp++] = make_int2(cf, __float_as_int(tf));
+    m &= ~(1u << kf);
+  }
+  int cn = 0;
+#pragma unroll
+  for (int k = 0; k < kWide; ++k)
+    if ((m >> k) & 1u) cn = cc[k];
+  if (cn < 0) {
+    t.pend = ~cn;
     t.node = -1;
   } else {
-    t.node = cc[0];
+    t.node = cn;
   }
 }
 

@@ -21,7 +21,7 @@ DTYPES = dict(control_points=(np.float32, 4), segments=(np.int32, 1), vertices=(
               normals=(np.float32, 3), triangles=(np.int32, 3), env=(np.float32, 4), env_cpdf=(np.float32, 1),
               env_ccdf=(np.float32, 1), env_mpdf=(np.float32, 1), env_mcdf=(np.float32, 1),
               dir_lights=(np.float32, 6), bvh_nodes=(np.float32, 16), bvh_leaves=(np.int32, 1),
-              camera=(np.float32, 12), materials=(np.float32, 16), bvh_wide_nodes=(np.float32, 32),
+              camera=(np.float32, 12), materials=(np.float32, 16), bvh_wide_nodes=(np.float32, 56),
               strand_groups=(np.int32, 1), group_materials=(np.float32, 10), segment_groups=(np.int32, 1))
 PT, MSNN, NRC = 0, 1, 2
 IMAGE_FINAL, IMAGE_SHORT, IMAGE_CACHE = 0, 1, 2
@@ -415,14 +415,14 @@ def straight_hair_scene(width=512, height=512, strands=10000, control_points=64,
 
 
 RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
-NODE_BYTES = 128              # one 4-wide BVH node: four child boxes + child codes
+NODE_BYTES = 224              # one 8-wide BVH node: eight child boxes + child codes
 PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
-# DRAM bytes per extension ray of the extension traversal kernel (4-wide
+# DRAM bytes per extension ray of the extension traversal kernel (8-wide
 # BVH), from ncu (dram__bytes_read.sum + dram__bytes_write.sum) of the first
-# launch of a 256x256 frame of this scene: 28.0 MB for its 65,536 camera
+# launch of a 256x256 frame of this scene: 42.1 MB for its 65,536 camera
 # rays.  ncu runs each launch with cold caches, so this is an upper bound
 # for warm frames.
-EXTEND_DRAM_BYTES_PER_RAY = 427
+EXTEND_DRAM_BYTES_PER_RAY = 643
 
 
 class RenderBenchWorkload:
@@ -579,8 +579,8 @@ class RenderBenchWorkload:
                         "traffic": (int(rays * EXTEND_DRAM_BYTES_PER_RAY) if dominant == "extend_ms" else None),
                         "traffic_basis": "DRAM bytes per frame: ncu cold-cache capture at 256x256 scaled by rays",
                         "algorithmic_bytes_per_frame": int(alg),
-                        "note": ("algorithmic bytes = rays x 48 B + 4-wide BVH nodes visited x 128 B + primitives "
-                                 "tested x 64 B, counted in an untimed frame; the 40 MB BVH and 10 MB of curves "
+                        "note": ("algorithmic bytes = rays x 48 B + 8-wide BVH nodes visited x 224 B + primitives "
+                                 "tested x 64 B, counted in an untimed frame; the 90 MB BVH and 10 MB of curves "
                                  "are L2-resident, so this can exceed the HBM copy peak ("
                                  + pk["source"] + ")")})
         else:
@@ -604,7 +604,7 @@ class RenderBenchWorkload:
                 "cache_precision": "fp16" if self.cache_precision == 1 else "fp32",
                 "pixels": self.P, "train_records": self.train_records,
                 "l2": "inputs larger than L2: each frame in flight streams its own ~90 MB path state, with "
-                      "several frames in flight, past the 129 MB L2 (scene: 4-wide BVH 40 MB + curves 10 MB); "
+                      "several frames in flight, past the 129 MB L2 (scene: 8-wide BVH 90 MB + curves 10 MB); "
                       "no flush kernel",
                 "frames_in_flight": self.r.depth(),
                 "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
@@ -1026,7 +1026,7 @@ class DiffBenchWorkload:
                                                                            "compact_ms", "infer_ms")},
                 "rays_per_forward_frame": {"extension": int(c.extension_rays), "shadow": int(c.shadow_rays)},
                 "algorithmic_bytes_per_frame": int(alg),
-                "note": ("algorithmic bytes = rays x 48 B + 4-wide BVH nodes visited x 128 B + primitives tested "
+                "note": ("algorithmic bytes = rays x 48 B + 8-wide BVH nodes visited x 224 B + primitives tested "
                          "x 64 B, counted in an untimed forward frame; the replay re-traces the same rays. "
                          "Peak " + pk["source"])}
 

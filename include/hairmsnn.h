@@ -215,7 +215,7 @@ typedef struct hm_scene_desc {
   int shading_catrom; /* 1: curves shaded as Catmull-Rom (reference closest-hit quirk) */
   float scene_scale;
   float bounds_min[3], bounds_max[3];
-  int n_bvh_wide_nodes; /* 4-wide nodes traversed by the kernels (0 before the build) */
+  int n_bvh_wide_nodes; /* 8-wide nodes traversed by the kernels (0 before the build) */
   int n_groups;         /* strand groups with their own material (0: one material) */
   int segment_splits;   /* BVH leaves per hair segment (integrator.segment_splits: 1, 2 (default), 4);
                            HM_SCENE_BVH_LEAVES ids: segment k's part j is k + j * n_segments,
@@ -238,9 +238,9 @@ enum hm_scene_array {
   HM_SCENE_BVH_LEAVES = 12,    /* int32 primitive of each leaf slot */
   HM_SCENE_CAMERA = 13,        /* pos, dir_00, dir_du, dir_dv (12 floats) */
   HM_SCENE_MATERIALS = 14,     /* 16 floats: hair params, diffuse, alpha, env scale/rotation */
-  HM_SCENE_BVH_WIDE_NODES = 15, /* 128 bytes each: lo.x[4] hi.x[4] lo.y[4] hi.y[4] lo.z[4] hi.z[4]
-                                   child[4] (>= 0 wide node, < 0 leaf ~slot) + 16 bytes of padding;
-                                   empty slots hold the box [+inf, +inf] */
+  HM_SCENE_BVH_WIDE_NODES = 15, /* 224 bytes each: lo.x[8] hi.x[8] lo.y[8] hi.y[8] lo.z[8] hi.z[8]
+                                   child[8] (>= 0 wide node, < 0 leaf ~slot); empty slots hold
+                                   code -1 and the box [+inf, +inf] */
   HM_SCENE_STRAND_GROUPS = 16,   /* int32 group of each strand (empty: one material) */
   HM_SCENE_GROUP_MATERIALS = 17, /* hm_hair_params of each group */
   HM_SCENE_SEGMENT_GROUPS = 18   /* int32 group of each segment (empty: one material) */

@@ -226,15 +226,25 @@ def _render_nrc(self, accum_id=0, every_nth=1, n_train=0, c=0.01, p0=0, n=None, 
 OracleScene.render_nrc = _render_nrc
 
 
-def wide_collapse(nodes):
-    """The 4-wide tree the kernels traverse, built from the binary LBVH
+def _half_area(lo, hi):
+    """Surface area / 2 of float32 boxes, in the library's operation order."""
+    ex = hi[..., 0] - lo[..., 0]
+    ey = hi[..., 1] - lo[..., 1]
+    ez = hi[..., 2] - lo[..., 2]
+    return (ex * ey + ey * ez) + ex * ez
+
+
+def wide_collapse(nodes, width=8):
+    """The 8-wide tree the kernels traverse, built from the binary LBVH
     (nodes [n, 16] float32: child-0 box, child-1 box, child codes) the way
     the library collapses it: breadth first, the wide node of binary node r
-    holds r's children with every internal child replaced by its own two
-    children; wide nodes are numbered level by level in the order their
-    parents list them.  Returns [n_wide, 32] float32: lo.x[4] hi.x[4]
-    lo.y[4] hi.y[4] lo.z[4] hi.z[4] child[4] (int bits; >= 0 wide node,
-    < 0 leaf ~slot, -1 in empty slots whose box is [+inf, +inf]) padding."""
+    starts with r's two children; while it has fewer than 8, its internal
+    child of largest surface area (the first of equals) is replaced by that
+    child's first child and the second child is appended.  Wide nodes are
+    numbered level by level in the order their parents list them.  Returns
+    [n_wide, 56] float32: lo.x[8] hi.x[8] lo.y[8] hi.y[8] lo.z[8] hi.z[8]
+    child[8] (int bits; >= 0 wide node, < 0 leaf ~slot, -1 in empty slots
+    whose box is [+inf, +inf])."""
     nodes = np.ascontiguousarray(nodes, np.float32)
     codes = nodes.view(np.int32)[:, 12:14]
     boxes = nodes[:, :12].reshape(-1, 2, 6)
@@ -243,35 +253,39 @@ def wide_collapse(nodes):
     base = 0
     while len(roots):
         n = len(roots)
-        lo = np.full((n, 4, 3), np.inf, np.float32)
-        hi = np.full((n, 4, 3), np.inf, np.float32)
-        kc = np.full((n, 4), -1, np.int32)
-        k = np.zeros(n, np.int64)
         rows = np.arange(n)
+        lo = np.full((n, width, 3), np.inf, np.float32)
+        hi = np.full((n, width, 3), np.inf, np.float32)
+        kc = np.full((n, width), -1, np.int32)
+        area = np.zeros((n, width), np.float32)
         for slot in (0, 1):
-            c = codes[roots, slot]
-            leaf = c < 0
-            i = rows[leaf]
-            lo[i, k[i]] = boxes[roots[i], slot, :3]
-            hi[i, k[i]] = boxes[roots[i], slot, 3:]
-            kc[i, k[i]] = c[leaf]
-            k[i] += 1
-            i = rows[~leaf]
-            ci = c[~leaf]
-            for s2 in (0, 1):
-                lo[i, k[i]] = boxes[ci, s2, :3]
-                hi[i, k[i]] = boxes[ci, s2, 3:]
-                kc[i, k[i]] = codes[ci, s2]
-                k[i] += 1
+            lo[:, slot] = boxes[roots, slot, :3]
+            hi[:, slot] = boxes[roots, slot, 3:]
+            kc[:, slot] = codes[roots, slot]
+            area[:, slot] = _half_area(lo[:, slot], hi[:, slot])
+        k = np.full(n, 2, np.int64)
+        for _ in range(width - 2):
+            cand = (kc >= 0) & (np.arange(width)[None] < k[:, None])
+            r = rows[cand.any(1)]
+            if not len(r):
+                break
+            best = np.argmax(np.where(cand[r], area[r], -np.inf), axis=1)
+            c = kc[r, best].astype(np.int64)
+            for slot, col in ((0, best), (1, k[r])):
+                lo[r, col] = boxes[c, slot, :3]
+                hi[r, col] = boxes[c, slot, 3:]
+                kc[r, col] = codes[c, slot]
+                area[r, col] = _half_area(lo[r, col], hi[r, col])
+            k[r] += 1
         internal = kc >= 0
         nxt = kc[internal].astype(np.int64)
         kc = kc.copy()
         kc[internal] = base + n + np.arange(len(nxt), dtype=np.int32)
-        w = np.zeros((n, 32), np.float32)
+        w = np.zeros((n, 7 * width), np.float32)
         for a in range(3):
-            w[:, 8 * a:8 * a + 4] = lo[:, :, a]
-            w[:, 8 * a + 4:8 * a + 8] = hi[:, :, a]
-        w[:, 24:28] = kc.view(np.float32)
+            w[:, 2 * a * width:(2 * a + 1) * width] = lo[:, :, a]
+            w[:, (2 * a + 1) * width:(2 * a + 2) * width] = hi[:, :, a]
+        w[:, 6 * width:] = kc.view(np.float32)
         out.append(w)
         base += n
         roots = nxt

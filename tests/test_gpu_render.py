@@ -1,7 +1,7 @@
 """GPU parity of the scene LBVH, traversal and wavefront integrator.
 
 * BVH: device node array == the oracle's host build, bit for bit; so is
-  the 4-wide collapse the kernels traverse (1, 2 or 4 leaves per segment).
+  the 8-wide collapse the kernels traverse (1, 2 or 4 leaves per segment).
 * Traversal: same closest primitive for >= 99.5% of rays; t within
   1e-4 relative where the primitive matches (the device contracts
   multiply-adds in traversal; the oracle does not).

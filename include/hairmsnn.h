@@ -305,7 +305,7 @@ typedef struct hm_render_options {
   int cache_precision;           /* HM_PREC_* */
   uint32_t seed;                 /* cache initialisation */
   const char* cache_config_json; /* NULL: the scene's tcnn.config, else the built-in one */
-  int frames_in_flight;          /* frames pipelined on their own streams (1..8); 0: up to 6,
+  int frames_in_flight;          /* frames pipelined on their own streams (1..8); 0: up to 8,
                                     fewer when their path state would pass ~2 GB */
   float nrc_c;                   /* NRC spread threshold multiplier c (0: 0.01, render_nrc.h:132) */
 } hm_render_options;

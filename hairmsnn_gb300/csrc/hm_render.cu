@@ -63,19 +63,36 @@ struct ShadowRays {
   const int* queue;
   const int* count;
   uint8_t* vis;  // [P][2]: 1 = unoccluded
+  // ray i < count: the light sample of queued path i; ray count + i: its
+  // BSDF sample.  Light samples share few directions (the directional
+  // lights, the bright part of the sky), so keeping the two kinds apart
+  // keeps a warp's rays alike.
   HM_D int n() const { return 2 * *count; }
-  HM_D int path(int i) const { return queue[i >> 1]; }
+  HM_D int entry(int i, int* slot) const {
+    const int c = *count;
+    *slot = i >= c ? 1 : 0;
+    return *slot ? i - c : i;
+  }
+  HM_D int path(int i) const {
+    int slot;
+    return queue[entry(i, &slot)];
+  }
   HM_D bool ray(int i, f3* o, f3* d) const {
-    const int pid = queue[i >> 1];
+    int slot;
+    const int pid = queue[entry(i, &slot)];
     if (!(ps.flags[pid] & F_DL)) return false;
-    const float4 a = (i & 1) ? ps.sh_o1[pid] : ps.sh_o0[pid];
+    const float4 a = slot ? ps.sh_o1[pid] : ps.sh_o0[pid];
     if (a.w == 0.f) return false;
-    const float4 b = (i & 1) ? ps.sh_d1[pid] : ps.sh_d0[pid];
+    const float4 b = slot ? ps.sh_d1[pid] : ps.sh_d0[pid];
     *o = mk(a.x, a.y, a.z);
     *d = mk(b.x, b.y, b.z);
     return true;
   }
-  HM_D void write(int i, const Hit& h) const { vis[2 * queue[i >> 1] + (i & 1)] = h.prim < 0 ? 1 : 0; }
+  HM_D void write(int i, const Hit& h) const {
+    int slot;
+    const int pid = queue[entry(i, &slot)];
+    vis[2 * pid + slot] = h.prim < 0 ? 1 : 0;
+  }
 };
 
 struct BatchRays {

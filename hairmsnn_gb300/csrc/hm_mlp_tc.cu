@@ -257,12 +257,21 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
         // bin of x on the period [0, 1) (x itself may lie outside it)
         b0 = (((int)floorf(x * nb)) % s.n_bins + s.n_bins) % s.n_bins;
         const float c0 = oneblob_cdf(0.f, x, nb);
+        // mass of window bin t = right edge - left edge; bin t's right edge
+        // is bin t+1's left edge (+1 where bin t is the last bin: the edge
+        // wraps to 0), so six edge evaluations give the five masses
+        float left[5];
+        int wb[5];
 #pragma unroll
         for (int t = 0; t < 5; ++t) {
-          const int wb = ((b0 - 2 + t) % s.n_bins + s.n_bins) % s.n_bins;
-          const float left = wb == 0 ? c0 : oneblob_cdf((float)wb / nb, x, nb);
-          const float right = (wb == s.n_bins - 1) ? c0 + 1.f : oneblob_cdf((float)(wb + 1) / nb, x, nb);
-          wv[t] = right - left;
+          wb[t] = ((b0 - 2 + t) % s.n_bins + s.n_bins) % s.n_bins;
+          left[t] = wb[t] == 0 ? c0 : oneblob_cdf((float)wb[t] / nb, x, nb);
+        }
+        const float right4 = (wb[4] == s.n_bins - 1) ? c0 + 1.f : oneblob_cdf((float)(wb[4] + 1) / nb, x, nb);
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+          const float right = t < 4 ? ((wb[t] == s.n_bins - 1) ? left[t + 1] + 1.f : left[t + 1]) : right4;
+          wv[t] = right - left[t];
         }
       };
       window(dim);

@@ -193,10 +193,12 @@ class VertexWorkload:
                 "note": f"peak = {pk['source']} ({'HBM copy' if bound == 'hbm' else 'cuBLAS bf16 burst'})",
                 "per_kernel_ms": {k: round(v[4], 4) for k, v in segs.items()}}
 
+    workload_name = ("vertex: 2^18 hair-vertex queries, BSDF eval+sample (alpha=2deg, beta_m=beta_n=0.3, "
+                     "sigma_a=(0.06,0.1,0.2)) + cache MLP Freq12/OneBlob32/Identity->5x64 FP16 on tcgen05 "
+                     "(FP32 accumulation)")
+
     def config(self):
-        return {"workload": "vertex: 2^18 hair-vertex queries, BSDF eval+sample (alpha=2deg, beta_m=beta_n=0.3, "
-                            "sigma_a=(0.06,0.1,0.2)) + cache MLP Freq12/OneBlob32/Identity->5x64 FP16 on tcgen05 "
-                            "(FP32 accumulation)",
+        return {"workload": self.workload_name,
                 "queries": self.n, "l2": "flushed between timed steps (256 MiB write)",
                 "parallelism": "replicas"}
 
@@ -410,7 +412,8 @@ def run_reference(args):
             mo.forward(cfg, params, x)
         units, metric, unit = n, VertexWorkload.metric, VertexWorkload.unit
         sample = f"{n} queries per step (oracle port: C++ BSDF on {threads} threads + FP64 numpy MLP)"
-        cfgd = {"workload": "vertex (bounded sample)", "queries_per_step": n}
+        cfgd = {"workload": VertexWorkload.workload_name, "sample": "bounded: queries_per_step of the workload",
+                "queries_per_step": n}
     else:
         from hairmsnn_gb300 import build as hb
         from hairmsnn_gb300 import render as hr
@@ -432,7 +435,8 @@ def run_reference(args):
         sample = (f"{n} pixels (1 spp) per step of the 512x512 render: the reference's per-pixel path code "
                   f"(rayGenCam / msnnPathTrace / msnnTrainingPath, oracle port) on {threads} threads; "
                   f"cache network not included")
-        cfgd = {"workload": "render (bounded pixel sample per step)", "pixels_per_step": n}
+        cfgd = {"workload": hr.RenderBenchWorkload.workload_name,
+                "sample": "bounded: pixels_per_step of the frame per step", "pixels_per_step": n}
     for _ in range(args.warmup):
         step()
     times = []

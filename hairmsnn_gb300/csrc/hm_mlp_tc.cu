@@ -264,7 +264,12 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
         int wb[5];
 #pragma unroll
         for (int t = 0; t < 5; ++t) {
-          wb[t] = ((b0 - 2 + t) % s.n_bins + s.n_bins) % s.n_bins;
+          // (b0 - 2 + t) mod n_bins: b0 is in [0, n_bins), so with two or
+          // more bins one correction lands in range (one bin: always 0)
+          int w = b0 - 2 + t;
+          w += w < 0 ? s.n_bins : 0;
+          w -= w >= s.n_bins ? s.n_bins : 0;
+          wb[t] = s.n_bins == 1 ? 0 : w;
           left[t] = wb[t] == 0 ? c0 : oneblob_cdf((float)wb[t] / nb, x, nb);
         }
         const float right4 = (wb[4] == s.n_bins - 1) ? c0 + 1.f : oneblob_cdf((float)(wb[4] + 1) / nb, x, nb);

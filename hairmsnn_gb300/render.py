@@ -596,11 +596,13 @@ class RenderBenchWorkload:
                         "1 BVH leaf per segment; same scene and GPU"}
         return out
 
+    workload_name = ("render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments, 2 BVH "
+                     "leaves each), 20k-tri head, Preetham sky T=3 + directional (3,3,3), 512x512, "
+                     "path_v1=1, path_v2=40, BETA=1, cache HashGrid/OneBlob MLP 64x2 in FP16 on tcgen05 "
+                     "(training and inference; FP32 master weights), 2^16 training records/frame")
+
     def config(self):
-        return {"workload": "render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments, 2 BVH "
-                            "leaves each), 20k-tri head, Preetham sky T=3 + directional (3,3,3), 512x512, "
-                            "path_v1=1, path_v2=40, BETA=1, cache HashGrid/OneBlob MLP 64x2 in FP16 on tcgen05 "
-                            "(training and inference; FP32 master weights), 2^16 training records/frame",
+        return {"workload": self.workload_name,
                 "cache_precision": "fp16" if self.cache_precision == 1 else "fp32",
                 "pixels": self.P, "train_records": self.train_records,
                 "l2": "inputs larger than L2: each frame in flight streams its own ~90 MB path state, with "

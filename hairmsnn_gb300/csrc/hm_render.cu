@@ -494,8 +494,10 @@ struct Render {
   int depth = 0;  // 0: chosen from the frame size in render_setup
   std::vector<Slot> slots;
   double *acc_pt = nullptr, *acc_nn = nullptr, *acc_final = nullptr;
-  cudaEvent_t ev_submit = nullptr, ev_mlp = nullptr, ev_compose = nullptr, ev_read = nullptr;
-  bool have_mlp_ev = false, have_compose_ev = false, have_read_ev = false;
+  double* read_stage = nullptr;  // hm_render_read_async: device snapshot of the sums being read
+  cudaEvent_t ev_submit = nullptr, ev_mlp = nullptr, ev_compose = nullptr, ev_read = nullptr,
+              ev_staged = nullptr;
+  bool have_mlp_ev = false, have_compose_ev = false, have_read_ev = false, have_staged_ev = false;
   int* h_count = nullptr;  // pinned (synchronous instrumented frames)
   std::vector<void*> allocs;
   int64_t rays_extend = 0;
@@ -528,7 +530,7 @@ struct Render {
     if (h_count) cudaFreeHost(h_count);
     if (mlp) hm_mlp_destroy(mlp);
     for (auto e : ev) cudaEventDestroy(e);
-    for (cudaEvent_t e : {ev_submit, ev_mlp, ev_compose, ev_read})
+    for (cudaEvent_t e : {ev_submit, ev_mlp, ev_compose, ev_read, ev_staged})
       if (e) cudaEventDestroy(e);
   }
   cudaEvent_t event(size_t i) {
@@ -645,6 +647,7 @@ static int render_setup(Render* r, const hm_render_options* o) {
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_mlp, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_compose, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_read, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&r->ev_staged, cudaEventDisableTiming);
   if (e != cudaSuccess) return hm_cuda_status(e, "render buffers");
   cudaMemset(r->acc_pt, 0, (size_t)P * 3 * sizeof(double));
   cudaMemset(r->acc_nn, 0, (size_t)P * 3 * sizeof(double));
@@ -1114,11 +1117,20 @@ extern "C" int hm_render_read_async(hm_render* h, int which, double* host_dst, v
   if (r->mode != MODE_MSNN && which != HM_IMAGE_FINAL)
     return hm_set_error("hm_render_read_async: PT and NRC renders have only the final image"), HM_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
+  const size_t bytes = (size_t)r->P * 3 * sizeof(double);
+  cudaError_t e = cudaSuccess;
+  if (!r->read_stage) e = r->alloc(&r->read_stage, (size_t)r->P * 3);
+  // the sums are snapshotted on the device and the host copy is made from the
+  // snapshot, so the next frame's accumulation waits only for the device copy
   if (r->have_compose_ev) cudaStreamWaitEvent(s, r->ev_compose, 0);
-  cudaError_t e = cudaMemcpyAsync(host_dst, src, (size_t)r->P * 3 * sizeof(double), cudaMemcpyDeviceToHost, s);
+  if (r->have_staged_ev) cudaStreamWaitEvent(s, r->ev_staged, 0);  // the previous host copy is done
+  if (e == cudaSuccess) e = cudaMemcpyAsync(r->read_stage, src, bytes, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = cudaEventRecord(r->ev_read, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host_dst, r->read_stage, bytes, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaEventRecord(r->ev_staged, s);
   if (e != cudaSuccess) return hm_cuda_status(e, "hm_render_read_async");
   r->have_read_ev = true;
+  r->have_staged_ev = true;
   return HM_OK;
 }
 

@@ -375,7 +375,9 @@ int hm_render_frames_in_flight(const hm_render* render);
 int hm_render_wait(hm_render* render, void* stream);
 /* Asynchronous read-back on `stream` of the FP64 running sums (divide by the
  * number of frames) of all frames enqueued so far, [H][W][3]; host_dst should
- * be pinned.  The next frame's accumulation waits for the copy. */
+ * be pinned.  The sums are first copied to a device snapshot (allocated on
+ * the first call, P x 3 doubles) and the host copy is made from it: the next
+ * frame's accumulation waits only for the device copy. */
 int hm_render_read_async(hm_render* render, int which, double* host_dst, void* stream);
 /* Restart accumulation (the reference's cameraChanged resets accumId). */
 int hm_render_reset(hm_render* render);

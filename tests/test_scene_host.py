@@ -118,6 +118,39 @@ def test_oracle_bvh_is_a_valid_hierarchy(R):
     assert sorted(seen) == list(range(len(leaves)))
 
 
+@pytest.mark.parametrize("strands", [1, 300])
+def test_wide_collapse_structure(R, strands):
+    """The 8-wide restatement over the oracle's LBVH: every leaf slot in
+    exactly one wide slot, child boxes copied bit for bit from the binary
+    tree (a wide child box is a binary child box, never a union), wide
+    nodes numbered breadth first, and the greedy fill: a node with fewer
+    than eight children holds only leaves."""
+    cfg = small()
+    cfg["hair"]["procedural"]["strands"] = strands
+    if strands == 1:
+        cfg.pop("surface", None)
+    s = R.Scene(cfg)
+    nodes, leaves = po.OracleScene.from_library(s).bvh()
+    w = po.wide_collapse(nodes)
+    codes = w[:, 48:56].view(np.int32)
+    empty = np.isinf(w[:, 0:8]) & np.isinf(w[:, 8:16]) & (codes == -1)
+    used = ~empty
+    n_used = used.sum(1)
+    assert np.all(n_used >= 2)
+    assert np.all((n_used == 8) | np.all((codes < 0) | ~used, axis=1))
+    # every wide child box is one of the binary child boxes, bit for bit
+    bbox = np.ascontiguousarray(nodes[:, :12]).reshape(-1, 6).view(np.dtype((np.void, 24))).ravel()
+    wbox = np.stack([w[:, 0:8], w[:, 16:24], w[:, 32:40], w[:, 8:16], w[:, 24:32], w[:, 40:48]], -1)
+    wbox = np.ascontiguousarray(wbox[used]).view(np.dtype((np.void, 24))).ravel()
+    assert np.isin(wbox, bbox).all()
+    rows = np.nonzero(used)[0]
+    c = codes[used]
+    assert np.all((c < 0) | ((c > rows) & (c < len(w))))
+    assert np.array_equal(np.sort(~c[c < 0]), np.arange(len(leaves)))
+    internal = codes[codes >= 0]
+    assert np.array_equal(internal, np.arange(1, len(w)))  # breadth-first numbering
+
+
 def test_oracle_render_runs_and_is_deterministic(R):
     s = R.Scene(small())
     o = po.OracleScene.from_library(s)

@@ -171,9 +171,9 @@ HM_D uint32_t pack4_e4m3(float a, float b, float c, float d) {
 
 // ---------------------------------------------------------------- encoding
 // Features are produced in increasing order and packed through a 128-bit
-// shift register into 16-byte groups, one conflict-free shared-memory store
-// per group (the 32 rows of a warp are 32 consecutive 16-byte core-matrix
-// rows).
+// shift register into 16-byte groups, one conflict-free store per group
+// (the 32 rows of a warp are 32 consecutive 16-byte core-matrix rows);
+// 16-bit operands take consecutive features in pairs where they can.
 template <int PREC>
 struct RowPacker {
   static constexpr int kPer = PREC == TC_E4M3 ? 16 : 8;  // values per 16 bytes
@@ -197,12 +197,29 @@ struct RowPacker {
     w1 = __funnelshift_r(w1, w2, SH);
     w2 = __funnelshift_r(w2, w3, SH);
     w3 = (w3 >> SH) | (h << (32 - SH));
-    if (++cnt == kPer) {
-      *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, group * 16)) = make_uint4(w0, w1, w2, w3);
-      if (mirror) *reinterpret_cast<uint4*>(mirror + group * 16) = make_uint4(w0, w1, w2, w3);
-      ++group;
-      cnt = 0;
+    if (++cnt == kPer) flush();
+  }
+  // Two consecutive features: for 16-bit operands at an even fill, one
+  // paired conversion (the same round-to-nearest of each value) and one
+  // 32-bit step of the register; otherwise two pushes.
+  HM_D void push2(float a, float b) {
+    if (PREC == TC_E4M3 || (cnt & 1)) {
+      push(a);
+      push(b);
+      return;
     }
+    w0 = w1;
+    w1 = w2;
+    w2 = w3;
+    w3 = pack2<PREC>(a, b);
+    cnt += 2;
+    if (cnt == kPer) flush();
+  }
+  HM_D void flush() {
+    *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, group * 16)) = make_uint4(w0, w1, w2, w3);
+    if (mirror) *reinterpret_cast<uint4*>(mirror + group * 16) = make_uint4(w0, w1, w2, w3);
+    ++group;
+    cnt = 0;
   }
 };
 
@@ -224,20 +241,27 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
     if (lo >= hi) continue;
     const int j0 = lo - s.out_off, j1 = hi - s.out_off;
     if (s.type == ENC_IDENTITY) {
-      for (int j = j0; j < j1; ++j) pk.push(xin[s.in_off + j]);
+      int j = j0;
+      for (; j + 1 < j1; j += 2) pk.push2(xin[s.in_off + j], xin[s.in_off + j + 1]);
+      if (j < j1) pk.push(xin[s.in_off + j]);
     } else if (s.type == ENC_FREQUENCY) {
       int u = j0 >> 1;
       int dim = u / s.n_freq, f = u - dim * s.n_freq;
       for (int j = j0; j < j1;) {
         float sn, cs;
         sincospif(ldexpf(xin[s.in_off + dim], f), &sn, &cs);
-        if (!(j & 1)) {
-          pk.push(sn);
-          ++j;
-        }
-        if (j < j1) {
-          pk.push(cs);
-          ++j;
+        if (!(j & 1) && j + 1 < j1) {
+          pk.push2(sn, cs);
+          j += 2;
+        } else {
+          if (!(j & 1)) {
+            pk.push(sn);
+            ++j;
+          }
+          if (j < j1) {
+            pk.push(cs);
+            ++j;
+          }
         }
         if (++f == s.n_freq) {
           f = 0;
@@ -280,8 +304,8 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
         }
       };
       window(dim);
-      for (int j = j0; j < j1; ++j) {
-        int dd = b - b0;
+      auto bin_value = [&](int bb) {
+        int dd = bb - b0;
         if (dd > (s.n_bins >> 1)) dd -= s.n_bins;
         if (dd < -(s.n_bins >> 1)) dd += s.n_bins;
         float v = 0.f;
@@ -290,8 +314,19 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
         v = dd == 0 ? wv[2] : v;
         v = dd == 1 ? wv[3] : v;
         v = dd == 2 ? wv[4] : v;
-        pk.push(v);
-        if (++b == s.n_bins && j + 1 < j1) {
+        return v;
+      };
+      for (int j = j0; j < j1;) {
+        if (b + 1 < s.n_bins && j + 1 < j1) {  // two bins of the same dimension
+          pk.push2(bin_value(b), bin_value(b + 1));
+          b += 2;
+          j += 2;
+        } else {
+          pk.push(bin_value(b));
+          ++b;
+          ++j;
+        }
+        if (b == s.n_bins && j < j1) {
           b = 0;
           ++dim;
           window(dim);
@@ -321,16 +356,30 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
             if (q < s.n_feat) acc[q] += w * __ldg(tv + q);
         }
 #pragma unroll
-        for (int q = 0; q < 8; ++q)
-          if (q >= f0 && q < s.n_feat && j < j1) {
-            pk.push(acc[q]);
-            ++j;
+        for (int q = 0; q < 8; q += 2) {
+          const bool ok0 = q >= f0 && q < s.n_feat && j < j1;
+          const bool ok1 = q + 1 >= f0 && q + 1 < s.n_feat && j + (ok0 ? 1 : 0) < j1;
+          if (ok0 && ok1) {
+            pk.push2(acc[q], acc[q + 1]);
+            j += 2;
+          } else {
+            if (ok0) {
+              pk.push(acc[q]);
+              ++j;
+            }
+            if (ok1) {
+              pk.push(acc[q + 1]);
+              ++j;
+            }
           }
+        }
         f0 = 0;
       }
     }
   }
-  for (int k = max(kb, d.n_enc); k < ke; ++k) pk.push(k < d.in_pad ? 1.f : 0.f);
+  int k = max(kb, d.n_enc);
+  for (; k + 1 < ke; k += 2) pk.push2(k < d.in_pad ? 1.f : 0.f, k + 1 < d.in_pad ? 1.f : 0.f);
+  if (k < ke) pk.push(k < d.in_pad ? 1.f : 0.f);
 }
 
 // Upper bound of |feature| over the row (E4M3 input scale).

@@ -203,26 +203,26 @@ class VertexWorkload:
                 "parallelism": "replicas"}
 
     def cpu_baseline(self, threads, budget_s=10.0):
-        """Oracle port: BSDF eval + sample (C++ threads) + FP64 numpy MLP, bounded sample."""
-        import numpy as np
+        """Oracle port in C++ on the host threads: BSDF eval + sample and the
+        cache network's FP32 inference (hm_oracle_mlp.cpp), bounded sample."""
         from oracle import mlp_oracle as mo
         from oracle import pyoracle as po
         n = 1 << 14
         wo, wi, t, h, u = po.gen_bsdf_queries(0, n)
         cfg = mo.Config(self.net.config_text, 16, 3)
-        params = self.net.params().astype(np.float64)
+        params = self.net.params()
         x = self.x_host[:n].numpy()
         reps, t0 = 0, time.perf_counter()
         while True:
             po.hair_eval(wo.T, wi.T, t.T, h, threads=threads)
             po.hair_sample(wo.T, t.T, h, u.T, threads=threads)
-            mo.forward(cfg, params, x)
+            po.mlp_forward_host(cfg, params, x, threads=threads)
             reps += 1
             el = time.perf_counter() - t0
             if el > budget_s or reps >= 50:
                 break
         return {"value": round(reps * n / el, 1), "unit": self.unit, "cores": threads, "kind": "port",
-                "sample": f"{reps} x {n} queries (eval+sample C++ on {threads} threads, MLP FP64 numpy)"}
+                "sample": f"{reps} x {n} queries (eval + sample and FP32 MLP inference, C++ on {threads} threads)"}
 
 
 # ========================================================= precision workload
@@ -409,9 +409,9 @@ def run_reference(args):
         def step():
             po.hair_eval(wo.T, wi.T, t.T, h, threads=threads)
             po.hair_sample(wo.T, t.T, h, u.T, threads=threads)
-            mo.forward(cfg, params, x)
+            po.mlp_forward_host(cfg, params, x, threads=threads)
         units, metric, unit = n, VertexWorkload.metric, VertexWorkload.unit
-        sample = f"{n} queries per step (oracle port: C++ BSDF on {threads} threads + FP64 numpy MLP)"
+        sample = f"{n} queries per step (oracle port: BSDF and FP32 MLP inference in C++ on {threads} threads)"
         cfgd = {"workload": VertexWorkload.workload_name, "sample": "bounded: queries_per_step of the workload",
                 "queries_per_step": n}
     else:

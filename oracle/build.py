@@ -19,7 +19,7 @@ REF_DIR = os.environ.get("HM_REF_DIR", "/root/reference")
 OUT_DIR = os.path.join(HERE, "_ref")
 ORACLE_DIR = os.path.join(HERE, "_build")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "libhmoracle.so")
-ORACLE_SOURCES = ["hm_oracle.cpp", "hm_oracle_render.cpp"]
+ORACLE_SOURCES = ["hm_oracle.cpp", "hm_oracle_render.cpp", "hm_oracle_mlp.cpp"]
 ORACLE_HEADERS = ["hm_oracle.h", "hm_oracle_math.h"]
 
 

@@ -38,6 +38,8 @@ def lib():
         L.hmo_hair_eval.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P]
         L.hmo_hair_sample.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P]
         L.hmo_hair_eval_mt.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
+        L.hmo_mlp_forward.restype = None
+        L.hmo_mlp_forward.argtypes = [F32P, i64, i32, I32P, i32, i32, i32, F32P, I32P, i32, i32, F32P, i32]
         L.hmo_hair_sample_mt.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
         L.hmo_gen_bsdf_queries.argtypes = [u32, i64, F32P, F32P, F32P, F32P, F32P]
         L.hmo_frostbite_ggx.argtypes = [F32P, F32P, F32P, f32, F32P]
@@ -374,3 +376,25 @@ def gen_bsdf_queries(seed, n):
     u = np.zeros((4, n), np.float32)
     lib().hmo_gen_bsdf_queries(seed, n, wo, wi, t, h, u)
     return wo, wi, t, h, u
+
+
+def mlp_forward_host(cfg, params, x, threads=1):
+    """The cache network's inference as the oracle's C++ FP32 transcription
+    on `threads` host threads (hm_oracle_mlp.cpp): cfg an mlp_oracle.Config
+    with Identity / Frequency / OneBlob encodings, params the network
+    weights (then encoding params), x [n, in_ch] -> [n, out_ch] float32."""
+    kinds = {"Identity": 0, "Frequency": 1, "OneBlob": 2}
+    seg = []
+    for s in cfg.segs:
+        if s["type"] not in kinds:
+            raise ValueError("host transcription: %s encoding not supported" % s["type"])
+        seg.append([kinds[s["type"]], s["in_off"], s["n_dims"], s["out_off"],
+                    s.get("n_freq", s.get("n_bins", 0))])
+    seg = np.ascontiguousarray(seg, np.int32).ravel()
+    shapes = np.ascontiguousarray([[fo, fi] for _, fo, fi in cfg.layer_shapes], np.int32).ravel()
+    w = f32(np.asarray(params)[:cfg.n_net_params])
+    x = f32(x)
+    out = np.zeros((x.shape[0], cfg.out_ch), np.float32)
+    lib().hmo_mlp_forward(x, x.shape[0], cfg.in_ch, seg, len(cfg.segs), cfg.n_enc, cfg.in_pad, w, shapes,
+                          len(cfg.layer_shapes), cfg.out_ch, out, int(threads))
+    return out

@@ -135,3 +135,20 @@ def test_oracle_output_grad_backward_matches_finite_differences():
         p2[i] -= eps
         fd = (f(p1) - f(p2)) / (2 * eps)
         assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd, g[i])
+
+
+@pytest.mark.parametrize("name", ["c1_cache_w64.json", "c1_cache_w128.json"])
+def test_host_mlp_transcription_matches_fp64_oracle(name):
+    """The C++ FP32 transcription of the cache network (the CPU baseline of
+    the vertex workload) against the FP64 statement: within 1e-4 of the rms
+    output on 4096 C1-style queries, the same on 1 and 4 threads."""
+    from oracle import pyoracle as po
+    cfg = mo.Config(cfg_text(name), 16, 3)
+    rng = np.random.default_rng(3)
+    params = rng.normal(scale=0.1, size=cfg.n_params)
+    x = rng.uniform(0, 1, (4096, 16)).astype(np.float32)
+    ref = mo.forward(cfg, params, x)[0][:, :3]
+    y1 = po.mlp_forward_host(cfg, params, x, threads=1)
+    y4 = po.mlp_forward_host(cfg, params, x, threads=4)
+    assert np.array_equal(y1, y4)
+    assert np.abs(y1 - ref).max() <= 1e-4 * np.sqrt((ref ** 2).mean())

@@ -163,3 +163,37 @@ def test_oracle_render_runs_and_is_deterministic(R):
     blocks = ((fl & 4) != 0).reshape(-1, 4).sum(axis=1)
     assert np.all(blocks == 1)
     assert np.isfinite(tr).all()
+
+
+def test_wide_collapse_expansion_order():
+    """A hand-built binary tree: the internal child of largest area is
+    opened first, in place (its first child takes its slot, the second is
+    appended); equal areas open the earlier slot."""
+    def box(lo, hi):
+        return list(lo) + list(hi)
+
+    def node(b0, c0, b1, c1):
+        return np.array(box(*b0) + box(*b1) + [0.0, 0.0, 0.0, 0.0], np.float32), (c0, c1)
+
+    unit = ((0, 0, 0), (1, 1, 1))
+    big = ((0, 0, 0), (4, 4, 4))
+    small = ((0, 0, 0), (2, 2, 2))
+    # 0: [1 (big), 2 (small)]; 1: [leaf 0, leaf 1]; 2: [3 (small), leaf 2]; 3: [leaf 3, leaf 4]
+    spec = [(big, 1, small, 2), (unit, ~0, unit, ~1), (small, 3, unit, ~2), (unit, ~3, unit, ~4)]
+    nodes = np.zeros((4, 16), np.float32)
+    for i, (b0, c0, b1, c1) in enumerate(spec):
+        v, cc = node(b0, c0, b1, c1)
+        nodes[i] = v
+        nodes[i, 12:14] = np.array(cc, np.int32).view(np.float32)
+    w = po.wide_collapse(nodes)
+    assert w.shape == (1, 56)
+    codes = w[0, 48:56].view(np.int32)
+    assert list(codes) == [~0, ~3, ~1, ~2, ~4, -1, -1, -1]
+    # equal areas: the earlier slot opens first
+    nodes[0, :12] = np.array(box(*small) + box(*small), np.float32)
+    w = po.wide_collapse(nodes)
+    assert list(w[0, 48:56].view(np.int32)) == [~0, ~3, ~1, ~2, ~4, -1, -1, -1]
+    nodes[0, :12] = np.array(box(*small) + box(*big), np.float32)
+    w = po.wide_collapse(nodes)
+    # node 2 opens first: [1, 3, 2] -> 1 opens -> [0, 3, 2, 1] -> 3 opens -> [0, 3', 2, 1, 4]
+    assert list(w[0, 48:56].view(np.int32)) == [~0, ~3, ~2, ~1, ~4, -1, -1, -1]

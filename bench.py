@@ -111,6 +111,17 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x, ws, device="cuda"):
+    """The largest of the ranks' x (x itself on one rank): the job's time is
+    its slowest rank's."""
+    if ws <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 # ============================================================ vertex workload
 class VertexWorkload:
     name = "vertex"
@@ -515,10 +526,7 @@ def main():
         torch.distributed.barrier()
     clocks = sampler.stop()
     launches = wl.kernels_per_step * args.steps
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, ws)
     units = wl.units_per_step() * ws
     value = units / (ms * 1e-3)
 
@@ -536,10 +544,7 @@ def main():
             wl.e2e_step()
         torch.cuda.synchronize()
         e2e_ms = 1e3 * (time.perf_counter() - t0) / e2e_steps
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, ws)
 
     if rank != 0:
         return 0

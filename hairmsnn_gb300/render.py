@@ -615,7 +615,8 @@ class RenderBenchWorkload:
     def cpu_baseline(self, threads, budget_s=20.0):
         """The oracle's reference-structured integrator (rayGenCam G-buffer pass,
         msnnPathTrace / msnnTrainingPath) on the host cores, bounded sample of
-        pixels of the same scene; cache inference + one training step in FP64 numpy."""
+        pixels of the same scene; the cache's inference and training gradient
+        by the oracle's C++ FP32 transcription on the same threads."""
         import time
         from oracle import mlp_oracle as mo
         from oracle import pyoracle as po
@@ -632,10 +633,10 @@ class RenderBenchWorkload:
         while True:
             col, nn_in, tr, fl = o.render_pixels(1, beta=1, accum_id=done // self.P, every_nth=every,
                                                  n_train=self.train_records, p0=p0, n=n, threads=threads)
-            mo.forward(oc, params, nn_in)
+            po.mlp_forward_host(oc, params, nn_in, threads=threads)
             tmask = (fl & 4) != 0
             if tmask.any():
-                mo.backward(oc, params, nn_in[tmask], tr[tmask])
+                po.mlp_grad_host(oc, params, nn_in[tmask], tr[tmask], threads=threads)
             done += n
             p0 = (p0 + n) % (self.P - n)
             if time.perf_counter() - t0 > budget_s:
@@ -643,7 +644,8 @@ class RenderBenchWorkload:
         el = time.perf_counter() - t0
         return {"value": round(done / el, 1), "unit": self.unit, "cores": threads, "kind": "port",
                 "sample": f"{done} pixels (1 spp) of the same scene: oracle rayGenCam/msnnPathTrace/"
-                          f"msnnTrainingPath on {threads} threads + FP64 numpy cache inference and training"}
+                          f"msnnTrainingPath on {threads} threads + the cache's inference and training "
+                          f"gradient in C++ FP32 on the same threads"}
 
 
 class RenderQualityWorkload(RenderBenchWorkload):

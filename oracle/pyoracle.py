@@ -39,7 +39,11 @@ def lib():
         L.hmo_hair_sample.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P]
         L.hmo_hair_eval_mt.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
         L.hmo_mlp_forward.restype = None
-        L.hmo_mlp_forward.argtypes = [F32P, i64, i32, I32P, i32, i32, i32, F32P, I32P, i32, i32, F32P, i32]
+        L.hmo_mlp_forward.argtypes = [F32P, i64, i32, I32P, i32, i32, i32, F32P, i64, I32P, i32, i32,
+                                      F32P, I32P, I32P, I32P, F32P, i32]
+        L.hmo_mlp_grad.restype = ctypes.c_double
+        L.hmo_mlp_grad.argtypes = [F32P, F32P, i64, i32, I32P, i32, i32, i32, F32P, i64, i64, I32P, i32, i32,
+                                   F32P, I32P, I32P, I32P, i32, F32P, i32]
         L.hmo_hair_sample_mt.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
         L.hmo_gen_bsdf_queries.argtypes = [u32, i64, F32P, F32P, F32P, F32P, F32P]
         L.hmo_frostbite_ggx.argtypes = [F32P, F32P, F32P, f32, F32P]
@@ -378,23 +382,55 @@ def gen_bsdf_queries(seed, n):
     return wo, wi, t, h, u
 
 
-def mlp_forward_host(cfg, params, x, threads=1):
-    """The cache network's inference as the oracle's C++ FP32 transcription
-    on `threads` host threads (hm_oracle_mlp.cpp): cfg an mlp_oracle.Config
-    with Identity / Frequency / OneBlob encodings, params the network
-    weights (then encoding params), x [n, in_ch] -> [n, out_ch] float32."""
-    kinds = {"Identity": 0, "Frequency": 1, "OneBlob": 2}
-    seg = []
+def _mlp_desc(cfg):
+    """Segment and hash-grid level tables of an mlp_oracle.Config in the
+    layout hm_oracle_mlp.cpp reads."""
+    kinds = {"Identity": 0, "Frequency": 1, "OneBlob": 2, "HashGrid": 3, "Grid": 3}
+    seg, scale, res, size, off = [], [], [], [], []
     for s in cfg.segs:
         if s["type"] not in kinds:
             raise ValueError("host transcription: %s encoding not supported" % s["type"])
-        seg.append([kinds[s["type"]], s["in_off"], s["n_dims"], s["out_off"],
-                    s.get("n_freq", s.get("n_bins", 0))])
-    seg = np.ascontiguousarray(seg, np.int32).ravel()
+        k = kinds[s["type"]]
+        if k == 3:
+            seg.append([k, s["in_off"], s["n_dims"], s["out_off"], s["n_levels"], s["n_feat"], len(scale),
+                        s["param_off"]])
+            for sc, rs, sz, of in s["levels"]:
+                scale.append(sc)
+                res.append(rs)
+                size.append(sz)
+                off.append(of)
+        else:
+            seg.append([k, s["in_off"], s["n_dims"], s["out_off"], s.get("n_freq", s.get("n_bins", 0)), 0, 0, 0])
     shapes = np.ascontiguousarray([[fo, fi] for _, fo, fi in cfg.layer_shapes], np.int32).ravel()
-    w = f32(np.asarray(params)[:cfg.n_net_params])
+    lv = (f32(scale + [0.0]), np.ascontiguousarray(res + [0], np.int32), np.ascontiguousarray(size + [0], np.int32),
+          np.ascontiguousarray(off + [0], np.int32))
+    return np.ascontiguousarray(seg, np.int32).ravel(), shapes, lv
+
+
+def mlp_forward_host(cfg, params, x, threads=1):
+    """The cache network's inference as the oracle's C++ FP32 transcription
+    on `threads` host threads (hm_oracle_mlp.cpp): cfg an mlp_oracle.Config,
+    params the network weights then the encoding parameters, x [n, in_ch]
+    -> [n, out_ch] float32."""
+    seg, shapes, lv = _mlp_desc(cfg)
+    w = f32(np.asarray(params)[:cfg.n_params])
     x = f32(x)
     out = np.zeros((x.shape[0], cfg.out_ch), np.float32)
-    lib().hmo_mlp_forward(x, x.shape[0], cfg.in_ch, seg, len(cfg.segs), cfg.n_enc, cfg.in_pad, w, shapes,
-                          len(cfg.layer_shapes), cfg.out_ch, out, int(threads))
+    lib().hmo_mlp_forward(x, x.shape[0], cfg.in_ch, seg, len(cfg.segs), cfg.n_enc, cfg.in_pad, w,
+                          cfg.n_net_params, shapes, len(cfg.layer_shapes), cfg.out_ch, *lv, out, int(threads))
     return out
+
+
+def mlp_grad_host(cfg, params, x, target, threads=1):
+    """The loss (cfg.loss) over the rows and its gradient with respect to
+    every parameter, as the C++ FP32 transcription: (loss, grads [n_params]
+    float32)."""
+    seg, shapes, lv = _mlp_desc(cfg)
+    w = f32(np.asarray(params)[:cfg.n_params])
+    x, target = f32(x), f32(target)
+    grads = np.zeros(cfg.n_params, np.float32)
+    kind = {"L2": 0, "RelativeL2": 1}.get(cfg.loss, 2)
+    loss = lib().hmo_mlp_grad(x, target, x.shape[0], cfg.in_ch, seg, len(cfg.segs), cfg.n_enc, cfg.in_pad, w,
+                              cfg.n_net_params, cfg.n_params, shapes, len(cfg.layer_shapes), cfg.out_ch, *lv, kind,
+                              grads, int(threads))
+    return loss, grads

@@ -137,18 +137,30 @@ def test_oracle_output_grad_backward_matches_finite_differences():
         assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(g[i])), (i, fd, g[i])
 
 
-@pytest.mark.parametrize("name", ["c1_cache_w64.json", "c1_cache_w128.json"])
-def test_host_mlp_transcription_matches_fp64_oracle(name):
-    """The C++ FP32 transcription of the cache network (the CPU baseline of
-    the vertex workload) against the FP64 statement: within 1e-4 of the rms
-    output on 4096 C1-style queries, the same on 1 and 4 threads."""
+@pytest.mark.parametrize("name,in_ch", [("c1_cache_w64.json", 16), ("c1_cache_w128.json", 16),
+                                        ("hairmsnn_cache.json", 12)])
+def test_host_mlp_transcription_matches_fp64_oracle(name, in_ch):
+    """The C++ FP32 transcription of the cache network (the CPU baselines'
+    cache work) against the FP64 statement on 2048 random queries: outputs
+    within 1e-4 of their rms, the loss within 1e-5, every gradient
+    (weights and hash-grid tables) within 1e-4 of the largest; the same
+    results on 1 and 4 threads."""
     from oracle import pyoracle as po
-    cfg = mo.Config(cfg_text(name), 16, 3)
+    cfg = mo.Config(cfg_text(name), in_ch, 3)
     rng = np.random.default_rng(3)
     params = rng.normal(scale=0.1, size=cfg.n_params)
-    x = rng.uniform(0, 1, (4096, 16)).astype(np.float32)
+    params[cfg.n_net_params:] = rng.uniform(-1e-2, 1e-2, cfg.n_params - cfg.n_net_params)
+    x = rng.uniform(0, 1, (2048, in_ch)).astype(np.float32)
+    target = rng.uniform(0, 1, (2048, 3)).astype(np.float32)
     ref = mo.forward(cfg, params, x)[0][:, :3]
     y1 = po.mlp_forward_host(cfg, params, x, threads=1)
     y4 = po.mlp_forward_host(cfg, params, x, threads=4)
     assert np.array_equal(y1, y4)
     assert np.abs(y1 - ref).max() <= 1e-4 * np.sqrt((ref ** 2).mean())
+    l_ref, g_ref = mo.backward(cfg, params, x, target)
+    l_c, g_c = po.mlp_grad_host(cfg, params, x, target, threads=4)
+    assert abs(l_c - l_ref) <= 1e-5 * abs(l_ref)
+    assert np.abs(g_c - g_ref).max() <= 1e-4 * np.abs(g_ref).max()
+    if cfg.n_params > cfg.n_net_params:  # the tables' gradients on their own scale
+        gt, rt = g_c[cfg.n_net_params:], g_ref[cfg.n_net_params:]
+        assert np.abs(gt - rt).max() <= 1e-4 * np.abs(rt).max()

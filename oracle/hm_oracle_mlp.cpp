@@ -270,6 +270,10 @@ double hmo_mlp_grad(const float* x, const float* target, int64_t n, int in_ch, c
                     const int* lvl_size, const int* lvl_off, int loss_kind, float* grads, int threads) {
   const Net m{seg, n_segs, n_enc, in_pad, in_ch, params, n_net_params, shapes, n_layers, out_ch,
               lvl_scale, lvl_res, lvl_size, lvl_off};
+  if (n <= 0) {
+    std::fill(grads, grads + n_params, 0.f);
+    return 0.0;
+  }
   threads = std::max(1, threads);
   const int64_t per = (n + threads - 1) / threads;
   const double total = (double)n * out_ch;

@@ -164,3 +164,5 @@ def test_host_mlp_transcription_matches_fp64_oracle(name, in_ch):
     if cfg.n_params > cfg.n_net_params:  # the tables' gradients on their own scale
         gt, rt = g_c[cfg.n_net_params:], g_ref[cfg.n_net_params:]
         assert np.abs(gt - rt).max() <= 1e-4 * np.abs(rt).max()
+    l0, g0 = po.mlp_grad_host(cfg, params, x[:0], target[:0], threads=2)  # no rows: zero loss and gradient
+    assert l0 == 0.0 and not g0.any()

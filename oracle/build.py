@@ -45,10 +45,15 @@ def build_oracle(verbose: bool = False) -> str:
         os.replace(tmp, ORACLE_LIB)
     return ORACLE_LIB
 
-# (output library, entry source, extra defines)
+# (output library, entry source, extra flags, links the oracle library).
+# The integrator targets include the reference's own raygen sources
+# (cuda/hair_msnn.cu, cuda/path_tracing.cu); __CUDA_ARCH__ is defined only so
+# that common.cuh declares its ray types (common.cuh:28-32), and traceRay is
+# answered by the oracle library's BVH.
 TARGETS = [
-    ("libhmref_math.so", "ref_math_entry.cpp", []),
-    ("libhmref_path.so", "ref_path_entry.cpp", ["-D__CUDA_ARCH__=860"]),
+    ("libhmref_math.so", "ref_math_entry.cpp", [], False),
+    ("libhmref_path.so", "ref_path_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
+    ("libhmref_pt.so", "ref_pt_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
 ]
 
 
@@ -63,22 +68,25 @@ def build_ref(verbose: bool = False) -> list:
             print("build_ref: reference checkout not found; skipped")
         return []
     os.makedirs(OUT_DIR, exist_ok=True)
+    oracle_lib = build_oracle()
     built = []
-    for lib, src, defs in TARGETS:
+    for lib, src, defs, link_oracle in TARGETS:
         src_path = os.path.join(HERE, "ref_shim", src)
-        if not os.path.isfile(src_path):
-            continue
         out = os.path.join(OUT_DIR, lib)
         deps = [src_path, os.path.join(HERE, "ref_shim", "hm_owl_shim.h"),
+                os.path.join(HERE, "ref_shim", "ref_harness.h"), os.path.join(HERE, "ref_shim", "ref_eval_order.h"),
                 os.path.join(HERE, "hm_oracle.h"), os.path.join(HERE, "hm_oracle.cpp")]
+        if link_oracle:
+            deps.append(oracle_lib)
         if not _stale(out, deps):
             built.append(out)
             continue
+        link = ["-L", ORACLE_DIR, "-lhmoracle", "-Wl,-rpath,$ORIGIN/../_build"] if link_oracle else []
         cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off",
-               "-fno-fast-math", "-w", *defs,
+               "-fno-fast-math", "-fno-strict-aliasing", "-w", *defs,
                "-I", os.path.join(HERE, "ref_shim"), "-I", HERE,
-               "-I", os.path.join(REF_DIR, "cuda_headers"),
-               src_path, "-o", out, "-lpthread"]
+               "-I", os.path.join(REF_DIR, "cuda_headers"), "-I", os.path.join(REF_DIR, "cuda"),
+               src_path, "-o", out, *link, "-Wl,-Bsymbolic", "-lpthread"]
         if verbose:
             print(" ".join(cmd))
         subprocess.run(cmd, check=True)

@@ -525,9 +525,44 @@ V3 sample_env(const OScene& s, SI& si, uint32_t& rng, float* pdf) {  // sampleEn
   return rval;
 }
 
+// ------------------------------------------------------------ per-path event log
+// Every ray a path traces, in the order it traces them: the record the tests
+// compare with the reference's own integrator (every owl::traceRay call) and
+// with the device's per-path log.  kEvFloats floats per event:
+//   [0] kind (int bits: 0 radiance, 1 light-sample shadow, 2 BSDF-sample shadow)
+//   [1] result (int bits: radiance = hit primitive, -1 miss; shadow = 1 unoccluded)
+//   [2] t of the hit (radiance), [3] u of the hit
+//   [4..6] origin, [7..9] direction, [10] RNG state when the ray was traced
+//   (radiance rays only; uint bits), [11] 0
+constexpr int kEvFloats = 12;
+struct EvLog {
+  float* ev = nullptr;
+  int cap = 0, n = 0;
+};
+thread_local EvLog* tl_log = nullptr;
+
+void log_event(int kind, int result, float t, float u, V3 o, V3 d, uint32_t rng) {
+  EvLog* L = tl_log;
+  if (!L) return;
+  if (L->n < L->cap) {
+    float* e = L->ev + (size_t)L->n * kEvFloats;
+    memcpy(e + 0, &kind, 4);
+    memcpy(e + 1, &result, 4);
+    e[2] = t;
+    e[3] = u;
+    e[4] = o.x; e[5] = o.y; e[6] = o.z;
+    e[7] = d.x; e[8] = d.y; e[9] = d.z;
+    memcpy(e + 10, &rng, 4);
+    e[11] = 0.f;
+  }
+  ++L->n;
+}
+
 // owl::traceRay(RADIANCE): closest hit -> hairCH / triangleMeshCH, else miss.
-void trace_radiance(const OScene& s, V3 o, V3 d, SI& si) {
+// rng: the path's RNG state when the ray is traced (logged only).
+void trace_radiance(const OScene& s, V3 o, V3 d, SI& si, uint32_t rng = 0) {
   OHit h = trace(s, o, d, 0.f, 1e30f, false);
+  log_event(0, h.prim < 0 ? -1 : h.prim, h.prim < 0 ? 0.f : h.t, h.prim < 0 ? 0.f : h.u, o, d, rng);
   if (h.prim < 0) {  // miss (optix_common.cuh:604-616)
     si.hit = false;
     si.Le = V3(0.f);
@@ -577,7 +612,12 @@ void trace_radiance(const OScene& s, V3 o, V3 d, SI& si) {
   }
 }
 
-bool visible(const OScene& s, V3 o, V3 d) { return trace(s, o, d, 0.f, 1e30f, true).prim < 0; }
+// owl::traceRay(SHADOW); kind 1 = light sample, 2 = BSDF sample (logged only).
+bool visible(const OScene& s, V3 o, V3 d, int kind) {
+  const bool v = trace(s, o, d, 0.f, 1e30f, true).prim < 0;
+  log_event(kind, v ? 1 : 0, 0.f, 0.f, o, d, 0u);
+  return v;
+}
 
 V3 hair_f(const OScene& s, const SI& si, float* pdf) {
   return disney_hair(si.wo_local, si.wi_local, dot(si.to_local[1], si.n), hair_of(s, si), pdf);
@@ -610,7 +650,7 @@ V3 sample_lights(const OScene& s, SI& si, uint32_t& rng, bool& is_delta) {  // s
     nd = -si.n;
     si.p = si.p + 2.f * si.radius * nd;
   }
-  if (visible(s, si.p + 1e-3f * nd, si.wi)) {
+  if (visible(s, si.p + 1e-3f * nd, si.wi, 1)) {
     V3 bsdf(0.f);
     if (!si.surface) {
       bsdf = hair_f(s, si, &bsdf_pdf);
@@ -651,7 +691,7 @@ V3 sample_bsdf(const OScene& s, SI& si, uint32_t& rng) {  // sampleBSDF
     nd = -si.n;
     si.p = si.p + 2.f * si.radius * nd;
   }
-  if (visible(s, si.p + 1e-3f * nd, si.wi)) {
+  if (visible(s, si.p + 1e-3f * nd, si.wi, 2)) {
     int nt = s.n_dl() + (s.has_env ? 1 : 0);
     emit = env_radiance(s, si.wi);
     light_pdf = env_pdf(s, si.wi) * 1.f / nt;
@@ -708,7 +748,7 @@ V3 next_vertex(const OScene& s, SI& si, uint32_t& rng, float* pdf_out = nullptr)
   V3 mul = next_pdf == 0.f ? next_bsdf : next_bsdf / next_pdf;
   if (isnan(mul.x) || isnan(mul.y) || isnan(mul.z)) mul = V3(1.f);
   if (pdf_out) *pdf_out = next_pdf;  // nextPathVertexNRC returns it (nrc.cu:17-66)
-  trace_radiance(s, si.p + 1e-3f * nd, -si.wo, si);
+  trace_radiance(s, si.p + 1e-3f * nd, -si.wo, si, rng);
   return mul;
 }
 
@@ -945,7 +985,7 @@ void hmo_render_nrc(void* h, int accum_id, int every_nth, int n_train, float c, 
       si.hit = false;
       si.wo = -1.f * dir;
       si.wi = dir;
-      trace_radiance(*s, s->cam_pos, dir, si);
+      trace_radiance(*s, s->cam_pos, dir, si, rng);
       std::unique_ptr<NrcOut> o(new NrcOut());
       memset(o->query, 0, sizeof(o->query));
       memset(o->suffix_query, 0, sizeof(o->suffix_query));
@@ -1018,11 +1058,24 @@ void hmo_trace_rays(void* h, const float* org, const float* dir, int n, float tm
 // (color = the G-buffer's shortPathColor, nn_in = the cache input row,
 // train_out = the training target of a training pixel, flags bit0 hit,
 // bit1 surface, bit2 training pixel).
-void hmo_render_pixels(void* h, int mode, int beta_knob, int accum_id, int every_nth, int n_train, int p0, int np,
-                       float* color, float* nn_in, float* train_out, int* flags, int threads) {
+//
+// hmo_render_pixels_ev: the same, plus each path's event log (events
+// [np][max_events][kEvFloats], see log_event; n_events [np] = events the
+// path traced, possibly more than max_events) and its RNG state when the
+// path ended (rng_end [np]).  events / n_events / rng_end may be NULL.
+void hmo_render_pixels_ev(void* h, int mode, int beta_knob, int accum_id, int every_nth, int n_train, int p0, int np,
+                          float* color, float* nn_in, float* train_out, int* flags, float* events, int* n_events,
+                          uint32_t* rng_end, int max_events, int threads) {
   OScene* s = (OScene*)h;
   auto work = [&](int b, int e) {
+    EvLog log;
     for (int pid = b; pid < e; ++pid) {
+      if (events) {
+        log.ev = events + (size_t)(pid - p0) * max_events * kEvFloats;
+        log.cap = max_events;
+        log.n = 0;
+        tl_log = &log;
+      }
       const int x = pid % s->width, y = pid / s->width;
       uint32_t rng = get_rng(accum_id + 10007, (uint32_t)x, (uint32_t)y, (uint32_t)s->width, (uint32_t)s->height);
       bool training = false;
@@ -1041,7 +1094,7 @@ void hmo_render_pixels(void* h, int mode, int beta_knob, int accum_id, int every
       si.hit = false;
       si.wo = -1.f * dir;
       si.wi = dir;
-      trace_radiance(*s, s->cam_pos, dir, si);
+      trace_radiance(*s, s->cam_pos, dir, si, rng);
       V3 c(0.f), sc(0.f);
       const int i = pid - p0;
       if (mode == 0) {
@@ -1070,7 +1123,10 @@ void hmo_render_pixels(void* h, int mode, int beta_knob, int accum_id, int every
       color[3 * i + 1] = c.y;
       color[3 * i + 2] = c.z;
       flags[i] = (si.hit ? 1 : 0) | (si.hit && si.surface ? 2 : 0) | (training ? 4 : 0);
+      if (n_events) n_events[i] = log.n;
+      if (rng_end) rng_end[i] = rng;
     }
+    tl_log = nullptr;
   };
   if (threads <= 1) {
     work(p0, p0 + np);
@@ -1083,6 +1139,15 @@ void hmo_render_pixels(void* h, int mode, int beta_knob, int accum_id, int every
     if (b < e) pool.emplace_back(work, b, e);
   }
   for (auto& t : pool) t.join();
+}
+
+// The training-pixel permutation (the reference's shuffled trainIdxs table).
+uint32_t hmo_feistel_perm(uint32_t i, uint32_t n, uint32_t key) { return feistel_perm(i, n, key); }
+
+void hmo_render_pixels(void* h, int mode, int beta_knob, int accum_id, int every_nth, int n_train, int p0, int np,
+                       float* color, float* nn_in, float* train_out, int* flags, int threads) {
+  hmo_render_pixels_ev(h, mode, beta_knob, accum_id, every_nth, n_train, p0, np, color, nn_in, train_out, flags,
+                       nullptr, nullptr, nullptr, 0, threads);
 }
 
 }  // extern "C"

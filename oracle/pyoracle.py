@@ -127,6 +127,11 @@ def _declare_render(L):
     L.hmo_trace_rays.argtypes = [vp, F32P, F32P, i32, f32, f32, i32, F32P]
     L.hmo_render_pixels.restype = None
     L.hmo_render_pixels.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, F32P, F32P, F32P, I32P, i32]
+    L.hmo_render_pixels_ev.restype = None
+    L.hmo_render_pixels_ev.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, F32P, F32P, F32P, I32P, F32P, I32P,
+                                       U32P, i32, i32]
+    L.hmo_feistel_perm.restype = ctypes.c_uint32
+    L.hmo_feistel_perm.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
     L.hmo_render_nrc.restype = None
     L.hmo_render_nrc.argtypes = [vp, i32, i32, i32, f32, i32, i32, F32P, F32P, F32P, F32P, I32P, i32]
     L.hmo_scene_set_groups.restype = None
@@ -159,6 +164,9 @@ class OracleScene:
             a["camera"].astype(np.float32).ravel(), a["materials"].astype(np.float32).ravel(), sets,
             float(scene_scale))
         self.width, self.height = int(settings["width"]), int(settings["height"])
+        self.settings = sets
+        self.env_wh = (env_w, env_h)
+        self.scene_scale = float(scene_scale)
 
     @classmethod
     def from_library(cls, scene):
@@ -213,6 +221,83 @@ class OracleScene:
         lib().hmo_render_pixels(self.h, mode, beta, accum_id, every_nth, n_train, p0, n, color, nn_in, train, flags,
                                 threads)
         return color, nn_in, train, flags
+
+
+# Event log of a path (kEvFloats = 12 floats per traced ray, in order):
+# kind (0 radiance, 1 light-sample shadow, 2 BSDF-sample shadow), result
+# (radiance: hit primitive or -1; shadow: 1 unoccluded), t, u, origin[3],
+# direction[3], RNG state when a radiance ray was traced, 0.
+EV_FLOATS = 12
+
+
+def _render_pixels_ev(self, mode, beta=1, accum_id=0, every_nth=1, n_train=0, max_events=128, threads=8):
+    """render_pixels over the whole frame plus every path's ray log:
+    (color, nn_in, train, flags, events [P, max_events, 12] float32,
+    n_events [P], rng_end [P] uint32)."""
+    n = self.width * self.height
+    color = np.zeros((n, 3), np.float32)
+    nn_in = np.zeros((n, 12), np.float32)
+    train = np.zeros((n, 3), np.float32)
+    flags = np.zeros(n, np.int32)
+    ev = np.zeros((n, max_events, EV_FLOATS), np.float32)
+    nev = np.zeros(n, np.int32)
+    rng_end = np.zeros(n, np.uint32)
+    lib().hmo_render_pixels_ev(self.h, mode, beta, accum_id, every_nth, n_train, 0, n, color, nn_in, train, flags,
+                               ev, nev, rng_end, max_events, threads)
+    return color, nn_in, train, flags, ev, nev, rng_end
+
+
+OracleScene.render_pixels_ev = _render_pixels_ev
+
+
+def event_digest(ev, n_ev):
+    """One 64-bit FNV-1a digest per path over its logged rays, in the form
+    the reference's trace hook records them (kinds 1 and 2 both read as
+    shadow rays; the RNG word is left out)."""
+    ev = np.array(ev, np.float32, copy=True)
+    k = ev[:, :, 0].view(np.int32)
+    k[k == 2] = 1
+    ev[:, :, 10] = 0.0
+    raw = ev.view(np.uint8).reshape(len(ev), -1)
+    out = np.zeros(len(ev), np.uint64)
+    per = ev.shape[2] * 4
+    for p in range(len(ev)):
+        h = 0xcbf29ce484222325
+        for b in raw[p, :min(int(n_ev[p]), ev.shape[1]) * per].tobytes():
+            h = ((h ^ b) * 0x100000001b3) & 0xFFFFFFFFFFFFFFFF
+        out[p] = h
+    return out
+
+
+def feistel_perm(i, n, key):
+    """The library's training-pixel permutation of [0, n) (keyed by the frame)."""
+    return int(lib().hmo_feistel_perm(int(i), int(n), int(key) & 0xFFFFFFFF))
+
+
+def msnn_render(gbuf, nn_out, accum_id=0, acc=None):
+    """The RENDER pass of hair_msnn.cu:314-356 in float32: gbuf [P, 8] (hit,
+    isSurface, p, shortPathColor), nn_out [P, 3], acc (dict pt/nn/final of
+    [P, 4] float32 running sums, read when accum_id > 0).  Returns
+    {"acc": ..., "avg": ...} like the reference's six float4 buffers."""
+    f = np.float32
+    g = np.asarray(gbuf, f)
+    sc = g[:, 5:8].copy()
+    nn = np.asarray(nn_out, f).copy()
+    other = (g[:, 0] == 0) | (g[:, 1] != 0)  # escaped or hit the surface
+    color = (sc + nn).astype(f)
+    color[other] = sc[other]
+    nn[other] = sc[other]
+    if accum_id > 0:
+        sc = (sc + np.asarray(acc["pt"], f)[:, :3]).astype(f)
+        nn = (nn + np.asarray(acc["nn"], f)[:, :3]).astype(f)
+        color = (color + np.asarray(acc["final"], f)[:, :3]).astype(f)
+    one = np.ones((len(g), 1), f)
+    out = {"acc": {}, "avg": {}}
+    w = f(f(1.0) / f(accum_id + 1))
+    for k, v in (("pt", sc), ("nn", nn), ("final", color)):
+        out["acc"][k] = np.concatenate([v, one], 1)
+        out["avg"][k] = np.concatenate([(w * v).astype(f), one], 1)
+    return out
 
 
 def _render_nrc(self, accum_id=0, every_nth=1, n_train=0, c=0.01, p0=0, n=None, threads=8):

@@ -89,7 +89,7 @@ struct vec3f {
   vec3f(float a, float b, float c) : x(a), y(b), z(c) {}
   explicit vec3f(const vec4f& o);
   vec3f(const float3& o) : x(o.x), y(o.y), z(o.z) {}
-  explicit vec3f(const float4& o) : x(o.x), y(o.y), z(o.z) {}
+  vec3f(const float4& o) : x(o.x), y(o.y), z(o.z) {}  // implicit, as OWL's
   float& operator[](int i) { return (&x)[i]; }
   const float& operator[](int i) const { return (&x)[i]; }
 };
@@ -195,12 +195,14 @@ inline float3 optixGetWorldRayDirection() { return hm_shim_ctx.ray_dir; }
 inline float2 optixGetTriangleBarycentrics() { return hm_shim_ctx.barycentrics; }
 inline OptixTraversableHandle optixGetGASTraversableHandle() { return 0; }
 inline unsigned optixGetSbtGASIndex() { return 0; }
+// The reference passes a vec4f array cast to float4* (curve_utils.cuh:230):
+// written with memcpy, which may store into objects of any type (the build
+// also uses -fno-strict-aliasing for the reference's casts).
 inline void optixGetCatmullRomVertexData(OptixTraversableHandle, unsigned, unsigned, float, float4* out) {
-  for (int i = 0; i < 4; ++i) out[i] = hm_shim_ctx.cps[i];
+  memcpy((void*)out, hm_shim_ctx.cps, 4 * sizeof(float4));
 }
 inline void optixGetLinearCurveVertexData(OptixTraversableHandle, unsigned, unsigned, float, float4* out) {
-  out[0] = hm_shim_ctx.cps[0];
-  out[1] = hm_shim_ctx.cps[1];
+  memcpy((void*)out, hm_shim_ctx.cps, 2 * sizeof(float4));
 }
 inline void optixTerminateRay() { hm_shim_ctx.terminated = 1; }
 inline void optixIgnoreIntersection() {}

@@ -1,0 +1,179 @@
+"""The oracle's integrator pinned to the reference's own integrator.
+
+The reference's cuda/hair_msnn.cu and cuda/path_tracing.cu (rayGenCam,
+msnnPathTrace, msnnTrainingPath, msnnNextPathVertex, pathTrace, and through
+optix_common.cuh directLighting, sampleLights, sampleBSDF, the environment
+light, hairCH, triangleMeshCH, miss) are compiled unmodified on the host
+(oracle/ref_shim/ref_path_entry.cpp, ref_pt_entry.cpp); owl::traceRay is
+answered by the oracle's BVH, the one closed piece (OptiX's intersector).
+The oracle restatement (oracle/hm_oracle_render.cpp), which the GPU tests
+compare the wavefront kernels with, must reproduce it bit for bit: every
+ray each path traces (kind, hit primitive or visibility, t, u, origin,
+direction), every path colour, cache-input row and training target, and the
+RENDER pass's six float4 buffers.
+
+Two ways: live against the reference-compiled libraries (where the
+reference checkout is present), and against tests/golden/ref_path_golden.npz
+(tests/golden/make_ref_path_golden.py), which carries its scene's arrays and
+so needs neither the reference nor the library.  The scene shades curves
+with the reference's Catmull-Rom interpolator (curve_utils.cuh:226-234).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden", "ref_path_golden.npz")
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def events_as_reference(ev):
+    """The oracle logs light / BSDF shadow rays as kinds 1 / 2 and the RNG
+    state of radiance rays; the reference's trace hook sees a shadow ray
+    type only and no RNG."""
+    ev = np.array(ev, np.float32, copy=True)
+    k = ev[:, :, 0].view(np.int32)
+    k[k == 2] = 1
+    ev[:, :, 10] = 0.0
+    return ev
+
+
+@pytest.fixture(autouse=True)
+def _reference_fp32_mode():
+    po.set_mp_force_fp32(True)  # the reference keeps M_p's log branch in FP32
+    yield
+    po.set_mp_force_fp32(False)
+
+
+# ------------------------------------------------------------------ golden
+@pytest.fixture(scope="module")
+def gold():
+    return np.load(GOLDEN)
+
+
+@pytest.fixture(scope="module")
+def gold_scene(gold):
+    names = ["control_points", "segments", "vertices", "normals", "triangles", "env", "env_cpdf", "env_ccdf",
+             "env_mpdf", "env_mcdf", "dir_lights", "camera", "materials"]
+    s = gold["settings"]
+    settings = dict(width=s[0], height=s[1], path_v1=s[2], path_v2=s[3], mis=s[4], env_pdf=s[5], has_env=s[6],
+                    catrom=s[7], seg_split=s[8], env_w=gold["env_wh"][0], env_h=gold["env_wh"][1])
+    return po.OracleScene({k: gold[k] for k in names}, settings, float(gold["scene_scale"]))
+
+
+def digest(ev, n_ev):
+    return po.event_digest(ev, n_ev)
+
+
+@pytest.mark.parametrize("beta", [1, 3])
+def test_oracle_msnn_gbuffer_matches_reference_golden(gold, gold_scene, beta):
+    en = int(gold["every_nth"])
+    P = gold_scene.width * gold_scene.height
+    col, nn_in, train, flags, ev, nev, _ = gold_scene.render_pixels_ev(1, beta=beta, accum_id=3, every_nth=en,
+                                                                       n_train=P // en, max_events=48)
+    g = gold[f"msnn_b{beta}_gbuf"]
+    assert np.array_equal(bits(col), bits(g[:, 5:8]))
+    assert np.array_equal(flags & 1, g[:, 0].astype(np.int32))
+    assert np.array_equal((flags >> 1) & 1, (g[:, 1] * g[:, 0]).astype(np.int32))
+    assert np.array_equal(bits(nn_in), bits(gold[f"msnn_b{beta}_nn_in"]))
+    tp = np.nonzero(flags & 4)[0]
+    assert len(tp) == P // en
+    assert np.array_equal(bits(train[tp]), bits(gold[f"msnn_b{beta}_train_out"][tp // en]))
+    assert np.array_equal(nev, gold[f"msnn_b{beta}_n_events"])
+    assert nev.max() <= 48
+    assert np.array_equal(digest(ev, nev), gold[f"msnn_b{beta}_events"])
+
+
+def test_oracle_pt_matches_reference_golden(gold, gold_scene):
+    col, _, _, _, ev, nev, _ = gold_scene.render_pixels_ev(0, accum_id=3, max_events=48)
+    assert np.array_equal(bits(col), bits(gold["pt_accum"][:, :3]))
+    assert np.array_equal(nev, gold["pt_n_events"])
+    assert np.array_equal(digest(ev, nev), gold["pt_events"])
+
+
+def test_oracle_render_pass_matches_reference_golden(gold):
+    for a_id, tag in ((0, "first"), (3, "later")):
+        acc = None if a_id == 0 else {k: gold[f"render_acc_in_{k}"] for k in ("pt", "nn", "final")}
+        out = po.msnn_render(gold["msnn_b1_gbuf"], gold["render_nn_out"], accum_id=a_id, acc=acc)
+        for k in ("pt", "nn", "final"):
+            assert np.array_equal(bits(out["acc"][k]), bits(gold[f"render_{tag}_acc_{k}"]))
+            assert np.array_equal(bits(out["avg"][k]), bits(gold[f"render_{tag}_avg_{k}"]))
+
+
+def test_golden_scene_exercises_the_branches(gold):
+    """The fixture reaches the branches a frame bar would hide: head-surface
+    (GGX) vertices, hair vertices, misses, training pixels, multi-bounce paths."""
+    g = gold["msnn_b3_gbuf"]
+    assert (g[:, 0] == 0).sum() > 20          # camera misses
+    assert ((g[:, 0] == 1) & (g[:, 1] == 1)).sum() > 20  # head surface
+    assert ((g[:, 0] == 1) & (g[:, 1] == 0)).sum() > 100  # hair
+    assert gold["msnn_b3_n_events"].max() >= 10
+
+
+# ------------------------------------------------------------------ live
+refpath = pytest.importorskip("oracle.refpath")
+
+
+def _live_scene(strands, v1=1, mis=True, res=48):
+    from hairmsnn_gb300 import render as R
+    cfg = R.straight_hair_scene(res, res, strands=strands, control_points=32, sky_w=128, sky_h=64, triangles=4000)
+    cfg["integrator"]["shade_catmull_rom"] = True
+    cfg["integrator"]["path_v1"] = v1
+    cfg["integrator"]["MIS"] = mis
+    s = R.Scene(cfg)
+    return po.OracleScene.from_library(s)
+
+
+needs_ref = pytest.mark.skipif(not refpath.available(), reason="reference checkout absent (live reference build)")
+
+
+@needs_ref
+@pytest.mark.parametrize("beta,strands,mis", [(1, 2000, True), (2, 4000, True), (4, 2000, False)])
+def test_oracle_msnn_matches_reference_live(beta, strands, mis):
+    o = _live_scene(strands, mis=mis)
+    P = o.width * o.height
+    en = 4
+    ref = refpath.RefIntegrator(o, "path").msnn_gbuffer(beta=beta, accum_id=7, every_nth=en, n_train=P // en,
+                                                         max_events=96)
+    col, nn_in, train, flags, ev, nev, _ = o.render_pixels_ev(1, beta=beta, accum_id=7, every_nth=en,
+                                                              n_train=P // en, max_events=96)
+    assert np.array_equal(bits(col), bits(ref["gbuf"][:, 5:8]))
+    assert np.array_equal(bits(nn_in), bits(ref["nn_in"]))
+    tp = np.nonzero(flags & 4)[0]
+    assert np.array_equal(bits(train[tp]), bits(ref["train_out"][tp // en]))
+    assert np.array_equal(nev, ref["n_events"])
+    assert np.array_equal(bits(events_as_reference(ev)), bits(ref["events"]))
+
+
+@needs_ref
+@pytest.mark.parametrize("v1,mis", [(1, True), (2, True), (1, False)])
+def test_oracle_pt_matches_reference_live(v1, mis):
+    o = _live_scene(3000, v1=v1, mis=mis)
+    ref = refpath.RefIntegrator(o, "pt").pt_frame(accum_id=11, max_events=96)
+    col, _, _, _, ev, nev, _ = o.render_pixels_ev(0, accum_id=11, max_events=96)
+    assert np.array_equal(bits(col), bits(ref["accum"][:, :3]))
+    assert np.array_equal(nev, ref["n_events"])
+    assert np.array_equal(bits(events_as_reference(ev)), bits(ref["events"]))
+
+
+@needs_ref
+def test_oracle_render_pass_matches_reference_live():
+    o = _live_scene(1500, res=32)
+    P = o.width * o.height
+    ref = refpath.RefIntegrator(o, "path")
+    g = ref.msnn_gbuffer(beta=1, accum_id=0, every_nth=4, n_train=P // 4)["gbuf"]
+    nn = np.random.default_rng(1).normal(0, 0.5, (P, 3)).astype(np.float32)
+    acc = {k: np.random.default_rng(2 + j).uniform(0, 3, (P, 4)).astype(np.float32)
+           for j, k in enumerate(("pt", "nn", "final"))}
+    for a_id in (0, 5):
+        r = ref.msnn_render(g, nn, accum_id=a_id, acc=None if a_id == 0 else acc)
+        o_ = po.msnn_render(g, nn, accum_id=a_id, acc=acc)
+        for k in ("pt", "nn", "final"):
+            assert np.array_equal(bits(o_["acc"][k]), bits(r["acc"][k]))
+            assert np.array_equal(bits(o_["avg"][k]), bits(r["avg"][k]))

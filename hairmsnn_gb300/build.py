@@ -19,7 +19,10 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB_PATH = os.path.join(OUT_DIR, "libhairmsnn.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3",
+# Host code is compiled without multiply-add contraction (g++ contracts by
+# default on aarch64 but not on x86-64): the procedural scenes, BVH builds and
+# environment tables come out the same on both.
+NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off",
                      "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills",
                      "-I", os.path.join(ROOT, "include"), "-I", CSRC]
 

@@ -1223,6 +1223,8 @@ extern "C" int hm_mlp_describe_config(const char* config_json, int in_ch, int ou
 //  * The first call on a device resolves the array's address with
 //    cudaGetSymbolAddress with that device current (this can load the
 //    library's device code); make that first call before any stream capture.
+//    The address is cached for the life of the process, so a device reset
+//    (a new primary context) while the library is loaded is not supported.
 constexpr int64_t kNoAllocScratchFloats = (int64_t)1 << 20;
 constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];

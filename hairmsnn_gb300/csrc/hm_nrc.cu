@@ -101,6 +101,10 @@ __global__ void __launch_bounds__(128) nrc_shade_kernel(const __grid_constant__ 
     const bool train = flags & F_TRAIN;
     const int tr = pid / fp.every_nth;
     const f3 ro = ld4(ps.ray_o, pid), rd = ld4(ps.ray_d, pid);
+    const float4 hr = hit ? refit_hit(s, ro, rd, h) : h;
+    if (fp.log.ev)
+      log_ray(fp.log, pid, 3 * k, 0, hit ? __float_as_int(hr.y) : -1, hit ? hr.x : 0.f, hit ? hr.z : 0.f,
+              ps.rng[pid], ro, rd);
     nb.dl_rec[pid] = -1;
     if (k == 0 && !hit) {  // camera ray missed: G-buffer = Le, no cache (rayGenCam, nrc.cu:343-350)
       st4(fb.gbuf, pid, env_radiance(s, rd), 0.f);
@@ -114,7 +118,7 @@ __global__ void __launch_bounds__(128) nrc_shade_kernel(const __grid_constant__ 
       keep[i] = 0;
       continue;
     }
-    const Vertex v = setup_vertex(s, ro, rd, h);
+    const Vertex v = setup_vertex(s, ro, rd, hr);
     float4 sp = nb.spread[pid];  // spread, a0
     f3 beta = ld4(ps.beta, pid);
     if (k == 0) {
@@ -169,6 +173,11 @@ __global__ void __launch_bounds__(128) nrc_shade_kernel(const __grid_constant__ 
     // ---- direct lighting at this vertex
     ShadowSample ss[2];
     direct_lighting(s, v, rng, ss);
+    if (fp.log.ev) {
+      fp.log.vcur[pid] = k;
+      for (int j = 0; j < 2; ++j)
+        if (ss[j].valid) log_ray(fp.log, pid, 3 * k + 1 + j, 1 + j, kLogPending, 0.f, 0.f, 0u, ss[j].o, ss[j].d);
+    }
     st4(ps.sh_o0, pid, ss[0].o, ss[0].valid ? 1.f : 0.f);
     st4(ps.sh_d0, pid, ss[0].d);
     st4(ps.sh_c0, pid, ss[0].c);

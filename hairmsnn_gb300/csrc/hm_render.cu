@@ -236,12 +236,21 @@ __global__ void __launch_bounds__(256) shadow_resolve_kernel(PathState ps, const
                                                              const int* __restrict__ count,
                                                              const uint8_t* __restrict__ vis, DiffParams dp,
                                                              const int* __restrict__ rec_idx = nullptr,
-                                                             float4* __restrict__ rec = nullptr) {
+                                                             float4* __restrict__ rec = nullptr,
+                                                             PathLog log = PathLog{}) {
   const int n = *count;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const int pid = queue[i];
     const uint32_t flags = ps.flags[pid];
     if (!(flags & F_DL)) continue;
+    if (log.ev) {  // the shadow rays' results into the path's ray log
+      const int k = log.vcur[pid];
+      for (int j = 0; j < 2; ++j) {
+        const int slot = 3 * k + 1 + j;
+        if ((j ? ps.sh_o1[pid].w : ps.sh_o0[pid].w) != 0.f && slot < log.slots)
+          log.ev[((size_t)pid * log.slots + slot) * 3].x = __int_as_float(vis[2 * pid + j] ? 1 : 0);
+      }
+    }
     float c0x = 0.f, c0y = 0.f, c0z = 0.f, c1x = 0.f, c1y = 0.f, c1z = 0.f;
     bool use0 = false, use1 = false;
     if (ps.sh_o0[pid].w != 0.f && vis[2 * pid]) {
@@ -508,6 +517,10 @@ struct Render {
   int blocks_extend_max = 0, blocks_shadow_max = 0;
   int shade_blocks_per_sm = 8;                // shading grid = SMs x this
   int last_error = 0;
+  // per-path ray log of the last frame (hm_render_set_path_log; tests)
+  float4* log_ev = nullptr;
+  int* log_vcur = nullptr;
+  int log_slots = 0;
   // instrumentation (synchronous frames)
   bool timing = false, counting = false;
   unsigned long long* d_cnt = nullptr;
@@ -526,6 +539,7 @@ struct Render {
     for (void* p : allocs) cudaFree(p);
     if (d_samples) cudaFree(d_samples);
     for (void* p : {(void*)diff_col, (void*)diff_in, (void*)diff_dy, (void*)diff_gframe}) cudaFree(p);
+    for (void* p : {(void*)log_ev, (void*)log_vcur}) cudaFree(p);
     if (h_gsum) cudaFreeHost(h_gsum);
     if (h_count) cudaFreeHost(h_count);
     if (mlp) hm_mlp_destroy(mlp);
@@ -785,6 +799,10 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
   FrameParams fp{r->mode, r->beta_knob - 1, r->accum_id, r->accum_id + 10007, r->every_nth, r->n_train, r->in_ch,
                  0, nullptr, 0, 0u};
   FrameBufs fb = sl.fb;
+  if (r->log_ev && !r->diff_fwd) {
+    fp.log = PathLog{r->log_ev, r->log_vcur, r->log_slots};
+    cudaMemsetAsync(r->log_ev, 0xff, (size_t)r->P * r->log_slots * 3 * sizeof(float4), st);
+  }
   if (!r->diff_fwd) r->diff_frames = 0;  // a plain frame ends the replayable forward
   if (r->diff_fwd) {  // a frame of a differentiable forward
     fp.no_train = 1;
@@ -849,7 +867,7 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
         return e;
       shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{},
                                                          tfp.mode == MODE_NRC ? sl.nrc.dl_rec : nullptr,
-                                                         sl.nrc.rec);
+                                                         sl.nrc.rec, tfp.log);
       HM_CHECK_LAUNCH("shadow_resolve_kernel");
       mark(S_COMPACT);
       scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
@@ -879,7 +897,8 @@ static int render_frame(Render* r, cudaStream_t user, bool sync_bounces) {
     FrameParams tfp = fp;
     tfp.d_frame = sl.d_frame;
     const int64_t key[10] = {rounds, r->blocks_extend, r->blocks_shadow, grid, s->material_version, tfp.no_train,
-                             (int64_t)(uintptr_t)tfp.eval_hc, (int64_t)(uintptr_t)sl.ps.beta_d, r->mode, 1};
+                             (int64_t)(uintptr_t)tfp.eval_hc, (int64_t)(uintptr_t)sl.ps.beta_d, r->mode,
+                             (int64_t)(uintptr_t)tfp.log.ev};
     if (!sl.trace_exec || memcmp(key, sl.trace_key, sizeof(key)) != 0) {
       if (sl.trace_exec) cudaGraphExecDestroy(sl.trace_exec);
       sl.trace_exec = nullptr;
@@ -1597,6 +1616,41 @@ extern "C" int hm_render_set_instrumentation(hm_render* h, int timing, int count
   r->timing = timing != 0;
   r->counting = counting != 0;
   return HM_OK;
+}
+
+extern "C" int hm_render_set_path_log(hm_render* h, int vertices) {
+  if (!h || vertices < 0 || vertices > 4096) return hm_set_error("hm_render_set_path_log: bad arguments"), HM_EINVAL;
+  Render* r = (Render*)h;
+  if (vertices > 0 && (r->depth != 1 || !r->bscenes.empty()))
+    return hm_set_error("hm_render_set_path_log: single-scene renderers with one frame in flight"), HM_EINVAL;
+  if (int e = render_sync(r)) return e;
+  cudaFree(r->log_ev);
+  cudaFree(r->log_vcur);
+  r->log_ev = nullptr;
+  r->log_vcur = nullptr;
+  r->log_slots = 0;
+  if (vertices == 0) return HM_OK;
+  const int slots = 3 * vertices;
+  cudaError_t e = cudaMalloc(&r->log_ev, (size_t)r->P * slots * 3 * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&r->log_vcur, (size_t)r->P * sizeof(int));
+  if (e != cudaSuccess) {
+    cudaFree(r->log_ev);
+    r->log_ev = nullptr;
+    return hm_cuda_status(e, "hm_render_set_path_log");
+  }
+  r->log_slots = slots;
+  return HM_OK;
+}
+
+extern "C" int hm_render_read_path_log(hm_render* h, float* host_dst, int64_t n_floats) {
+  if (!h || !host_dst) return hm_set_error("hm_render_read_path_log: bad arguments"), HM_EINVAL;
+  Render* r = (Render*)h;
+  const int64_t need = (int64_t)r->P * r->log_slots * 12;
+  if (!r->log_ev || n_floats < need)
+    return hm_set_error("hm_render_read_path_log: no log, or %lld floats needed", (long long)need), HM_EINVAL;
+  if (int e = render_sync(r)) return e;
+  cudaError_t e = cudaMemcpy(host_dst, r->log_ev, need * sizeof(float), cudaMemcpyDeviceToHost);
+  return e == cudaSuccess ? HM_OK : hm_cuda_status(e, "hm_render_read_path_log");
 }
 
 extern "C" int hm_render_get_timings(const hm_render* h, hm_render_timings* out) {

@@ -57,6 +57,30 @@ struct PathState {
   float4* beta_d; // detached renders: throughput of the sampling material (Russian roulette)
 };
 
+// Per-path ray log (hm_render_set_path_log; ev == nullptr in ordinary
+// frames).  Slot 3k + j of a path holds vertex k's extension-ray result
+// (j = 0: the ray that found the vertex), its light-sample shadow ray (1) and
+// its BSDF-sample shadow ray (2), three float4 each:
+//   (result int bits, t, u, RNG state bits), (direction, kind int bits),
+//   (origin, 0)
+// with result = hit primitive or -1 (extension), 1 unoccluded / 0 occluded
+// (shadow); kind -1 marks an empty slot.
+struct PathLog {
+  float4* ev;  // [P][slots][3]
+  int* vcur;   // [P] vertex of the pending shadow rays
+  int slots;
+};
+constexpr int kLogPending = -2;  // a logged shadow ray not resolved yet
+
+HM_D void log_ray(const PathLog& L, int pid, int slot, int kind, int result, float t, float u, uint32_t rng,
+                  f3 o, f3 d) {
+  if (slot >= L.slots) return;
+  float4* e = L.ev + ((size_t)pid * L.slots + slot) * 3;
+  e[0] = make_float4(__int_as_float(result), t, u, __uint_as_float(rng));
+  e[1] = make_float4(d.x, d.y, d.z, __int_as_float(kind));
+  e[2] = make_float4(o.x, o.y, o.z, 0.f);
+}
+
 struct FrameParams {
   int mode;        // RenderMode
   int beta;        // BETA - 1 (render_hair_msnn.cu:1170)
@@ -80,6 +104,7 @@ struct FrameParams {
   const HairConsts* eval_hc;
   // frames replayed from a CUDA graph read the frame number (accum_id) here
   const int* d_frame;
+  PathLog log;
 };
 
 // Path replay (Vicini et al. 2021, "Path Replay Backpropagation"): a frame

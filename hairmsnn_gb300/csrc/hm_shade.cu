@@ -158,10 +158,14 @@ __global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ Scen
     const int rec = c.train_base + c.local / c.every_nth;  // training record of a training path
     uint32_t flags = ps.flags[pid];
     const int k = ps.bounce[pid];
-    const float4 h = ps.hit[pid];
-    const bool hit = __float_as_int(h.y) >= 0;
+    const float4 h_trav = ps.hit[pid];
+    const bool hit = __float_as_int(h_trav.y) >= 0;
     const bool train = flags & F_TRAIN;
     const f3 ro = ld3(ps.ray_o, pid), rd = ld3(ps.ray_d, pid);
+    const float4 h = hit ? refit_hit(s, ro, rd, h_trav) : h_trav;
+    if (fp.log.ev)
+      log_ray(fp.log, pid, 3 * k, 0, hit ? __float_as_int(h.y) : -1, hit ? h.x : 0.f, hit ? h.z : 0.f, ps.rng[pid],
+              ro, rd);
     int k_keep = 0;
     if (k == 0 && !hit) {
       // miss program (optix_common.cuh:604-616): Le of the camera ray
@@ -203,6 +207,11 @@ __global__ void __launch_bounds__(128) shade_kernel(const __grid_constant__ Scen
     ss[0].valid = ss[1].valid = 0;
     if (do_dl) {
       direct_lighting(s, v, rng, ss);
+      if (fp.log.ev) {
+        fp.log.vcur[pid] = k;
+        for (int j = 0; j < 2; ++j)
+          if (ss[j].valid) log_ray(fp.log, pid, 3 * k + 1 + j, 1 + j, kLogPending, 0.f, 0.f, 0u, ss[j].o, ss[j].d);
+      }
       st3(ps.sh_o0, pid, ss[0].o, ss[0].valid ? 1.f : 0.f);
       st3(ps.sh_d0, pid, ss[0].d);
       st3(ps.sh_c0, pid, ss[0].c);

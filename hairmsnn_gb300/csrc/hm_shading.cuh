@@ -8,6 +8,7 @@
 #pragma once
 #include "hm_hair_bsdf.cuh"
 #include "hm_scene.h"
+#include "hm_trace.cuh"
 
 namespace hm {
 
@@ -261,8 +262,31 @@ struct Vertex {
   const HairConsts* hc_eval;  // material of the BSDF values (== hc but in detached renders)
 };
 
+// The traversal's hit recomputed for its own primitive with every operation
+// rounded on its own: the shading translation units are compiled without
+// multiply-add contraction, while the traversal contracts (its box and leaf
+// tests run fused).  The hit point, and so the shading frame and the offset
+// h across the fibre, then follow from exactly the same arithmetic as in an
+// FP32 host build of the same intersector: at a grazing hit on a 0.04 mm
+// fibre a contracted t moved h by percents.  A leaf that the refit no longer
+// hits (a contracted near-miss) keeps the traversal's values.
+HM_D float4 refit_hit(const SceneDev& s, f3 ro, f3 rd, float4 hit) {
+  const int prim = __float_as_int(hit.y);
+  const Ray r{ro, rd, 0.f, 1e30f};
+  float t = 0.f, u = 0.f, v = 0.f;
+  bool ok;
+  if (prim < s.n_seg) {
+    const int part = clampi((int)(hit.z * (float)s.seg_split), 0, s.seg_split - 1);
+    ok = curve_intersect(s, prim, part, r, 1e30f, &t, &u);
+  } else {
+    ok = tri_intersect(s, prim - s.n_seg, r, 1e30f, &t, &u, &v);
+  }
+  return ok ? make_float4(t, hit.y, u, v) : hit;
+}
+
 // hairCH (optix_common.cuh:558-599) with computeCurveIntersection
-// (curve_utils.cuh:218-256); triangleMeshCH (:527-556).
+// (curve_utils.cuh:218-256); triangleMeshCH (:527-556).  `hit` is the
+// refit hit (refit_hit).
 HM_D Vertex setup_vertex(const SceneDev& s, f3 ro, f3 rd, const float4 hit) {
   Vertex v;
   const int prim = __float_as_int(hit.y);

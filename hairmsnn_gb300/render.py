@@ -112,6 +112,8 @@ def _declare():
     L.hm_render_buffer.argtypes = [vp, i32, P(vp), P(i64)]
     L.hm_copy_to_host.argtypes = [vp, vp, i64]
     L.hm_render_set_instrumentation.argtypes = [vp, i32, i32]
+    L.hm_render_set_path_log.argtypes = [vp, i32]
+    L.hm_render_read_path_log.argtypes = [vp, vp, i64]
     L.hm_render_get_timings.argtypes = [vp, P(hm_render_timings)]
     L.hm_scene_set_strand_groups.argtypes = [vp, P(i32), i32, i32]
     L.hm_scene_set_group_materials.argtypes = [vp, vp, i32]
@@ -288,6 +290,20 @@ class Renderer:
 
     def instrument(self, timing=True, counting=False):
         check(lib().hm_render_set_instrumentation(self._h, 1 if timing else 0, 1 if counting else 0))
+
+    def set_path_log(self, vertices):
+        """Record every path's rays at its first `vertices` vertices in later
+        frames (0: off); see hm_render_set_path_log."""
+        self._log_slots = 3 * int(vertices)
+        check(lib().hm_render_set_path_log(self._h, int(vertices)))
+
+    def read_path_log(self):
+        """The last frame's per-path ray log: [P, 3 * vertices, 12] float32
+        (see hm_render_set_path_log for the layout)."""
+        P = self.width * self.height
+        out = np.zeros((P, self._log_slots, 12), np.float32)
+        check(lib().hm_render_read_path_log(self._h, out.ctypes.data_as(ctypes.c_void_p), out.size))
+        return out
 
     def timings(self):
         t = hm_render_timings()

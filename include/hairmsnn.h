@@ -156,7 +156,10 @@ int hm_mlp_inference(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, vo
  * width <= 2^20 floats, else HM_ECAPACITY; FP16/BF16/E4M3 handles encode
  * inside the tensor-core kernel and use no scratch).  Calls on one device must not
  * overlap (they share the scratch); make the first call on each device before
- * any stream capture (it resolves the scratch address). */
+ * any stream capture (it resolves the scratch address).  The address is kept
+ * for the life of the process: resetting a device (cudaDeviceReset, or any
+ * other end of its primary context) while the library is loaded is not
+ * supported by this entry point. */
 int hm_mlp_inference_noalloc(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, void* stream);
 /* Trainer::training_step + Trainer::loss (render_hair_msnn.cu:690-691),
  * split into its three phases and fused: forward keeps the activations
@@ -400,6 +403,19 @@ typedef struct hm_render_timings {
 } hm_render_timings;
 int hm_render_set_instrumentation(hm_render* render, int timing, int counting);
 int hm_render_get_timings(const hm_render* render, hm_render_timings* out);
+/* Per-path ray log (no reference counterpart; parity tests).  With
+ * vertices > 0 every later frame records, for each path, the rays it traced
+ * at its first `vertices` vertices; hm_render_read_path_log copies the last
+ * frame's log, [P][3 * vertices][12] floats: slot 3k + j is vertex k's
+ * extension ray (j = 0, the ray that found the vertex), light-sample shadow
+ * ray (1) and BSDF-sample shadow ray (2) as
+ *   result (int bits: hit primitive or -1; shadow: 1 unoccluded, 0 occluded),
+ *   t, u, RNG state when the ray was traced (extension rays; uint bits),
+ *   direction[3], kind (int bits: 0, 1, 2; -1 empty slot), origin[3], 0.
+ * Single-scene renderers (PT, HairMSNN, NRC) created with frames_in_flight = 1.
+ * vertices = 0 turns the log off. */
+int hm_render_set_path_log(hm_render* render, int vertices);
+int hm_render_read_path_log(hm_render* render, float* host_dst, int64_t n_floats);
 /* The render's cache network (owned by the render; NULL in PT mode). */
 hm_mlp* hm_render_cache(hm_render* render);
 /* Device buffers of the last frame: 0 cache inputs [P][12], 1 cache outputs

@@ -19,7 +19,7 @@ REF_DIR = os.environ.get("HM_REF_DIR", "/root/reference")
 OUT_DIR = os.path.join(HERE, "_ref")
 ORACLE_DIR = os.path.join(HERE, "_build")
 ORACLE_LIB = os.path.join(ORACLE_DIR, "libhmoracle.so")
-ORACLE_SOURCES = ["hm_oracle.cpp", "hm_oracle_render.cpp", "hm_oracle_mlp.cpp"]
+ORACLE_SOURCES = ["hm_oracle.cpp", "hm_oracle_render.cpp", "hm_oracle_mlp.cpp", "hm_oracle_scene.cpp"]
 ORACLE_HEADERS = ["hm_oracle.h", "hm_oracle_math.h"]
 
 
@@ -47,13 +47,14 @@ def build_oracle(verbose: bool = False) -> str:
 
 # (output library, entry source, extra flags, links the oracle library).
 # The integrator targets include the reference's own raygen sources
-# (cuda/hair_msnn.cu, cuda/path_tracing.cu); __CUDA_ARCH__ is defined only so
+# (cuda/hair_msnn.cu, cuda/path_tracing.cu, cuda/nrc.cu); __CUDA_ARCH__ is defined only so
 # that common.cuh declares its ray types (common.cuh:28-32), and traceRay is
 # answered by the oracle library's BVH.
 TARGETS = [
     ("libhmref_math.so", "ref_math_entry.cpp", [], False),
     ("libhmref_path.so", "ref_path_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
     ("libhmref_pt.so", "ref_pt_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
+    ("libhmref_nrc.so", "ref_nrc_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
 ]
 
 

@@ -18,6 +18,7 @@ using namespace hmo;
 
 int hmo::g_mp_force_fp32 = 0;
 extern "C" void hmo_set_mp_force_fp32(int on) { g_mp_force_fp32 = on; }
+extern "C" void hmo_set_ulp_perturb(int k) { hmo::ulp_perturb = k < -1 ? -1 : k; }
 
 // ============================================================== RNG
 extern "C" uint32_t hmo_get_rng(int frame_id, uint32_t px, uint32_t py, uint32_t dimx, uint32_t dimy) {

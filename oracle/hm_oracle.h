@@ -36,6 +36,11 @@ void hmo_setup_hair(const float* hp, float* out10);
 // 1: keep the M_p log branch in FP32 for every beta_m (bit-for-bit the
 // reference); 0 (default): FP64 for that branch when beta_m < 0.1.
 void hmo_set_mp_force_fp32(int on);
+// 0 (default): libm's transcendental functions; +1 / -1: each result moved
+// one ulp up / down; k >= 2: each result moved by a pseudo-random -2..+2 ulps
+// (stream k, reseeded per pixel): the sensitivity of a path to last-ulp
+// differences of its transcendental functions.
+void hmo_set_ulp_perturb(int k);
 // wo, wi, t: [n][3] world vectors; h: [n]; f: [n][3]; pdf: [n]
 void hmo_hair_eval(int64_t n, const float* wo, const float* wi, const float* t, const float* h,
                    const float* hp, float* f, float* pdf);

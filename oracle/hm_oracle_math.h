@@ -9,7 +9,44 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <cmath>
+
 namespace hmo {
+
+// ---- last-ulp perturbation (test infrastructure)
+// The float transcendental functions of the restatement go through these
+// wrappers.  With ulp_perturb = 0 (the default) they are libm's own, which is
+// what the reference's host build and the golden vectors use.  Otherwise
+// every result is moved by a few ulps: +1 / -1 one ulp up / down; k >= 2 a
+// pseudo-random -2..+2 ulps per call, from a per-path stream (seeded by k and
+// the pixel, so runs are reproducible).  The tests render a frame that way to
+// see which paths depend on last-ulp differences of the transcendentals
+// (where the device's functions and libm's can differ).  Set only between
+// renders; read-only while one runs.
+inline int ulp_perturb = 0;
+inline thread_local uint32_t ulp_stream = 0;
+inline void ulp_seed_path(uint32_t pixel) { ulp_stream = (uint32_t)ulp_perturb * 0x9e3779b9u ^ (pixel * 0x85ebca6bu); }
+inline float nudge(float v) {
+  if (ulp_perturb == 0 || !std::isfinite(v)) return v;
+  int k = ulp_perturb > 0 ? 1 : -1;
+  if (ulp_perturb >= 2) {
+    ulp_stream = ulp_stream * 1664525u + 1013904223u;
+    k = (int)((ulp_stream >> 16) % 5u) - 2;
+  }
+  for (; k > 0; --k) v = std::nextafter(v, INFINITY);
+  for (; k < 0; ++k) v = std::nextafter(v, -INFINITY);
+  return v;
+}
+inline float oexpf(float x) { return nudge(::expf(x)); }
+inline float ologf(float x) { return nudge(::logf(x)); }
+inline float osinf(float x) { return nudge(::sinf(x)); }
+inline float ocosf(float x) { return nudge(::cosf(x)); }
+inline float oasinf(float x) { return nudge(::asinf(x)); }
+inline float oacosf(float x) { return nudge(::acosf(x)); }
+inline float oatan2f(float y, float x) { return nudge(::atan2f(y, x)); }
+inline float opowf(float x, float y) { return nudge(::powf(x, y)); }
+inline float osinhf(float x) { return nudge(::sinhf(x)); }
+
 
 // utils.cuh:10-11 — note the two different pi literals.
 static const float kPi = 3.1415926f;
@@ -53,7 +90,7 @@ inline V4 operator*(V4 a, float s) { return V4(a.x * s, a.y * s, a.z * s, a.w * 
 inline V4 operator/(V4 a, float s) { return V4(a.x / s, a.y / s, a.z / s, a.w / s); }
 
 inline float sqr(float v) { return v * v; }                                 // disney_hair.cuh:13
-inline float safe_asin(float x) { return asinf(fminf(fmaxf(x, -1.f), 1.f)); }  // :16-18
+inline float safe_asin(float x) { return oasinf(fminf(fmaxf(x, -1.f), 1.f)); }  // :16-18
 inline float safe_sqrt(float x) { return sqrtf(fmaxf(0.f, x)); }            // :21-23
 
 // ------------------------------------------------------------ RNG
@@ -96,7 +133,7 @@ inline V3 uniform_sample_sphere(float u0, float u1) {                           
   float z = 1.f - 2.f * u0;
   float r = sqrtf(fmaxf(0.f, 1.f - z * z));
   float phi = 2.f * kPi * u1;
-  return normalize(V3(r * cosf(phi), r * sinf(phi), z));
+  return normalize(V3(r * ocosf(phi), r * osinf(phi), z));
 }
 inline void orthonormal_basis(V3 n, V3 mat[3], V3 inv[3]) {  // :232-259
   V3 c1, c2, c3;
@@ -118,10 +155,10 @@ inline void orthonormal_basis(V3 n, V3 mat[3], V3 inv[3]) {  // :232-259
   inv[2] = V3(c1.z, c2.z, c3.z);
 }
 inline float spherical_phi(V3 v) {  // :269-273
-  float p = atan2f(v.y, v.x);
+  float p = oatan2f(v.y, v.x);
   return (p < 0.f) ? (p + 2.f * kPi) : p;
 }
-inline float spherical_theta(V3 p) { return acosf(p.z); }  // :275-278
+inline float spherical_theta(V3 p) { return oacosf(p.z); }  // :275-278
 inline float power_heuristic(float fp, float gp) {        // :290-293 with nf = ng = 1
   float f = fp, g = gp;
   return (f * f) / (f * f + g * g);
@@ -145,12 +182,12 @@ struct HairShading {
 inline HairShading setup_hair_shading(const float* hp) {
   HairShading hs;
   float bm = hp[3], bn = hp[4], alpha = hp[5];
-  hs.v[0] = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * powf(bm, 20.f));
+  hs.v[0] = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * opowf(bm, 20.f));
   hs.v[1] = (float)(.25 * (double)hs.v[0]);
   hs.v[2] = 4.f * hs.v[0];
-  hs.s = kSqrtPiOver8 * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * powf(bn, 22.f));
+  hs.s = kSqrtPiOver8 * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * opowf(bn, 22.f));
   hs.v[3] = hs.s;
-  hs.sin2k[0] = sinf(alpha);
+  hs.sin2k[0] = osinf(alpha);
   hs.cos2k[0] = safe_sqrt(1.f - sqr(hs.sin2k[0]));
   for (int i = 1; i < 3; ++i) {
     hs.sin2k[i] = 2.f * hs.cos2k[i - 1] * hs.sin2k[i - 1];
@@ -183,8 +220,8 @@ inline float bessel_i0(float x) {  // disney_hair.cuh:54-67
 
 inline float log_i0(float x) {  // disney_hair.cuh:70-75 (the `0.5 *` is a double product)
   if (x > 12.f)
-    return (float)((double)x + 0.5 * (double)(-logf(2.f * kPi) + logf(1.f / x) + 1.f / (8.f * x)));
-  return logf(bessel_i0(x));
+    return (float)((double)x + 0.5 * (double)(-ologf(2.f * kPi) + ologf(1.f / x) + 1.f / (8.f * x)));
+  return ologf(bessel_i0(x));
 }
 
 // FP64 restatement of the v <= 0.1 branch, used when beta_m < 0.1 (where the
@@ -213,8 +250,8 @@ inline float mp(float cti, float cto, float sti, float sto, float v, bool fp64) 
   }
   float a = cti * cto / v;
   float b = sti * sto / v;
-  if (v <= 0.1f) return expf(log_i0(a) - b - 1.f / v + 0.6931f + logf(1.f / (2.f * v)));
-  return (expf(-b) * bessel_i0(a)) / (sinhf(1.f / v) * 2.f * v);
+  if (v <= 0.1f) return oexpf(log_i0(a) - b - 1.f / v + 0.6931f + ologf(1.f / (2.f * v)));
+  return (oexpf(-b) * bessel_i0(a)) / (osinhf(1.f / v) * 2.f * v);
 }
 
 inline float phi_p(int p, float gamma_o, float gamma_t) {  // :112-114
@@ -222,9 +259,9 @@ inline float phi_p(int p, float gamma_o, float gamma_t) {  // :112-114
 }
 inline float logistic(float x, float s) {  // :117-120
   x = fabsf(x);
-  return expf(-x / s) / (s * sqr(1.f + expf(-x / s)));
+  return oexpf(-x / s) / (s * sqr(1.f + oexpf(-x / s)));
 }
-inline float logistic_cdf(float x, float s) { return 1.f / (1.f + expf(-x / s)); }  // :123-125
+inline float logistic_cdf(float x, float s) { return 1.f / (1.f + oexpf(-x / s)); }  // :123-125
 inline float trimmed_logistic(float x, float s, float a, float b) {                 // :128-130
   return logistic(x, s) / (logistic_cdf(b, s) - logistic_cdf(a, s));
 }
@@ -255,7 +292,7 @@ inline void ap_pdf(const HairShading& hs, float sin_to, float cos_to, float cos_
   float sin_gt = h / etap;
   float cos_gt = safe_sqrt(1.f - sqr(sin_gt));
   float fac = (2.f * cos_gt / cos_tt);
-  V3 T(expf(-hs.sigma_a[0] * fac), expf(-hs.sigma_a[1] * fac), expf(-hs.sigma_a[2] * fac));
+  V3 T(oexpf(-hs.sigma_a[0] * fac), oexpf(-hs.sigma_a[1] * fac), oexpf(-hs.sigma_a[2] * fac));
   float fr = fresnel(eta, cos_to * cos_go);
   Ap ap = attenuation(fr, T);
   for (int p = 0; p < 4; ++p) out[p] = (ap.a[p].x + ap.a[p].y + ap.a[p].z) / 3.f;
@@ -268,20 +305,20 @@ inline V3 disney_hair(V3 wo, V3 wi, float h, const HairShading& hs, float* pdf) 
   const bool fp64 = hs.beta_m < 0.1f;
   float sin_to = wo.x;
   float cos_to = safe_sqrt(1.f - sqr(sin_to));
-  float phi_o = atan2f(wo.z, wo.y);
+  float phi_o = oatan2f(wo.z, wo.y);
   float sin_ti = wi.x;
   float cos_ti = safe_sqrt(1.f - sqr(sin_ti));
-  float phi_i = atan2f(wi.z, wi.y);
+  float phi_i = oatan2f(wi.z, wi.y);
   float sin_tt = sin_to / kEta;
   float cos_tt = safe_sqrt(1.f - sqr(sin_tt));
-  float gamma_o = asinf(h);
-  float cos_go = cosf(gamma_o);
+  float gamma_o = oasinf(h);
+  float cos_go = ocosf(gamma_o);
   float etap = sqrtf(kEta * kEta - sqr(sin_to)) / cos_to;
   float sin_gt = h / etap;
   float cos_gt = safe_sqrt(1.f - sqr(sin_gt));
   float gamma_t = safe_asin(sin_gt);
   float fac = (2.f * cos_gt / cos_tt);
-  V3 T(expf(-hs.sigma_a[0] * fac), expf(-hs.sigma_a[1] * fac), expf(-hs.sigma_a[2] * fac));
+  V3 T(oexpf(-hs.sigma_a[0] * fac), oexpf(-hs.sigma_a[1] * fac), oexpf(-hs.sigma_a[2] * fac));
   float fr = fresnel(kEta, cos_to * cos_go);
   Ap ap = attenuation(fr, T);
   float phi = phi_i - phi_o;
@@ -322,7 +359,7 @@ inline V3 disney_hair(V3 wo, V3 wi, float h, const HairShading& hs, float* pdf) 
 
 inline float sample_trimmed_logistic(float u, float s, float a, float b) {  // :269-274
   float k = logistic_cdf(b, s) - logistic_cdf(a, s);
-  float x = -s * logf(1.f / (u * k + logistic_cdf(a, s)) - 1.f);
+  float x = -s * ologf(1.f / (u * k + logistic_cdf(a, s)) - 1.f);
   return fminf(fmaxf(x, a), b);
 }
 
@@ -332,9 +369,9 @@ inline V3 sample_disney_hair(V3 wo, float h, const float r[4], const HairShading
                              V3* wi_local, float* pdf, float* margin) {
   float sin_to = wo.x;
   float cos_to = safe_sqrt(1.f - sqr(sin_to));
-  float phi_o = atan2f(wo.z, wo.y);
-  float gamma_o = asinf(h);
-  float cos_go = cosf(gamma_o);
+  float phi_o = oatan2f(wo.z, wo.y);
+  float gamma_o = oasinf(h);
+  float cos_go = ocosf(gamma_o);
   float apdf[4];
   ap_pdf(hs, sin_to, cos_to, cos_go, kEta, h, apdf);
   int p = 0;
@@ -362,9 +399,9 @@ inline V3 sample_disney_hair(V3 wo, float h, const float r[4], const HairShading
   }
   float eps2 = fmaxf(r[1], 1e-5f);
   float vp = hs.v[p];
-  float cos_theta = 1.f + vp * logf(eps2 + (1.f - eps2) * expf(-2.f / vp));
+  float cos_theta = 1.f + vp * ologf(eps2 + (1.f - eps2) * oexpf(-2.f / vp));
   float sin_theta = safe_sqrt(1.f - sqr(cos_theta));
-  float cos_phi = cosf(2.f * kPi * r[2]);
+  float cos_phi = ocosf(2.f * kPi * r[2]);
   float sin_ti = -cos_theta * sop + sin_theta * cos_phi * cop;
   float cos_ti = safe_sqrt(1.f - sqr(sin_ti));
   float etap = sqrtf(kEta * kEta - sqr(sin_to)) / cos_to;
@@ -376,7 +413,7 @@ inline V3 sample_disney_hair(V3 wo, float h, const float r[4], const HairShading
   else
     dphi = 2.f * kPi * r[3];
   float phi_i = phi_o + dphi;
-  V3 wil = normalize(V3(sin_ti, cos_ti * cosf(phi_i), cos_ti * sinf(phi_i)));
+  V3 wil = normalize(V3(sin_ti, cos_ti * ocosf(phi_i), cos_ti * osinf(phi_i)));
   *wi_local = wil;
   return disney_hair(wo, wil, h, hs, pdf);
 }
@@ -405,7 +442,7 @@ inline HairFrame hair_frame(V3 wo, V3 t) {
 // ------------------------------------------------------------ GGX (frostbite_anisotropic.cuh)
 inline float ggx_d(float ax, float ay, V3 N) {  // :24-32
   float t1 = N.x / ax, t2 = N.y / ay, t3 = N.z;
-  float value = kPi * ax * ay * powf(t1 * t1 + t2 * t2 + t3 * t3, 2.0f);
+  float value = kPi * ax * ay * opowf(t1 * t1 + t2 * t2 + t3 * t3, 2.0f);
   return 1.0f / value;
 }
 inline float ggx_lambda(float ax, float ay, V3 V) {  // :34-42
@@ -446,8 +483,8 @@ inline V3 sample_vndf(float ax, float ay, V3 V, float U1, float U2) {  // :102-1
   V3 T2 = cross(Vh, T1);
   float r = sqrtf(U1);
   float phi = 2.0f * kPi * U2;
-  float t1 = r * cosf(phi);
-  float t2 = r * sinf(phi);
+  float t1 = r * ocosf(phi);
+  float t2 = r * osinf(phi);
   float s = 0.5f * (1.0f + Vh.z);
   t2 = (1.0f - s) * sqrtf(1.0f - t1 * t1) + s * t2;
   V3 Nh = t1 * T1 + t2 * T2 + sqrtf(fmaxf(0.0f, 1.0f - t1 * t1 - t2 * t2)) * Vh;

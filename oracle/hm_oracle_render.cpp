@@ -464,7 +464,7 @@ float env_pdf(const OScene& s, V3 wi) {  // getEnvironmentPdf
   int cw = s.env_w + 1;
   float cdf_last_u = tex_nearest(s.cpdf, cw, s.env_h, 1.f, iv / height);
   float cdf_last_v = tex_nearest(s.mpdf, s.env_h + 1, 1, 1.f, 0.f);
-  float sin_theta = sinf(theta);
+  float sin_theta = osinf(theta);
   float denom = (2.f * kPi * kPi * sin_theta) * cdf_last_u * cdf_last_v;
   float cdf_u = tex_nearest(s.cpdf, cw, s.env_h, iu / width, iv / height);
   float cdf_v = tex_nearest(s.mpdf, s.env_h + 1, 1, iv / height, 0.f);
@@ -507,12 +507,12 @@ V3 sample_env(const OScene& s, SI& si, uint32_t& rng, float* pdf) {  // sampleEn
     float pu = tex_nearest(s.cpdf, cw, s.env_h, iu / width, iv / height);
     float pv = tex_nearest(s.mpdf, mh, 1, iv / height, 0.f);
     float theta = kPi * v;
-    float sin_theta = sinf(theta);
+    float sin_theta = osinf(theta);
     float denom = (2.f * kPi * kPi * sin_theta) * cdf_last_u * cdf_last_v;
     *pdf = denom != 0.f ? (pu * pv) / denom : 0.f;
     float phi = 2.f * kPi * u - s.env_rot;
     if (phi < 0) phi = kTwoPi + phi;
-    si.wi = V3(sin_theta * cosf(phi), sin_theta * sinf(phi), cosf(theta));
+    si.wi = V3(sin_theta * ocosf(phi), sin_theta * osinf(phi), ocosf(theta));
     si.wi_local = normalize(apply_mat(si.to_local, si.wi));
   } else {
     float a = lcg_randomf(rng);
@@ -963,11 +963,23 @@ void hmo_scene_free(void* h) { delete (OScene*)h; }
 // [p0, p0 + np): gbuf [np][7] = radiance, beta, hit; query / suffix_query
 // [np][9]; records [np][40][15]; tinfo [np][4] = bounces, suffix ended at a
 // query, unbiased, training pixel.
-void hmo_render_nrc(void* h, int accum_id, int every_nth, int n_train, float c, int p0, int np, float* gbuf,
-                    float* query, float* suffix_query, float* records, int* tinfo, int threads) {
+//
+// hmo_render_nrc_ev: the same plus each path's ray log and event count (as
+// hmo_render_pixels_ev; events / n_events may be NULL).
+void hmo_render_nrc_ev(void* h, int accum_id, int every_nth, int n_train, float c, int p0, int np, float* gbuf,
+                       float* query, float* suffix_query, float* records, int* tinfo, float* events, int* n_events,
+                       int max_events, int threads) {
   OScene* s = (OScene*)h;
   auto work = [&](int b, int e) {
+    EvLog log;
     for (int pid = b; pid < e; ++pid) {
+      if (events) {
+        log.ev = events + (size_t)(pid - p0) * max_events * kEvFloats;
+        log.cap = max_events;
+        log.n = 0;
+        tl_log = &log;
+      }
+      ulp_seed_path((uint32_t)pid);
       const int x = pid % s->width, y = pid / s->width;
       uint32_t rng = get_rng(accum_id + 10007, (uint32_t)x, (uint32_t)y, (uint32_t)s->width, (uint32_t)s->height);
       bool training = false;
@@ -1005,7 +1017,9 @@ void hmo_render_nrc(void* h, int accum_id, int every_nth, int n_train, float c, 
       memcpy(records + (size_t)i * kNrcMaxBounces * 15, o->rec, sizeof(o->rec));
       int t[4] = {o->bounces, o->thit, unbiased ? 1 : 0, training ? 1 : 0};
       memcpy(tinfo + 4 * (size_t)i, t, sizeof(t));
+      if (n_events) n_events[i] = log.n;
     }
+    tl_log = nullptr;
   };
   if (threads <= 1) {
     work(p0, p0 + np);
@@ -1018,6 +1032,12 @@ void hmo_render_nrc(void* h, int accum_id, int every_nth, int n_train, float c, 
     if (b < e) pool.emplace_back(work, b, e);
   }
   for (auto& t : pool) t.join();
+}
+
+void hmo_render_nrc(void* h, int accum_id, int every_nth, int n_train, float c, int p0, int np, float* gbuf,
+                    float* query, float* suffix_query, float* records, int* tinfo, int threads) {
+  hmo_render_nrc_ev(h, accum_id, every_nth, n_train, c, p0, np, gbuf, query, suffix_query, records, tinfo, nullptr,
+                    nullptr, 0, threads);
 }
 
 // Strand groups: group of every segment, each group's 10 material floats.
@@ -1077,6 +1097,7 @@ void hmo_render_pixels_ev(void* h, int mode, int beta_knob, int accum_id, int ev
         tl_log = &log;
       }
       const int x = pid % s->width, y = pid / s->width;
+      ulp_seed_path((uint32_t)pid);
       uint32_t rng = get_rng(accum_id + 10007, (uint32_t)x, (uint32_t)y, (uint32_t)s->width, (uint32_t)s->height);
       bool training = false;
       if (mode == 1) {

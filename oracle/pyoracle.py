@@ -35,6 +35,7 @@ def lib():
         L.hmo_query_rng.argtypes = [u32, u32]
         L.hmo_setup_hair.argtypes = [F32P, F32P]
         L.hmo_set_mp_force_fp32.argtypes = [i32]
+        L.hmo_set_ulp_perturb.argtypes = [i32]
         L.hmo_hair_eval.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P]
         L.hmo_hair_sample.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P]
         L.hmo_hair_eval_mt.argtypes = [i64, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
@@ -81,6 +82,13 @@ def setup_hair(hp):
 
 def set_mp_force_fp32(on):
     lib().hmo_set_mp_force_fp32(1 if on else 0)
+
+
+def set_ulp_perturb(k):
+    """0: libm's transcendentals (default); +1 / -1: every result one ulp up /
+    down; k >= 2: a pseudo-random -2..+2 ulps per call (stream k) -- to
+    measure a path's sensitivity to last-ulp differences."""
+    lib().hmo_set_ulp_perturb(int(k))
 
 
 def hair_eval(wo, wi, t, h, hp=C1_HAIR, threads=1):
@@ -134,6 +142,9 @@ def _declare_render(L):
     L.hmo_feistel_perm.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
     L.hmo_render_nrc.restype = None
     L.hmo_render_nrc.argtypes = [vp, i32, i32, i32, f32, i32, i32, F32P, F32P, F32P, F32P, I32P, i32]
+    L.hmo_render_nrc_ev.restype = None
+    L.hmo_render_nrc_ev.argtypes = [vp, i32, i32, i32, f32, i32, i32, F32P, F32P, F32P, F32P, I32P, F32P, I32P,
+                                    i32, i32]
     L.hmo_scene_set_groups.restype = None
     L.hmo_scene_set_groups.argtypes = [vp, I32P, i32, F32P, i32]
     L._render_declared = True
@@ -300,17 +311,26 @@ def msnn_render(gbuf, nn_out, accum_id=0, acc=None):
     return out
 
 
-def _render_nrc(self, accum_id=0, every_nth=1, n_train=0, c=0.01, p0=0, n=None, threads=8):
+def _render_nrc(self, accum_id=0, every_nth=1, n_train=0, c=0.01, p0=0, n=None, threads=8, max_events=0):
     """One frame of the NRC G_BUFFER pass for pixels [p0, p0+n): dict of
     gbuf [n,7] (radiance, beta, hit), query [n,9], suffix_query [n,9],
     records [n,40,15] (vert, wo, n, direct light, factor), tinfo [n,4]
-    (bounces, suffix ended at a query, unbiased, training pixel)."""
+    (bounces, suffix ended at a query, unbiased, training pixel); with
+    max_events > 0 also events [n, max_events, 12] and n_events [n] (the
+    ray log of render_pixels_ev)."""
     n = self.width * self.height - p0 if n is None else n
     out = dict(gbuf=np.zeros((n, 7), np.float32), query=np.zeros((n, 9), np.float32),
                suffix_query=np.zeros((n, 9), np.float32), records=np.zeros((n, 40, 15), np.float32),
                tinfo=np.zeros((n, 4), np.int32))
-    lib().hmo_render_nrc(self.h, accum_id, every_nth, n_train, c, p0, n, out["gbuf"], out["query"],
-                         out["suffix_query"], out["records"], out["tinfo"], threads)
+    if max_events > 0:
+        out["events"] = np.zeros((n, max_events, EV_FLOATS), np.float32)
+        out["n_events"] = np.zeros(n, np.int32)
+        lib().hmo_render_nrc_ev(self.h, accum_id, every_nth, n_train, c, p0, n, out["gbuf"], out["query"],
+                                out["suffix_query"], out["records"], out["tinfo"], out["events"], out["n_events"],
+                                max_events, threads)
+    else:
+        lib().hmo_render_nrc(self.h, accum_id, every_nth, n_train, c, p0, n, out["gbuf"], out["query"],
+                             out["suffix_query"], out["records"], out["tinfo"], threads)
     return out
 
 
@@ -454,6 +474,110 @@ def camera_vectors(frm, at, up, cos_fovy, width, height):
     d00 = (d00 - np.float32(0.5) * ddu).astype(np.float32)
     d00 = (d00 - np.float32(0.5) * ddv).astype(np.float32)
     return f(frm), d00, ddu, ddv
+
+
+def _declare_scene(L):
+    if getattr(L, "_scene_declared", False):
+        return
+    i32, f32_, u32 = ctypes.c_int, ctypes.c_float, ctypes.c_uint32
+    L.hmo_gen_hair.restype = None
+    L.hmo_gen_hair.argtypes = [i32, i32, i32, f32_, f32_, f32_, f32_, f32_, u32, F32P, F32P, I32P]
+    L.hmo_gen_ellipsoid.restype = None
+    L.hmo_gen_ellipsoid.argtypes = [i32, F32P, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.hmo_bake_sky.restype = None
+    L.hmo_bake_sky.argtypes = [f32_, F32P, i32, i32, f32_, F32P]
+    L.hmo_env_tables.restype = None
+    L.hmo_env_tables.argtypes = [F32P, i32, i32, F32P, F32P, F32P, F32P]
+    L._scene_declared = True
+
+
+def _normalize32(v):
+    v = np.asarray(v, np.float32)
+    d = np.float32(np.float32(v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])
+    return (v * np.float32(np.float32(1.0) / np.float32(np.sqrt(d)))).astype(np.float32)
+
+
+def _length32(v):
+    v = np.asarray(v, np.float32)
+    return np.float32(np.sqrt(np.float32(np.float32(v[0] * v[0] + v[1] * v[1]) + v[2] * v[2])))
+
+
+def procedural_scene(cfg):
+    """An OracleScene built from a procedural scene config (the keys the
+    library's scene parser reads: hair.procedural, surface.procedural,
+    lights.sky / directional, camera, integrator), generated by the oracle
+    alone (hm_oracle_scene.cpp) -- no shipped library involved.  The arrays
+    equal the library's for the same config on the same host."""
+    L = lib()
+    _declare_scene(L)
+    f = np.float32
+    hp = cfg["hair"].get("procedural", {})
+    sp = cfg.get("surface", {}).get("procedural", {})
+    head_r = np.asarray(sp.get("radii", [0.85, 0.95, 1.0]), np.float32)
+    arrays = {}
+    strands, cps = int(hp.get("strands", 10000)), int(hp.get("control_points", 64))
+    cp = np.zeros((strands * cps, 4), np.float32)
+    seg = np.zeros(strands * (cps - 3), np.int32)
+    L.hmo_gen_hair(1 if hp.get("type", "straight") == "curly" else 0, strands, cps, hp.get("length", 2.0),
+                   hp.get("radius", 4e-4), hp.get("root_min_z", 0.25), hp.get("helix_radius", 0.05),
+                   hp.get("helix_pitch", 0.1), int(hp.get("seed", 1)), head_r, cp.ravel(), seg)
+    arrays["control_points"], arrays["segments"] = cp, seg
+    if sp:
+        nv, nt = ctypes.c_int(), ctypes.c_int()
+        tris = int(sp.get("triangles", 20000))
+        L.hmo_gen_ellipsoid(tris, head_r, None, None, None, ctypes.byref(nv), ctypes.byref(nt))
+        vtx = np.zeros((nv.value, 3), np.float32)
+        nrm = np.zeros((nv.value, 3), np.float32)
+        tri = np.zeros((nt.value, 3), np.int32)
+        L.hmo_gen_ellipsoid(tris, head_r, vtx.ctypes.data, nrm.ctypes.data, tri.ctypes.data, ctypes.byref(nv),
+                            ctypes.byref(nt))
+        diffuse, alpha_raw = sp.get("diffuse", [0.35, 0.25, 0.2]), sp.get("alpha", 1.0)
+    else:
+        vtx, nrm, tri = np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+        diffuse, alpha_raw = [0.35, 0.25, 0.2], 1.0
+    arrays.update(vertices=vtx, normals=nrm, triangles=tri)
+    lights = cfg.get("lights", {})
+    sky = lights.get("sky")
+    env_w = env_h = 0
+    env_scale, env_rot = f(1.0), f(0.0)
+    if sky:
+        env_w, env_h = int(sky.get("width", 512)), int(sky.get("height", 256))
+        env = np.zeros((env_h, env_w, 4), np.float32)
+        L.hmo_bake_sky(sky.get("turbidity", 3.0), np.asarray(sky.get("sun", [3, 3, 3]), np.float32), env_w, env_h,
+                       sky.get("radiance_scale", 1.0), env.ravel())
+        cpdf = np.zeros((env_h, env_w + 1), np.float32)
+        ccdf = np.zeros((env_h, env_w + 1), np.float32)
+        mpdf = np.zeros(env_h + 1, np.float32)
+        mcdf = np.zeros(env_h + 1, np.float32)
+        L.hmo_env_tables(env.ravel(), env_w, env_h, cpdf.ravel(), ccdf.ravel(), mpdf, mcdf)
+        env_scale, env_rot = f(sky.get("scale", 1.0)), f(sky.get("rotation", 0.0))
+        arrays.update(env=env, env_cpdf=cpdf, env_ccdf=ccdf, env_mpdf=mpdf, env_mcdf=mcdf)
+    else:
+        z = np.zeros(0, np.float32)
+        arrays.update(env=z, env_cpdf=z, env_ccdf=z, env_mpdf=z, env_mcdf=z)
+    dl = [np.concatenate([_normalize32(d.get("from", [0, 0, 1])), np.asarray(d.get("emit", [1, 1, 1]), np.float32)])
+          for d in lights.get("directional", [])]
+    arrays["dir_lights"] = np.asarray(dl, np.float32).reshape(-1, 6)
+    it = cfg["integrator"]
+    w, h = int(it.get("width", 512)), int(it.get("height", 512))
+    c = cfg["camera"]
+    pos, d00, du, dv = camera_vectors(c["from"], c["to"], c["up"], c["cos_fovy"], w, h)
+    arrays["camera"] = np.concatenate([pos, d00, du, dv]).astype(np.float32)
+    hair = cfg["hair"]
+    alpha = f(f(f(3.14159) * f(hair["alpha"])) / f(180.0)) if "alpha" in hair else f(0.0)
+    mat = [*hair.get("sigma_a", [0.06, 0.1, 0.2]), hair.get("beta_m", 0.3), hair.get("beta_n", 0.3), alpha,
+           hair.get("Gain R", 1.0), hair.get("Gain TT", 1.0), hair.get("Gain TRT", 1.0), hair.get("Gain TRRT", 1.0),
+           *diffuse, alpha_raw, env_scale, env_rot]
+    arrays["materials"] = np.asarray(mat, np.float32).reshape(1, 16)
+    # bounds and scale (render_hair_msnn.cu:318-357)
+    surf_scale = _length32(vtx.max(0) - vtx.min(0)) if len(vtx) else f(0.0)
+    hair_scale = _length32(cp[:, :3].max(0) - cp[:, :3].min(0)) if len(cp) else f(0.0)
+    settings = dict(width=w, height=h, path_v1=int(it.get("path_v1", 1)), path_v2=int(it.get("path_v2", 40)),
+                    mis=int(bool(it.get("MIS", True))), env_pdf=int(bool(it.get("ENV_PDF", True))),
+                    has_env=int(bool(sky)), catrom=int(bool(it.get("shade_catmull_rom", False))), env_w=env_w,
+                    env_h=env_h, seg_split=int(it.get("segment_splits", 2)))
+    return OracleScene(arrays, settings, float(max(hair_scale, surf_scale)))
 
 
 def gen_bsdf_queries(seed, n):

@@ -92,6 +92,7 @@ struct vec3f {
   vec3f(const float4& o) : x(o.x), y(o.y), z(o.z) {}  // implicit, as OWL's
   float& operator[](int i) { return (&x)[i]; }
   const float& operator[](int i) const { return (&x)[i]; }
+  operator float3() const { float3 r; r.x = x; r.y = y; r.z = z; return r; }  // as OWL's
 };
 struct vec4f {
   float x, y, z, w;

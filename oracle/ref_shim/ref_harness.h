@@ -1,7 +1,8 @@
 // Host harness for the reference's own OptiX programs (test infrastructure
-// only).  Included by ref_path_entry.cpp and ref_pt_entry.cpp after the
-// reference's raygen source, so that `LaunchParams` and `optixLaunchParams`
-// are the reference's own (hair_msnn.cuh or path_tracing.cuh).
+// only).  Included by ref_path_entry.cpp, ref_pt_entry.cpp and
+// ref_nrc_entry.cpp after the reference's raygen source, so that
+// `LaunchParams` and `optixLaunchParams` are the reference's own
+// (hair_msnn.cuh, path_tracing.cuh or nrc.cuh).
 //
 // What it emulates:
 //  * owl::traceRay (hm_shim_trace_hook): the ray is answered by the oracle's
@@ -81,8 +82,8 @@ inline void log_event(int kind, int result, float t, float u, const float* o, co
   ++L->n;
 }
 
-// Fills optixLaunchParams' scene fields (shared by the MSNN and PT launch
-// parameter blocks) and the texture registry.
+// Fills optixLaunchParams' scene fields (shared by the MSNN, PT and NRC
+// launch parameter blocks) and the texture registry.
 template <class LP>
 void set_scene_params(LP& lp, const Scene& s, const float* camera12, const float* mat16, const int* settings9,
                       float scene_scale) {
@@ -115,8 +116,6 @@ void set_scene_params(LP& lp, const Scene& s, const float* camera12, const float
   lp.hairData.TRT_G = mat16[8];
   lp.hairData.TRRT_G = mat16[9];
   lp.MIS = settings9[4] != 0;
-  lp.pathV1 = settings9[2];
-  lp.pathV2 = settings9[3];
   lp.sceneScale = scene_scale;
   if (lp.hasEnvLight) {
     const int w = lp.envWidth, h = lp.envHeight;

@@ -67,6 +67,8 @@ void hmr_msnn_gbuffer(void* h, const float* camera12, const float* mat16, const 
   LaunchParams& lp = optixLaunchParams;
   lp = LaunchParams();
   hmref::set_scene_params(lp, *s, camera12, mat16, settings9, scene_scale);
+  lp.pathV1 = settings9[2];
+  lp.pathV2 = settings9[3];
   std::vector<GBuffer> gb(P);
   std::vector<int> tidx(train_idx, train_idx + n_train_idx);
   lp.pass = G_BUFFER;

@@ -38,6 +38,8 @@ void hmr_pt_frame(void* h, const float* camera12, const float* mat16, const int*
   LaunchParams& lp = optixLaunchParams;
   lp = LaunchParams();
   hmref::set_scene_params(lp, *s, camera12, mat16, settings9, scene_scale);
+  lp.pathV1 = settings9[2];
+  lp.pathV2 = settings9[3];
   lp.accumId = accum_id;
   lp.accumBuffer = (float4*)accum;
   lp.averageBuffer = (float4*)avg;

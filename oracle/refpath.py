@@ -2,8 +2,9 @@
 (test infrastructure only).
 
 oracle/_ref/libhmref_path.so holds the reference's cuda/hair_msnn.cu (with
-optix_common.cuh and the BSDF headers) and libhmref_pt.so its
-cuda/path_tracing.cu, both compiled unmodified through oracle/ref_shim/;
+optix_common.cuh and the BSDF headers), libhmref_pt.so its
+cuda/path_tracing.cu and libhmref_nrc.so its cuda/nrc.cu, all compiled
+unmodified through oracle/ref_shim/;
 their owl::traceRay is answered by the oracle's BVH (ref_harness.h).  They
 exist only where the reference checkout is present (oracle/build.py
 build_ref); everything here returns None / raises when they are absent.
@@ -34,7 +35,7 @@ def available():
 def _load(which):
     if which in _libs:
         return _libs[which]
-    name = {"path": "libhmref_path.so", "pt": "libhmref_pt.so"}[which]
+    name = {"path": "libhmref_path.so", "pt": "libhmref_pt.so", "nrc": "libhmref_nrc.so"}[which]
     path = os.path.join(_build.OUT_DIR, name)
     if not os.path.isfile(path):
         if not _build.ref_available():
@@ -55,6 +56,13 @@ def _load(which):
                                        F32P, I32P, i32, i32]
         L.hmr_msnn_render.restype = None
         L.hmr_msnn_render.argtypes = [vp, i32, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
+    elif which == "nrc":
+        L.hmr_nrc_scene_new.restype = vp
+        L.hmr_nrc_scene_new.argtypes = scene_args
+        L.hmr_nrc_scene_free.argtypes = [vp]
+        L.hmr_nrc_gbuffer.restype = None
+        L.hmr_nrc_gbuffer.argtypes = [vp, F32P, F32P, I32P, f32, i32, i32, I32P, i32, f32, i32, F32P, F32P, F32P,
+                                      I32P, F32P, I32P, i32]
     else:
         L.hmr_pt_scene_new.restype = vp
         L.hmr_pt_scene_new.argtypes = scene_args
@@ -90,7 +98,7 @@ class RefIntegrator:
             mat=np.ascontiguousarray(a["materials"], np.float32).ravel()[:16].copy(),
             sets=np.ascontiguousarray(osc.settings, np.int32))
         r = self._arr
-        new = L.hmr_scene_new if which == "path" else L.hmr_pt_scene_new
+        new = getattr(L, {"path": "hmr_scene_new", "pt": "hmr_pt_scene_new", "nrc": "hmr_nrc_scene_new"}[which])
         self.h = new(osc.h, r["cp"], len(r["cp"]) // 4, r["seg"], len(r["seg"]), r["vtx"], r["nrm"],
                      len(r["vtx"]) // 3, r["tri"], len(r["tri"]) // 3, r["env"], env_w, env_h, r["cpdf"], r["ccdf"],
                      r["mpdf"], r["mcdf"], r["dl"], len(a["dir_lights"]), r["mat"], r["sets"])
@@ -98,7 +106,8 @@ class RefIntegrator:
 
     def __del__(self):
         try:
-            (self.L.hmr_scene_free if self.which == "path" else self.L.hmr_pt_scene_free)(self.h)
+            getattr(self.L, {"path": "hmr_scene_free", "pt": "hmr_pt_scene_free",
+                             "nrc": "hmr_nrc_scene_free"}[self.which])(self.h)
         except Exception:
             pass
 
@@ -145,4 +154,20 @@ class RefIntegrator:
                    events=np.zeros((P, max_events, po.EV_FLOATS), np.float32), n_events=np.zeros(P, np.int32))
         self.L.hmr_pt_frame(self.h, r["cam"], r["mat"], r["sets"], self.osc.scene_scale, accum_id, out["accum"],
                             out["avg"], out["events"], out["n_events"], max_events, threads)
+        return out
+
+    def nrc_gbuffer(self, accum_id=0, every_nth=1, n_train=0, c=0.01, all_unbiased=False, max_events=128):
+        """The NRC G_BUFFER pass.  Returns a dict: gbuf [P, 8] (hit,
+        pathRadiance, beta, bounces), query [P + n_train, 9], train
+        [P, 40, 15] (each pixel's own train buffer), tinfo [P, 2] (bounces,
+        hit), events [P, max_events, 12], n_events [P]."""
+        assert self.which == "nrc"
+        P, r = self.P, self._arr
+        tidx = np.array([po.feistel_perm(t, n_train, accum_id) for t in range(n_train)], np.int32)
+        out = dict(gbuf=np.zeros((P, 8), np.float32), query=np.zeros((P + n_train, 9), np.float32),
+                   train=np.zeros((P, 40, 15), np.float32), tinfo=np.zeros((P, 2), np.int32),
+                   events=np.zeros((P, max_events, po.EV_FLOATS), np.float32), n_events=np.zeros(P, np.int32))
+        self.L.hmr_nrc_gbuffer(self.h, r["cam"], r["mat"], r["sets"], self.osc.scene_scale, accum_id, every_nth,
+                               tidx, len(tidx), c, 1 if all_unbiased else 0, out["gbuf"], out["query"], out["train"],
+                               out["tinfo"], out["events"], out["n_events"], max_events)
         return out

@@ -5,7 +5,7 @@ optix_common.cuh and the BSDF headers) are compiled unmodified on the host by
 oracle/build.py (build_ref) through oracle/ref_shim/; their traceRay is
 answered by the oracle's BVH.  This script renders one small seeded scene
 with them (the HairMSNN G_BUFFER pass at BETA 1 and 3, the RENDER pass over
-a seeded cache output, and the plain path tracer) and stores the scene's
+a seeded cache output, the NRC G_BUFFER pass and the plain path tracer) and stores the scene's
 arrays with the outputs, so the oracle restatement can be pinned against
 them wherever the reference checkout is absent
 (tests/test_ref_integrator.py).  Needs the reference checkout (HM_REF_DIR);
@@ -71,6 +71,14 @@ def main():
                     data[f"render_{tag}_avg_{k}"] = rr["avg"][k]
             for k in ("pt", "nn", "final"):
                 data[f"render_acc_in_{k}"] = acc[k]
+    nrc = rp.RefIntegrator(o, "nrc").nrc_gbuffer(accum_id=ACCUM, every_nth=every_nth, n_train=TRAIN, c=0.01,
+                                                  max_events=MAX_EV)
+    for k in ("gbuf", "query", "tinfo", "n_events"):
+        data[f"nrc_{k}"] = nrc[k]
+    tp = np.array([t * every_nth + po.feistel_perm(t, TRAIN, ACCUM) % every_nth for t in range(TRAIN)])
+    data["nrc_train_pixels"] = tp
+    data["nrc_train"] = nrc["train"][tp]
+    data["nrc_events"] = event_digest(nrc["events"], nrc["n_events"])
     pt = rp.RefIntegrator(o, "pt").pt_frame(accum_id=ACCUM, max_events=MAX_EV)
     data["pt_accum"] = pt["accum"]
     data["pt_n_events"] = pt["n_events"]

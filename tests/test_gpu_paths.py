@@ -1,0 +1,138 @@
+"""Per-path parity of the wavefront integrator against the oracle.
+
+The oracle's integrator is pinned ray by ray and bit for bit to the
+reference's own hair_msnn.cu / path_tracing.cu compiled on the host
+(tests/test_ref_integrator.py).  Here every GPU path is compared with the
+oracle's path of the same pixel through the per-path ray logs
+(hm_render_set_path_log and the oracle's event log): at every vertex the
+extension ray's origin, direction and hit (primitive, t, u), the RNG state
+when it was traced, and each shadow ray's origin, direction and visibility.
+
+The two can differ only through the transcendental functions (expf, logf,
+sinf, cosf, asinf, atan2f, powf, sinhf): every other operation of the
+shading is rounded the same way (no contraction), and the GPU recomputes
+each hit on its primitive with the oracle's arithmetic (refit_hit).
+
+The yardstick for "last-ulp differences" is the oracle itself: it renders
+the frame again with every transcendental result moved by a few ulps (one
+ulp up; one ulp down; pseudo-random -2..+2 ulps per call with four seeds:
+hmo_set_ulp_perturb), which gives, per path, whether it separates from
+itself and how far its colour moves (its spread).
+
+* A path whose log equals the oracle's to FINE (every ray within 2e-6, same
+  hits, same visibilities, same RNG state at every vertex) must agree in
+  colour (and, in HairMSNN frames, in its training target) within
+  COLOR_RTOL * |oracle| + COLOR_ATOL + SPREAD_K * spread; its cache-input row
+  bit for bit.  Most such paths meet COLOR_RTOL alone (reported): the spread
+  term covers grazing hits on a 0.04 mm fibre, where a u that differs in the
+  seventh digit moves the offset h across the fibre, and the BSDF with it,
+  by far more.
+* A path whose log separates from the oracle's must be one whose oracle
+  path also separates under the perturbed runs (its outcome is decided by
+  last-ulp differences: a grazing hit, a lobe or roulette threshold, an
+  ill-conditioned sample), or whose colour still meets the bar above.
+  Unexplained separations must not exceed UNEXPLAINED_MAX, and separations
+  must stay rare (SEPARATE_MAX, and no more than the oracle's own).
+
+The RNG state at each vertex pins the number of draws per vertex; their
+order inside a vertex is pinned by the colours (the oracle's draw order is
+the reference's: same RNG streams, same results, bit for bit).  Scenes shade
+curves with the reference's Catmull-Rom interpolator (the reference's own
+mode) and with the B-spline basis the renderer uses by default.
+Set HM_PATHS_DUMP=<dir> to keep every case's logs and colours as .npz.
+The comparison itself is tests/pathcheck.py.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from pathcheck import check_paths, color_excess, oracle_runs, separation, spread_of
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+VERTICES = 42
+
+
+@pytest.fixture(scope="module")
+def R():
+    from hairmsnn_gb300 import build, render
+    build.build()
+    return render
+
+
+def scene(R, catrom, res=64, strands=3000, view="side"):
+    cfg = R.straight_hair_scene(res, res, strands=strands, control_points=32, triangles=8000)
+    cfg["integrator"]["shade_catmull_rom"] = bool(catrom)
+    if view == "top":  # the head's top with the hair standing out of it: more hair vertices
+        cfg["camera"].update({"from": [0.0, -3.8, 1.0], "to": [0.0, 0.0, 0.6], "cos_fovy": 0.5})
+    return R.Scene(cfg)
+
+
+@pytest.mark.parametrize("catrom", [True, False])
+@pytest.mark.parametrize("view", ["side", "top"])
+def test_pt_paths_match_oracle(R, catrom, view):
+    s = scene(R, catrom, view=view)
+    r = R.Renderer(s, R.PT, frames_in_flight=1)
+    r.set_path_log(VERTICES)
+    r.frame()
+    img = r.read(R.IMAGE_FINAL).reshape(-1, 3)
+    g_log = r.read_path_log()
+    o = po.OracleScene.from_library(s)
+    runs = oracle_runs(o, 0, 3 * VERTICES, accum_id=0)
+    check_paths(g_log, img, runs, f"PT catrom={catrom} {view}", os.environ.get("HM_PATHS_DUMP"))
+
+
+@pytest.mark.parametrize("catrom", [True, False])
+@pytest.mark.parametrize("beta,view", [(1, "side"), (3, "top")])
+def test_msnn_paths_match_oracle(R, catrom, beta, view):
+    """The G-buffer pass: short-path colours, cache inputs and training
+    targets (full path minus short path) per path."""
+    s = scene(R, catrom, view=view)
+    r = R.Renderer(s, R.MSNN, beta=beta, train_records=1024, train=False, frames_in_flight=1)
+    r.set_path_log(VERTICES)
+    r.frame()
+    gbuf, nn_in, targets = r.buffer(4), r.buffer(0), r.buffer(3)
+    g_log = r.read_path_log()
+    st = r.stats()
+    o = po.OracleScene.from_library(s)
+    runs = oracle_runs(o, 1, 3 * VERTICES, beta=beta, accum_id=0, every_nth=st.every_nth,
+                       n_train=st.train_records)
+    agree = check_paths(g_log, gbuf[:, :3].astype(np.float64), runs, f"MSNN BETA={beta} catrom={catrom} {view}",
+                        os.environ.get("HM_PATHS_DUMP"))
+    o0 = runs[0]
+    assert np.array_equal(gbuf[:, 3].astype(np.int32)[agree], (o0["flags"] & 3)[agree])
+    # the cache-input row comes from the primary hit alone: bit for bit
+    prim_same = separation(g_log[:, :1], o0["log"][:, :1], tol=0.0)[0]
+    assert prim_same.mean() >= 0.99
+    assert np.array_equal(nn_in[prim_same].view(np.uint32), o0["nn_in"][prim_same].view(np.uint32))
+    train_px = np.nonzero(o0["flags"] & 4)[0]
+    assert len(train_px) == st.train_records
+    tm = train_px[agree[train_px]]
+    assert len(tm) >= 0.9 * len(train_px)
+    rec = tm // st.every_nth
+    err = color_excess(targets[rec], o0["train"][tm], spread_of(runs, "train")[tm])
+    assert err.max() <= 0, err.max()
+
+
+def test_compose_matches_oracle_render_pass(R):
+    """The RENDER pass (short path + cache on hair pixels; a training pixel
+    keeps its full colour and still gets the cache) against the oracle's
+    restatement, which is pinned bit for bit to the reference's own RENDER
+    pass: the first frame's FP64 sums hold the FP32 compose exactly."""
+    s = scene(R, True)
+    r = R.Renderer(s, R.MSNN, beta=1, train_records=1024, train=True, frames_in_flight=1)
+    r.frame()
+    gb = r.buffer(4)
+    nn_out = r.buffer(1)
+    g8 = np.zeros((len(gb), 8), np.float32)
+    flags = gb[:, 3].astype(np.int32)
+    g8[:, 0] = flags & 1
+    g8[:, 1] = (flags >> 1) & 1
+    g8[:, 5:8] = gb[:, :3]
+    ref = po.msnn_render(g8, nn_out, accum_id=0)
+    for which, k in ((R.IMAGE_FINAL, "final"), (R.IMAGE_SHORT, "pt"), (R.IMAGE_CACHE, "nn")):
+        img = r.read(which).reshape(-1, 3)
+        assert np.array_equal(img, ref["avg"][k][:, :3].astype(np.float64)), k

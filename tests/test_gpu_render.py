@@ -1,17 +1,16 @@
-"""GPU parity of the scene LBVH, traversal and wavefront integrator.
+"""GPU parity of the scene LBVH and traversal, and frame-level properties of
+the wavefront integrator.
 
 * BVH: device node array == the oracle's host build, bit for bit; so is
   the 8-wide collapse the kernels traverse (1, 2 or 4 leaves per segment).
 * Traversal: same closest primitive for >= 99.5% of rays; t within
   1e-4 relative where the primitive matches (the device contracts
-  multiply-adds in traversal; the oracle does not).
-* One frame of plain PT and of the HairMSNN G-buffer pass against the
-  oracle's integrator, which follows the reference's own per-pixel loops
-  (rayGenCam / msnnPathTrace / msnnTrainingPath / pathTrace): primary-hit
-  flags agree on >= 99.5% of pixels, cache-input rows within 1e-5 where the
-  primary hit agrees, and >= 95% of per-pixel path colours within
-  1e-3 * |ref| + 1e-4 (the rest diverge after a bounce through last-ulp
-  differences of transcendentals, which change later hits).
+  multiply-adds in traversal; the oracle does not; the shading then refits
+  each hit without contraction).
+* The integrator's per-path parity with the oracle is tests/test_gpu_paths.py;
+  here a PT frame lit by an OpenEXR environment map goes through the same
+  per-path comparison, and the frame-level properties are checked:
+  determinism, pipelined = serial frames bit for bit, read-back, training.
 """
 import numpy as np
 import pytest
@@ -95,29 +94,11 @@ def test_traversal_matches_oracle(R, split):
         assert np.all(np.abs(hg[hit, 0] - ho[hit, 0]) <= 1e-4 * np.abs(ho[hit, 0]) + 1e-6)
 
 
-def frame_compare(gpu_col, ref_col):
-    tol = 1e-3 * np.abs(ref_col) + 1e-4
-    ok = np.all(np.abs(gpu_col - ref_col) <= tol, axis=1)
-    return ok.mean()
-
-
-def test_pt_frame_matches_oracle_integrator(R):
-    res = 64
-    cfg = small_cfg(R, 1500, res)
-    s = R.Scene(cfg)
-    r = R.Renderer(s, R.PT)
-    r.frame()
-    img = r.read(R.IMAGE_FINAL).reshape(-1, 3)
-    o = po.OracleScene.from_library(s)
-    col, _, _, flags = o.render_pixels(0)
-    frac = frame_compare(img, col.astype(np.float64))
-    assert frac >= 0.95, frac
-    assert abs(img.mean() - col.mean()) <= 0.02 * col.mean()
-
-
-def test_pt_frame_with_exr_environment_matches_oracle(R, tmp_path):
-    """The same comparison with the sky replaced by an OpenEXR environment
-    map (ZIP-compressed, half floats) read from a file."""
+def test_pt_frame_with_exr_environment_matches_oracle_per_path(R, tmp_path):
+    """A PT frame with the sky replaced by an OpenEXR environment map
+    (ZIP-compressed, half floats) read from a file, compared with the oracle
+    path by path (tests/pathcheck.py)."""
+    from pathcheck import check_paths, oracle_runs
     from test_exr_env import write_exr
     h, w = 64, 128
     y, x = np.mgrid[0:h, 0:w].astype(np.float64)
@@ -128,38 +109,12 @@ def test_pt_frame_with_exr_environment_matches_oracle(R, tmp_path):
     cfg["lights"] = {"environment": {"exr": "env.exr", "scale": 1.0, "rotation": 0.3}}
     s = R.Scene(cfg, str(tmp_path))
     assert s.info().env_width == w
-    r = R.Renderer(s, R.PT)
+    r = R.Renderer(s, R.PT, frames_in_flight=1)
+    r.set_path_log(42)
     r.frame()
     img = r.read(R.IMAGE_FINAL).reshape(-1, 3)
-    col, _, _, _ = po.OracleScene.from_library(s).render_pixels(0)
-    frac = frame_compare(img, col.astype(np.float64))
-    assert frac >= 0.95, frac
-    assert abs(img.mean() - col.mean()) <= 0.02 * col.mean()
-
-
-def test_msnn_gbuffer_matches_oracle_integrator(R):
-    res = 64
-    cfg = small_cfg(R, 1500, res)
-    s = R.Scene(cfg)
-    r = R.Renderer(s, R.MSNN, beta=1, train_records=1024, train=False)
-    r.frame()
-    gbuf = r.buffer(4)
-    nn_in = r.buffer(0)
-    targets = r.buffer(3)
-    o = po.OracleScene.from_library(s)
-    st = r.stats()
-    col, onn, otr, flags = o.render_pixels(1, beta=1, accum_id=0, every_nth=st.every_nth, n_train=st.train_records)
-    gflags = gbuf[:, 3].astype(np.int32)
-    assert (gflags == (flags & 3)).mean() >= 0.995
-    same = gflags == (flags & 3)
-    assert np.abs(nn_in[same] - onn[same]).max() <= 1e-5
-    frac = frame_compare(gbuf[:, :3].astype(np.float64), col.astype(np.float64))
-    assert frac >= 0.95, frac
-    train_px = np.nonzero(flags & 4)[0]
-    assert len(train_px) == st.train_records
-    rec = train_px // st.every_nth
-    tfrac = frame_compare(targets[rec].astype(np.float64), otr[train_px].astype(np.float64))
-    assert tfrac >= 0.9, tfrac
+    runs = oracle_runs(po.OracleScene.from_library(s), 0, 126, accum_id=0)
+    check_paths(r.read_path_log(), img, runs, "PT EXR environment")
 
 
 def test_render_is_deterministic_and_finite(R):

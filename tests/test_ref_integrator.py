@@ -1,6 +1,6 @@
 """The oracle's integrator pinned to the reference's own integrator.
 
-The reference's cuda/hair_msnn.cu and cuda/path_tracing.cu (rayGenCam,
+The reference's cuda/hair_msnn.cu, cuda/path_tracing.cu and cuda/nrc.cu (rayGenCam,
 msnnPathTrace, msnnTrainingPath, msnnNextPathVertex, pathTrace, and through
 optix_common.cuh directLighting, sampleLights, sampleBSDF, the environment
 light, hairCH, triangleMeshCH, miss) are compiled unmodified on the host
@@ -106,6 +106,25 @@ def test_oracle_render_pass_matches_reference_golden(gold):
             assert np.array_equal(bits(out["avg"][k]), bits(gold[f"render_{tag}_avg_{k}"]))
 
 
+def test_oracle_nrc_matches_reference_golden(gold, gold_scene):
+    """nrcTracePaths / rayGenCam of cuda/nrc.cu: G-buffer, the pixels' and
+    training suffixes' cache queries, the training pixels' train buffers."""
+    en = int(gold["every_nth"])
+    P = gold_scene.width * gold_scene.height
+    o = gold_scene.render_nrc(accum_id=3, every_nth=en, n_train=P // en, c=0.01, max_events=48)
+    g = gold["nrc_gbuf"]
+    assert np.array_equal(o["gbuf"][:, 6], g[:, 0])
+    assert np.array_equal(bits(o["gbuf"][:, 0:6]), bits(g[:, 1:7]))
+    assert np.array_equal(bits(o["query"]), bits(gold["nrc_query"][:P]))
+    tp = gold["nrc_train_pixels"]
+    assert np.array_equal(np.nonzero(o["tinfo"][:, 3])[0], np.sort(tp))
+    assert np.array_equal(bits(o["suffix_query"][tp]), bits(gold["nrc_query"][P + tp // en]))
+    assert np.array_equal(o["tinfo"][tp, :2], gold["nrc_tinfo"][tp])
+    assert np.array_equal(bits(o["records"][tp]), bits(gold["nrc_train"]))
+    assert np.array_equal(o["n_events"], gold["nrc_n_events"])
+    assert np.array_equal(digest(o["events"], o["n_events"]), gold["nrc_events"])
+
+
 def test_golden_scene_exercises_the_branches(gold):
     """The fixture reaches the branches a frame bar would hide: head-surface
     (GGX) vertices, hair vertices, misses, training pixels, multi-bounce paths."""
@@ -177,3 +196,29 @@ def test_oracle_render_pass_matches_reference_live():
         for k in ("pt", "nn", "final"):
             assert np.array_equal(bits(o_["acc"][k]), bits(r["acc"][k]))
             assert np.array_equal(bits(o_["avg"][k]), bits(r["avg"][k]))
+
+
+@needs_ref
+@pytest.mark.parametrize("unbiased", [False, True])
+def test_oracle_nrc_matches_reference_live(unbiased):
+    o = _live_scene(6000)
+    P = o.width * o.height
+    en = 4
+    ref = refpath.RefIntegrator(o, "nrc").nrc_gbuffer(accum_id=5, every_nth=en, n_train=P // en, c=0.01,
+                                                      all_unbiased=unbiased, max_events=160)
+    on = o.render_nrc(accum_id=5, every_nth=en, n_train=P // en, c=0.01, max_events=160)
+    if unbiased:  # the oracle has no all-unbiased switch: compare the unbiased pixels only
+        keep = (np.arange(P) // en) % 16 == 0
+    else:
+        keep = np.ones(P, bool)
+    g = ref["gbuf"]
+    assert np.array_equal(on["gbuf"][keep, 6], g[keep, 0])
+    assert np.array_equal(bits(on["gbuf"][keep, 0:6]), bits(g[keep, 1:7]))
+    assert np.array_equal(bits(on["query"][keep]), bits(ref["query"][:P][keep]))
+    tp = np.nonzero(on["tinfo"][:, 3] & keep)[0]
+    assert len(tp) > 10
+    assert np.array_equal(bits(on["suffix_query"][tp]), bits(ref["query"][P + tp // en]))
+    assert np.array_equal(on["tinfo"][tp, :2], ref["tinfo"][tp])
+    assert np.array_equal(bits(on["records"][tp]), bits(ref["train"][tp]))
+    assert np.array_equal(on["n_events"][keep], ref["n_events"][keep])
+    assert np.array_equal(bits(events_as_reference(on["events"])[keep]), bits(ref["events"][keep]))

@@ -99,20 +99,36 @@ def spread_of(runs, key):
     return np.max([np.abs(runs[k][key] - o0) for k in PERTURBED], axis=0)
 
 
-def color_excess(got, ref, spread):
-    """> 0 where `got` misses the bar around `ref`."""
-    return np.abs(got - ref) - (COLOR_RTOL * np.abs(ref) + COLOR_ATOL + SPREAD_K * spread)
+def color_excess(got, ref, spread, extra=0.0):
+    """> 0 where `got` misses the bar around `ref` (extra: an added
+    tolerance, e.g. hit_normal_tolerance for surface normals)."""
+    return np.abs(got - ref) - (COLOR_RTOL * np.abs(ref) + COLOR_ATOL + SPREAD_K * spread + extra)
 
 
-def check_paths(g_log, g_col, runs, label, dump=None):
-    """Applies the per-path criterion; returns the paths whose logs agree."""
+def hit_normal_tolerance(g_log, o_log, radius):
+    """Per path: how far a hair normal may turn between the two logs' hits.
+    The normal points from the fibre's axis to the hit point, so a hit point
+    that moves by dp along a fibre of radius r turns it by up to dp / r; dp
+    is bounded by the largest difference of the extension hits' distance,
+    direction (times t) and origin.  Four times that, in each component."""
+    ext = g_log.view(np.int32)[:, :, 7] == 0
+    t = np.abs(o_log[:, :, 1])
+    dp = np.abs(g_log[:, :, 1] - o_log[:, :, 1]) + t * np.abs(g_log[:, :, 4:7] - o_log[:, :, 4:7]).max(-1) + \
+        np.abs(g_log[:, :, 8:11] - o_log[:, :, 8:11]).max(-1)
+    dp = np.where(ext & np.isfinite(dp), dp, 0.0).max(1)
+    return 4.0 * dp / radius
+
+
+def check_paths(g_log, g_col, runs, label, dump=None, extra_tol=0.0):
+    """Applies the per-path criterion; returns the paths whose logs agree.
+    extra_tol [P, m] (or a scalar): an added tolerance per path and column."""
     o0 = runs[0]
     agree, first = separation(g_log, o0["log"])
     self_sep = np.zeros(len(agree), bool)
     for k in PERTURBED:
         self_sep |= ~separation(runs[k]["log"], o0["log"])[0]
     spread = spread_of(runs, "col")
-    excess = color_excess(g_col, o0["col"], spread).max(1)
+    excess = color_excess(g_col, o0["col"], spread, extra_tol).max(1)
     strict = (np.abs(g_col - o0["col"]) <= COLOR_RTOL * np.abs(o0["col"]) + COLOR_ATOL).all(1)
     sep = ~agree
     unexplained = sep & ~self_sep & (excess > 0)

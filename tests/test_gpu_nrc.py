@@ -6,7 +6,9 @@ Per path, through the per-path ray logs (tests/pathcheck.py, the criterion
 of tests/test_gpu_paths.py): paths whose rays agree with the oracle's must
 agree in their G-buffer (radiance gathered before the cache, throughput at
 the cache query), their cache-query row and their training suffix's query
-row; training pixels with agreeing paths in their train-buffer records and
+row (a query's hair normal points from the fibre axis to the hit point, so
+it may turn by the hit point's difference over the fibre radius:
+hit_normal_tolerance); training pixels with agreeing paths in their train-buffer records and
 bounce counts; the unbiased pixels (every 16th) exactly.  Paths that
 separate must be ones the oracle separates itself under last-ulp changes.
 Frames with online training give a finite image, lower the training loss,
@@ -32,7 +34,7 @@ def R():
 
 @pytest.mark.parametrize("catrom", [True, False])
 def test_nrc_paths_match_oracle(R, catrom):
-    from pathcheck import check_paths, color_excess, nrc_oracle_runs, spread_of
+    from pathcheck import check_paths, color_excess, hit_normal_tolerance, nrc_oracle_runs, spread_of
     res = 64
     cfg = R.straight_hair_scene(res, res, strands=6000)
     cfg["integrator"]["shade_catmull_rom"] = catrom
@@ -54,7 +56,13 @@ def test_nrc_paths_match_oracle(R, catrom):
     suffix = np.zeros((P, 9), np.float32)
     suffix[tp] = q[P + tr]
     g_col = np.concatenate([gbuf[:, :3], gbeta[:, :3], q[:P], suffix], 1).astype(np.float64)
-    agree = check_paths(r.read_path_log(), g_col, runs, f"NRC catrom={catrom}", os.environ.get("HM_PATHS_DUMP"))
+    g_log = r.read_path_log()
+    # the query rows' normals (columns 12-14, 21-23) turn with the hit point
+    extra = np.zeros_like(g_col)
+    nt = hit_normal_tolerance(g_log, o0["log"], cfg["hair"]["procedural"]["radius"])
+    extra[:, 12:15] = nt[:, None]
+    extra[:, 21:24] = nt[:, None]
+    agree = check_paths(g_log, g_col, runs, f"NRC catrom={catrom}", os.environ.get("HM_PATHS_DUMP"), extra)
     assert ((gbuf[:, 3] > 0.5) == (o0["hit"] > 0.5))[agree].all()
     # training pixels: unbiased flags exactly; bounce counts and records where the path agrees
     ot = o0["tinfo"][tp]

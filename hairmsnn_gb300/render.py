@@ -430,341 +430,6 @@ def straight_hair_scene(width=512, height=512, strands=10000, control_points=64,
     }
 
 
-RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
-NODE_BYTES = 224              # one 8-wide BVH node: eight child boxes + child codes
-PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
-# DRAM bytes per extension ray of the extension traversal kernel (8-wide
-# BVH), from ncu (dram__bytes_read.sum + dram__bytes_write.sum) of the first
-# launch of a 256x256 frame of this scene: 42.1 MB for its 65,536 camera
-# rays.  ncu runs each launch with cold caches, so this is an upper bound
-# for warm frames.
-EXTEND_DRAM_BYTES_PER_RAY = 643
-
-
-class RenderBenchWorkload:
-    """bench.py workload: one frame (1 spp) of the full HairMSNN render per
-    step, in the chosen form: FP16 cache network on the tensor cores
-    (training and inference), frames in flight, graph replay, autotuned
-    launch shapes, two BVH leaves per segment."""
-
-    name = "render"
-    metric = "paths/s (HairMSNN full wavefront render, 512x512, 1 spp/frame, online cache training 2^16/frame)"
-    unit = "paths/s"
-    cache_precision = 1  # FP16 (tcgen05); its relMSE equals the FP32 cache's (quality workload)
-    dtype = "f32 (traversal, shading, FP64 sums); f16 cache MLP with f32 accumulation"
-
-    def __init__(self, torch, width=512, height=512, train_records=1 << 16, frames_in_flight=0):
-        self.torch = torch
-        self.width, self.height, self.train_records = width, height, train_records
-        self.frames_in_flight = frames_in_flight
-        self.cfg = straight_hair_scene(width, height)
-        self.scene = Scene(self.cfg)
-        self.scene.build()
-        self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True,
-                          precision=self.cache_precision, frames_in_flight=frames_in_flight)
-        self.tuning = self.r.autotune(frames=6)
-        self.P = width * height
-        self.h2d_bytes = 0
-        self.d2h_bytes = self.P * 3 * 8
-        self.stage_ms = []
-        self.launches = []
-        self.read_stream = torch.cuda.Stream()
-        self.host_sums = [torch.empty((height, width, 3), dtype=torch.float64, pin_memory=True) for _ in range(2)]
-
-    def step(self, events=None):
-        """One frame enqueued (frames run pipelined on the renderer's own streams)."""
-        self.r.frame()
-        self.launches.append(self.r.timings().kernel_launches)
-
-    def timed_region(self, steps, flush):
-        """Device time of `steps` pipelined frames: an event on the submitting
-        stream before the first frame, the renderer's completion joined back
-        (hm_render_wait) before the closing event.  No L2 flush: every frame
-        streams its own path state (about 90 MB per frame in flight at
-        512x512, several frames in flight) past the 129 MB L2, and a flush
-        kernel on the submitting stream would run beside the frames in
-        flight rather than between them."""
-        torch = self.torch
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        for k in range(steps):
-            self.step()
-        self.r.wait()
-        t1.record()
-        torch.cuda.synchronize()
-        self.last_ms = t0.elapsed_time(t1) / steps
-        return self.last_ms
-
-    @property
-    def kernels_per_step(self):
-        return int(round(np.mean(self.launches[-8:]))) if self.launches else 0
-
-    def e2e_region(self, steps):
-        """Wall time per frame through the public API with the result read back
-        every frame: hm_render_frame, then hm_render_read_async of the FP64
-        image sums into pinned host memory on a separate stream (the next
-        frame's accumulation waits for that copy); host synchronisation at
-        both ends."""
-        import time
-        torch = self.torch
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k in range(steps):
-            self.r.frame()
-            self.r.read_async(self.host_sums[k & 1], IMAGE_FINAL, stream=self.read_stream)
-        torch.cuda.synchronize()
-        el = time.perf_counter() - t0
-        self.host_img = self.host_sums[(steps - 1) & 1].numpy() / self.r.stats().frames
-        return 1e3 * el / steps
-
-    def e2e_step(self):
-        self.r.frame()
-        self.r.read_async(self.host_sums[0], IMAGE_FINAL, stream=self.read_stream)
-
-    def n_events(self):
-        return 2
-
-    def units_per_step(self):
-        return self.P
-
-    def profile_frames(self, n=4):
-        """Synchronous instrumented frames (per-stage CUDA events on the frame's
-        stream) for the stage breakdown and the roofline."""
-        self.r.instrument(timing=True, counting=False)
-        for _ in range(n):
-            self.r.frame()
-            self.stage_ms.append(self.r.timings().as_dict())
-        self.r.instrument(timing=False, counting=False)
-
-    def counted_frame(self):
-        """One untimed frame with traversal work counters."""
-        self.r.instrument(timing=True, counting=True)
-        self.r.frame()
-        t = self.r.timings()
-        self.r.instrument(timing=False, counting=False)
-        return t
-
-    def plain_form(self, frames=20):
-        """The plain FP32 wavefront form on the same scene and GPU: FP32 cache,
-        one frame in flight, kernel-by-kernel launches, default launch
-        shapes, one BVH leaf per segment.  Pipelined frame time."""
-        torch = self.torch
-        cfg = dict(self.cfg)
-        cfg["integrator"] = dict(cfg["integrator"], segment_splits=1)
-        sc = Scene(cfg)
-        r = Renderer(sc, MSNN, beta=1, train_records=self.train_records, train=True, precision=0,
-                     frames_in_flight=1)
-        r.set_graphs(False)
-        for _ in range(3):
-            r.frame()
-        r.wait()
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        for _ in range(frames):
-            r.frame()
-        r.wait()
-        t1.record()
-        torch.cuda.synchronize()
-        ms = t0.elapsed_time(t1) / frames
-        r.close()
-        sc.close()
-        return ms
-
-    def roofline(self, seg_ms, pk):
-        keys = ["extend_ms", "shade_ms", "shadow_ms", "compact_ms", "train_ms", "infer_ms", "compose_ms",
-                "camera_ms", "finalize_ms"]
-        if not self.stage_ms:
-            self.profile_frames()
-        n = max(1, min(len(self.stage_ms), 16))
-        mean = {k: float(np.mean([s[k] for s in self.stage_ms[-n:]])) for k in keys}
-        c = self.counted_frame()
-        dominant = max(("extend_ms", "shadow_ms", "shade_ms", "train_ms", "infer_ms"), key=lambda k: mean[k])
-        out = {"stage_ms_per_frame": {k: round(v, 4) for k, v in mean.items()},
-               "rays_per_frame": {"extension": int(c.extension_rays), "shadow": int(c.shadow_rays)},
-               "bvh_work_per_frame": {"extend_nodes": int(c.extend_nodes), "extend_prims": int(c.extend_prims),
-                                      "shadow_nodes": int(c.shadow_nodes), "shadow_prims": int(c.shadow_prims)}}
-        if dominant in ("extend_ms", "shadow_ms"):
-            if dominant == "extend_ms":
-                rays, nodes, prims = c.extension_rays, c.extend_nodes, c.extend_prims
-            else:
-                rays, nodes, prims = c.shadow_rays, c.shadow_nodes, c.shadow_prims
-            alg = rays * RAY_RECORD_BYTES + nodes * NODE_BYTES + prims * PRIM_BYTES
-            ach = alg / (mean[dominant] * 1e-3) / 1e9
-            out.update({"kernel": dominant.replace("_ms", "_kernel"), "bound": "hbm", "achieved": round(ach, 2),
-                        "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
-                        "traffic": (int(rays * EXTEND_DRAM_BYTES_PER_RAY) if dominant == "extend_ms" else None),
-                        "traffic_basis": "DRAM bytes per frame: ncu cold-cache capture at 256x256 scaled by rays",
-                        "algorithmic_bytes_per_frame": int(alg),
-                        "note": ("algorithmic bytes = rays x 48 B + 8-wide BVH nodes visited x 224 B + primitives "
-                                 "tested x 64 B, counted in an untimed frame; the 90 MB BVH and 10 MB of curves "
-                                 "are L2-resident, so this can exceed the HBM copy peak ("
-                                 + pk["source"] + ")")})
-        else:
-            out.update({"kernel": dominant, "bound": "tensor", "achieved": None, "peak": pk["bf16_tflops"],
-                        "unit": "TFLOP/s", "frac": None, "traffic": None})
-        if type(self) is RenderBenchWorkload:
-            plain = self.plain_form()
-            chosen = self.last_ms if getattr(self, "last_ms", None) else None
-            out["plain_fp32_wavefront_form"] = {
-                "ms_per_frame": round(plain, 3), "paths_per_s": round(self.P / (plain * 1e-3), 1),
-                "chosen_form_speedup": round(plain / chosen, 3) if chosen else None,
-                "what": "FP32 cache, 1 frame in flight, kernel-by-kernel launches, default launch shapes, "
-                        "1 BVH leaf per segment; same scene and GPU"}
-        return out
-
-    workload_name = ("render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments, 2 BVH "
-                     "leaves each), 20k-tri head, Preetham sky T=3 + directional (3,3,3), 512x512, "
-                     "path_v1=1, path_v2=40, BETA=1, cache HashGrid/OneBlob MLP 64x2 in FP16 on tcgen05 "
-                     "(training and inference; FP32 master weights), 2^16 training records/frame")
-
-    def config(self):
-        return {"workload": self.workload_name,
-                "cache_precision": "fp16" if self.cache_precision == 1 else "fp32",
-                "pixels": self.P, "train_records": self.train_records,
-                "l2": "inputs larger than L2: each frame in flight streams its own ~90 MB path state, with "
-                      "several frames in flight, past the 129 MB L2 (scene: 8-wide BVH 90 MB + curves 10 MB); "
-                      "no flush kernel",
-                "frames_in_flight": self.r.depth(),
-                "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
-                "parallelism": "replicas"}
-
-    def cpu_baseline(self, threads, budget_s=20.0):
-        """The oracle's reference-structured integrator (rayGenCam G-buffer pass,
-        msnnPathTrace / msnnTrainingPath) on the host cores, bounded sample of
-        pixels of the same scene; the cache's inference and training gradient
-        by the oracle's C++ FP32 transcription on the same threads."""
-        import time
-        from oracle import mlp_oracle as mo
-        from oracle import pyoracle as po
-        o = po.OracleScene.from_library(self.scene)
-        net = self.r
-        cfg_text = json.dumps(_default_cache_config())
-        oc = mo.Config(cfg_text, 12, 3)
-        params = np.random.default_rng(0).normal(scale=0.05, size=oc.n_params)
-        every = max(1, self.P // self.train_records)
-        n = 4096
-        t0 = time.perf_counter()
-        done = 0
-        p0 = (self.height // 2) * self.width  # a band through the hair
-        while True:
-            col, nn_in, tr, fl = o.render_pixels(1, beta=1, accum_id=done // self.P, every_nth=every,
-                                                 n_train=self.train_records, p0=p0, n=n, threads=threads)
-            po.mlp_forward_host(oc, params, nn_in, threads=threads)
-            tmask = (fl & 4) != 0
-            if tmask.any():
-                po.mlp_grad_host(oc, params, nn_in[tmask], tr[tmask], threads=threads)
-            done += n
-            p0 = (p0 + n) % (self.P - n)
-            if time.perf_counter() - t0 > budget_s:
-                break
-        el = time.perf_counter() - t0
-        return {"value": round(done / el, 1), "unit": self.unit, "cores": threads, "kind": "port",
-                "sample": f"{done} pixels (1 spp) of the same scene: oracle rayGenCam/msnnPathTrace/"
-                          f"msnnTrainingPath on {threads} threads + the cache's inference and training "
-                          f"gradient in C++ FP32 on the same threads"}
-
-
-class RenderQualityWorkload(RenderBenchWorkload):
-    """HairMSNN (BETA=1, online cache training) against plain path tracing and
-    the reference's NRC comparison renderer (online training, 65536 records
-    per frame) on the render workload's scene: relMSE of each at 16 spp against a
-    converged PT reference of the same scene, their frame times, and the PT
-    sample count (and time) needed to reach HairMSNN's relMSE, assuming PT's
-    relMSE falls as 1/spp (it is unbiased).  The reference uses frames
-    16 .. 16 + ref_spp of one PT run, so it shares no random numbers with
-    the 16-spp estimates (the path RNG is seeded by the frame index, as in
-    the reference).  The HairMSNN relMSE is also reported with the cache's
-    inference in FP16, BF16 and E4M3 on the tensor cores (training FP32).
-    One step = one HairMSNN frame, as the render workload."""
-
-    name = "quality"
-    metric = "paths/s at fixed relMSE vs PT (HairMSNN BETA=1, 512x512, 16 spp, online cache training 2^16/frame)"
-
-    def __init__(self, torch, width=512, height=512, train_records=1 << 16, spp=16, ref_spp=1024,
-                 pretrain_passes=256):
-        super().__init__(torch, width, height, train_records)
-        self.spp, self.ref_spp, self.pretrain_passes = spp, ref_spp, pretrain_passes
-
-    def _timed_frames(self, r, n):
-        torch = self.torch
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        for _ in range(n):
-            r.frame()
-        r.wait()
-        t1.record()
-        torch.cuda.synchronize()
-        return t0.elapsed_time(t1) / n
-
-    def quality(self):
-        spp = self.spp
-        pt = Renderer(self.scene, PT, frames_in_flight=self.frames_in_flight)
-        pt_ms = self._timed_frames(pt, spp)
-        pt_img = pt.read(IMAGE_FINAL)
-        ref_ms = self._timed_frames(pt, self.ref_spp)
-        total = pt.read(IMAGE_FINAL) * (spp + self.ref_spp)
-        ref = (total - pt_img * spp) / self.ref_spp
-        pt.close()
-        by_prec = {}
-        for name, prec in (("fp32", 0), ("fp16", 1), ("bf16", 2), ("fp8", 3)):
-            ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
-                          precision=prec, frames_in_flight=self.frames_in_flight)
-            t_ms = self._timed_frames(ms, spp)
-            img = ms.read(IMAGE_FINAL)
-            ms.close()
-            by_prec[name] = {"relmse": round(relmse(img, ref), 6), "ms_per_frame": round(t_ms, 3)}
-            if name == "fp32":
-                ms_ms, ms_img = t_ms, img
-        # the reference's initial training before the first frame (one second
-        # of scene-sample passes there; a fixed pass count here)
-        ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
-                      frames_in_flight=self.frames_in_flight)
-        torch = self.torch
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        ms.pretrain(self.pretrain_passes)
-        t1.record()
-        torch.cuda.synchronize()
-        pre_ms = t0.elapsed_time(t1)
-        t_pre = self._timed_frames(ms, spp)
-        e_pre = relmse(ms.read(IMAGE_FINAL), ref)
-        ms.close()
-        # the reference's comparison renderer: NRC with online training
-        # (65536 records per frame, c = 0.01), same frames
-        nrc = Renderer(self.scene, NRC, train=True, frames_in_flight=self.frames_in_flight)
-        nrc_ms = self._timed_frames(nrc, spp)
-        e_nrc = relmse(nrc.read(IMAGE_FINAL), ref)
-        nrc.close()
-        e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
-        eq_spp = spp * e_pt / e_ms
-        return {"spp": spp, "reference_spp": self.ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
-                "msnn": {"relmse": round(e_ms, 6), "ms_per_frame": round(ms_ms, 3),
-                         "paths_per_s": round(self.P / (ms_ms * 1e-3), 1)},
-                "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
-                       "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
-                "nrc": {"relmse": round(e_nrc, 6), "ms_per_frame": round(nrc_ms, 3),
-                        "paths_per_s": round(self.P / (nrc_ms * 1e-3), 1),
-                        "pt_spp_for_same_relmse": round(spp * e_pt / e_nrc, 2),
-                        "speedup_at_equal_relmse": round((spp * e_pt / e_nrc) * pt_ms / (spp * nrc_ms), 3)},
-                "msnn_by_cache_precision": by_prec,
-                "msnn_after_scene_sample_training": {
-                    "passes": self.pretrain_passes, "training_ms": round(pre_ms, 1), "relmse": round(e_pre, 6),
-                    "ms_per_frame": round(t_pre, 3), "pt_spp_for_same_relmse": round(spp * e_pt / e_pre, 2),
-                    "speedup_at_equal_relmse": round((spp * e_pt / e_pre) * pt_ms / (spp * t_pre), 3)},
-                "pt_spp_for_msnn_relmse": round(eq_spp, 2),
-                "speedup_at_equal_relmse": round(eq_spp * pt_ms / (spp * ms_ms), 3)}
-
-    def roofline(self, seg_ms, pk):
-        out = super().roofline(seg_ms, pk)
-        out["quality"] = self.quality()
-        return out
-
-    def config(self):
-        c = super().config()
-        c["workload"] = "quality: " + c["workload"] + f"; relMSE at {self.spp} spp vs PT {self.ref_spp} spp"
-        return c
-
-
 def batch_scene_configs(n=64, seed=0):
     """The batched-render workload's scenes (seeded): square images of side
     128, 256, 512 or 1024; log-uniform 2k-50k curly strands (helix radius
@@ -785,65 +450,6 @@ def batch_scene_configs(n=64, seed=0):
         cfgs.append(cfg)
         betas.append(int(rng.integers(0, 11)))
     return cfgs, betas
-
-
-class BatchBenchWorkload(RenderBenchWorkload):
-    """bench.py workload: one frame (1 spp) of each of 64 uneven scenes,
-    rendered as one batch with one shared FP32 cache network (width 64)."""
-
-    dtype = "f32"
-
-    name = "batch"
-    metric = "paths/s (64 concurrent HairMSNN scenes, 128^2..1024^2, 2k-50k curly strands, one shared cache)"
-    unit = "paths/s"
-
-    def __init__(self, torch, n_scenes=64, train_records=1 << 16):
-        import time
-        self.torch = torch
-        self.train_records = train_records
-        t0 = time.perf_counter()
-        cfgs, self.betas = batch_scene_configs(n_scenes)
-        self.scenes = [Scene(c) for c in cfgs]
-        for sc in self.scenes:
-            sc.build()
-        self.setup_s = time.perf_counter() - t0
-        self.r = BatchRenderer(self.scenes, MSNN, betas=self.betas, train_records=train_records, train=True)
-        self.tuning = self.r.autotune(frames=1)
-        self.P = self.r.pixels
-        self.h2d_bytes = 0
-        self.d2h_bytes = self.P * 3 * 8
-        self.stage_ms = []
-        self.launches = []
-        self.read_stream = torch.cuda.Stream()
-        self.host_sums = [torch.empty((self.P, 3), dtype=torch.float64, pin_memory=True) for _ in range(2)]
-        self.n_scenes = n_scenes
-        infos = [sc.info() for sc in self.scenes]
-        self.stats_scenes = {"pixels": self.P, "segments": int(sum(i.n_segments for i in infos)),
-                             "strands": int(sum(i.n_strands for i in infos))}
-
-    def e2e_region(self, steps):
-        import time
-        torch = self.torch
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for k in range(steps):
-            self.r.frame()
-            self.r.read_async(self.host_sums[k & 1], IMAGE_FINAL, stream=self.read_stream)
-        torch.cuda.synchronize()
-        return 1e3 * (time.perf_counter() - t0) / steps
-
-    def config(self):
-        return {"workload": f"batch: {self.n_scenes} scenes (seeded), sides 128/256/512/1024, log-uniform 2k-50k "
-                            "curly strands (helix r 2-8 mm, pitch 5-20 mm, 48-128 CPs), BETA 0..10, sigma_a "
-                            "U[0.02,0.5]^3, one shared FP32 cache (HashGrid/OneBlob MLP 64x2), 2^16 records/frame",
-                **self.stats_scenes, "frames_in_flight": self.r.depth(), "scene_setup_s": round(self.setup_s, 1),
-                "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
-                "l2": "inputs larger than L2 (path state of tens of millions of paths); no flush kernel",
-                "parallelism": "replicas"}
-
-    def cpu_baseline(self, threads, budget_s=20.0):
-        return {"value": None, "unit": self.unit, "cores": threads, "kind": "port",
-                "sample": "not run for the batch workload (see the render workload's CPU baseline)"}
 
 
 def _default_cache_config():
@@ -890,201 +496,3 @@ def curly_hair_diff_scene(width=256, height=256, strands=20000, control_points=9
         {"sigma_a": [float(x) for x in r[0:3]], "beta_m": float(r[3]), "beta_n": float(r[4]),
          "alpha": float(np.rad2deg(r[5]))} for r in mats]}
     return cfg, mats
-
-
-class DiffBenchWorkload:
-    """bench.py workload: one gradient evaluation per step of the
-    differentiable appearance fit.  A step renders 64 frames (1 spp each) of
-    20k curly strands at 256x256, HairMSNN with BETA=2 and the cache frozen
-    (hm_render_diff_forward), forms the L2 image loss against a target
-    rendered at the true materials, and replays the paths
-    (hm_render_diff_backward) for dL/d(sigma_a, beta_m, beta_n, alpha) of 4
-    strand groups and dL/dW of the cache.  The target is rendered once with
-    the same frame seeds; the materials start with sigma_a 50% off."""
-
-    name = "diff"
-    metric = ("gradient evaluations/s (path replay: dL/d(material) of 4 strand groups + dL/dW, 20k curly strands, "
-              "256x256, 64 spp, BETA=2)")
-    unit = "gradient evaluations/s"
-
-    def __init__(self, torch, width=256, height=256, spp=64, strands=20000, groups=4, pretrain_passes=64):
-        self.torch = torch
-        self.width, self.height, self.spp, self.groups = width, height, spp, groups
-        self.cfg, self.truth = curly_hair_diff_scene(width, height, strands=strands, groups=groups)
-        self.scene = Scene(self.cfg)
-        self.scene.build()
-        self.scene.set_group_materials(self.truth)
-        self.r = Renderer(self.scene, MSNN, beta=2, train_records=1 << 14, train=True)
-        self.tuning = self.r.autotune(frames=4)
-        self.r.pretrain(pretrain_passes)
-        self.P = width * height
-        self.n = self.P * 3
-        self.r.diff_forward(spp)
-        self.target = (self.r.device_sums(5) / spp).clone()
-        self.target_host = self.target.cpu().numpy()
-        self.start = self.truth.copy()
-        self.start[:, 0:3] *= np.where(np.random.default_rng(11).random((groups, 3)) < 0.5, 0.5, 1.5)
-        self.scene.set_group_materials(self.start)
-        self.h2d_bytes = self.P * 3 * 4
-        self.d2h_bytes = self.P * 3 * 8 + groups * 6 * 8
-        self.launches = []
-        self.adj_host = torch.empty((height, width, 3), dtype=torch.float32, pin_memory=True)
-        self.adj_dev = torch.empty((height, width, 3), dtype=torch.float32, device="cuda")
-
-    def gradient(self):
-        """One gradient evaluation on the device: forward, adjoint, replay."""
-        self.r.diff_forward(self.spp)
-        img = self.r.device_sums(5) / self.spp
-        adj = ((2.0 / self.n) * (img - self.target)).float()
-        return self.r.diff_backward(adj)
-
-    def step(self, events=None):
-        self.last_grad = self.gradient()
-
-    def timed_region(self, steps, flush):
-        """CUDA events on the submitting stream around `steps` evaluations;
-        every evaluation streams 64 frames of path state (about 20 MB per
-        frame at 256x256, several in flight) and 4.2M cache queries through
-        the backward, far past the 129 MB L2: no flush kernel."""
-        torch = self.torch
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        for _ in range(steps):
-            self.step()
-        t1.record()
-        torch.cuda.synchronize()
-        return t0.elapsed_time(t1) / steps
-
-    def e2e_region(self, steps):
-        """Through the public API with host buffers: forward, image read to the
-        host (FP64), adjoint on the host, copied in from pinned memory,
-        replay returning the gradients to the host."""
-        import time
-        torch = self.torch
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(steps):
-            self.r.diff_forward(self.spp)
-            img = self.r.read()
-            self.adj_host.numpy()[...] = (2.0 / self.n) * (img - self.target_host)
-            self.adj_dev.copy_(self.adj_host, non_blocking=True)
-            self.last_grad = self.r.diff_backward(self.adj_dev)
-        torch.cuda.synchronize()
-        return 1e3 * (time.perf_counter() - t0) / steps
-
-    @property
-    def kernels_per_step(self):
-        # forward frames (bounce loop, cache inference, compose) + replay frames
-        # (bounce loop, cache adjoint, two gradient sums) + group duals, total,
-        # cache forward + backward
-        rounds = 3  # BETA + 1 vertices at BETA = 2
-        md = self.r.cache().info()
-        # cache forward (encode, layers) + backward (fused dgrad, loss sum,
-        # per-layer weight-gradient partials and reduction, hash-grid scatter
-        # and conversion)
-        mlp = 2 + 2 + 2 * (md.n_hidden_layers + 1) + 2
-        fwd = 1 + 7 * rounds + 1 + 2 + 1
-        rep = 1 + 7 * rounds + 3
-        return self.spp * (fwd + rep) + 2 + mlp
-
-    def units_per_step(self):
-        return 1
-
-    def paths_per_step(self):
-        return 2 * self.P * self.spp
-
-    def fit(self, steps=200, lr=0.05):
-        """Adam on log(sigma_a) of every group from the +-50% start; returns
-        the final relative error per component (the other materials fixed)."""
-        torch = self.torch
-        x = torch.tensor(np.log(self.start[:, 0:3].astype(np.float64)), requires_grad=True)
-        opt = torch.optim.Adam([x], lr=lr)
-        for _ in range(steps):
-            m = self.truth.copy()
-            m[:, 0:3] = np.exp(x.detach().numpy())
-            self.scene.set_group_materials(m)
-            g = self.gradient()
-            opt.zero_grad()
-            x.grad = torch.from_numpy(g[:, 0:3] * m[:, 0:3])
-            opt.step()
-        self.scene.set_group_materials(self.start)
-        got = np.exp(x.detach().numpy())
-        return np.abs(got - self.truth[:, 0:3]) / self.truth[:, 0:3]
-
-    def roofline(self, seg_ms, pk):
-        """Traversal of the forward frames (instrumented, one frame at a time)
-        and the split of an evaluation into forward, replay and cache backward."""
-        torch = self.torch
-        self.r.instrument(timing=True, counting=False)
-        self.r.diff_forward(4)
-        t = self.r.timings().as_dict()
-        self.r.instrument(timing=True, counting=True)
-        self.r.diff_forward(1)
-        c = self.r.timings()
-        self.r.instrument(timing=False, counting=False)
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        ev[0].record()
-        self.r.diff_forward(self.spp)
-        ev[1].record()
-        img = self.r.device_sums(5) / self.spp
-        self.r.diff_backward(((2.0 / self.n) * (img - self.target)).float())
-        ev[2].record()
-        torch.cuda.synchronize()
-        dominant = "extend_ms" if t["extend_ms"] >= t["shadow_ms"] else "shadow_ms"
-        if dominant == "extend_ms":
-            rays, nodes, prims = c.extension_rays, c.extend_nodes, c.extend_prims
-        else:
-            rays, nodes, prims = c.shadow_rays, c.shadow_nodes, c.shadow_prims
-        alg = rays * RAY_RECORD_BYTES + nodes * NODE_BYTES + prims * PRIM_BYTES
-        ach = alg / (t[dominant] * 1e-3) / 1e9
-        return {"kernel": dominant.replace("_ms", "_kernel") + " (forward frames)", "bound": "hbm",
-                "achieved": round(ach, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": round(ach / pk["hbm_gbs"], 4), "traffic": None,
-                "evaluation_split_ms": {"forward_64_frames": round(ev[0].elapsed_time(ev[1]), 3),
-                                        "replay_and_cache_backward": round(ev[1].elapsed_time(ev[2]), 3)},
-                "stage_ms_per_forward_frame": {k: round(t[k], 4) for k in ("extend_ms", "shade_ms", "shadow_ms",
-                                                                           "compact_ms", "infer_ms")},
-                "rays_per_forward_frame": {"extension": int(c.extension_rays), "shadow": int(c.shadow_rays)},
-                "algorithmic_bytes_per_frame": int(alg),
-                "note": ("algorithmic bytes = rays x 48 B + 8-wide BVH nodes visited x 224 B + primitives tested "
-                         "x 64 B, counted in an untimed forward frame; the replay re-traces the same rays. "
-                         "Peak " + pk["source"])}
-
-    def config(self):
-        return {"workload": "diff: 20k curly procedural strands x 96 B-spline CPs (helix r 5 mm, pitch 10 mm), "
-                            "20k-tri head, sky + directional light, 256x256, 64 spp per evaluation, HairMSNN BETA=2, "
-                            "cache FP32 (frozen, 64 scene-sample training passes), 4 azimuthal strand groups; "
-                            "L2 image loss against a target at the true materials (same frame seeds)",
-                "pixels": self.P, "spp": self.spp, "groups": self.groups,
-                "paths_per_evaluation": self.paths_per_step(),
-                "l2": "inputs larger than L2: 64 frames of path state and 4.2M cache queries per evaluation",
-                "launch_shapes": {k: v for k, v in self.tuning.items() if k != "ms_per_frame"},
-                "parallelism": "replicas"}
-
-    def cpu_baseline(self, threads, budget_s=20.0):
-        """The reference has no gradient path.  Baseline: central finite
-        differences on the host, the way to differentiate it as it is: one
-        gradient of 4 groups x 6 parameters = 49 forward renders of 256x256 x
-        64 spp, each timed as the oracle's reference-structured integrator
-        (rayGenCam / msnnPathTrace G-buffer pass) on a bounded pixel sample."""
-        import time
-        from oracle import pyoracle as po
-        o = po.OracleScene.from_library(self.scene)
-        n = 4096
-        t0 = time.perf_counter()
-        done = 0
-        p0 = (self.height // 2) * self.width
-        while True:
-            o.render_pixels(1, beta=2, accum_id=done // self.P, every_nth=self.P, n_train=0, p0=p0, n=n,
-                            threads=threads)
-            done += n
-            p0 = (p0 + n) % (self.P - n)
-            if time.perf_counter() - t0 > budget_s:
-                break
-        rate = done / (time.perf_counter() - t0)
-        renders = 2 * self.groups * 6 + 1
-        value = rate / (self.P * self.spp * renders)
-        return {"value": value, "unit": self.unit, "cores": threads, "kind": "port",
-                "sample": f"{done} pixels (1 spp) of the oracle's forward integrator on {threads} threads "
-                          f"({rate:.0f} paths/s); a finite-difference gradient = {renders} renders of "
-                          f"{self.P} pixels x {self.spp} spp; cache not included"}

@@ -362,42 +362,50 @@ static void bake_sky(float T, f3 sun, int W, int H, float scale, std::vector<flo
   }
 }
 
-// generateEnvSamplingTables (scene.cpp:349-425), same single-precision order.
-void env_sampling_tables(const float4* env, int width, int height, std::vector<float>& cPdf,
-                         std::vector<float>& cCdf, std::vector<float>& mPdf, std::vector<float>& mCdf) {
-  const int cw = width + 1;
-  cPdf.assign((size_t)cw * height, 0.f);
-  cCdf.assign((size_t)cw * height, 0.f);
-  auto average = [](float4 a) { return (a.x + a.y + a.z) * (1.0f / 3.0f); };
+// generateEnvSamplingTables (scene.cpp:349-425): row-conditional and
+// marginal tables of the map's mean radiance weighted by sin(theta), in the
+// same single-precision operation order (the tables must be bit-identical).
+// Row y of the conditional tables holds W + 1 entries: the running sum
+// (cdf, normalised by the row's total) and the weights (pdf, whose last
+// entry is the row's total); the marginal tables do the same over the rows'
+// totals.
+void env_sampling_tables(const float4* env, int width, int height, std::vector<float>& row_pdf,
+                         std::vector<float>& row_cdf, std::vector<float>& marg_pdf, std::vector<float>& marg_cdf) {
+  const int stride = width + 1;
+  row_pdf.assign((size_t)stride * height, 0.f);
+  row_cdf.assign((size_t)stride * height, 0.f);
+  auto mean_rgb = [](float4 c) { return (c.x + c.y + c.z) * (1.0f / 3.0f); };
   for (int y = 0; y < height; y++) {
-    float sinTheta = sinf(3.14159f * (y + 0.5f) / height);
-    cPdf[y * cw] = average(env[y * width]) * sinTheta;
-    cCdf[y * cw] = 0.0f;
+    float* w = row_pdf.data() + (size_t)y * stride;
+    float* acc = row_cdf.data() + (size_t)y * stride;
+    const float sin_t = sinf(3.14159f * (y + 0.5f) / height);
+    w[0] = mean_rgb(env[y * width]) * sin_t;
+    acc[0] = 0.0f;
     for (int x = 1; x < width; x++) {
-      cPdf[y * cw + x] = average(env[y * width + x]) * sinTheta;
-      cCdf[y * cw + x] = cCdf[y * cw + x - 1] + cPdf[y * cw + x - 1] / width;
+      w[x] = mean_rgb(env[y * width + x]) * sin_t;
+      acc[x] = acc[x - 1] + w[x - 1] / width;
     }
-    const float cdfTotal = cCdf[y * cw + width - 1] + cPdf[y * cw + width - 1] / width;
-    cPdf[y * cw + width] = cdfTotal;
-    if (cdfTotal > 0.0f) {
-      const float inv = 1.0f / cdfTotal;
-      for (int x = 1; x < width; x++) cCdf[y * cw + x] *= inv;
+    const float row_total = acc[width - 1] + w[width - 1] / width;
+    w[width] = row_total;
+    if (row_total > 0.0f) {
+      const float scale = 1.0f / row_total;
+      for (int x = 1; x < width; x++) acc[x] *= scale;
     }
-    cCdf[y * cw + width] = 1.0f;
+    acc[width] = 1.0f;
   }
-  mPdf.assign(height + 1, 0.f);
-  mCdf.assign(height + 1, 0.f);
-  mPdf[0] = cPdf[width];
-  mCdf[0] = 0.0f;
-  for (int i = 1; i < height; i++) {
-    mPdf[i] = cPdf[i * cw + width];
-    mCdf[i] = mCdf[i - 1] + mPdf[i - 1] / height;
+  marg_pdf.assign(height + 1, 0.f);
+  marg_cdf.assign(height + 1, 0.f);
+  marg_pdf[0] = row_pdf[width];
+  marg_cdf[0] = 0.0f;
+  for (int r = 1; r < height; r++) {
+    marg_pdf[r] = row_pdf[(size_t)r * stride + width];
+    marg_cdf[r] = marg_cdf[r - 1] + marg_pdf[r - 1] / height;
   }
-  float total = mCdf[height - 1] + mPdf[height - 1] / height;
-  mPdf[height] = total;
+  const float total = marg_cdf[height - 1] + marg_pdf[height - 1] / height;
+  marg_pdf[height] = total;
   if (total > 0.0f)
-    for (int i = 1; i < height; i++) mCdf[i] /= total;
-  mCdf[height] = 1.0f;
+    for (int r = 1; r < height; r++) marg_cdf[r] /= total;
+  marg_cdf[height] = 1.0f;
 }
 
 static void grow(f3& lo, f3& hi, f3 p) {

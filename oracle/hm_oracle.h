@@ -7,7 +7,7 @@
 //
 // Pinning: the RNG, hair BSDF, GGX, curve and utility functions are checked
 // bit-for-bit against the reference's own headers compiled on the host
-// (oracle/build_ref.py -> oracle/_ref, golden vectors in tests/golden/).
+// (oracle/build.py build_ref -> oracle/_ref, golden vectors in tests/golden/).
 // The integrator is checked against the reference's own rayGenCam /
 // msnnPathTrace / directLighting compiled the same way, with this oracle's
 // BVH standing in for OptiX traversal (which is closed driver code).  The MLP

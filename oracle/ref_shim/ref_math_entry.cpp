@@ -1,5 +1,5 @@
 // C entry points around the reference's own header-only device math, compiled
-// unmodified on the host through hm_owl_shim.h.  Built by oracle/build_ref.py
+// unmodified on the host through hm_owl_shim.h.  Built by oracle/build.py (build_ref)
 // into oracle/_ref/ (never committed, never shipped); used only to generate
 // and check golden vectors for the oracle restatement.
 //

@@ -5,8 +5,8 @@ frostbite_anisotropic.cuh, curve_utils.cuh, utils.cuh) is compiled unmodified
 on the host by oracle/build.py (build_ref) through the OWL/OptiX stand-ins in
 oracle/ref_shim/, and called here through ctypes on seeded inputs.  The
 outputs are the golden vectors the oracle restatement and the GPU kernels are
-checked against.  Needs the reference checkout (HM_REF_DIR, default
-/root/reference); run:  python tests/golden/make_golden.py
+checked against.  Needs the reference checkout (where oracle/build.py looks
+for it, or HM_REF_DIR); run:  python tests/golden/make_golden.py
 """
 import ctypes
 import os

@@ -45,7 +45,8 @@ def test_reference_cache_config_sizes():
 
 
 def test_reference_config_file_parses_when_present():
-    path = "/root/reference/scenes/straight/tcnn_hairmsnn.json"
+    from oracle import build as ob
+    path = os.path.join(ob.REF_DIR, "scenes", "straight", "tcnn_hairmsnn.json")
     if not os.path.isfile(path):
         pytest.skip("reference checkout not present")
     from hairmsnn_gb300 import build, mlp

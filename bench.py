@@ -197,6 +197,9 @@ def main():
     ap.add_argument("--fit-steps", type=int, default=200,
                     help="diff workload: Adam steps of the sigma_a recovery reported after the timing")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="render workload: skip the other configurations' figures (vertex batch, precision sweep, "
+                         "equal-accuracy relMSE, ablation)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -284,6 +287,8 @@ def main():
         err = wl.fit(args.fit_steps)
         line["fit"] = {"adam_steps": args.fit_steps, "sigma_a_rel_error_max": round(float(err.max()), 5),
                        "sigma_a_rel_error_mean": round(float(err.mean()), 5), "start": "sigma_a x 0.5 or 1.5"}
+    if hasattr(wl, "extras") and type(wl).__name__ == "RenderBenchWorkload" and not args.no_extras:
+        line["other_configs"] = wl.extras(pk)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = wl.cpu_baseline(host_threads())
     print(json.dumps(line), flush=True)

@@ -14,6 +14,7 @@ cores.  The shipped package hairmsnn_gb300/ never imports the oracle.
 """
 import json
 import os
+import statistics
 import time
 
 import numpy as np
@@ -290,6 +291,12 @@ PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's 
 # rays.  ncu runs each launch with cold caches, so this is an upper bound
 # for warm frames.
 EXTEND_DRAM_BYTES_PER_RAY = 643
+# DRAM bytes per ray of the shadow-ray traversal launch timed by
+# RenderBenchWorkload.shadow_launch (one launch over a 512x512 frame's shadow
+# rays), and the counters that bind it, from one ncu capture of that launch
+# (profiles/shadow_trace_launch_512.md).
+SHADOW_DRAM_BYTES_PER_RAY = 0
+SHADOW_NCU_COUNTERS = {}
 
 
 class RenderBenchWorkload:
@@ -396,6 +403,11 @@ class RenderBenchWorkload:
         return t
 
     def plain_form(self, frames=20):
+        if getattr(self, "_plain_ms", None) is None:
+            self._plain_ms = self._plain_form(frames)
+        return self._plain_ms
+
+    def _plain_form(self, frames=20):
         """The plain FP32 wavefront form on the same scene and GPU: FP32 cache,
         one frame in flight, kernel-by-kernel launches, default launch
         shapes, one BVH leaf per segment.  Pipelined frame time."""
@@ -421,6 +433,69 @@ class RenderBenchWorkload:
         sc.close()
         return ms
 
+    def shadow_launch(self, pk, reps=5):
+        """The dominant kernel timed alone, in the same process: one launch of
+        the persistent any-hit traversal (the shadow-ray stage's kernel, fed
+        from a ray array) over every shadow ray of one 512x512 frame of this
+        workload, in the frame's order (bounce by bounce, light samples, then
+        BSDF samples, pixel order).  The rays come from the per-path ray log
+        of a frame rendered with one frame in flight, whose traversal work
+        counters count exactly these rays; CUDA events on the launching
+        stream, a 256 MiB write before each launch flushes L2.  Algorithmic
+        bytes = rays x 48 B + 8-wide nodes visited x 224 B + primitives
+        tested x 64 B."""
+        torch = self.torch
+        r = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
+                     precision=self.cache_precision, frames_in_flight=1)
+        vertices = self.scene.info().path_v2 + 1
+        r.set_path_log(vertices)
+        r.instrument(timing=True, counting=True)
+        r.frame()
+        c = r.timings()
+        log = r.read_path_log()
+        r.close()
+        kind = log[:, :, 7].view(np.int32)
+        order = []
+        for k in range(vertices):
+            for kd in (1, 2):
+                order.append(np.nonzero(kind[:, 3 * k + kd] == kd)[0] * log.shape[1] + 3 * k + kd)
+        idx = np.concatenate(order)
+        flat = log.reshape(-1, 12)[idx]
+        del log
+        vis = flat[:, 0].view(np.int32)
+        org = torch.from_numpy(np.ascontiguousarray(flat[:, 8:11])).cuda()
+        dirs = torch.from_numpy(np.ascontiguousarray(flat[:, 4:7])).cuda()
+        n = len(flat)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        hits = self.scene.trace(org, dirs, any_hit=True)
+        same = float(((hits[:, 1].cpu().numpy().view(np.int32) < 0) == (vis == 1)).mean())
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+        for k, (a, b) in enumerate(ev):
+            flush.fill_(k & 0xFF)
+            a.record()
+            self.scene.trace(org, dirs, any_hit=True)
+            b.record()
+        torch.cuda.synchronize()
+        ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+        alg = n * RAY_RECORD_BYTES + c.shadow_nodes * NODE_BYTES + c.shadow_prims * PRIM_BYTES
+        ach = alg / (ms * 1e-3) / 1e9
+        return {"kernel": "persistent_trace_kernel<any hit> (shadow rays of one frame, one launch)",
+                "bound": "hbm", "achieved": round(ach, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": round(ach / pk["hbm_gbs"], 4),
+                "traffic": int(n * SHADOW_DRAM_BYTES_PER_RAY),
+                "traffic_basis": ("ncu dram__bytes_read.sum + dram__bytes_write.sum of this launch "
+                                  f"({SHADOW_DRAM_BYTES_PER_RAY} B per ray), scaled by the rays"),
+                "launch_ms": round(ms, 4), "rays": n, "rays_counted_in_frame": int(c.shadow_rays),
+                "visibility_equal_to_frame": round(same, 6),
+                "algorithmic_bytes": int(alg),
+                "per_ray": {"nodes": round(c.shadow_nodes / max(1, c.shadow_rays), 2),
+                            "prims": round(c.shadow_prims / max(1, c.shadow_rays), 2)},
+                "binding_counters": SHADOW_NCU_COUNTERS,
+                "note": ("algorithmic bytes as in the frame's counted shadow stage; the 90 MB BVH and 10 MB of "
+                         "curves are mostly L2-resident, so the DRAM traffic is far below them; the bound is "
+                         "instruction issue with few lanes active (binding_counters); peak = HBM copy ("
+                         + pk["source"] + ")")}
+
     def roofline(self, seg_ms, pk):
         keys = ["extend_ms", "shade_ms", "shadow_ms", "compact_ms", "train_ms", "infer_ms", "compose_ms",
                 "camera_ms", "finalize_ms"]
@@ -428,31 +503,10 @@ class RenderBenchWorkload:
             self.profile_frames()
         n = max(1, min(len(self.stage_ms), 16))
         mean = {k: float(np.mean([s[k] for s in self.stage_ms[-n:]])) for k in keys}
-        c = self.counted_frame()
-        dominant = max(("extend_ms", "shadow_ms", "shade_ms", "train_ms", "infer_ms"), key=lambda k: mean[k])
-        out = {"stage_ms_per_frame": {k: round(v, 4) for k, v in mean.items()},
-               "rays_per_frame": {"extension": int(c.extension_rays), "shadow": int(c.shadow_rays)},
-               "bvh_work_per_frame": {"extend_nodes": int(c.extend_nodes), "extend_prims": int(c.extend_prims),
-                                      "shadow_nodes": int(c.shadow_nodes), "shadow_prims": int(c.shadow_prims)}}
-        if dominant in ("extend_ms", "shadow_ms"):
-            if dominant == "extend_ms":
-                rays, nodes, prims = c.extension_rays, c.extend_nodes, c.extend_prims
-            else:
-                rays, nodes, prims = c.shadow_rays, c.shadow_nodes, c.shadow_prims
-            alg = rays * RAY_RECORD_BYTES + nodes * NODE_BYTES + prims * PRIM_BYTES
-            ach = alg / (mean[dominant] * 1e-3) / 1e9
-            out.update({"kernel": dominant.replace("_ms", "_kernel"), "bound": "hbm", "achieved": round(ach, 2),
-                        "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
-                        "traffic": (int(rays * EXTEND_DRAM_BYTES_PER_RAY) if dominant == "extend_ms" else None),
-                        "traffic_basis": "DRAM bytes per frame: ncu cold-cache capture at 256x256 scaled by rays",
-                        "algorithmic_bytes_per_frame": int(alg),
-                        "note": ("algorithmic bytes = rays x 48 B + 8-wide BVH nodes visited x 224 B + primitives "
-                                 "tested x 64 B, counted in an untimed frame; the 90 MB BVH and 10 MB of curves "
-                                 "are L2-resident, so this can exceed the HBM copy peak ("
-                                 + pk["source"] + ")")})
-        else:
-            out.update({"kernel": dominant, "bound": "tensor", "achieved": None, "peak": pk["bf16_tflops"],
-                        "unit": "TFLOP/s", "frac": None, "traffic": None})
+        out = {"stage_ms_per_frame_synchronous": {k: round(v, 4) for k, v in mean.items()},
+               "stage_note": "synchronous instrumented frames (one frame at a time), after the timed region; "
+                             "the timed frames overlap eight at a time"}
+        out.update(self.shadow_launch(pk))
         if type(self) is RenderBenchWorkload:
             plain = self.plain_form()
             chosen = self.last_ms if getattr(self, "last_ms", None) else None
@@ -461,6 +515,162 @@ class RenderBenchWorkload:
                 "chosen_form_speedup": round(plain / chosen, 3) if chosen else None,
                 "what": "FP32 cache, 1 frame in flight, kernel-by-kernel launches, default launch shapes, "
                         "1 BVH leaf per segment; same scene and GPU"}
+        return out
+
+    def _frame_ms(self, r, frames=20):
+        torch = self.torch
+        for _ in range(3):
+            r.frame()
+        r.wait()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(frames):
+            r.frame()
+        r.wait()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / frames
+
+    def _timed_frames(self, r, n):
+        torch = self.torch
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for _ in range(n):
+            r.frame()
+        r.wait()
+        t1.record()
+        torch.cuda.synchronize()
+        return t0.elapsed_time(t1) / n
+
+    def quality(self, spp=None, ref_spp=None, pretrain_passes=None):
+        """relMSE at `spp` of HairMSNN (each cache precision), PT, NRC and
+        HairMSNN after scene-sample training, against a converged PT image of
+        the same scene (frames 16 .. 16 + ref_spp of one PT run); frame times
+        and the PT sample count needed for the same error."""
+        spp = spp or getattr(self, "spp", 16)
+        ref_spp = ref_spp or getattr(self, "ref_spp", 1024)
+        pretrain_passes = pretrain_passes or getattr(self, "pretrain_passes", 256)
+        pt = Renderer(self.scene, PT, frames_in_flight=self.frames_in_flight)
+        pt_ms = self._timed_frames(pt, spp)
+        pt_img = pt.read(IMAGE_FINAL)
+        ref_ms = self._timed_frames(pt, ref_spp)
+        total = pt.read(IMAGE_FINAL) * (spp + ref_spp)
+        ref = (total - pt_img * spp) / ref_spp
+        pt.close()
+        by_prec = {}
+        for name, prec in (("fp32", 0), ("fp16", 1), ("bf16", 2), ("fp8", 3)):
+            ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
+                          precision=prec, frames_in_flight=self.frames_in_flight)
+            t_ms = self._timed_frames(ms, spp)
+            img = ms.read(IMAGE_FINAL)
+            ms.close()
+            by_prec[name] = {"relmse": round(relmse(img, ref), 6), "ms_per_frame": round(t_ms, 3)}
+            if name == "fp32":
+                ms_ms, ms_img = t_ms, img
+        # the reference's initial training before the first frame (one second
+        # of scene-sample passes there; a fixed pass count here)
+        ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
+                      frames_in_flight=self.frames_in_flight)
+        torch = self.torch
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record()
+        ms.pretrain(pretrain_passes)
+        t1.record()
+        torch.cuda.synchronize()
+        pre_ms = t0.elapsed_time(t1)
+        t_pre = self._timed_frames(ms, spp)
+        e_pre = relmse(ms.read(IMAGE_FINAL), ref)
+        ms.close()
+        # the reference's comparison renderer: NRC with online training
+        # (65536 records per frame, c = 0.01), same frames
+        nrc = Renderer(self.scene, NRC, train=True, frames_in_flight=self.frames_in_flight)
+        nrc_ms = self._timed_frames(nrc, spp)
+        e_nrc = relmse(nrc.read(IMAGE_FINAL), ref)
+        nrc.close()
+        e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
+        eq_spp = spp * e_pt / e_ms
+        return {"spp": spp, "reference_spp": ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
+                "msnn": {"relmse": round(e_ms, 6), "ms_per_frame": round(ms_ms, 3),
+                         "paths_per_s": round(self.P / (ms_ms * 1e-3), 1)},
+                "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
+                       "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
+                "nrc": {"relmse": round(e_nrc, 6), "ms_per_frame": round(nrc_ms, 3),
+                        "paths_per_s": round(self.P / (nrc_ms * 1e-3), 1),
+                        "pt_spp_for_same_relmse": round(spp * e_pt / e_nrc, 2),
+                        "speedup_at_equal_relmse": round((spp * e_pt / e_nrc) * pt_ms / (spp * nrc_ms), 3)},
+                "msnn_by_cache_precision": by_prec,
+                "msnn_after_scene_sample_training": {
+                    "passes": pretrain_passes, "training_ms": round(pre_ms, 1), "relmse": round(e_pre, 6),
+                    "ms_per_frame": round(t_pre, 3), "pt_spp_for_same_relmse": round(spp * e_pt / e_pre, 2),
+                    "speedup_at_equal_relmse": round((spp * e_pt / e_pre) * pt_ms / (spp * t_pre), 3)},
+                "pt_spp_for_msnn_relmse": round(eq_spp, 2),
+                "speedup_at_equal_relmse": round(eq_spp * pt_ms / (spp * ms_ms), 3)}
+
+    def extras(self, pk):
+        """The other configurations' figures, measured in the same run: the
+        2^18-query vertex batch (BSDF eval + sample + FP16 cache inference)
+        with its kernels' rooflines, the cache precision sweep at 2^20
+        queries (time, TFLOP/s, training step, error against the FP64
+        oracle), the equal-accuracy comparison of the chosen and plain forms
+        (relMSE at 16 spp against a converged PT image), and the ablation of
+        the chosen form."""
+        torch = self.torch
+        out = {}
+        vw = VertexWorkload(torch)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        for _ in range(3):
+            vw.step()
+        evs = [[torch.cuda.Event(enable_timing=True) for _ in range(vw.n_events())] for _ in range(10)]
+        for k, ev in enumerate(evs):
+            flush.fill_(k & 0xFF)
+            vw.step(ev)
+        torch.cuda.synchronize()
+        seg = [statistics.mean(ev[i].elapsed_time(ev[i + 1]) for ev in evs) for i in range(vw.n_events() - 1)]
+        step_ms = statistics.mean(ev[0].elapsed_time(ev[-1]) for ev in evs)
+        out["vertex_2^18"] = {"queries_per_s": round(vw.n / (step_ms * 1e-3), 1), "ms_per_step": round(step_ms, 4),
+                              "roofline": vw.roofline(seg, pk), "workload": vw.workload_name}
+        pw = PrecisionWorkload(torch)
+        out["precision_2^20"] = pw.sweep(pk)
+        out["quality_16spp"] = self.quality(16, 1024, 256)
+        plain = self.plain_form()
+        q = out["quality_16spp"]
+        out["equal_accuracy"] = {
+            "chosen_form": {"relmse": q["msnn_by_cache_precision"]["fp16"]["relmse"],
+                            "ms_per_frame": round(self.last_ms, 3) if getattr(self, "last_ms", None) else None},
+            "plain_fp32_form": {"relmse": q["msnn_by_cache_precision"]["fp32"]["relmse"],
+                                "ms_per_frame": round(plain, 3)},
+            "relmse_ratio_chosen_to_plain": round(q["msnn_by_cache_precision"]["fp16"]["relmse"]
+                                                  / q["msnn_by_cache_precision"]["fp32"]["relmse"], 4),
+            "speedup": round(plain / self.last_ms, 3) if getattr(self, "last_ms", None) else None}
+        out["ablation"] = self.ablation()
+        return out
+
+    def ablation(self):
+        """Which choice gives the speed-up: the chosen form with one factor
+        changed at a time (same scene, same GPU, pipelined frames)."""
+        out = {}
+        variants = [("chosen", {}), ("fp32_cache", {"precision": 0}), ("one_frame_in_flight", {"fif": 1}),
+                    ("no_graph_replay", {"graphs": False}), ("one_leaf_per_segment", {"split": 1}),
+                    ("untuned_launch_shapes", {"tune": False})]
+        scenes = {2: self.scene}
+        for name, v in variants:
+            split = v.get("split", 2)
+            if split not in scenes:
+                cfg = dict(self.cfg)
+                cfg["integrator"] = dict(cfg["integrator"], segment_splits=split)
+                scenes[split] = Scene(cfg)
+            r = Renderer(scenes[split], MSNN, beta=1, train_records=self.train_records, train=True,
+                         precision=v.get("precision", self.cache_precision),
+                         frames_in_flight=v.get("fif", self.frames_in_flight))
+            if v.get("tune", True):
+                r.autotune(frames=6)
+            r.set_graphs(v.get("graphs", True))
+            ms = self._frame_ms(r)
+            out[name] = {"ms_per_frame": round(ms, 3), "paths_per_s": round(self.P / (ms * 1e-3), 1)}
+            r.close()
+        base = out["chosen"]["ms_per_frame"]
+        for name in out:
+            out[name]["slowdown_vs_chosen"] = round(out[name]["ms_per_frame"] / base, 3)
         return out
 
     workload_name = ("render: straight procedural hair 10k strands x 64 B-spline CPs (610k segments, 2 BVH "
@@ -555,75 +765,6 @@ class RenderQualityWorkload(RenderBenchWorkload):
                  pretrain_passes=256):
         super().__init__(torch, width, height, train_records)
         self.spp, self.ref_spp, self.pretrain_passes = spp, ref_spp, pretrain_passes
-
-    def _timed_frames(self, r, n):
-        torch = self.torch
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        for _ in range(n):
-            r.frame()
-        r.wait()
-        t1.record()
-        torch.cuda.synchronize()
-        return t0.elapsed_time(t1) / n
-
-    def quality(self):
-        spp = self.spp
-        pt = Renderer(self.scene, PT, frames_in_flight=self.frames_in_flight)
-        pt_ms = self._timed_frames(pt, spp)
-        pt_img = pt.read(IMAGE_FINAL)
-        ref_ms = self._timed_frames(pt, self.ref_spp)
-        total = pt.read(IMAGE_FINAL) * (spp + self.ref_spp)
-        ref = (total - pt_img * spp) / self.ref_spp
-        pt.close()
-        by_prec = {}
-        for name, prec in (("fp32", 0), ("fp16", 1), ("bf16", 2), ("fp8", 3)):
-            ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
-                          precision=prec, frames_in_flight=self.frames_in_flight)
-            t_ms = self._timed_frames(ms, spp)
-            img = ms.read(IMAGE_FINAL)
-            ms.close()
-            by_prec[name] = {"relmse": round(relmse(img, ref), 6), "ms_per_frame": round(t_ms, 3)}
-            if name == "fp32":
-                ms_ms, ms_img = t_ms, img
-        # the reference's initial training before the first frame (one second
-        # of scene-sample passes there; a fixed pass count here)
-        ms = Renderer(self.scene, MSNN, beta=1, train_records=self.train_records, train=True,
-                      frames_in_flight=self.frames_in_flight)
-        torch = self.torch
-        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        t0.record()
-        ms.pretrain(self.pretrain_passes)
-        t1.record()
-        torch.cuda.synchronize()
-        pre_ms = t0.elapsed_time(t1)
-        t_pre = self._timed_frames(ms, spp)
-        e_pre = relmse(ms.read(IMAGE_FINAL), ref)
-        ms.close()
-        # the reference's comparison renderer: NRC with online training
-        # (65536 records per frame, c = 0.01), same frames
-        nrc = Renderer(self.scene, NRC, train=True, frames_in_flight=self.frames_in_flight)
-        nrc_ms = self._timed_frames(nrc, spp)
-        e_nrc = relmse(nrc.read(IMAGE_FINAL), ref)
-        nrc.close()
-        e_pt, e_ms = relmse(pt_img, ref), relmse(ms_img, ref)
-        eq_spp = spp * e_pt / e_ms
-        return {"spp": spp, "reference_spp": self.ref_spp, "reference_ms_per_frame": round(ref_ms, 3),
-                "msnn": {"relmse": round(e_ms, 6), "ms_per_frame": round(ms_ms, 3),
-                         "paths_per_s": round(self.P / (ms_ms * 1e-3), 1)},
-                "pt": {"relmse": round(e_pt, 6), "ms_per_frame": round(pt_ms, 3),
-                       "paths_per_s": round(self.P / (pt_ms * 1e-3), 1)},
-                "nrc": {"relmse": round(e_nrc, 6), "ms_per_frame": round(nrc_ms, 3),
-                        "paths_per_s": round(self.P / (nrc_ms * 1e-3), 1),
-                        "pt_spp_for_same_relmse": round(spp * e_pt / e_nrc, 2),
-                        "speedup_at_equal_relmse": round((spp * e_pt / e_nrc) * pt_ms / (spp * nrc_ms), 3)},
-                "msnn_by_cache_precision": by_prec,
-                "msnn_after_scene_sample_training": {
-                    "passes": self.pretrain_passes, "training_ms": round(pre_ms, 1), "relmse": round(e_pre, 6),
-                    "ms_per_frame": round(t_pre, 3), "pt_spp_for_same_relmse": round(spp * e_pt / e_pre, 2),
-                    "speedup_at_equal_relmse": round((spp * e_pt / e_pre) * pt_ms / (spp * t_pre), 3)},
-                "pt_spp_for_msnn_relmse": round(eq_spp, 2),
-                "speedup_at_equal_relmse": round(eq_spp * pt_ms / (spp * ms_ms), 3)}
 
     def roofline(self, seg_ms, pk):
         out = super().roofline(seg_ms, pk)

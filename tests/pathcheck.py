@@ -119,9 +119,10 @@ def hit_normal_tolerance(g_log, o_log, radius):
     return 4.0 * dp / radius
 
 
-def check_paths(g_log, g_col, runs, label, dump=None, extra_tol=0.0):
+def check_paths(g_log, g_col, runs, label, dump=None, extra_tol=0.0, separate_max=SEPARATE_MAX):
     """Applies the per-path criterion; returns the paths whose logs agree.
-    extra_tol [P, m] (or a scalar): an added tolerance per path and column."""
+    extra_tol [P, m] (or a scalar): an added tolerance per path and column;
+    separate_max: the cap on the fraction of separating paths."""
     o0 = runs[0]
     agree, first = separation(g_log, o0["log"])
     self_sep = np.zeros(len(agree), bool)
@@ -142,6 +143,6 @@ def check_paths(g_log, g_col, runs, label, dump=None, extra_tol=0.0):
         np.savez_compressed(os.path.join(dump, label.replace(" ", "_").replace("=", "") + ".npz"), g_log=g_log,
                             g_col=g_col, **{f"o{k}_{n}": runs[k][n] for k in runs for n in ("log", "col", "nev")})
     assert not bad.any(), (label, np.nonzero(bad)[0][:10], excess[bad].max())
-    assert sep.mean() <= min(SEPARATE_MAX, self_sep.mean()), (label, sep.mean(), self_sep.mean())
+    assert sep.mean() <= min(separate_max, self_sep.mean()), (label, sep.mean(), self_sep.mean())
     assert unexplained.sum() <= UNEXPLAINED_MAX, (label, np.nonzero(unexplained)[0][:10], first[unexplained][:10])
     return agree

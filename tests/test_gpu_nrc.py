@@ -62,7 +62,10 @@ def test_nrc_paths_match_oracle(R, catrom):
     nt = hit_normal_tolerance(g_log, o0["log"], cfg["hair"]["procedural"]["radius"])
     extra[:, 12:15] = nt[:, None]
     extra[:, 21:24] = nt[:, None]
-    agree = check_paths(g_log, g_col, runs, f"NRC catrom={catrom}", os.environ.get("HM_PATHS_DUMP"), extra)
+    # NRC paths run up to 40 vertices without Russian roulette: more of them
+    # reach a last-ulp decision (the oracle's own perturbed runs separate ~35%)
+    agree = check_paths(g_log, g_col, runs, f"NRC catrom={catrom}", os.environ.get("HM_PATHS_DUMP"), extra,
+                        separate_max=0.15)
     assert ((gbuf[:, 3] > 0.5) == (o0["hit"] > 0.5))[agree].all()
     # training pixels: unbiased flags exactly; bounce counts and records where the path agrees
     ot = o0["tinfo"][tp]

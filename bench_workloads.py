@@ -295,8 +295,11 @@ EXTEND_DRAM_BYTES_PER_RAY = 643
 # RenderBenchWorkload.shadow_launch (one launch over a 512x512 frame's shadow
 # rays), and the counters that bind it, from one ncu capture of that launch
 # (profiles/shadow_trace_launch_512.md).
-SHADOW_DRAM_BYTES_PER_RAY = 0
-SHADOW_NCU_COUNTERS = {}
+SHADOW_DRAM_BYTES_PER_RAY = 333  # 189.4 MB for 568,386 rays
+SHADOW_NCU_COUNTERS = {"lanes_active_per_instruction": 9.02, "issue_active_pct": 55.8,
+                       "alu_pipe_active_pct": 63.8, "warps_active_pct": 33.8, "l2_hit_rate_pct": 84.6,
+                       "dram_throughput_pct": 2.3,
+                       "source": "profiles/shadow_trace_launch_512.md (ncu --set full, cold caches)"}
 
 
 class RenderBenchWorkload:

@@ -13,39 +13,9 @@
 
 namespace hm {
 
-// setupHairShading (disney_hair.cuh:26-41) and every other material-only term,
-// evaluated once on the host in the same single-precision order.
-HairConsts hair_consts_from_params(const hm_hair_params& p) {
-  HairConsts hc;
-  const float bm = p.beta_m, bn = p.beta_n;
-  hc.v[0] = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * powf(bm, 20.f));
-  hc.v[1] = (float)(.25 * (double)hc.v[0]);
-  hc.v[2] = 4.f * hc.v[0];
-  hc.s = kSqrtPiOver8 * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * powf(bn, 22.f));
-  hc.v[3] = hc.s;
-  hc.sin2k[0] = sinf(p.alpha);
-  hc.cos2k[0] = safe_sqrt(1.f - sqr(hc.sin2k[0]));
-  for (int i = 1; i < 3; ++i) {
-    hc.sin2k[i] = 2.f * hc.cos2k[i - 1] * hc.sin2k[i - 1];
-    hc.cos2k[i] = sqr(hc.cos2k[i - 1]) - sqr(hc.sin2k[i - 1]);
-  }
-  for (int i = 0; i < 3; ++i) hc.sigma_a[i] = p.sigma_a[i];
-  hc.gain[0] = p.gain_r;
-  hc.gain[1] = p.gain_tt;
-  hc.gain[2] = p.gain_trt;
-  hc.gain[3] = p.gain_trrt;
-  auto cdf = [&](float x) { return 1.f / (1.f + expf(-x / hc.s)); };  // LogisticCDF :123-125
-  hc.trim_den = cdf(kPi) - cdf(-kPi);
-  hc.cdf_lo = cdf(-kPi);
-  for (int k = 0; k < 3; ++k) {
-    hc.inv_v[k] = 1.f / hc.v[k];
-    hc.mp_logc[k] = logf(1.f / (2.f * hc.v[k]));
-    hc.mp_den[k] = sinhf(1.f / hc.v[k]) * 2.f * hc.v[k];
-  }
-  for (int k = 0; k < 4; ++k) hc.exp_m2v[k] = expf(-2.f / hc.v[k]);
-  hc.fp64_mp = bm < 0.1f ? 1 : 0;
-  return hc;
-}
+// setupHairShading and the other material-only terms, evaluated once on the
+// host (hair_consts, hm_hair_bsdf.cuh).
+HairConsts hair_consts_from_params(const hm_hair_params& p) { return hair_consts(p); }
 
 HM_D float ldg(const float* p) { return __ldg(p); }
 

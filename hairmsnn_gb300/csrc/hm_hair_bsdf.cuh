@@ -31,7 +31,44 @@ struct HairConsts {
   int fp64_mp;        // beta_m < 0.1
 };
 
-// Host-side precompute (identical formulas; see hm_bsdf.cu).
+HM_HD float logistic_cdf_s(float x, float s) { return 1.f / (1.f + expf(-x / s)); }  // LogisticCDF :123-125
+
+// setupHairShading (disney_hair.cuh:26-41) and every other material-only
+// term, in the reference's single-precision order.  The library evaluates it
+// once per material on the host (hair_consts_from_params); code that
+// includes include/hairmsnn_device.cuh may also call it on the device.
+HM_HD HairConsts hair_consts(const hm_hair_params& p) {
+  HairConsts hc;
+  const float bm = p.beta_m, bn = p.beta_n;
+  hc.v[0] = sqr(0.726f * bm + 0.812f * sqr(bm) + 3.7f * powf(bm, 20.f));
+  hc.v[1] = (float)(.25 * (double)hc.v[0]);
+  hc.v[2] = 4.f * hc.v[0];
+  hc.s = kSqrtPiOver8 * (0.265f * bn + 1.194f * sqr(bn) + 5.372f * powf(bn, 22.f));
+  hc.v[3] = hc.s;
+  hc.sin2k[0] = sinf(p.alpha);
+  hc.cos2k[0] = safe_sqrt(1.f - sqr(hc.sin2k[0]));
+  for (int i = 1; i < 3; ++i) {
+    hc.sin2k[i] = 2.f * hc.cos2k[i - 1] * hc.sin2k[i - 1];
+    hc.cos2k[i] = sqr(hc.cos2k[i - 1]) - sqr(hc.sin2k[i - 1]);
+  }
+  for (int i = 0; i < 3; ++i) hc.sigma_a[i] = p.sigma_a[i];
+  hc.gain[0] = p.gain_r;
+  hc.gain[1] = p.gain_tt;
+  hc.gain[2] = p.gain_trt;
+  hc.gain[3] = p.gain_trrt;
+  hc.trim_den = logistic_cdf_s(kPi, hc.s) - logistic_cdf_s(-kPi, hc.s);
+  hc.cdf_lo = logistic_cdf_s(-kPi, hc.s);
+  for (int k = 0; k < 3; ++k) {
+    hc.inv_v[k] = 1.f / hc.v[k];
+    hc.mp_logc[k] = logf(1.f / (2.f * hc.v[k]));
+    hc.mp_den[k] = sinhf(1.f / hc.v[k]) * 2.f * hc.v[k];
+  }
+  for (int k = 0; k < 4; ++k) hc.exp_m2v[k] = expf(-2.f / hc.v[k]);
+  hc.fp64_mp = bm < 0.1f ? 1 : 0;
+  return hc;
+}
+
+// Host-side precompute of hair_consts (see hm_bsdf.cu).
 HairConsts hair_consts_from_params(const hm_hair_params& p);
 
 HM_D float bessel_i0(float x) {  // disney_hair.cuh:54-67

@@ -15,6 +15,7 @@
 //   grid_bwd_kernel    hash-grid gradient scatter (float atomics)
 #include <math.h>
 #include <stdio.h>
+#include <ctype.h>
 #include <string.h>
 
 #include <algorithm>
@@ -1133,9 +1134,142 @@ extern "C" int hm_mlp_last_loss(hm_mlp* h, float* host_loss) {
 // ---- save / load: "HMMLP1\n" + one JSON line {n_params, step, lr} + raw
 // float32 params.  TINY_MLP::loadWeights (cuda/neural_network.cu:23-32)
 // deserialised a tcnn JSON snapshot; that format belongs to tcnn.
+// ---- tiny-cuda-nn trainer snapshots (TINY_MLP::loadWeights deserializes
+// one, neural_network.cu:23-32, from the scene's tcnn.init_weights,
+// scene.cpp:330-331).  tiny-cuda-nn is an absent submodule of the
+// reference; its Trainer serialises to a JSON object
+//   {"n_params": N, "params_type": "float" | "__half",
+//    "params_binary": <N parameters of that type, little-endian>, ...}
+// where a binary value written as JSON text is {"bytes": [b0, b1, ...],
+// "subtype": null}.  The parameters are the network's weight matrices, layer
+// after layer, each row-major [outputs][inputs] with the input width padded
+// to 16 and the last layer's outputs padded to 16, then the encoding's
+// parameters (hash-grid tables level after level): the layout of this
+// library's own parameter vector.  Optimizer state in a snapshot is not read
+// (the optimizer restarts, as after TINY_MLP::reset).
+
+static bool ends_with(const char* s, const char* suffix) {
+  const size_t a = strlen(s), b = strlen(suffix);
+  return a >= b && strcmp(s + a - b, suffix) == 0;
+}
+
+static float half_to_float(uint16_t h) {  // IEEE 754 binary16 -> binary32
+  const uint32_t sign = (uint32_t)(h >> 15) << 31;
+  uint32_t exp = (h >> 10) & 0x1f, man = h & 0x3ff, bits;
+  if (exp == 0x1f) {
+    bits = sign | 0x7f800000u | (man << 13);
+  } else if (exp != 0) {
+    bits = sign | ((exp + 112) << 23) | (man << 13);
+  } else if (man == 0) {
+    bits = sign;
+  } else {  // subnormal: normalise
+    int e = -1;
+    do {
+      ++e;
+      man <<= 1;
+    } while (!(man & 0x400));
+    bits = sign | ((uint32_t)(112 - e) << 23) | ((man & 0x3ff) << 13);
+  }
+  float f;
+  memcpy(&f, &bits, 4);
+  return f;
+}
+
+// The value of "key": <number> / "key": "<word>" anywhere in text (the
+// snapshot's top-level scalars), or false.
+static bool scan_scalar(const std::string& text, const char* key, std::string* out) {
+  const std::string k = std::string("\"") + key + "\"";
+  size_t at = text.find(k);
+  if (at == std::string::npos) return false;
+  at = text.find(':', at + k.size());
+  if (at == std::string::npos) return false;
+  ++at;
+  while (at < text.size() && isspace((unsigned char)text[at])) ++at;
+  size_t end = at;
+  if (at < text.size() && text[at] == '"') {
+    end = text.find('"', at + 1);
+    if (end == std::string::npos) return false;
+    *out = text.substr(at + 1, end - at - 1);
+    return true;
+  }
+  while (end < text.size() && (isdigit((unsigned char)text[end]) || text[end] == '.' || text[end] == '-' ||
+                               text[end] == '+' || text[end] == 'e' || text[end] == 'E'))
+    ++end;
+  *out = text.substr(at, end - at);
+  return end > at;
+}
+
+static int load_tcnn_snapshot(Mlp* m, const char* path) {
+  FILE* f = fopen(path, "rb");
+  if (!f) return hm_set_error("hm_mlp_load: cannot open %s", path), HM_EINVAL;
+  std::string text;
+  char buf[1 << 16];
+  size_t r;
+  while ((r = fread(buf, 1, sizeof(buf), f)) > 0) text.append(buf, r);
+  fclose(f);
+  std::string v;
+  if (!scan_scalar(text, "n_params", &v)) return hm_set_error("hm_mlp_load: no n_params in %s", path), HM_EPARSE;
+  const long long n = atoll(v.c_str());
+  if (n != m->n_params)
+    return hm_set_error("hm_mlp_load: %s holds %lld parameters, the network has %lld", path, n,
+                        (long long)m->n_params),
+           HM_EINVAL;
+  std::string type = "float";
+  scan_scalar(text, "params_type", &type);
+  const int elem = type == "float" ? 4 : (type == "__half" ? 2 : 0);
+  if (!elem) return hm_set_error("hm_mlp_load: params_type %s not supported", type.c_str()), HM_EUNSUPPORTED;
+  size_t at = text.find("\"params_binary\"");
+  if (at != std::string::npos) at = text.find("\"bytes\"", at);
+  if (at != std::string::npos) at = text.find('[', at);
+  if (at == std::string::npos) return hm_set_error("hm_mlp_load: no params_binary bytes in %s", path), HM_EPARSE;
+  std::vector<uint8_t> bytes;
+  bytes.reserve((size_t)n * elem);
+  const char* p = text.c_str() + at + 1;
+  for (;;) {
+    while (*p && (isspace((unsigned char)*p) || *p == ',')) ++p;
+    if (*p == ']') break;
+    char* end = nullptr;
+    const long b = strtol(p, &end, 10);
+    if (end == p || b < 0 || b > 255) return hm_set_error("hm_mlp_load: bad byte in params_binary"), HM_EPARSE;
+    bytes.push_back((uint8_t)b);
+    p = end;
+  }
+  if ((long long)bytes.size() != n * elem)
+    return hm_set_error("hm_mlp_load: params_binary holds %zu bytes, %lld expected", bytes.size(), n * elem),
+           HM_EPARSE;
+  std::vector<float> params((size_t)n);
+  for (long long i = 0; i < n; ++i) {
+    if (elem == 4) {
+      memcpy(&params[i], &bytes[4 * i], 4);
+    } else {
+      uint16_t h;
+      memcpy(&h, &bytes[2 * i], 2);
+      params[i] = half_to_float(h);
+    }
+  }
+  m->step = 0;
+  m->lr = m->cfg.adam.lr;
+  return hm_mlp_set_params((hm_mlp*)m, params.data());
+}
+
+static int save_tcnn_snapshot(const Mlp* m, const char* path) {
+  std::vector<float> p(m->n_params);
+  if (int s = hm_mlp_get_params((const hm_mlp*)m, p.data())) return s;
+  FILE* f = fopen(path, "wb");
+  if (!f) return hm_set_error("hm_mlp_save: cannot open %s", path), HM_EINVAL;
+  fprintf(f, "{\"n_params\": %lld, \"params_type\": \"float\", \"params_binary\": {\"bytes\": [",
+          (long long)m->n_params);
+  const uint8_t* b = (const uint8_t*)p.data();
+  for (size_t i = 0; i < p.size() * 4; ++i) fprintf(f, i ? ",%u" : "%u", (unsigned)b[i]);
+  fprintf(f, "], \"subtype\": null}}\n");
+  const bool ok = fclose(f) == 0;
+  return ok ? HM_OK : (hm_set_error("hm_mlp_save: write failed"), HM_EINVAL);
+}
+
 extern "C" int hm_mlp_save(const hm_mlp* h, const char* path) {
   const Mlp* m = (const Mlp*)h;
   if (!m || !path) return hm_set_error("hm_mlp_save: NULL"), HM_EINVAL;
+  if (ends_with(path, ".json")) return save_tcnn_snapshot(m, path);
   std::vector<float> p(m->n_params);
   if (int s = hm_mlp_get_params(h, p.data())) return s;
   FILE* f = fopen(path, "wb");
@@ -1151,6 +1285,13 @@ extern "C" int hm_mlp_load(hm_mlp* h, const char* path) {
   if (!m || !path) return hm_set_error("hm_mlp_load: NULL"), HM_EINVAL;
   FILE* f = fopen(path, "rb");
   if (!f) return hm_set_error("hm_mlp_load: cannot open %s", path), HM_EINVAL;
+  int first = fgetc(f);
+  while (first == ' ' || first == '\n' || first == '\r' || first == '\t') first = fgetc(f);
+  if (first == '{') {
+    fclose(f);
+    return load_tcnn_snapshot(m, path);
+  }
+  rewind(f);
   char magic[16] = {0}, line[512] = {0};
   if (!fgets(magic, sizeof(magic), f) || strcmp(magic, "HMMLP1\n") != 0 || !fgets(line, sizeof(line), f)) {
     fclose(f);

@@ -743,6 +743,9 @@ static int render_setup(Render* r, const hm_render_options* o) {
     int st = 0;
     r->mlp = hm_mlp_create(cfg.c_str(), r->in_ch, 3, o ? o->cache_precision : HM_PREC_FP32, r->seed, &st);
     if (!r->mlp) return st;
+    // the scene's tcnn.init_weights (render_hair_msnn.cu:109-110)
+    if (!s->cache_weights.empty())
+      if (int e3 = hm_mlp_load(r->mlp, s->cache_weights.c_str())) return e3;
   }
   cudaError_t e2 = cudaDeviceSynchronize();
   return e2 == cudaSuccess ? HM_OK : hm_cuda_status(e2, "render setup");

@@ -609,6 +609,8 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
       if (!cfg.empty() && !read_file(join_path(base, cfg), &s->cache_config))
         throw JsonError("scene: cannot read tcnn.config " + cfg);
       s->cache_train = tc.bool_or("init_train", false);
+      const std::string w = tc.string_or("init_weights", "");  // scene.cpp:330-331
+      if (!w.empty()) s->cache_weights = join_path(base, w);
     }
   } catch (const std::exception& e) {
     hm_set_error("%s", e.what());

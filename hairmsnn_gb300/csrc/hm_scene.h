@@ -113,6 +113,7 @@ struct Scene {
   f3 bmin{1e30f, 1e30f, 1e30f}, bmax{-1e30f, -1e30f, -1e30f};
   float scene_scale = 1.f;
   std::string cache_config;  // tcnn JSON text (scene "tcnn.config")
+  std::string cache_weights;  // path of a weight snapshot (scene "tcnn.init_weights"), "" for none
   bool cache_train = true;
   std::string image_output, stats_output;
 

@@ -184,7 +184,13 @@ int hm_mlp_reset(hm_mlp* mlp);
 int hm_mlp_get_params(const hm_mlp* mlp, float* host_out);
 int hm_mlp_set_params(hm_mlp* mlp, const float* host_in);
 int hm_mlp_get_gradients(const hm_mlp* mlp, float* host_out);
-/* TINY_MLP::loadWeights, neural_network.cu:23-32 (own binary snapshot format). */
+/* TINY_MLP::loadWeights, neural_network.cu:23-32.  hm_mlp_load reads either
+ * a tiny-cuda-nn trainer snapshot as JSON text ({"n_params", "params_type"
+ * "float" or "__half", "params_binary": {"bytes": [...]}}: what
+ * TINY_MLP::loadWeights deserialises; optimizer state is not read) or the
+ * library's own binary snapshot (which keeps the step and learning rate);
+ * hm_mlp_save writes the JSON form when `path` ends in ".json", else the
+ * binary one. */
 int hm_mlp_save(const hm_mlp* mlp, const char* path);
 int hm_mlp_load(hm_mlp* mlp, const char* path);
 

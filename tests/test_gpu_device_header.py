@@ -1,0 +1,82 @@
+"""include/hairmsnn_device.cuh from user code: the reference-named device API
+(setupHairShading, disney_hair, sample_disney_hair over a HairVertex) and the
+head-surface GGX, compiled into a user kernel (tests/device_header_kernel.cu)
+with nvcc for sm_103a.
+
+* disney_hair / sample_disney_hair per query equal the batched hm_bsdf_eval /
+  hm_bsdf_sample bit for bit (same code, both built without multiply-add
+  contraction), with the vertex's frame built as hairCH builds it and h the
+  vertex's own dot(Y, n);
+* frostbite_GGX / sample_GGX / pdf_GGX against the golden vectors of the
+  reference's own frostbite_anisotropic.cuh (tests/golden/ref_math_golden.npz)
+  within 1e-5 relative (the GPU's powf / sinf / cosf against libm's).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def dh(tmp_path_factory):
+    from hairmsnn_gb300 import build
+    build.build()
+    out = str(tmp_path_factory.mktemp("dh") / "libdh.so")
+    cmd = [build.nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-fmad=false", "-std=c++17",
+           "--expt-relaxed-constexpr", "-shared", "-Xcompiler", "-fPIC", "-cudart", "static",
+           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "hairmsnn_gb300", "csrc"),
+           os.path.join(ROOT, "tests", "device_header_kernel.cu"), "-o", out]
+    subprocess.run(cmd, check=True, capture_output=True)
+    L = ctypes.CDLL(out)
+    vp, i32 = ctypes.c_void_p, ctypes.c_int
+    L.dh_eval.argtypes = [vp] * 9 + [i32]
+    L.dh_sample.argtypes = [vp] * 10 + [i32]
+    L.dh_ggx.argtypes = [vp] * 9 + [i32]
+    return L
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def test_device_header_hair_bsdf_equals_batched_api(dh):
+    import hairmsnn_gb300 as hm
+    n = 1 << 15
+    wo, wi, t, h, u = hm.gen_bsdf_queries(11, n)
+    p = hm.hair_params()
+    f = torch.empty((3, n), device="cuda")
+    pdf = torch.empty(n, device="cuda")
+    hu = torch.empty(n, device="cuda")
+    assert dh.dh_eval(ptr(wo), ptr(wi), ptr(t), ptr(h), ctypes.byref(p), ptr(f), ptr(pdf), ptr(hu), n) == 0
+    rf, rpdf = hm.bsdf_eval(wo, wi, t, hu)
+    torch.cuda.synchronize()
+    assert torch.isfinite(f).all()
+    assert torch.equal(f, rf) and torch.equal(pdf, rpdf)
+    wi2 = torch.empty((3, n), device="cuda")
+    assert dh.dh_sample(ptr(wo), ptr(t), ptr(h), ptr(u), ctypes.byref(p), ptr(wi2), ptr(f), ptr(pdf), ptr(hu),
+                        n) == 0
+    rwi, rf, rpdf = hm.bsdf_sample(wo, t, hu, u)
+    torch.cuda.synchronize()
+    assert torch.equal(wi2, rwi) and torch.equal(f, rf) and torch.equal(pdf, rpdf)
+
+
+def test_gpu_ggx_matches_reference_golden(dh, golden):
+    n = len(golden["ggx_alpha"])
+    d = lambda k: torch.from_numpy(np.ascontiguousarray(golden[k], np.float32)).cuda()
+    f = torch.empty((n, 3), device="cuda")
+    L = torch.empty((n, 3), device="cuda")
+    pdf = torch.empty(n, device="cuda")
+    hpdf = torch.empty(n, device="cuda")
+    args = [d("ggx_wo"), d("ggx_wi"), d("ggx_color"), d("ggx_alpha"), d("ggx_r2")]
+    assert dh.dh_ggx(*[ptr(a) for a in args], ptr(f), ptr(L), ptr(pdf), ptr(hpdf), n) == 0
+    for got, key in ((f, "ggx_f"), (L, "ggx_L"), (pdf, "ggx_pdf"), (hpdf, "ggx_hvec_pdf")):
+        ref = golden[key].astype(np.float64)
+        g = got.cpu().numpy().astype(np.float64)
+        assert np.all(np.abs(g - ref) <= 1e-5 * np.abs(ref) + 1e-7 * np.abs(ref).max()), key

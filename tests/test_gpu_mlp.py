@@ -143,3 +143,57 @@ def test_zero_and_bad_batches(mlpmod):
     assert net.inference(x).shape == (0, 3)
     with pytest.raises(HMError):
         net.backward(torch.zeros((5, 3), device="cuda"))  # no matching forward
+
+
+def _write_snapshot(path, params, dtype):
+    """A tiny-cuda-nn trainer snapshot as JSON text, the form
+    TINY_MLP::loadWeights reads (params_binary as {"bytes": [...]})."""
+    raw = np.ascontiguousarray(params, dtype).tobytes()
+    with open(path, "w") as f:
+        f.write('{"n_params": %d, "params_type": "%s", "params_binary": {"bytes": [%s], "subtype": null}, '
+                '"optimizer": {"current_step": 7}}\n'
+                % (len(params), "float" if dtype == np.float32 else "__half", ",".join(map(str, raw))))
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float16])
+def test_loads_tcnn_snapshot(mlpmod, tmp_path, dtype):
+    """hm_mlp_load on a tiny-cuda-nn trainer snapshot (float or __half
+    parameters) and hm_mlp_save's JSON form: the parameters arrive exactly
+    (half -> float exactly), and inference runs on them."""
+    net = mlpmod.TinyMLP("hairmsnn_cache.json", 12, 3, seed=3)
+    n = net.info().n_params
+    p = np.random.default_rng(4).normal(scale=0.05, size=n).astype(dtype)
+    path = str(tmp_path / "weights.json")
+    _write_snapshot(path, p, dtype)
+    net.load_weights(path)
+    assert np.array_equal(net.params(), p.astype(np.float32))
+    x = torch.from_numpy(ref_inputs(4096)).cuda()
+    y = net.inference(x)
+    net2 = mlpmod.TinyMLP("hairmsnn_cache.json", 12, 3, seed=9)
+    out = str(tmp_path / "again.json")
+    net.save(out)
+    net2.load_weights(out)
+    assert np.array_equal(net2.params(), net.params())
+    assert torch.equal(net2.inference(x), y)
+    bad = str(tmp_path / "short.json")
+    _write_snapshot(bad, p[:-1], dtype)
+    with pytest.raises(Exception):
+        net2.load_weights(bad)
+
+
+def test_scene_init_weights_loads_the_cache(tmp_path):
+    """tcnn.init_weights of the scene JSON (scene.cpp:330-331) is loaded into
+    the render's cache network when the renderer is made
+    (render_hair_msnn.cu:109-110)."""
+    from hairmsnn_gb300 import build, render as R
+    build.build()
+    cfg = R.straight_hair_scene(64, 64, strands=200)
+    s0 = R.Scene(cfg)
+    r0 = R.Renderer(s0, R.MSNN, beta=1, train_records=1024, train=False)
+    n = r0.cache().info().n_params
+    p = np.random.default_rng(5).normal(scale=0.03, size=n).astype(np.float32)
+    _write_snapshot(str(tmp_path / "w.json"), p, np.float32)
+    cfg["tcnn"] = {"init_train": False, "init_weights": "w.json"}
+    s = R.Scene(cfg, str(tmp_path))
+    r = R.Renderer(s, R.MSNN, beta=1, train_records=1024, train=False)
+    assert np.array_equal(r.cache().params(), p)

@@ -1621,6 +1621,36 @@ extern "C" int hm_render_set_instrumentation(hm_render* h, int timing, int count
   return HM_OK;
 }
 
+extern "C" int hm_queue_compact(const int32_t* d_keep, const int32_t* d_queue, int64_t n, int32_t* d_out,
+                                int64_t* out_count, void* stream) {
+  if (n < 0 || n > (int64_t)1 << 30 || (n > 0 && (!d_keep || !d_queue || !d_out)) || !out_count)
+    return hm_set_error("hm_queue_compact: bad arguments"), HM_EINVAL;
+  *out_count = 0;
+  if (n == 0) return HM_OK;
+  const cudaStream_t st = (cudaStream_t)stream;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int nblocks = (int)((n + kScanBlock - 1) / kScanBlock);
+  int* buf = nullptr;  // [0] count in, [1] count out, [2..] block sums
+  cudaError_t e = cudaMalloc(&buf, (size_t)(nblocks + 3) * sizeof(int));
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_queue_compact");
+  const int nn = (int)n;
+  cudaMemcpyAsync(buf, &nn, sizeof(int), cudaMemcpyHostToDevice, st);
+  // the launches of a bounce round's compaction (render_frame)
+  scan_count_kernel<<<std::min(nblocks, sms * 2), kScanBlock, 0, st>>>(d_keep, buf, buf + 2, nblocks);
+  scan_blocks_kernel<<<1, 1024, 0, st>>>(buf + 2, buf, buf + 1);
+  scatter_kernel<<<std::min(nblocks, sms * 2), kScanBlock, 0, st>>>(d_keep, d_queue, buf, buf + 2, d_out, nblocks);
+  e = cudaGetLastError();
+  int out = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&out, buf + 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(buf);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_queue_compact");
+  *out_count = out;
+  return HM_OK;
+}
+
 extern "C" int hm_render_set_path_log(hm_render* h, int vertices) {
   if (!h || vertices < 0 || vertices > 4096) return hm_set_error("hm_render_set_path_log: bad arguments"), HM_EINVAL;
   Render* r = (Render*)h;

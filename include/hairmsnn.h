@@ -409,6 +409,14 @@ typedef struct hm_render_timings {
 } hm_render_timings;
 int hm_render_set_instrumentation(hm_render* render, int timing, int counting);
 int hm_render_get_timings(const hm_render* render, hm_render_timings* out);
+/* The wavefront's queue compaction (no reference counterpart: the OptiX
+ * megakernel has no queues): out = the entries queue[i] with keep[i] != 0,
+ * in order (a stable partition), *out_count their number.  The same three
+ * kernels (block counts, block-offset scan, scatter) that compact the path
+ * queue between bounce rounds of a frame.  Device arrays of n int32; waits
+ * for the stream. */
+int hm_queue_compact(const int32_t* d_keep, const int32_t* d_queue, int64_t n, int32_t* d_out, int64_t* out_count,
+                     void* stream);
 /* Per-path ray log (no reference counterpart; parity tests).  With
  * vertices > 0 every later frame records, for each path, the rays it traced
  * at its first `vertices` vertices; hm_render_read_path_log copies the last

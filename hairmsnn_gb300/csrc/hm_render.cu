@@ -111,7 +111,7 @@ struct BatchRays {
   HM_D void write(int i, const Hit& h) const { out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v); }
 };
 
-constexpr int kStragglers = 2;        // lanes a warp does not wait for before its leaf phase
+constexpr int kStragglers = 4;        // lanes a warp does not wait for before its leaf phase
 constexpr int kMaxRounds = 1 << 22;   // per-warp round cap (~6k rounds per warp at 512x512)
 
 // COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
       if (lane == 0) atomicOr(err, TRACE_ERR_STEPS);
       break;
     }
-    // box phase: walk inner nodes until every lane has parked a leaf or
+    // box phase: walk inner nodes until every lane has parked two leaves or
     // finished; once some lane has a leaf parked, up to kStragglers lanes
     // that still need steps are not waited for (they continue next round).
     // Every iteration advances at least one lane, so the phase terminates.
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
       const bool need = cur >= 0 && trav_needs_step(t);
       const unsigned needm = __ballot_sync(FULL, need);
       if (needm == 0) break;
-      const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.pend >= 0);
+      const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.np > 0);
       if (parked != 0 && __popc(needm) <= kStragglers) break;
       if (need) trav_inner_step<COUNT>(*sp, t, stack, err, &tc);
     }

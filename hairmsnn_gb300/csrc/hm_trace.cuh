@@ -236,7 +236,8 @@ struct TravState {
   int node;
   int sp;
   int visits;
-  int pend;  // parked leaf slot, -1: none
+  int np;          // parked leaves (0 .. 2)
+  int pend0, pend1;  // their leaf slots
 };
 
 HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
@@ -251,17 +252,28 @@ HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
   t.node = 0;
   t.sp = 0;
   t.visits = 0;
-  t.pend = -1;
+  t.np = 0;
+  t.pend0 = t.pend1 = -1;
 }
 
 // Leaf-postponing traversal ("while-while", Aila & Laine 2009): an inner
-// step only walks boxes; a leaf reached is parked (t.pend = leaf slot) and
-// tested later together with the other lanes' parked leaves, so the expensive
-// curve test runs with most lanes of the warp active.
+// step only walks boxes; a leaf reached is parked and tested later together
+// with the other lanes' parked leaves, so the expensive curve test runs with
+// most lanes of the warp active.  A lane parks up to two leaves before it
+// waits for the leaf phase: fewer leaf rounds per ray, and more lanes still
+// walking boxes in each box round.
 //   t.node >= 0: next wide node to visit; t.node < 0: pop next.
-//   A lane needs inner steps while nothing is parked and work remains.
-HM_D bool trav_needs_step(const TravState& t) { return t.pend < 0 && (t.node >= 0 || t.sp > 0); }
-HM_D bool trav_finished(const TravState& t) { return t.pend < 0 && t.node < 0 && t.sp == 0; }
+//   A lane needs inner steps while it has room to park and work remains.
+constexpr int kParked = 2;
+HM_D bool trav_needs_step(const TravState& t) { return t.np < kParked && (t.node >= 0 || t.sp > 0); }
+HM_D bool trav_finished(const TravState& t) { return t.np == 0 && t.node < 0 && t.sp == 0; }
+HM_D void trav_park(TravState& t, int slot) {
+  if (t.np == 0)
+    t.pend0 = slot;
+  else
+    t.pend1 = slot;
+  ++t.np;
+}
 
 template <bool COUNT>
 HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err, TraceCount* cnt) {
@@ -286,7 +298,7 @@ HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err
     }
     if (!popped) return;  // finished
     if (cur < 0) {        // a leaf left on the stack
-      t.pend = ~cur;
+      trav_park(t, ~cur);
       return;
     }
   }
@@ -327,26 +339,31 @@ HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err
   for (int k = 0; k < kWide; ++k)
     if ((m >> k) & 1u) cn = cc[k];
   if (cn < 0) {
-    t.pend = ~cn;
+    trav_park(t, ~cn);
     t.node = -1;
   } else {
     t.node = cn;
   }
 }
 
-// Tests the parked leaf.  Returns true if an any-hit ray is finished.
+// Tests the parked leaves, in the order they were parked.  Returns true if
+// an any-hit ray is finished.
 template <bool ANY_HIT, bool COUNT>
 HM_D bool trav_leaf(const SceneDev& s, TravState& t, TraceCount* cnt) {
-  if (t.pend < 0) return false;
-  const int prim = __ldg(s.prim_of_leaf + t.pend);
-  t.pend = -1;
-  if (COUNT) cnt->prims += 1;
-  float th, u, v;
-  int id;
-  if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v, &id)) {
-    t.h = Hit{th, id, u, v};
-    if (ANY_HIT) return true;
+  for (int j = 0; j < t.np; ++j) {
+    const int prim = __ldg(s.prim_of_leaf + (j == 0 ? t.pend0 : t.pend1));
+    if (COUNT) cnt->prims += 1;
+    float th, u, v;
+    int id;
+    if (prim_intersect(s, prim, Ray{t.o, t.d, t.tmin, t.h.t}, t.h.t, &th, &u, &v, &id)) {
+      t.h = Hit{th, id, u, v};
+      if (ANY_HIT) {
+        t.np = 0;
+        return true;
+      }
+    }
   }
+  t.np = 0;
   return false;
 }
 

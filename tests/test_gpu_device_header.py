@@ -39,7 +39,7 @@ def dh(tmp_path_factory):
     L = ctypes.CDLL(out)
     vp, i32 = ctypes.c_void_p, ctypes.c_int
     L.dh_eval.argtypes = [vp] * 8 + [i32]
-    L.dh_sample.argtypes = [vp] * 10 + [i32]
+    L.dh_sample.argtypes = [vp] * 9 + [i32]
     L.dh_ggx.argtypes = [vp] * 9 + [i32]
     return L
 

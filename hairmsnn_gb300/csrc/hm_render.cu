@@ -112,6 +112,8 @@ struct BatchRays {
 };
 
 constexpr int kStragglers = 4;        // lanes a warp does not wait for before its leaf phase
+constexpr int kParkAnyHit = 2;        // leaves a lane parks before the leaf phase: shadow rays
+constexpr int kParkClosest = 2;       // ... extension rays
 constexpr int kMaxRounds = 1 << 22;   // per-warp round cap (~6k rounds per warp at 512x512)
 
 // COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
     // that still need steps are not waited for (they continue next round).
     // Every iteration advances at least one lane, so the phase terminates.
     for (int guard = 0; guard < kMaxVisits; ++guard) {
-      const bool need = cur >= 0 && trav_needs_step(t);
+      const bool need = cur >= 0 && trav_needs_step<(ANY_HIT ? kParkAnyHit : kParkClosest)>(t);
       const unsigned needm = __ballot_sync(FULL, need);
       if (needm == 0) break;
       const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.np > 0);

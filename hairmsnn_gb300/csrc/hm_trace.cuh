@@ -264,8 +264,9 @@ HM_D void trav_init(TravState& t, f3 o, f3 d, float tmin, float tmax) {
 // walking boxes in each box round.
 //   t.node >= 0: next wide node to visit; t.node < 0: pop next.
 //   A lane needs inner steps while it has room to park and work remains.
-constexpr int kParked = 2;
-HM_D bool trav_needs_step(const TravState& t) { return t.np < kParked && (t.node >= 0 || t.sp > 0); }
+//   PARK: leaves a lane may park (1 or 2).
+template <int PARK>
+HM_D bool trav_needs_step(const TravState& t) { return t.np < PARK && (t.node >= 0 || t.sp > 0); }
 HM_D bool trav_finished(const TravState& t) { return t.np == 0 && t.node < 0 && t.sp == 0; }
 HM_D void trav_park(TravState& t, int slot) {
   if (t.np == 0)

@@ -17,8 +17,8 @@ Workloads (synthetic, seeded):
 One JSON line is printed by rank 0.  `value` times the kernels with inputs
 resident in HBM (vertex: CUDA events per step on the launching stream, L2
 flushed between steps outside the events; render: CUDA events around K
-pipelined frames on the submitting stream, a 256 MiB L2-flush write before
-each frame's submission inside the region); `e2e` times the same step
+pipelined frames on the submitting stream, no flush: each frame in flight
+streams its own ~90 MB of path state past the 129 MB L2); `e2e` times the same step
 through the public API with pinned host inputs copied in and results copied
 out inside the timed region.  Multi-GPU runs are independent replicas (the path has no
 exchange step on one box).
@@ -125,9 +125,12 @@ def host_threads():
 
 def run_reference(args):
     """--impl reference: the reference's per-pixel path on the host cores,
-    with the oracle alone (the reference compiles only as OptiX programs;
-    its host build under oracle/_ref exists only where the reference checkout
-    does, and never on the GPU host).  Rank 0 only; no GPU work.
+    with the oracle alone, which reproduces the reference's own integrator
+    bit for bit (the host build of the reference's code under oracle/_ref
+    needs the reference checkout, which the GPU host does not have).  No
+    product library is loaded: the scene comes from the oracle's generator
+    (hairmsnn_gb300.render only supplies the config dict; the package loads
+    its library lazily).  Rank 0 only; no GPU work.
       render: the same frame work as the GPU arm per pixel (CpuFrameSample:
               G-buffer paths, cache inference, cache training gradient) over
               a band of pixels per step;
@@ -189,7 +192,8 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200,
+                    help="timed steps (render: 200 frames, about a second of device time)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default=os.environ.get("HM_BENCH_WORKLOAD", "render"),

@@ -1345,6 +1345,10 @@ static int render_pretrain(Render* r, int passes, cudaStream_t user) {
     const int id = r->pretrain_passes++;
     FrameParams fp{r->mode, r->beta_knob - 1, id, id + 10007, 1, r->n_train, r->in_ch,
                    1, r->d_samples, r->n_samples, 0x9e37u + (uint32_t)id};
+    if (r->log_ev && r->n_train <= r->P) {  // the log holds P paths
+      fp.log = PathLog{r->log_ev, r->log_vcur, r->log_slots};
+      cudaMemsetAsync(r->log_ev, 0xff, (size_t)r->P * r->log_slots * 3 * sizeof(float4), st);
+    }
     int* q_cur = sl.q_a;
     int* q_next = sl.q_b;
     int* c_cur = sl.counts;
@@ -1362,7 +1366,8 @@ static int render_pretrain(Render* r, int passes, cudaStream_t user) {
                                                       sl.fetch + 2 * it + 1, sl.err, r->d_cnt + 3, false,
                                                       r->blocks_shadow, st))
         return e;
-      shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{});
+      shadow_resolve_kernel<false><<<grid, 256, 0, st>>>(sl.ps, q_cur, c_cur, sl.vis, DiffParams{}, nullptr,
+                                                         nullptr, fp.log);
       scan_count_kernel<<<std::min(nblocks, r->sm_count * 2), kScanBlock, 0, st>>>(sl.keep, c_cur, sl.block_sums,
                                                                                     nblocks);
       scan_blocks_kernel<<<1, 1024, 0, st>>>(sl.block_sums, c_cur, c_next);
@@ -1722,6 +1727,11 @@ extern "C" int hm_render_buffer(hm_render* h, int which, void** dptr, int64_t* c
     case 5: *dptr = r->acc_final; if (count) *count = (int64_t)r->P * 3; break;
     case 6: *dptr = r->acc_pt; if (count) *count = (int64_t)r->P * 3; break;
     case 7: *dptr = r->acc_nn; if (count) *count = (int64_t)r->P * 3; break;
+    case 11:
+      if (!r->d_samples) return hm_set_error("hm_render_buffer: no scene samples before hm_render_pretrain"), HM_EINVAL;
+      *dptr = r->d_samples;
+      if (count) *count = (int64_t)r->n_samples;
+      break;
     case 8: case 9: case 10: {
       if (r->mode != MODE_NRC) return hm_set_error("hm_render_buffer: NRC buffers of a non-NRC renderer"), HM_EINVAL;
       const NrcBufs& nb = r->slots[r->accum_id > 0 ? (r->accum_id - 1) % r->depth : 0].nrc;

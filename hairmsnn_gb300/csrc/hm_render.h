@@ -23,6 +23,9 @@ enum RenderMode { MODE_PT = 0, MODE_MSNN = 1, MODE_NRC = 2 };
 // NRC buffers of one frame slot.
 constexpr int kNrcMaxBounces = 40;  // MAX_BOUNCES (nrc.cuh:13)
 constexpr int kNrcRecordF4 = 5;     // per vertex: position / scale, wo, n, direct light, throughput factor
+// width of the scene-sample pass's launch grid (numTrainRecordsX,
+// render_hair_msnn.h:127): record r is launch index (r % 128, r / 128)
+constexpr int kTrainRecordsX = 128;
 struct NrcBufs {
   float4* prev;    // [P] previous vertex and the pdf of the direction sampled there
   float4* spread;  // [P] accumulated spread, a0

@@ -25,7 +25,9 @@ HM_D void st3(float4* p, int i, f3 v, float w = 0.f) { p[i] = make_float4(v.x, v
 
 // Camera rays of one frame, or (fp.pretrain) the rays of the scene-sample
 // training pass: record r aims from the camera at sample perm(r) (the
-// reference's sceneIndices[trOfs], a shuffled index, hair_msnn.cu:222-233).
+// reference's sceneIndices[trOfs], a shuffled index, hair_msnn.cu:222-233)
+// with the RNG of its launch index (r % 128, r / 128) over the frame's
+// width (get_rng with the frame buffer's size, hair_msnn.cu:193-194).
 template <bool MULTI>
 __global__ void __launch_bounds__(256) camera_kernel(const __grid_constant__ SceneDev s0, FrameParams fp, Batch b,
                                                      PathState ps, int* queue, int* count) {
@@ -36,7 +38,8 @@ __global__ void __launch_bounds__(256) camera_kernel(const __grid_constant__ Sce
   if (fp.pretrain) {
     const uint32_t si = feistel_perm((uint32_t)pid, (uint32_t)fp.n_samples, fp.sample_key);
     const float4 sp = fp.samples[si];
-    ps.rng[pid] = rng_seed(fp.frame_seed, (uint32_t)pid);
+    const uint32_t lx = (uint32_t)pid % kTrainRecordsX, ly = (uint32_t)pid / kTrainRecordsX;
+    ps.rng[pid] = rng_seed(fp.frame_seed, lx + ly * (uint32_t)s0.width);
     ps.flags[pid] = F_TRAIN;
     ps.bounce[pid] = 0;
     st3(ps.ray_o, pid, s0.cam_pos);

@@ -353,13 +353,14 @@ class Renderer:
     def buffer(self, which):
         """Host copy of a device buffer of the last frame (see hm_render_buffer):
         0 cache inputs [P,12], 1 cache outputs [P,3], 2 training inputs [R,12],
-        3 training targets [R,3], 4 G-buffer [P,4]."""
+        3 training targets [R,3], 4 G-buffer [P,4], 11 scene samples of the
+        scene-sample training pass [N,4] (after pretrain)."""
         p = ctypes.c_void_p()
         n = ctypes.c_int64()
         check(lib().hm_render_buffer(self._h, which, ctypes.byref(p), ctypes.byref(n)))
         in_ch = 9 if self.mode == NRC else 12
-        width = {0: in_ch, 1: 3, 2: in_ch, 3: 3, 4: 4, 8: 4, 9: 20, 10: 4}[which]
-        count = n.value * (4 if which in (4, 8, 9, 10) else 1)
+        width = {0: in_ch, 1: 3, 2: in_ch, 3: 3, 4: 4, 8: 4, 9: 20, 10: 4, 11: 4}[which]
+        count = n.value * (4 if which in (4, 8, 9, 10, 11) else 1)
         host = np.zeros(count, np.int32 if which == 10 else np.float32)
         check(lib().hm_copy_to_host(host.ctypes.data_as(ctypes.c_void_p), p, count * 4))
         return host.reshape(-1, width)

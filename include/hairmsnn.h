@@ -356,8 +356,14 @@ int hm_render_batch_scene(const hm_render* render, int scene, int* pixel_offset,
  * explicit number of passes.  Each pass traces train_records training paths
  * aimed from the camera at points sampled on the hair (about 10^6, placed
  * by segment length as fetchSceneSamples, render_hair_msnn.cu:34-97) and
- * takes one training step.  HairMSNN renderers only; waits for frames in
- * flight and returns when the passes have finished. */
+ * takes one training step.  Record r of the k-th pass (k counted over the
+ * renderer's life from 0) aims at sample perm_k(r), a keyed permutation of
+ * the samples standing in for the reference's shuffled sceneIndices, and
+ * seeds its RNG as the reference's launch index (r % 128, r / 128) over the
+ * frame's width with frame number k.  With a path log on and train_records
+ * <= pixels, the log holds the last pass's paths (record r at path r).
+ * HairMSNN renderers only; waits for frames in flight and returns when the
+ * passes have finished. */
 int hm_render_pretrain(hm_render* render, int passes, void* stream);
 /* Launch-shape autotuner (no reference counterpart): times `frames`
  * pipelined frames per candidate and keeps the fastest persistent-traversal
@@ -440,7 +446,8 @@ hm_mlp* hm_render_cache(hm_render* render);
  * suffix queries): 8 throughput at each pixel's cache query (float4 [P]),
  * 9 train buffer (float4 [T][40][5]: position / scale, wo, n, direct light,
  * throughput factor), 10 per training pixel (int4: bounces, suffix ended at
- * a query, unbiased, primary hit). */
+ * a query, unbiased, primary hit).  11: the points of the scene-sample
+ * training pass (float4 [N], xyz; after hm_render_pretrain). */
 int hm_render_buffer(hm_render* render, int which, void** dptr, int64_t* count);
 
 /* ------------------------------------------------------------------------

@@ -1162,6 +1162,71 @@ void hmo_render_pixels_ev(void* h, int mode, int beta_knob, int accum_id, int ev
   for (auto& t : pool) t.join();
 }
 
+// One TRAIN_DATA_GEN launch of rayGenCam (hair_msnn.cu:187-275) for
+// training records [p0, p0 + np) of a rec_x-wide launch grid: record r =
+// x + rec_x * y aims from the camera at points[r] (the reference's
+// sampledPoints[sceneIndices[trOfs]], gathered by the caller), seeds its RNG
+// with launch index (x, y) over the frame's width (get_rng with the frame
+// buffer's size, hair_msnn.cu:193-194) and runs msnnTrainingPath.
+// train_in [np][12] / train_out [np][3]: nnTrainInput / nnTrainOutput at
+// trOfs; flags bit0 hit, bit1 surface; events / n_events / rng_end as in
+// hmo_render_pixels_ev (may be NULL).
+void hmo_render_traingen_ev(void* h, int beta_knob, int accum_id, int rec_x, const float* points, int p0, int np,
+                            float* train_in, float* train_out, int* flags, float* events, int* n_events,
+                            uint32_t* rng_end, int max_events, int threads) {
+  OScene* s = (OScene*)h;
+  auto work = [&](int b, int e) {
+    EvLog log;
+    for (int r = b; r < e; ++r) {
+      const int i = r - p0;
+      if (events) {
+        log.ev = events + (size_t)i * max_events * kEvFloats;
+        log.cap = max_events;
+        log.n = 0;
+        tl_log = &log;
+      }
+      ulp_seed_path((uint32_t)r);
+      const int x = r % rec_x, y = r / rec_x;
+      uint32_t rng = get_rng(accum_id + 10007, (uint32_t)x, (uint32_t)y, (uint32_t)s->width, (uint32_t)s->height);
+      const V3 sp(points[3 * (size_t)i], points[3 * (size_t)i + 1], points[3 * (size_t)i + 2]);
+      const V3 dir = normalize(sp - s->cam_pos);
+      SI si;
+      si.hit = false;
+      si.wo = -1.f * dir;
+      si.wi = dir;
+      trace_radiance(*s, s->cam_pos, dir, si, rng);
+      V3 c(0.f), sc(0.f);
+      if (si.hit) c = msnn_training_path(*s, si, rng, &sc, beta_knob - 1);
+      if (isnan(c.x) || isnan(c.y) || isnan(c.z)) c = V3(0.f);
+      if (isinf(c.x) || isinf(c.y) || isinf(c.z)) c = V3(1e5f);
+      if (isnan(sc.x) || isnan(sc.y) || isnan(sc.z)) sc = V3(0.01f);
+      if (isinf(sc.x) || isinf(sc.y) || isinf(sc.z)) sc = V3(1e5f);
+      train_out[3 * (size_t)i] = c.x - sc.x;
+      train_out[3 * (size_t)i + 1] = c.y - sc.y;
+      train_out[3 * (size_t)i + 2] = c.z - sc.z;
+      V3 p = si.hit ? si.p / s->scene_scale : V3(0.f);
+      V3 t = si.hit ? si.t : V3(0.f);
+      float row[12] = {p.x, p.y, p.z, si.wo.x, si.wo.y, si.wo.z, t.x, t.y, t.z, 0.f, 0.f, 0.f};
+      memcpy(train_in + 12 * (size_t)i, row, sizeof(row));
+      flags[i] = (si.hit ? 1 : 0) | (si.hit && si.surface ? 2 : 0);
+      if (n_events) n_events[i] = log.n;
+      if (rng_end) rng_end[i] = rng;
+    }
+    tl_log = nullptr;
+  };
+  if (threads <= 1) {
+    work(p0, p0 + np);
+    return;
+  }
+  std::vector<std::thread> pool;
+  int chunk = (np + threads - 1) / threads;
+  for (int k = 0; k < threads; ++k) {
+    int b = p0 + k * chunk, e = std::min(p0 + np, b + chunk);
+    if (b < e) pool.emplace_back(work, b, e);
+  }
+  for (auto& t : pool) t.join();
+}
+
 // The training-pixel permutation (the reference's shuffled trainIdxs table).
 uint32_t hmo_feistel_perm(uint32_t i, uint32_t n, uint32_t key) { return feistel_perm(i, n, key); }
 

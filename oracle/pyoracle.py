@@ -138,6 +138,9 @@ def _declare_render(L):
     L.hmo_render_pixels_ev.restype = None
     L.hmo_render_pixels_ev.argtypes = [vp, i32, i32, i32, i32, i32, i32, i32, F32P, F32P, F32P, I32P, F32P, I32P,
                                        U32P, i32, i32]
+    L.hmo_render_traingen_ev.restype = None
+    L.hmo_render_traingen_ev.argtypes = [vp, i32, i32, i32, F32P, i32, i32, F32P, F32P, I32P, F32P, I32P, U32P,
+                                         i32, i32]
     L.hmo_feistel_perm.restype = ctypes.c_uint32
     L.hmo_feistel_perm.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
     L.hmo_render_nrc.restype = None
@@ -259,6 +262,27 @@ def _render_pixels_ev(self, mode, beta=1, accum_id=0, every_nth=1, n_train=0, ma
 
 
 OracleScene.render_pixels_ev = _render_pixels_ev
+
+
+def _render_traingen_ev(self, points, beta=1, accum_id=0, rec_x=128, max_events=128, threads=8):
+    """The scene-sample training pass (TRAIN_DATA_GEN) for len(points)
+    records: record r aims at points[r] (float [R, 3]) and sits at launch
+    index (r % rec_x, r // rec_x).  Returns (train_in [R, 12], train_out
+    [R, 3], flags [R], events [R, max_events, 12], n_events [R], rng_end [R])."""
+    pts = np.ascontiguousarray(np.asarray(points, np.float32)[:, :3])
+    n = len(pts)
+    tin = np.zeros((n, 12), np.float32)
+    tout = np.zeros((n, 3), np.float32)
+    flags = np.zeros(n, np.int32)
+    ev = np.zeros((n, max_events, EV_FLOATS), np.float32)
+    nev = np.zeros(n, np.int32)
+    rng_end = np.zeros(n, np.uint32)
+    lib().hmo_render_traingen_ev(self.h, beta, accum_id, rec_x, pts, 0, n, tin, tout, flags, ev, nev, rng_end,
+                                 max_events, threads)
+    return tin, tout, flags, ev, nev, rng_end
+
+
+OracleScene.render_traingen_ev = _render_traingen_ev
 
 
 def event_digest(ev, n_ev):

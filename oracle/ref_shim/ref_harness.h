@@ -172,12 +172,13 @@ inline Scene* new_scene(void* trace_scene, const float* cp, int n_cp, const int*
   return s;
 }
 
-// Runs fn(pixel) for every pixel of the frame with the launch index and the
-// raygen's program data set; ev/n_ev/max_ev: optional per-pixel event logs.
+// Runs fn(index) for every index of an lw x lh launch grid with the launch
+// index and the raygen's program data (whose frameBufferSize stays the
+// frame's) set; ev/n_ev/max_ev: optional per-index event logs.
 template <class Fn>
-void launch(Scene* s, int threads, float* ev, int* n_ev, int max_ev, Fn fn) {
+void launch_grid(Scene* s, int lw, int lh, int threads, float* ev, int* n_ev, int max_ev, Fn fn) {
   g_scene = s;
-  const int P = s->width * s->height;
+  const int P = lw * lh;
   auto work = [&](int b, int e) {
     EvLog log;
     for (int pid = b; pid < e; ++pid) {
@@ -188,8 +189,8 @@ void launch(Scene* s, int threads, float* ev, int* n_ev, int max_ev, Fn fn) {
         tl_log = &log;
       }
       hm_shim_ctx = HmShimHitContext();
-      hm_shim_ctx.launch_x = pid % s->width;
-      hm_shim_ctx.launch_y = pid / s->width;
+      hm_shim_ctx.launch_x = pid % lw;
+      hm_shim_ctx.launch_y = pid / lw;
       hm_shim_ctx.program_data = &s->raygen;
       fn(pid);
       if (n_ev) n_ev[pid] = log.n;
@@ -208,6 +209,12 @@ void launch(Scene* s, int threads, float* ev, int* n_ev, int max_ev, Fn fn) {
     if (b < e) pool.emplace_back(work, b, e);
   }
   for (auto& t : pool) t.join();
+}
+
+// The frame-sized launch: fn(pixel) for every pixel.
+template <class Fn>
+void launch(Scene* s, int threads, float* ev, int* n_ev, int max_ev, Fn fn) {
+  launch_grid(s, s->width, s->height, threads, ev, n_ev, max_ev, fn);
 }
 
 }  // namespace hmref

@@ -86,6 +86,38 @@ void hmr_msnn_gbuffer(void* h, const float* camera12, const float* mat16, const 
   for (int i = 0; i < P; ++i) gbuf_to_f(gb[i], gbuf + 8 * (size_t)i);
 }
 
+// One TRAIN_DATA_GEN launch of rayGenCam (hair_msnn.cu:187-275,
+// render_hair_msnn.cu:654-662) over a rec_x x rec_y grid: record trOfs =
+// x + rec_x * y aims at points3[scene_indices[trOfs]] and writes
+// nnTrainInput / nnTrainOutput [rec_x * rec_y][12] / [..][3] at trOfs.
+void hmr_msnn_traingen(void* h, const float* camera12, const float* mat16, const int* settings9, float scene_scale,
+                       int beta_knob, int accum_id, int rec_x, int rec_y, const int* scene_indices,
+                       const float* points3, int n_points, float* train_in, float* train_out, float* ev, int* n_ev,
+                       int max_ev, int threads) {
+  hmref::Scene* s = (hmref::Scene*)h;
+  LaunchParams& lp = optixLaunchParams;
+  lp = LaunchParams();
+  hmref::set_scene_params(lp, *s, camera12, mat16, settings9, scene_scale);
+  lp.pathV1 = settings9[2];
+  lp.pathV2 = settings9[3];
+  std::vector<int> sidx(scene_indices, scene_indices + (size_t)rec_x * rec_y);
+  std::vector<float3> pts(n_points);
+  for (int i = 0; i < n_points; ++i) pts[i] = float3{points3[3 * i], points3[3 * i + 1], points3[3 * i + 2]};
+  lp.pass = TRAIN_DATA_GEN;
+  lp.accumId = accum_id;
+  lp.numTrainRecordsX = rec_x;
+  lp.numTrainRecordsY = rec_y;
+  lp.numSamples = n_points;
+  lp.sceneIndices = sidx.data();
+  lp.sampledPoints = pts.data();
+  lp.mlpInputCh = 12;
+  lp.mlpOutputCh = 3;
+  lp.nnTrainInput = train_in;
+  lp.nnTrainOutput = train_out;
+  lp.beta = beta_knob - 1;
+  hmref::launch_grid(s, rec_x, rec_y, threads, ev, n_ev, max_ev, [&](int) { __raygen__rayGenCam(); });
+}
+
 // One RENDER launch (hair_msnn.cu:314-356): gbuf_in [P][8] and nn_out [P][3]
 // in; the three accumulation buffers [P][4] are read (accum_id > 0) and
 // written; the three average buffers [P][4] are written.

@@ -54,6 +54,9 @@ def _load(which):
         L.hmr_msnn_gbuffer.restype = None
         L.hmr_msnn_gbuffer.argtypes = [vp, F32P, F32P, I32P, f32, i32, i32, i32, I32P, i32, F32P, F32P, F32P, F32P,
                                        F32P, I32P, i32, i32]
+        L.hmr_msnn_traingen.restype = None
+        L.hmr_msnn_traingen.argtypes = [vp, F32P, F32P, I32P, f32, i32, i32, i32, i32, I32P, F32P, i32, F32P, F32P,
+                                        F32P, I32P, i32, i32]
         L.hmr_msnn_render.restype = None
         L.hmr_msnn_render.argtypes = [vp, i32, F32P, F32P, F32P, F32P, F32P, F32P, F32P, F32P, i32]
     elif which == "nrc":
@@ -127,6 +130,24 @@ class RefIntegrator:
         self.L.hmr_msnn_gbuffer(self.h, r["cam"], r["mat"], r["sets"], self.osc.scene_scale, beta, accum_id,
                                 every_nth, tidx, len(tidx), out["gbuf"], out["nn_in"], out["train_in"],
                                 out["train_out"], out["events"], out["n_events"], max_events, threads)
+        return out
+
+    def msnn_traingen(self, points, scene_indices, rec_x, beta=1, accum_id=0, max_events=128, threads=8):
+        """The TRAIN_DATA_GEN pass over a rec_x-wide grid of len(scene_indices)
+        records aiming at points[scene_indices[r]] (points float [N, 3]).
+        Returns dict train_in [R, 12], train_out [R, 3], events [R,
+        max_events, 12], n_events [R]."""
+        assert self.which == "path"
+        r = self._arr
+        sidx = np.ascontiguousarray(scene_indices, np.int32)
+        R = len(sidx)
+        assert R % rec_x == 0
+        pts = np.ascontiguousarray(np.asarray(points, np.float32)[:, :3])
+        out = dict(train_in=np.zeros((R, 12), np.float32), train_out=np.zeros((R, 3), np.float32),
+                   events=np.zeros((R, max_events, po.EV_FLOATS), np.float32), n_events=np.zeros(R, np.int32))
+        self.L.hmr_msnn_traingen(self.h, r["cam"], r["mat"], r["sets"], self.osc.scene_scale, beta, accum_id, rec_x,
+                                 R // rec_x, sidx, pts, len(pts), out["train_in"], out["train_out"], out["events"],
+                                 out["n_events"], max_events, threads)
         return out
 
     def msnn_render(self, gbuf, nn_out, accum_id=0, acc=None, threads=8):

@@ -5,7 +5,8 @@ optix_common.cuh and the BSDF headers) are compiled unmodified on the host by
 oracle/build.py (build_ref) through oracle/ref_shim/; their traceRay is
 answered by the oracle's BVH.  This script renders one small seeded scene
 with them (the HairMSNN G_BUFFER pass at BETA 1 and 3, the RENDER pass over
-a seeded cache output, the NRC G_BUFFER pass and the plain path tracer) and stores the scene's
+a seeded cache output, the scene-sample training pass, the NRC G_BUFFER pass
+and the plain path tracer) and stores the scene's
 arrays with the outputs, so the oracle restatement can be pinned against
 them wherever the reference checkout is absent
 (tests/test_ref_integrator.py).  Needs the reference checkout (HM_REF_DIR);
@@ -79,6 +80,16 @@ def main():
     data["nrc_train_pixels"] = tp
     data["nrc_train"] = nrc["train"][tp]
     data["nrc_events"] = event_digest(nrc["events"], nrc["n_events"])
+    # the scene-sample training pass: 512 records on a 32-wide grid aiming at hair points
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_ref_integrator import hair_points
+    pts = hair_points(o, 512, 11)
+    tg = ref.msnn_traingen(pts, np.arange(512, dtype=np.int32), 32, beta=1, accum_id=ACCUM, max_events=MAX_EV)
+    data["traingen_points"] = pts
+    data["traingen_train_in"] = tg["train_in"]
+    data["traingen_train_out"] = tg["train_out"]
+    data["traingen_n_events"] = tg["n_events"]
+    data["traingen_events"] = event_digest(tg["events"], tg["n_events"])
     pt = rp.RefIntegrator(o, "pt").pt_frame(accum_id=ACCUM, max_events=MAX_EV)
     data["pt_accum"] = pt["accum"]
     data["pt_n_events"] = pt["n_events"]

@@ -75,6 +75,22 @@ def oracle_runs(o, mode, max_events, **kw):
     return runs
 
 
+def traingen_oracle_runs(o, points, max_events, **kw):
+    """oracle_runs for the scene-sample training pass
+    (OracleScene.render_traingen_ev over records aiming at `points`); `col`
+    holds each record's training target."""
+    runs = {}
+    for k in (0,) + PERTURBED:
+        po.set_ulp_perturb(k)
+        try:
+            tin, tout, flags, ev, nev, _ = o.render_traingen_ev(points, max_events=max_events, **kw)
+        finally:
+            po.set_ulp_perturb(0)
+        runs[k] = dict(col=tout.astype(np.float64), train_in=tin, flags=flags,
+                       log=oracle_slots(ev, nev, max_events), nev=nev)
+    return runs
+
+
 def nrc_oracle_runs(o, max_events, every_nth, n_train, accum_id=0, c=0.01):
     """oracle_runs for the NRC G_BUFFER pass (OracleScene.render_nrc); `col`
     holds each path's G-buffer (radiance, throughput at the cache query),

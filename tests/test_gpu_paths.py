@@ -48,7 +48,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from pathcheck import check_paths, color_excess, oracle_runs, separation, spread_of
+from pathcheck import check_paths, color_excess, oracle_runs, separation, spread_of, traingen_oracle_runs
 
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
@@ -136,3 +136,35 @@ def test_compose_matches_oracle_render_pass(R):
     for which, k in ((R.IMAGE_FINAL, "final"), (R.IMAGE_SHORT, "pt"), (R.IMAGE_CACHE, "nn")):
         img = r.read(which).reshape(-1, 3)
         assert np.array_equal(img, ref["avg"][k][:, :3].astype(np.float64)), k
+
+
+@pytest.mark.parametrize("catrom", [True, False])
+def test_pretrain_paths_match_oracle(R, catrom):
+    """The scene-sample training pass (hm_render_pretrain, the reference's
+    TRAIN_DATA_GEN pass): every record's training path against the oracle's
+    restatement of the pass (pinned bit for bit to the reference's own, see
+    tests/test_ref_integrator.py), aimed at the GPU's own sample points
+    through the same permutation.  Training targets per path as above; the
+    cache-input row of every record whose primary ray agrees bit for bit."""
+    s = scene(R, catrom, view="top")
+    T = 2048
+    r = R.Renderer(s, R.MSNN, beta=1, train_records=T, train=False, frames_in_flight=1)
+    r.set_path_log(VERTICES)
+    r.pretrain(1)
+    samples = r.buffer(11)
+    perm = np.array([po.feistel_perm(i, len(samples), 0x9E37) for i in range(T)])  # the first pass's key
+    pts = samples[perm, :3]
+    tin, tout = r.buffer(2), r.buffer(3)
+    g_log = r.read_path_log()[:T]
+    o = po.OracleScene.from_library(s)
+    runs = traingen_oracle_runs(o, pts, 3 * VERTICES, beta=1, accum_id=0, rec_x=128)
+    o0 = runs[0]
+    assert (o0["flags"] & 1).sum() > T // 2
+    # the rays cross the hair cloud from the camera to points inside it, with
+    # many grazing hits on the way: the oracle's own perturbed runs separate
+    # about a fifth of these paths (8% for the GPU), hence the cap of 15%
+    check_paths(g_log, tout.astype(np.float64), runs, f"pretrain catrom={catrom}", os.environ.get("HM_PATHS_DUMP"),
+                separate_max=0.15)
+    prim_same = separation(g_log[:, :1], o0["log"][:, :1], tol=0.0)[0]
+    assert prim_same.mean() >= 0.99
+    assert np.array_equal(tin[prim_same].view(np.uint32), o0["train_in"][prim_same].view(np.uint32))

@@ -125,6 +125,17 @@ def test_oracle_nrc_matches_reference_golden(gold, gold_scene):
     assert np.array_equal(digest(o["events"], o["n_events"]), gold["nrc_events"])
 
 
+def test_oracle_traingen_matches_reference_golden(gold, gold_scene):
+    """The scene-sample training pass (TRAIN_DATA_GEN) on the golden scene:
+    records aiming at stored hair points, a 32-wide launch grid."""
+    pts = gold["traingen_points"]
+    tin, tout, flags, ev, nev, _ = gold_scene.render_traingen_ev(pts, beta=1, accum_id=3, rec_x=32, max_events=48)
+    assert np.array_equal(bits(tin), bits(gold["traingen_train_in"]))
+    assert np.array_equal(bits(tout), bits(gold["traingen_train_out"]))
+    assert np.array_equal(nev, gold["traingen_n_events"])
+    assert np.array_equal(digest(ev, nev), gold["traingen_events"])
+
+
 def test_golden_scene_exercises_the_branches(gold):
     """The fixture reaches the branches a frame bar would hide: head-surface
     (GGX) vertices, hair vertices, misses, training pixels, multi-bounce paths."""
@@ -222,3 +233,44 @@ def test_oracle_nrc_matches_reference_live(unbiased):
     assert np.array_equal(bits(on["records"][tp]), bits(ref["train"][tp]))
     assert np.array_equal(on["n_events"][keep], ref["n_events"][keep])
     assert np.array_equal(bits(events_as_reference(on["events"])[keep]), bits(ref["events"][keep]))
+
+
+def hair_points(o, n, seed):
+    """n points on the scene's hair curves (uniform cubic B-spline segments at
+    random u): the targets of the scene-sample pass's rays."""
+    cp = np.asarray(o._keep["control_points"], np.float32).reshape(-1, 4)[:, :3]
+    seg = np.asarray(o._keep["segments"], np.int64)
+    rng = np.random.default_rng(seed)
+    k = rng.integers(len(seg), size=n)
+    u = rng.random(n).astype(np.float32)[:, None]
+    v = 1.0 - u
+    q = cp[seg[k][:, None] + np.arange(4)]
+    b = np.stack([v * v * v / 6, (3 * u ** 3 - 6 * u * u + 4) / 6, (-3 * u ** 3 + 3 * u * u + 3 * u + 1) / 6,
+                  u ** 3 / 6], 1)
+    return np.einsum("nk,nkc->nc", b[:, :, 0], q).astype(np.float32)
+
+
+@needs_ref
+@pytest.mark.parametrize("beta,rec_x", [(1, 32), (2, 128)])
+def test_oracle_traingen_matches_reference_live(beta, rec_x):
+    """The scene-sample training pass (TRAIN_DATA_GEN, hair_msnn.cu:222-233):
+    rays from the camera to sampled hair points, RNG seeded by the launch
+    index over the frame's width, msnnTrainingPath, nnTrainInput /
+    nnTrainOutput at trOfs."""
+    from hairmsnn_gb300 import render as Rn
+    cfg = Rn.straight_hair_scene(48, 48, strands=6000, control_points=32, sky_w=128, sky_h=64, triangles=4000)
+    cfg["integrator"]["shade_catmull_rom"] = True
+    cfg["camera"].update({"from": [0.0, -3.8, 1.0], "to": [0.0, 0.0, 0.6], "cos_fovy": 0.5})
+    o = po.OracleScene.from_library(Rn.Scene(cfg))
+    pts = hair_points(o, 3000, 3)
+    R = 1024
+    sidx = np.random.default_rng(4).permutation(len(pts))[:R].astype(np.int32)
+    ref = refpath.RefIntegrator(o, "path").msnn_traingen(pts, sidx, rec_x, beta=beta, accum_id=2, max_events=96)
+    tin, tout, flags, ev, nev, _ = o.render_traingen_ev(pts[sidx], beta=beta, accum_id=2, rec_x=rec_x,
+                                                        max_events=96)
+    assert (flags & 1).sum() > R // 2 and (flags & 2).sum() > 50  # hair and head-surface records
+    assert (np.abs(tout).sum(1) > 0).sum() > 5
+    assert np.array_equal(bits(tin), bits(ref["train_in"]))
+    assert np.array_equal(bits(tout), bits(ref["train_out"]))
+    assert np.array_equal(nev, ref["n_events"])
+    assert np.array_equal(bits(events_as_reference(ev)), bits(ref["events"]))

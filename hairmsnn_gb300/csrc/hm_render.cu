@@ -138,8 +138,10 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
   bool exhausted = false;
   int rounds = 0;
   for (;;) {
-    const unsigned idle = __ballot_sync(FULL, cur < 0);
-    if (idle && !exhausted) {
+    // refill idle lanes; a lane whose entry holds no ray (a shadow slot
+    // left empty) fetches again at once instead of idling for a round
+    unsigned idle = __ballot_sync(FULL, cur < 0);
+    while (idle && !exhausted) {
       const int leader = __ffs(idle) - 1;
       const int want = __popc(idle);
       int base = 0;
@@ -160,6 +162,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
           }
         }
       }
+      idle = __ballot_sync(FULL, cur < 0);
     }
     if (exhausted && __all_sync(FULL, cur < 0)) break;
     if (++rounds > kMaxRounds) {  // safety net: never spin on a logic error
@@ -176,7 +179,12 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
       if (needm == 0) break;
       const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.np > 0);
       if (parked != 0 && __popc(needm) <= kStragglers) break;
-      if (need) trav_inner_step<COUNT>(*sp, t, stack, err, &tc);
+      if (need) {
+        if (ANY_HIT)
+          trav_inner_step_any<COUNT, kParkAnyHit>(*sp, t, stack, err, &tc);
+        else
+          trav_inner_step<COUNT>(*sp, t, stack, err, &tc);
+      }
     }
     // leaf phase: the parked curve / triangle tests run together
     if (cur >= 0) {

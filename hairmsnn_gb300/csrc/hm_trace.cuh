@@ -5,8 +5,10 @@
 // The kernels walk the LBVH collapsed to 8-wide nodes (224 B, 14 x float4:
 // lo.x[8] hi.x[8] lo.y[8] hi.y[8] lo.z[8] hi.z[8] child[8]; child >= 0 wide
 // node, < 0 leaf slot ~i; empty slots hold a box that every ray misses).
-// The nearest child hit is visited next; the others go on a 96-entry stack
-// with their entry distance, farthest first.  A ray whose stack would
+// Closest-hit rays visit the nearest child hit next and put the others on a
+// 96-entry stack with their entry distance, farthest first; any-hit rays
+// put the children they leave for later on the stack as one group per node
+// (trav_inner_step_any).  A ray whose stack would
 // overflow or whose visit count passes a fixed cap is reported through the
 // error word instead of looping or writing out of bounds.
 //
@@ -345,6 +347,89 @@ HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err
   } else {
     t.node = cn;
   }
+}
+
+// The any-hit (shadow ray) inner step.  An occluder anywhere on the
+// segment ends the ray, so the ray's extent never shrinks and no entry
+// needs its distance: the children hit but not taken go on the stack as one
+// group (node, mask of the children still to visit), and a pop takes the
+// group's lowest child and reads its code from the node.  One push per
+// visit instead of one per child, and no sorting.  Leaves hit are parked at
+// once while the lane has room (PARK); the nearest inner child is walked
+// next (occluders near the ray's origin are the likeliest).
+template <bool COUNT, int PARK>
+HM_D void trav_inner_step_any(const SceneDev& s, TravState& t, int2* stack, int* err, TraceCount* cnt) {
+  if (++t.visits > kMaxVisits) {
+    atomicOr(err, TRACE_ERR_STEPS);
+    t.node = -1;
+    t.sp = 0;
+    return;
+  }
+  int cur;
+  if (t.node >= 0) {
+    cur = t.node;
+  } else {
+    if (t.sp == 0) return;  // finished
+    const int2 e = stack[t.sp - 1];
+    const unsigned gm = (unsigned)e.y;
+    const unsigned rest = gm & (gm - 1u);
+    if (rest)
+      stack[t.sp - 1].y = (int)rest;
+    else
+      --t.sp;
+    const int code = __ldg(reinterpret_cast<const int*>(s.wnodes + kWideF4 * (int64_t)e.x + 6 * (kWide / 4)) +
+                           (__ffs(gm) - 1));
+    if (code < 0) {  // a leaf of the group
+      trav_park(t, ~code);
+      return;
+    }
+    cur = code;
+  }
+  float tt[kWide];
+  int cc[kWide];
+  wnode_test(s.wnodes, cur, t.o, t.inv, t.oct, t.tmin, t.h.t, tt, cc);
+  if (COUNT) cnt->nodes += 1;
+  unsigned m = 0, leaves = 0;
+  float tn = INFINITY;
+  int kn = -1;
+#pragma unroll
+  for (int k = 0; k < kWide; ++k) {
+    const bool hit = tt[k] < INFINITY;
+    m |= (hit ? 1u : 0u) << k;
+    leaves |= (hit && cc[k] < 0 ? 1u : 0u) << k;
+    if (hit && cc[k] >= 0 && tt[k] < tn) {
+      tn = tt[k];
+      kn = k;
+    }
+  }
+  // park leaves while there is room
+  while (leaves && t.np < PARK) {
+    const int k = __ffs(leaves) - 1;
+    int code = 0;
+#pragma unroll
+    for (int j = 0; j < kWide; ++j)
+      if (j == k) code = cc[j];
+    trav_park(t, ~code);
+    leaves &= leaves - 1u;
+    m &= ~(1u << k);
+  }
+  int next = -1;
+  if (kn >= 0) {
+#pragma unroll
+    for (int j = 0; j < kWide; ++j)
+      if (j == kn) next = cc[j];
+    m &= ~(1u << kn);
+  }
+  if (m) {
+    if (t.sp >= kStack) {
+      atomicOr(err, TRACE_ERR_STACK);
+      t.node = -1;
+      t.sp = 0;
+      return;
+    }
+    stack[t.sp++] = make_int2(cur, (int)m);
+  }
+  t.node = next;
 }
 
 // Tests the parked leaves, in the order they were parked.  Returns true if

@@ -114,6 +114,7 @@ struct BatchRays {
 constexpr int kStragglers = 4;        // lanes a warp does not wait for before its leaf phase
 constexpr int kParkAnyHit = 2;        // leaves a lane parks before the leaf phase: shadow rays
 constexpr int kParkClosest = 2;       // ... extension rays
+constexpr bool kAnyHitNearest = false;  // shadow rays walk the first inner child hit next (true: the nearest)
 constexpr int kMaxRounds = 1 << 22;   // per-warp round cap (~6k rounds per warp at 512x512)
 
 // COUNT: accumulate BVH nodes visited / primitives tested (and rays) into
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
       if (parked != 0 && __popc(needm) <= kStragglers) break;
       if (need) {
         if (ANY_HIT)
-          trav_inner_step_any<COUNT, kParkAnyHit>(*sp, t, stack, err, &tc);
+          trav_inner_step_any<COUNT, kParkAnyHit, kAnyHitNearest>(*sp, t, stack, err, &tc);
         else
           trav_inner_step<COUNT>(*sp, t, stack, err, &tc);
       }

@@ -187,13 +187,15 @@ struct TraceCount {
   uint32_t nodes, prims;
 };
 
-// Slab test of the kWide children of wide node ni: entry distance per child
-// (INFINITY: missed or empty slot) and the child codes.  oct bit a is set
-// when the ray's direction is negative along axis a: the near plane of every
-// box is then its upper bound, so each slab needs one plane per side and no
-// min/max pairs (the near and far bound arrays are picked by address).
-HM_D void wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, int oct, float tmin, float tmax,
-                     float (&t)[kWide], int (&c)[kWide]) {
+// Slab test of the kWide children of wide node ni: returns the mask of the
+// children hit; t = entry distance per child (meaningful where hit), c =
+// the child codes.  oct bit a is set when the ray's direction is negative
+// along axis a: the near plane of every box is then its upper bound, so
+// each slab needs one plane per side and no min/max pairs (the near and far
+// bound arrays are picked by address).  Empty slots hold a box every ray
+// misses; a NaN distance misses too.
+HM_D unsigned wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, int oct, float tmin, float tmax,
+                         float (&t)[kWide], int (&c)[kWide]) {
   constexpr int G = kWide / 4;  // float4 per bound array
   const float4* p = wn + kWideF4 * (int64_t)ni;
   const int sx = oct & 1, sy = (oct >> 1) & 1, sz = (oct >> 2) & 1;
@@ -204,6 +206,7 @@ HM_D void wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, int o
   const float4* nzp = p + (4 + sz) * G;
   const float4* fzp = p + (5 - sz) * G;
   const float nx = -o.x * inv.x, ny = -o.y * inv.y, nz = -o.z * inv.z;
+  unsigned m = 0;
 #pragma unroll
   for (int q = 0; q < G; ++q) {
     const float4 a0 = __ldg(nxp + q), a1 = __ldg(fxp + q), b0 = __ldg(nyp + q), b1 = __ldg(fyp + q),
@@ -219,10 +222,12 @@ HM_D void wnode_test(const float4* wn, int ni, const f3& o, const f3& inv, int o
                              fmaxf(fmaf(n_z[k], inv.z, nz), tmin));
       const float tf = fminf(fminf(fmaf(f_x[k], inv.x, nx), fmaf(f_y[k], inv.y, ny)),
                              fminf(fmaf(f_z[k], inv.z, nz), tmax));
-      t[4 * q + k] = tn <= tf ? tn : INFINITY;
+      t[4 * q + k] = tn;
+      m |= (tn <= tf ? 1u : 0u) << (4 * q + k);
       c[4 * q + k] = cc[k];
     }
   }
+  return m;
 }
 
 // Resumable traversal of the wide tree: one node visit per inner step, so
@@ -307,11 +312,8 @@ HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err
   }
   float tt[kWide];
   int cc[kWide];
-  wnode_test(s.wnodes, cur, t.o, t.inv, t.oct, t.tmin, t.h.t, tt, cc);
+  unsigned m = wnode_test(s.wnodes, cur, t.o, t.inv, t.oct, t.tmin, t.h.t, tt, cc);
   if (COUNT) cnt->nodes += 1;
-  unsigned m = 0;
-#pragma unroll
-  for (int k = 0; k < kWide; ++k) m |= (tt[k] < INFINITY ? 1u : 0u) << k;
   if (m == 0) {
     t.node = -1;
     return;
@@ -355,9 +357,11 @@ HM_D void trav_inner_step(const SceneDev& s, TravState& t, int2* stack, int* err
 // group (node, mask of the children still to visit), and a pop takes the
 // group's lowest child and reads its code from the node.  One push per
 // visit instead of one per child, and no sorting.  Leaves hit are parked at
-// once while the lane has room (PARK); the nearest inner child is walked
-// next (occluders near the ray's origin are the likeliest).
-template <bool COUNT, int PARK>
+// once while the lane has room (PARK); the nearest inner child (NEAREST) or
+// the first in the node's order is walked next.  The node's order (the
+// LBVH's spatial order) measured better for shadow rays: 7% less time per
+// launch, 2% fewer node visits and 5% fewer curve tests per ray.
+template <bool COUNT, int PARK, bool NEAREST>
 HM_D void trav_inner_step_any(const SceneDev& s, TravState& t, int2* stack, int* err, TraceCount* cnt) {
   if (++t.visits > kMaxVisits) {
     atomicOr(err, TRACE_ERR_STEPS);
@@ -387,20 +391,23 @@ HM_D void trav_inner_step_any(const SceneDev& s, TravState& t, int2* stack, int*
   }
   float tt[kWide];
   int cc[kWide];
-  wnode_test(s.wnodes, cur, t.o, t.inv, t.oct, t.tmin, t.h.t, tt, cc);
+  unsigned m = wnode_test(s.wnodes, cur, t.o, t.inv, t.oct, t.tmin, t.h.t, tt, cc);
   if (COUNT) cnt->nodes += 1;
-  unsigned m = 0, leaves = 0;
-  float tn = INFINITY;
-  int kn = -1;
+  unsigned leafc = 0;
 #pragma unroll
-  for (int k = 0; k < kWide; ++k) {
-    const bool hit = tt[k] < INFINITY;
-    m |= (hit ? 1u : 0u) << k;
-    leaves |= (hit && cc[k] < 0 ? 1u : 0u) << k;
-    if (hit && cc[k] >= 0 && tt[k] < tn) {
-      tn = tt[k];
-      kn = k;
-    }
+  for (int k = 0; k < kWide; ++k) leafc |= (cc[k] < 0 ? 1u : 0u) << k;
+  unsigned leaves = m & leafc;
+  int kn = -1;
+  if (NEAREST) {
+    float tn = INFINITY;
+#pragma unroll
+    for (int k = 0; k < kWide; ++k)
+      if (((m & ~leafc) >> k) & 1u && tt[k] < tn) {
+        tn = tt[k];
+        kn = k;
+      }
+  } else {
+    kn = __ffs(m & ~leafc) - 1;
   }
   // park leaves while there is room
   while (leaves && t.np < PARK) {

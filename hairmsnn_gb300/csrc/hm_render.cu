@@ -111,7 +111,7 @@ struct BatchRays {
   HM_D void write(int i, const Hit& h) const { out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v); }
 };
 
-constexpr int kStragglers = 4;        // lanes a warp does not wait for before its leaf phase
+constexpr int kStragglers = 12;       // lanes a warp does not wait for before its leaf phase
 constexpr int kParkAnyHit = 2;        // leaves a lane parks before the leaf phase: shadow rays
 constexpr int kParkClosest = 2;       // ... extension rays
 constexpr bool kAnyHitNearest = false;  // shadow rays walk the first inner child hit next (true: the nearest)

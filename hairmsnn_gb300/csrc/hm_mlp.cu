@@ -807,7 +807,8 @@ extern "C" hm_mlp* hm_mlp_create(const char* config_json, int in_ch, int out_ch,
       if (st != HM_OK) e = cudaErrorMemoryAllocation;
     }
     m->tc_train = tc_trainable(m->cfg.d, precision);
-    m->loss_scale = precision == HM_PREC_FP16 ? 128.f : 1.f;
+    // FP16 operands in the backward pass (FP16 handles; E4M3 handles' backward)
+    m->loss_scale = precision == HM_PREC_FP16 || precision == HM_PREC_FP8_E4M3 ? 128.f : 1.f;
   }
   if (e != cudaSuccess) {
     *status = hm_cuda_status(e, "hm_mlp_create");

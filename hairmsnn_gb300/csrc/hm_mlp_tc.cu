@@ -183,9 +183,13 @@ struct RowPacker {
   int row;
   float scale;
   uint8_t* mirror = nullptr;  // training: the row's operand bytes also go here
+  // training with E4M3 operands: the row's features, unscaled, as FP16 (the
+  // backward pass runs on FP16 operands)
+  uint16_t* mirror16 = nullptr;
   HM_D RowPacker(uint8_t* a, int r, int first_group, float sc) : group(first_group), A(a), row(r), scale(sc) {}
   HM_D void push(float v) {
     constexpr int SH = PREC == TC_E4M3 ? 8 : 16;
+    if (PREC == TC_E4M3 && mirror16) mirror16[group * kPer + cnt] = __half_as_ushort(__float2half_rn(v));
     uint32_t h;
     if (PREC == TC_E4M3)
       h = (uint32_t)__nv_cvt_float_to_fp8(v * scale, __NV_SATFINITE, __NV_E4M3);
@@ -563,7 +567,12 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
         const int G = kn / CK, gsplit = (G + 1) >> 1;
         const int g0 = half ? gsplit : 0, g1 = half ? G : gsplit;
         RowPacker<PREC> pk(A, row, g0, row_scale);
-        if (STORE && valid) pk.mirror = reinterpret_cast<uint8_t*>(p.x16 + q * K0 + kc);
+        if (STORE && valid) {
+          if (F8)
+            pk.mirror16 = p.x16 + q * K0 + kc;
+          else
+            pk.mirror = reinterpret_cast<uint8_t*>(p.x16 + q * K0 + kc);
+        }
         if (valid) {
           enc_range<PREC>(d, xin, p.enc_params, kc + g0 * CK, kc + g1 * CK, pk);
         } else {
@@ -603,6 +612,16 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
                                   v[g * 16 + 4 * w4 + 3] * s);
           *reinterpret_cast<uint4*>(A + op_offset(kTcRows, row, half * HW + g * 16)) =
               make_uint4(word[0], word[1], word[2], word[3]);
+        }
+        if (STORE && valid) {  // the backward pass's FP16 copy of the activations
+#pragma unroll
+          for (int g = 0; g < HW / 8; ++g) {
+            uint32_t word[4];
+#pragma unroll
+            for (int w2 = 0; w2 < 4; ++w2) word[w2] = pack2<TC_FP16>(v[g * 8 + 2 * w2], v[g * 8 + 2 * w2 + 1]);
+            *reinterpret_cast<uint4*>(p.h16 + ((int64_t)(l - 1) * p.n + q) * W + half * HW + g * 8) =
+                make_uint4(word[0], word[1], word[2], word[3]);
+          }
         }
       } else {
 #pragma unroll
@@ -929,15 +948,20 @@ int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, cons
 }
 
 // =================================================================== training
+// E4M3 handles train with the E4M3 forward (the operands inference uses)
+// and the FP16 backward (dgrad chain and weight gradients on FP16 operands:
+// the activations and encoded inputs kept as FP16, W^T packed as FP16).
 bool tc_trainable(const MlpDims& d, int precision) {
-  return (precision == HM_PREC_FP16 || precision == HM_PREC_BF16) && d.width >= 16;
+  return ((precision == HM_PREC_FP16 || precision == HM_PREC_BF16) && d.width >= 16) ||
+         (precision == HM_PREC_FP8_E4M3 && d.width >= 32);
 }
 
 int tc_train_alloc(const MlpDims& d, int64_t cap, bool need_dx, TcTrainBufs* b) {
   tc_train_free(b);
   const int L = d.n_hidden;
   const int wz = std::max(d.width, 16);
-  cudaError_t e = cudaMalloc(&b->x16, (size_t)cap * d.in_pad * 2);
+  // encoded inputs at the widest layer-0 pitch (E4M3 pads K to 32)
+  cudaError_t e = cudaMalloc(&b->x16, (size_t)cap * round_up(d.in_pad, 32) * 2);
   if (e == cudaSuccess) e = cudaMalloc(&b->h16, (size_t)L * cap * d.width * 2);
   if (e == cudaSuccess) e = cudaMalloc(&b->dz16, (size_t)(L + 1) * cap * wz * 2);
   if (e == cudaSuccess) e = cudaMalloc(&b->pred, (size_t)cap * 16 * sizeof(float));
@@ -971,6 +995,9 @@ int tc_train_forward(const MlpDims& d, const TcPack& pk, const float* enc_params
   a.h16 = b.h16;
   a.pred = b.pred;
   const int W = d.width;
+  if (pk.precision == HM_PREC_FP8_E4M3)
+    return W == 32 ? tc_launch<TC_E4M3, 32, true>(a, smem, st) : W == 64 ? tc_launch<TC_E4M3, 64, true>(a, smem, st)
+           : tc_launch<TC_E4M3, 128, true>(a, smem, st);
   if (pk.precision == HM_PREC_BF16)
     return W == 16 ? tc_launch<TC_BF16, 16, true>(a, smem, st) : W == 32 ? tc_launch<TC_BF16, 32, true>(a, smem, st)
            : W == 64 ? tc_launch<TC_BF16, 64, true>(a, smem, st) : tc_launch<TC_BF16, 128, true>(a, smem, st);
@@ -1270,6 +1297,20 @@ __global__ void tc_reduce_kernel(const float* __restrict__ part, int splits, int
   }
 }
 
+// The same for a layer whose K is padded past its fan-in (E4M3 layer 0):
+// partial rows are K wide, the parameter rows fan_in wide.
+__global__ void tc_reduce_pad_kernel(const float* __restrict__ part, int splits, int N, int K, int fan_in,
+                                     float* __restrict__ out) {
+  const int64_t mn = (int64_t)N * K;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (int64_t)N * fan_in;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t src = (i / fan_in) * K + i % fan_in;
+    float s = 0.f;
+    for (int k = 0; k < splits; ++k) s += part[(int64_t)k * mn + src];
+    out[i] = s;
+  }
+}
+
 __global__ void tc_loss_reduce_kernel(const float* __restrict__ part, int nb, float* __restrict__ out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     float s = 0.f;
@@ -1386,7 +1427,8 @@ int tc_backward(const MlpDims& d, const TcPack& pk, const TcTrainBufs& b, const 
       tc_reduce_kernel<<<256, 256, 0, st>>>(*dw_part, splits, mn, grads + d.layer_off[l]);
       HM_CHECK_LAUNCH("tc_reduce_kernel");
     } else {
-      return hm_set_error("mlp: padded K in training"), HM_EUNSUPPORTED;
+      tc_reduce_pad_kernel<<<256, 256, 0, st>>>(*dw_part, splits, pk.N[l], pk.K[l], fan_in, grads + d.layer_off[l]);
+      HM_CHECK_LAUNCH("tc_reduce_pad_kernel");
     }
   }
   return HM_OK;

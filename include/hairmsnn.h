@@ -108,10 +108,14 @@ int hm_bsdf_gen_queries(uint32_t seed, int64_t n, float* wo, float* wi, float* t
  *   in_ch/out_ch input / output channels (the reference uses 12 / 3,
  *                headers/render_hair_msnn.h:145)
  *   precision    HM_PREC_*; seed: parameter initialisation stream.
- *                FP16 / BF16 / FP8_E4M3 run inference on the tensor cores
- *                (operands rounded to that type, FP32 accumulation; E4M3
- *                with per-layer weight scales and per-query activation
- *                scales); parameters, gradients and training stay FP32.
+ *                FP16 / BF16 / FP8_E4M3 run inference and training on the
+ *                tensor cores (operands rounded to that type, FP32
+ *                accumulation; E4M3 with per-layer weight scales and
+ *                per-query activation scales, its training backward on
+ *                FP16 operands); FP16 and E4M3 training use a static loss
+ *                scale of 128, divided out before the optimizer and by
+ *                hm_mlp_get_gradients.  Parameters and optimizer state
+ *                stay FP32.
  * Device buffers are row-major per query: in [n][in_ch], out [n][out_ch]
  * (tiny-cuda-nn's column-major GPUMatrix(ptr, ch, n)).  Any n >= 0 is
  * accepted (the reference needs n % 128 == 0, scene.cpp:300-306).  The

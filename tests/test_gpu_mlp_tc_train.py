@@ -1,17 +1,22 @@
-"""Cache training on the tensor cores (FP16 / BF16 operands, FP32 accumulation).
+"""Cache training on the tensor cores (FP32 accumulation).
 
 FP16 / BF16 handles run the training forward, the dgrad chain and the weight
 gradients on tcgen05 (FP16 with a static loss scale of 128, divided out by
-the optimizer and by hm_mlp_get_gradients).  Against the FP64 oracle on the
-same parameters and batch (rms of the error / rms of the reference, per
-weight matrix and for the hash tables):
-    loss         FP16 2e-3, BF16 1e-2 (relative)
-    gradients    FP16 2.5e-2, BF16 1e-1
+the optimizer and by hm_mlp_get_gradients).  E4M3 handles run the training
+forward on E4M3 operands (per-layer weight scales, per-row activation
+scales: the inference kernel's arithmetic) and the backward on FP16 operands
+with the same loss scale.  Against the FP64 oracle on the same parameters
+and batch (rms of the error / rms of the reference, per weight matrix and
+for the hash tables):
+    loss         FP16 2e-3, BF16 1e-2, E4M3 5e-2 (relative)
+    gradients    FP16 2.5e-2, BF16 1e-1, E4M3 3e-1
 (the errors scale with the operand precision: BF16 has 3 fewer mantissa
-bits than FP16 and its errors are about 4-8x larger; the first layer and the
-hash tables sit at the end of the dgrad chain and carry the most)
-and 60 training steps reduce the loss as the FP32 kernels do (final loss
-within 1.5x of FP32's).
+bits than FP16 and its errors are about 4-8x larger; E4M3 rounds every
+forward operand to 3 mantissa bits (measured: loss 0.6-2.8%, gradients
+3-19%, hash tables 23%); the first layer and the hash tables sit at the end
+of the dgrad chain and carry the most) and 60 training steps reduce the
+loss as the FP32 kernels do (final loss within 1.5x of FP32's; E4M3
+measured 1.09x).
 """
 import numpy as np
 import pytest
@@ -21,7 +26,7 @@ from oracle import mlp_oracle as mo
 torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp16": (2e-3, 2.5e-2), "bf16": (1e-2, 1e-1)}
+TOL = {"fp16": (2e-3, 2.5e-2), "bf16": (1e-2, 1e-1), "fp8": (5e-2, 3e-1)}
 
 
 @pytest.fixture(scope="module")
@@ -60,7 +65,7 @@ def rel_rms(a, b):
     return np.sqrt(np.mean((a - b) ** 2)) / max(np.sqrt(np.mean(b ** 2)), 1e-30)
 
 
-@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+@pytest.mark.parametrize("prec", ["fp16", "bf16", "fp8"])
 @pytest.mark.parametrize("cfg,in_ch,gen", CASES)
 def test_tensor_core_gradients_match_oracle(mlpmod, cfg, in_ch, gen, prec):
     net = mlpmod.TinyMLP(cfg, in_ch, 3, precision=prec, seed=11)
@@ -88,7 +93,7 @@ def test_tensor_core_gradients_match_oracle(mlpmod, cfg, in_ch, gen, prec):
         assert e <= tg, ("grid", e)
 
 
-@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+@pytest.mark.parametrize("prec", ["fp16", "bf16", "fp8"])
 def test_tensor_core_training_converges(mlpmod, prec):
     x = c1_inputs(1 << 14, seed=4)
     tgt = (np.abs(np.sin(3 * x[:, 0:3])) + 0.1).astype(np.float32)
@@ -105,12 +110,12 @@ def test_tensor_core_training_converges(mlpmod, prec):
     assert finals[prec] <= 1.5 * finals["fp32"], finals
 
 
-@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16", "fp8"])
 @pytest.mark.parametrize("cfg,in_ch,gen", CASES[:2])
 def test_output_grad_backward_matches_oracle(mlpmod, cfg, in_ch, gen, prec):
     """hm_mlp_backward_output_grad (tcnn's backward with dL_doutput) against
-    the FP64 oracle: FP32 within 1e-4, FP16 within 4e-2 and BF16 within
-    1.5e-1 (1.5x the loss-gradient bars: a random dL/d(output) is
+    the FP64 oracle: FP32 within 1e-4, FP16 within 4e-2, BF16 within
+    1.5e-1 and E4M3 within 4.5e-1 (1.5x the loss-gradient bars: a random dL/d(output) is
     uncorrelated with the outputs, so each weight's gradient is a sum with
     more cancellation and its relative error is larger; layer 0 measured
     2.7e-2 in FP16)."""

@@ -206,6 +206,8 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
 template <class Src, bool ANY_HIT>
 static int launch_persistent(const Src& src, const SceneDev& s, const Batch& b, float tmin, float tmax, int* fetch,
                              int* err, unsigned long long* cnt, bool counting, int max_blocks, cudaStream_t st) {
+  // the traversal reads nodes with 32-byte loads (batch scenes: checked when the batch is built)
+  if (((uintptr_t)s.wnodes & 31) != 0) return hm_set_error("traversal: wide nodes not 32-byte aligned"), HM_EINVAL;
   if (b.scenes) {
     if (counting)
       persistent_trace_kernel<Src, ANY_HIT, true, true><<<max_blocks, 128, 0, st>>>(src, s, b, tmin, tmax, fetch,
@@ -712,6 +714,8 @@ static int render_setup(Render* r, const hm_render_options* o) {
       Scene* b = r->bscenes[k];
       BatchScene bs{};
       bs.s = b->dev();
+      if (((uintptr_t)bs.s.wnodes & 31) != 0)  // the traversal's 32-byte node loads
+        return hm_set_error("batch scene %d: wide nodes not 32-byte aligned", (int)k), HM_EINVAL;
       bs.pix_off = pix;
       bs.n_pix = b->width * b->height;
       bs.every_nth = r->every_nth;

@@ -111,7 +111,8 @@ struct BatchRays {
   HM_D void write(int i, const Hit& h) const { out[i] = make_float4(h.t, __int_as_float(h.prim), h.u, h.v); }
 };
 
-constexpr int kStragglers = 12;       // lanes a warp does not wait for before its leaf phase
+constexpr int kStragglersAnyHit = 12;   // lanes a warp does not wait for before its leaf phase: shadow rays
+constexpr int kStragglersClosest = 12;  // ... extension rays
 constexpr int kParkAnyHit = 2;        // leaves a lane parks before the leaf phase: shadow rays
 constexpr int kParkClosest = 2;       // ... extension rays
 constexpr bool kAnyHitNearest = false;  // shadow rays walk the first inner child hit next (true: the nearest)
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
       break;
     }
     // box phase: walk inner nodes until every lane has parked two leaves or
-    // finished; once some lane has a leaf parked, up to kStragglers lanes
+    // finished; once some lane has a leaf parked, up to kStragglers* lanes
     // that still need steps are not waited for (they continue next round).
     // Every iteration advances at least one lane, so the phase terminates.
     for (int guard = 0; guard < kMaxVisits; ++guard) {
@@ -179,7 +180,7 @@ __global__ void __launch_bounds__(128) persistent_trace_kernel(Src src, const __
       const unsigned needm = __ballot_sync(FULL, need);
       if (needm == 0) break;
       const unsigned parked = __ballot_sync(FULL, cur >= 0 && t.np > 0);
-      if (parked != 0 && __popc(needm) <= kStragglers) break;
+      if (parked != 0 && __popc(needm) <= (ANY_HIT ? kStragglersAnyHit : kStragglersClosest)) break;
       if (need) {
         if (ANY_HIT)
           trav_inner_step_any<COUNT, kParkAnyHit, kAnyHitNearest>(*sp, t, stack, err, &tc);

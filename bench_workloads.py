@@ -464,6 +464,9 @@ class RenderBenchWorkload:
                 order.append(np.nonzero(kind[:, 3 * k + kd] == kd)[0] * log.shape[1] + 3 * k + kd)
         idx = np.concatenate(order)
         flat = log.reshape(-1, 12)[idx]
+        # the frame's extension rays (vertex by vertex, pixel order) for the closest-hit launch
+        eidx = np.concatenate([np.nonzero(kind[:, 3 * k] == 0)[0] * log.shape[1] + 3 * k for k in range(vertices)])
+        eflat = log.reshape(-1, 12)[eidx]
         del log
         vis = flat[:, 0].view(np.int32)
         org = torch.from_numpy(np.ascontiguousarray(flat[:, 8:11])).cuda()
@@ -482,6 +485,26 @@ class RenderBenchWorkload:
         ms = statistics.median(a.elapsed_time(b) for a, b in ev)
         alg = n * RAY_RECORD_BYTES + c.shadow_nodes * NODE_BYTES + c.shadow_prims * PRIM_BYTES
         ach = alg / (ms * 1e-3) / 1e9
+        # the other traversal kernel, the same way: the frame's extension rays in one closest-hit launch
+        eorg = torch.from_numpy(np.ascontiguousarray(eflat[:, 8:11])).cuda()
+        edir = torch.from_numpy(np.ascontiguousarray(eflat[:, 4:7])).cuda()
+        ehits = self.scene.trace(eorg, edir, any_hit=False)
+        esame = float((ehits[:, 1].cpu().numpy().view(np.int32) == eflat[:, 0].view(np.int32)).mean())
+        for k, (a, b) in enumerate(ev):
+            flush.fill_(k & 0xFF)
+            a.record()
+            self.scene.trace(eorg, edir, any_hit=False)
+            b.record()
+        torch.cuda.synchronize()
+        ems = statistics.median(a.elapsed_time(b) for a, b in ev)
+        ealg = len(eflat) * RAY_RECORD_BYTES + c.extend_nodes * NODE_BYTES + c.extend_prims * PRIM_BYTES
+        extension = {"kernel": "persistent_trace_kernel<closest hit> (extension rays of the same frame, one launch)",
+                     "launch_ms": round(ems, 4), "rays": len(eflat), "algorithmic_bytes": int(ealg),
+                     "achieved": round(ealg / (ems * 1e-3) / 1e9, 2),
+                     "frac": round(ealg / (ems * 1e-3) / 1e9 / pk["hbm_gbs"], 4),
+                     "hit_primitive_equal_to_frame": round(esame, 6),
+                     "per_ray": {"nodes": round(c.extend_nodes / max(1, c.extension_rays), 2),
+                                 "prims": round(c.extend_prims / max(1, c.extension_rays), 2)}}
         return {"kernel": "persistent_trace_kernel<any hit> (shadow rays of one frame, one launch)",
                 "bound": "hbm", "achieved": round(ach, 2), "peak": pk["hbm_gbs"], "unit": "GB/s",
                 "frac": round(ach / pk["hbm_gbs"], 4),
@@ -494,6 +517,7 @@ class RenderBenchWorkload:
                 "per_ray": {"nodes": round(c.shadow_nodes / max(1, c.shadow_rays), 2),
                             "prims": round(c.shadow_prims / max(1, c.shadow_rays), 2)},
                 "binding_counters": SHADOW_NCU_COUNTERS,
+                "extension_launch": extension,
                 "note": ("algorithmic bytes as in the frame's counted shadow stage; the 90 MB BVH and 10 MB of "
                          "curves are mostly L2-resident, so the DRAM traffic is far below them; the bound is "
                          "instruction issue with few lanes active (binding_counters); peak = HBM copy ("

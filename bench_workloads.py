@@ -285,20 +285,15 @@ class PrecisionWorkload:
 RAY_RECORD_BYTES = 32 + 16   # ray (origin, direction as float4 pairs) + hit record
 NODE_BYTES = 224              # one 8-wide BVH node: eight child boxes + child codes
 PRIM_BYTES = 64               # one segment's 4 control points (or a triangle's vertex data)
-# DRAM bytes per extension ray of the extension traversal kernel (8-wide
-# BVH), from ncu (dram__bytes_read.sum + dram__bytes_write.sum) of the first
-# launch of a 256x256 frame of this scene: 42.1 MB for its 65,536 camera
-# rays.  ncu runs each launch with cold caches, so this is an upper bound
-# for warm frames.
-EXTEND_DRAM_BYTES_PER_RAY = 643
 # DRAM bytes per ray of the shadow-ray traversal launch timed by
 # RenderBenchWorkload.shadow_launch (one launch over a 512x512 frame's shadow
 # rays), and the counters that bind it, from one ncu capture of that launch
 # (profiles/shadow_trace_launch_512.md).
-SHADOW_DRAM_BYTES_PER_RAY = 333  # 189.4 MB for 568,386 rays
-SHADOW_NCU_COUNTERS = {"lanes_active_per_instruction": 9.02, "issue_active_pct": 55.8,
-                       "alu_pipe_active_pct": 63.8, "warps_active_pct": 33.8, "l2_hit_rate_pct": 84.6,
-                       "dram_throughput_pct": 2.3,
+SHADOW_DRAM_BYTES_PER_RAY = 340  # 193.0 MB for 568,386 rays
+SHADOW_NCU_COUNTERS = {"lanes_active_per_instruction": 12.9, "issue_active_pct": 46.4,
+                       "alu_pipe_active_pct": 42.3, "l1tex_throughput_pct": 63.2, "warps_active_pct": 33.5,
+                       "long_scoreboard_stalls_per_issue": 6.39, "l2_hit_rate_pct": 87.3,
+                       "dram_throughput_pct": 3.3,
                        "source": "profiles/shadow_trace_launch_512.md (ncu --set full, cold caches)"}
 
 
@@ -519,8 +514,9 @@ class RenderBenchWorkload:
                 "binding_counters": SHADOW_NCU_COUNTERS,
                 "extension_launch": extension,
                 "note": ("algorithmic bytes as in the frame's counted shadow stage; the 90 MB BVH and 10 MB of "
-                         "curves are mostly L2-resident, so the DRAM traffic is far below them; the bound is "
-                         "instruction issue with few lanes active (binding_counters); peak = HBM copy ("
+                         "curves are mostly L2-resident, so the DRAM traffic is far below them; the bound is the "
+                         "latency of the node loads with a third of the warp slots occupied and the L1 the busiest "
+                         "unit (binding_counters); peak = HBM copy ("
                          + pk["source"] + ")")}
 
     def roofline(self, seg_ms, pk):

@@ -635,8 +635,9 @@ class RenderBenchWorkload:
         with its kernels' rooflines, the cache precision sweep at 2^20
         queries (time, TFLOP/s, training step, error against the FP64
         oracle), the equal-accuracy comparison of the chosen and plain forms
-        (relMSE at 16 spp against a converged PT image), and the ablation of
-        the chosen form."""
+        (relMSE at 16 spp against a converged PT image), the ablation of the
+        chosen form, the 64-scene batch and the differentiable fit's
+        gradient evaluation."""
         torch = self.torch
         out = {}
         vw = VertexWorkload(torch)
@@ -666,6 +667,51 @@ class RenderBenchWorkload:
                                                   / q["msnn_by_cache_precision"]["fp32"]["relmse"], 4),
             "speedup": round(plain / self.last_ms, 3) if getattr(self, "last_ms", None) else None}
         out["ablation"] = self.ablation()
+        out["batch_64_scenes"] = self.batch_extra()
+        out["diff_gradient"] = self.diff_extra()
+        return out
+
+    def batch_extra(self, warmup=2, frames=5):
+        """The 64-scene batch (BatchBenchWorkload): pipelined frames timed with
+        CUDA events, then the same through the public API with the image
+        sums read back every frame."""
+        torch = self.torch
+        import time
+        t0 = time.perf_counter()
+        bw = BatchBenchWorkload(torch)
+        for _ in range(warmup):
+            bw.step()
+        bw.r.wait()
+        ms = bw.timed_region(frames, None)
+        e2e_ms = bw.e2e_region(max(2, frames // 2))
+        out = {"metric": bw.metric, "paths_per_s": round(bw.P / (ms * 1e-3), 1), "ms_per_frame": round(ms, 3),
+               "e2e_paths_per_s": round(bw.P / (e2e_ms * 1e-3), 1), "frames": frames, **bw.stats_scenes,
+               "launch_shapes": {k: v for k, v in bw.tuning.items() if k != "ms_per_frame"},
+               "scene_setup_s": round(bw.setup_s, 1), "total_s": round(time.perf_counter() - t0, 1)}
+        bw.r.close()
+        del bw
+        torch.cuda.synchronize()
+        return out
+
+    def diff_extra(self, warmup=1, steps=3):
+        """The differentiable-fit workload (DiffBenchWorkload): gradient
+        evaluations timed with CUDA events (no Adam fit here)."""
+        torch = self.torch
+        import time
+        t0 = time.perf_counter()
+        dw = DiffBenchWorkload(torch)
+        for _ in range(warmup):
+            dw.step()
+        ms = dw.timed_region(steps, None)
+        e2e_ms = dw.e2e_region(2)
+        g = dw.last_grad
+        out = {"metric": dw.metric, "evaluations_per_s": round(1e3 / ms, 4), "ms_per_evaluation": round(ms, 2),
+               "e2e_evaluations_per_s": round(1e3 / e2e_ms, 4),
+               "paths_per_s": round(dw.paths_per_step() / (ms * 1e-3), 1), "steps": steps,
+               "gradient_finite": bool(np.isfinite(g).all()), "total_s": round(time.perf_counter() - t0, 1)}
+        dw.r.close()
+        del dw
+        torch.cuda.synchronize()
         return out
 
     def ablation(self):

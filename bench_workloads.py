@@ -318,7 +318,7 @@ class RenderBenchWorkload:
         self.scene.build()
         self.r = Renderer(self.scene, MSNN, beta=1, train_records=train_records, train=True,
                           precision=self.cache_precision, frames_in_flight=frames_in_flight)
-        self.tuning = self.r.autotune(frames=6)
+        self.tuning = self.r.autotune(frames=16)  # 6 frames per candidate picked less stable shapes (4% slower)
         self.P = width * height
         self.h2d_bytes = 0
         self.d2h_bytes = self.P * 3 * 8
@@ -732,7 +732,7 @@ class RenderBenchWorkload:
                          precision=v.get("precision", self.cache_precision),
                          frames_in_flight=v.get("fif", self.frames_in_flight))
             if v.get("tune", True):
-                r.autotune(frames=6)
+                r.autotune(frames=16)
             r.set_graphs(v.get("graphs", True))
             ms = self._frame_ms(r)
             out[name] = {"ms_per_frame": round(ms, 3), "paths_per_s": round(self.P / (ms * 1e-3), 1)}

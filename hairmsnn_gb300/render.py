@@ -245,7 +245,7 @@ class Renderer:
         """Enqueue one frame (asynchronous; see hm_render_frame)."""
         check(lib().hm_render_frame(self._h, _stream(stream)))
 
-    def autotune(self, frames=4, stream=None):
+    def autotune(self, frames=16, stream=None):
         """Pick the fastest launch shapes (see hm_render_autotune); returns them."""
         t = hm_render_tuning()
         check(lib().hm_render_autotune(self._h, int(frames), _stream(stream), ctypes.byref(t)))

@@ -19,10 +19,14 @@ HairConsts hair_consts_from_params(const hm_hair_params& p) { return hair_consts
 
 HM_D float ldg(const float* p) { return __ldg(p); }
 
-// Three 256-thread blocks per SM (at most 85 registers; the eval needs 79
-// without spilling): 37.5% occupancy instead of 25% at 92 registers, for a
-// kernel that waits on its transcendentals rather than on memory.
-__global__ void __launch_bounds__(256, 3) bsdf_eval_kernel(HairConsts hc, const float* __restrict__ wo,
+// Six 256-thread blocks per SM (40 registers; the eval needs 79 without
+// spilling, and spills about 250 bytes to L1 at 40): the kernels wait on the
+// latency of their transcendentals and dependent chains (a third of the
+// issue slots used at three blocks per SM), so more warps beat the spills.
+// Measured at 2^24 queries: eval 1.16 / 1.06 / 1.06 / 1.03 / 1.06 ms and
+// sample 1.59 / 1.47 / 1.50 / 1.45 / 1.46 ms at 3 / 4 / 5 / 6 / 8 blocks per
+// SM, results bit for bit the same.
+__global__ void __launch_bounds__(256, 6) bsdf_eval_kernel(HairConsts hc, const float* __restrict__ wo,
                                                         const float* __restrict__ wi,
                                                         const float* __restrict__ t,
                                                         const float* __restrict__ h,
@@ -44,7 +48,7 @@ __global__ void __launch_bounds__(256, 3) bsdf_eval_kernel(HairConsts hc, const 
   }
 }
 
-__global__ void __launch_bounds__(256, 3) bsdf_sample_kernel(HairConsts hc, const float* __restrict__ wo,
+__global__ void __launch_bounds__(256, 6) bsdf_sample_kernel(HairConsts hc, const float* __restrict__ wo,
                                                           const float* __restrict__ t,
                                                           const float* __restrict__ h,
                                                           const float* __restrict__ u,

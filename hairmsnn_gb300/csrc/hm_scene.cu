@@ -154,7 +154,10 @@ static int load_hair_file(const std::string& path, Scene* s, f3* raw_lo, f3* raw
     memcpy(&v, thk + 4 * i, 4);
     return v;
   };
-  f3 lo = mk(1e30f, 1e30f, 1e30f), hi = mk(-1e30f, -1e30f, -1e30f);
+  // extractHairData's bounds start from HairModel's defaults, (0, 0, 0)
+  // (model.h): the origin is always inside them, and with it in the scene
+  // scale (hairModel.scale, render_hair_msnn.cu:357)
+  f3 lo = mk(0.f, 0.f, 0.f), hi = mk(0.f, 0.f, 0.f);
   uint32_t strand = 0;
   int left = -1;
   s->cp.clear();
@@ -477,17 +480,25 @@ int scene_from_json(const char* text, const char* base_dir, Scene* s) {
     s->cos_fovy = (float)cam["cos_fovy"].as_number();
     // ---- hair BSDF (defaults of scene.cpp:186-231)
     s->hair.sigma_a[0] = 0.06f; s->hair.sigma_a[1] = 0.1f; s->hair.sigma_a[2] = 0.2f;
-    if (hair["sigma_a"].is_array()) {
-      f3 sa = f3_of(hair["sigma_a"], mk(0.06f, 0.1f, 0.2f));
-      s->hair.sigma_a[0] = sa.x; s->hair.sigma_a[1] = sa.y; s->hair.sigma_a[2] = sa.z;
+    s->hair.beta_m = 0.3f;
+    s->hair.beta_n = 0.3f;
+    s->hair.alpha = 0.03f;  // the Scene default (radians), kept when there is no hair.type
+    s->hair.gain_r = s->hair.gain_tt = s->hair.gain_trt = s->hair.gain_trrt = 1.f;
+    // parseScene reads the material only after hair.type (its first
+    // statement, scene.cpp:188): without it every field keeps the default
+    if (hair.has("type") && hair["type"].is_number()) {
+      if (hair["sigma_a"].is_array()) {
+        f3 sa = f3_of(hair["sigma_a"], mk(0.06f, 0.1f, 0.2f));
+        s->hair.sigma_a[0] = sa.x; s->hair.sigma_a[1] = sa.y; s->hair.sigma_a[2] = sa.z;
+      }
+      s->hair.beta_m = (float)hair.number_or("beta_m", 0.3);
+      s->hair.beta_n = (float)hair.number_or("beta_n", 0.3);
+      s->hair.alpha = hair.has("alpha") ? 3.14159f * (float)hair["alpha"].as_number() / 180.f : 0.f;
+      s->hair.gain_r = (float)hair.number_or("Gain R", 1.0);
+      s->hair.gain_tt = (float)hair.number_or("Gain TT", 1.0);
+      s->hair.gain_trt = (float)hair.number_or("Gain TRT", 1.0);
+      s->hair.gain_trrt = (float)hair.number_or("Gain TRRT", 1.0);
     }
-    s->hair.beta_m = (float)hair.number_or("beta_m", 0.3);
-    s->hair.beta_n = (float)hair.number_or("beta_n", 0.3);
-    s->hair.alpha = hair.has("alpha") ? 3.14159f * (float)hair["alpha"].as_number() / 180.f : 0.f;
-    s->hair.gain_r = (float)hair.number_or("Gain R", 1.0);
-    s->hair.gain_tt = (float)hair.number_or("Gain TT", 1.0);
-    s->hair.gain_trt = (float)hair.number_or("Gain TRT", 1.0);
-    s->hair.gain_trrt = (float)hair.number_or("Gain TRRT", 1.0);
     // ---- strand groups (no reference counterpart): per-group materials
     if (hair.has("groups")) {
       const Json& gj = hair["groups"];

@@ -3,9 +3,11 @@
 * build_oracle(): oracle/hm_oracle*.cpp -> oracle/_build/libhmoracle.so, the
   CPU restatement that tests/, smoke() and bench.py's CPU-baseline leg use as
   the checker.  Plain g++, -ffp-contract=off, no CUDA.
-* build_ref(): the reference's own header-only device math compiled unmodified
-  on the host through the OWL/OptiX stand-ins in oracle/ref_shim/, into
-  oracle/_ref/ (git-ignored).  It pins the oracle restatement and makes the
+* build_ref(): the reference's own code compiled unmodified on the host
+  through the stand-ins in oracle/ref_shim/ (OWL / OptiX names, cyHairFile,
+  nlohmann::json), into oracle/_ref/ (git-ignored): its header-only device
+  math, its integrators (hair_msnn.cu, path_tracing.cu, nrc.cu) and its
+  scene.cpp.  It pins the oracle restatement and makes the
   golden vectors under tests/golden/.  It needs the reference checkout
   (HM_REF_DIR, default /root/reference); where that is absent it is skipped
   and the committed golden vectors stand in for it.
@@ -55,6 +57,9 @@ TARGETS = [
     ("libhmref_path.so", "ref_path_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
     ("libhmref_pt.so", "ref_pt_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
     ("libhmref_nrc.so", "ref_nrc_entry.cpp", ["-D__CUDA_ARCH__=860"], True),
+    # scene.cpp (parseScene, extractHairData, generateEnvSamplingTables) with
+    # stand-ins for cyHairFile and nlohmann::json
+    ("libhmref_scene.so", "ref_scene_entry.cpp", [], False),
 ]
 
 
@@ -76,6 +81,7 @@ def build_ref(verbose: bool = False) -> list:
         out = os.path.join(OUT_DIR, lib)
         deps = [src_path, os.path.join(HERE, "ref_shim", "hm_owl_shim.h"),
                 os.path.join(HERE, "ref_shim", "ref_harness.h"), os.path.join(HERE, "ref_shim", "ref_eval_order.h"),
+                os.path.join(HERE, "ref_shim", "cyHairFile.h"), os.path.join(HERE, "ref_shim", "json", "json.hpp"),
                 os.path.join(HERE, "hm_oracle.h"), os.path.join(HERE, "hm_oracle.cpp")]
         if link_oracle:
             deps.append(oracle_lib)
@@ -87,6 +93,7 @@ def build_ref(verbose: bool = False) -> list:
                "-fno-fast-math", "-fno-strict-aliasing", "-w", *defs,
                "-I", os.path.join(HERE, "ref_shim"), "-I", HERE,
                "-I", os.path.join(REF_DIR, "cuda_headers"), "-I", os.path.join(REF_DIR, "cuda"),
+               "-I", os.path.join(REF_DIR, "headers"), "-I", REF_DIR,
                src_path, "-o", out, *link, "-Wl,-Bsymbolic", "-lpthread"]
         if verbose:
             print(" ".join(cmd))

@@ -589,7 +589,10 @@ def procedural_scene(cfg):
     pos, d00, du, dv = camera_vectors(c["from"], c["to"], c["up"], c["cos_fovy"], w, h)
     arrays["camera"] = np.concatenate([pos, d00, du, dv]).astype(np.float32)
     hair = cfg["hair"]
-    alpha = f(f(f(3.14159) * f(hair["alpha"])) / f(180.0)) if "alpha" in hair else f(0.0)
+    if isinstance(hair.get("type"), (int, float)) and not isinstance(hair.get("type"), bool):
+        alpha = f(f(f(3.14159) * f(hair["alpha"])) / f(180.0)) if "alpha" in hair else f(0.0)
+    else:  # parseScene reads the material only after hair.type (scene.cpp:188): the Scene defaults
+        hair, alpha = {}, f(0.03)
     mat = [*hair.get("sigma_a", [0.06, 0.1, 0.2]), hair.get("beta_m", 0.3), hair.get("beta_n", 0.3), alpha,
            hair.get("Gain R", 1.0), hair.get("Gain TT", 1.0), hair.get("Gain TRT", 1.0), hair.get("Gain TRRT", 1.0),
            *diffuse, alpha_raw, env_scale, env_rot]

@@ -58,6 +58,7 @@ struct vec2i {
   union { int x; int u; };
   union { int y; int v; };
   vec2i() : x(0), y(0) {}
+  vec2i(int s) : x(s), y(s) {}  // broadcast, as OWL's
   vec2i(int a, int b) : x(a), y(b) {}
 };
 struct vec3i {
@@ -140,6 +141,12 @@ inline uint32_t make_rgba(vec3f c) {
   auto q = [](float v) { int i = (int)(v * 255.9f); return (uint32_t)(i < 0 ? 0 : (i > 255 ? 255 : i)); };
   return q(c.x) | (q(c.y) << 8) | (q(c.z) << 16) | (0xffu << 24);
 }
+
+// axis-aligned box (OWL's box3f: lower / upper), for the reference's host
+// headers (Model::bounds)
+struct box3f {
+  vec3f lower = vec3f(1e30f), upper = vec3f(-1e30f);
+};
 
 // ----------------------------------------------------------- ray + traceRay
 template <int RAY_TYPE, int NUM_RAY_TYPES>

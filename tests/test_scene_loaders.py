@@ -3,7 +3,8 @@
 The control points, segment table and scene scale of a loaded HAIR file are
 compared with a restatement of Scene::extractHairData (scene.cpp:10-73):
 phantom points before and after each strand, one B-spline segment per
-original segment, radius 0.2 x thickness, bounds of the file's own points.
+original segment, radius 0.2 x thickness, bounds of the file's own points
+and the origin.
 """
 import json
 import struct
@@ -89,7 +90,8 @@ def test_hair_file_matches_extract_hair_data(tmp_path, with_segments, with_thick
     info = s.info()
     assert info.n_strands == len(segs)
     assert info.n_segments == sum(segs)
-    scale = np.float32(np.linalg.norm(pts.max(0) - pts.min(0)))
+    # extractHairData's bounds start at the origin (HairModel's defaults)
+    scale = np.float32(np.linalg.norm(np.maximum(pts.max(0), 0) - np.minimum(pts.min(0), 0)))
     assert abs(info.scene_scale - scale) <= 1e-6 * scale
 
 

@@ -335,6 +335,46 @@ def msnn_render(gbuf, nn_out, accum_id=0, acc=None):
     return out
 
 
+def nrc_render(rad, beta, hit, cache, train_px, unbiased, t_bounces, t_hit, records):
+    """The NRC RENDER pass (nrc.cu:365-380) and nrcGenerateTrainingData
+    (nrc.cu:70-133) in float32, operation by operation.  rad / beta [P, 3]:
+    the G-buffer's radiance and throughput, hit [P]; cache [P + T, 3]: the
+    cache outputs (pixels, then the T training suffixes); per training pixel
+    t: its pixel train_px[t], unbiased[t], its train buffer's bounces and hit
+    and records [T, 40, 15] (vert, wo, n, vertRadiance, vertBeta).  Returns
+    (color [P, 3] before accumulation, NaN as 0; train_in [T, 40, 9];
+    train_gt [T, 40, 3])."""
+    f = np.float32
+    rad, beta, cache = np.asarray(rad, f), np.asarray(beta, f), np.asarray(cache, f)
+    P = len(rad)
+    c = cache[:P].copy()
+    c[np.isnan(c).any(1)] = 0.0
+    color = (rad + (beta * np.maximum(c, f(0.0))).astype(f)).astype(f)
+    color[np.isnan(color).any(1)] = 0.0
+    T = len(train_px)
+    rec = np.asarray(records, f).reshape(T, 40, 15)
+    tin = np.zeros((T, 40, 9), f)
+    tgt = np.zeros((T, 40, 3), f)
+    hit_t = np.asarray(hit, bool)[np.asarray(train_px)]
+    bounces = np.where(hit_t, np.asarray(t_bounces), 0)
+    suffix = cache[P:P + T].copy()
+    use = hit_t & (np.asarray(t_hit) != 0) & ~np.asarray(unbiased, bool)
+    suffix[~use] = 0.0
+    for b in range(40):
+        on = bounces > b
+        col = np.zeros((T, 3), f)
+        bt = np.ones((T, 3), f)
+        for sub in range(b, 40):
+            m = on & (bounces > sub)
+            col = np.where(m[:, None], (col + (bt * rec[:, sub, 9:12]).astype(f)).astype(f), col)
+            bt = np.where(m[:, None], (bt * rec[:, sub, 12:15]).astype(f), bt)
+        t = (col + (bt * suffix).astype(f)).astype(f)
+        t[np.isnan(t).any(1)] = 0.0
+        tin[on, b] = rec[on, b, 0:9]
+        tgt[on, b] = t[on]
+    return color, tin, tgt
+
+
 def _render_nrc(self, accum_id=0, every_nth=1, n_train=0, c=0.01, p0=0, n=None, threads=8, max_events=0):
     """One frame of the NRC G_BUFFER pass for pixels [p0, p0+n): dict of
     gbuf [n,7] (radiance, beta, hit), query [n,9], suffix_query [n,9],

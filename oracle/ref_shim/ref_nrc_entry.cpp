@@ -91,4 +91,64 @@ void hmr_nrc_gbuffer(void* h, const float* camera12, const float* mat16, const i
   }
 }
 
+// One RENDER launch of the NRC rayGenCam (nrc.cu:365-380): per pixel the
+// composed colour through writePixel (accum [P][4] read when accum_id > 0 and
+// written; avg [P][4]); per training pixel nrcGenerateTrainingData
+// (nrc.cu:70-133): train_in [n_train_idx][40][9] and train_gt
+// [n_train_idx][40][3] at trOfs.  gbuf [P][8] and train [P][40][15] / tinfo
+// [P][2] in the layouts hmr_nrc_gbuffer returns (each pixel's own train
+// buffer stands at tBuffer[trOfs]); nn_out [(P + n_train_idx)][3] the cache
+// outputs (pixels' queries, then the training suffixes').
+void hmr_nrc_render(void* h, int accum_id, int every_nth, const int* train_idx, int n_train_idx, int all_unbiased,
+                    const float* gbuf, const float* train, const int* tinfo, const float* nn_out, float* accum,
+                    float* avg, float* train_in, float* train_gt) {
+  hmref::Scene* s = (hmref::Scene*)h;
+  const int P = s->width * s->height;
+  LaunchParams& lp = optixLaunchParams;
+  std::vector<GBuffer> gb(P);
+  std::vector<TrainBuffer> tb(P);
+  for (int i = 0; i < P; ++i) {
+    const float* g = gbuf + 8 * (size_t)i;
+    gb[i].hit = g[0] != 0.f;
+    gb[i].pathRadiance = vec3f(g[1], g[2], g[3]);
+    gb[i].beta = vec3f(g[4], g[5], g[6]);
+    gb[i].bounces = (int)g[7];
+    for (int b = 0; b < MAX_BOUNCES; ++b) {
+      const float* r = train + ((size_t)i * MAX_BOUNCES + b) * 15;
+      tb[i].vert[b] = vec3f(r[0], r[1], r[2]);
+      tb[i].wo[b] = vec3f(r[3], r[4], r[5]);
+      tb[i].n[b] = vec3f(r[6], r[7], r[8]);
+      tb[i].vertRadiance[b] = vec3f(r[9], r[10], r[11]);
+      tb[i].vertBeta[b] = vec3f(r[12], r[13], r[14]);
+    }
+    tb[i].bounces = tinfo[2 * i];
+    tb[i].hit = tinfo[2 * i + 1] != 0;
+  }
+  std::vector<int> tidx(train_idx, train_idx + n_train_idx);
+  std::vector<float3> gt((size_t)n_train_idx * MAX_BOUNCES, float3{0.f, 0.f, 0.f});
+  lp.pass = RENDER;
+  lp.accumId = accum_id;
+  lp.everyNth = every_nth;
+  lp.trainIdxs = tidx.data();
+  lp.allUnbiased = all_unbiased != 0;
+  lp.gBuffer = gb.data();
+  lp.mlpInputCh = 9;
+  lp.mlpOutputCh = 3;
+  lp.nnFrameOutput = (float3*)const_cast<float*>(nn_out);
+  lp.accumBuffer = (float4*)accum;
+  lp.averageBuffer = (float4*)avg;
+  lp.trainInput = train_in;
+  lp.trainGT = gt.data();
+  hmref::launch(s, 1, nullptr, nullptr, 0, [&](int pid) {
+    const int tr = pid / every_nth;
+    lp.tBuffer = tb.data() + pid - tr;  // tBuffer[trOfs] is this pixel's own buffer
+    __raygen__rayGenCam();
+  });
+  for (size_t k = 0; k < gt.size(); ++k) {
+    train_gt[3 * k] = gt[k].x;
+    train_gt[3 * k + 1] = gt[k].y;
+    train_gt[3 * k + 2] = gt[k].z;
+  }
+}
+
 }  // extern "C"

@@ -63,6 +63,8 @@ def _load(which):
         L.hmr_nrc_scene_new.restype = vp
         L.hmr_nrc_scene_new.argtypes = scene_args
         L.hmr_nrc_scene_free.argtypes = [vp]
+        L.hmr_nrc_render.restype = None
+        L.hmr_nrc_render.argtypes = [vp, i32, i32, I32P, i32, i32, F32P, F32P, I32P, F32P, F32P, F32P, F32P, F32P]
         L.hmr_nrc_gbuffer.restype = None
         L.hmr_nrc_gbuffer.argtypes = [vp, F32P, F32P, I32P, f32, i32, i32, I32P, i32, f32, i32, F32P, F32P, F32P,
                                       I32P, F32P, I32P, i32]
@@ -175,6 +177,22 @@ class RefIntegrator:
                    events=np.zeros((P, max_events, po.EV_FLOATS), np.float32), n_events=np.zeros(P, np.int32))
         self.L.hmr_pt_frame(self.h, r["cam"], r["mat"], r["sets"], self.osc.scene_scale, accum_id, out["accum"],
                             out["avg"], out["events"], out["n_events"], max_events, threads)
+        return out
+
+    def nrc_render(self, g, nn_out, accum_id=0, every_nth=1, n_train=0, all_unbiased=False, accum=None):
+        """The NRC RENDER pass over nrc_gbuffer's output g and cache outputs
+        nn_out [P + n_train, 3].  Returns dict accum / avg [P, 4], train_in
+        [n_train, 40, 9], train_gt [n_train, 40, 3]."""
+        assert self.which == "nrc"
+        P = self.P
+        tidx = np.array([po.feistel_perm(t, n_train, accum_id) for t in range(n_train)], np.int32)
+        out = dict(accum=np.zeros((P, 4), np.float32) if accum is None else np.array(accum, np.float32),
+                   avg=np.zeros((P, 4), np.float32), train_in=np.zeros((n_train, 40, 9), np.float32),
+                   train_gt=np.zeros((n_train, 40, 3), np.float32))
+        self.L.hmr_nrc_render(self.h, accum_id, every_nth, tidx, len(tidx), 1 if all_unbiased else 0,
+                              np.ascontiguousarray(g["gbuf"], np.float32), np.ascontiguousarray(g["train"], np.float32),
+                              np.ascontiguousarray(g["tinfo"], np.int32), np.ascontiguousarray(nn_out, np.float32),
+                              out["accum"], out["avg"], out["train_in"], out["train_gt"])
         return out
 
     def nrc_gbuffer(self, accum_id=0, every_nth=1, n_train=0, c=0.01, all_unbiased=False, max_events=128):

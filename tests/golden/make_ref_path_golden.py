@@ -80,6 +80,15 @@ def main():
     data["nrc_train_pixels"] = tp
     data["nrc_train"] = nrc["train"][tp]
     data["nrc_events"] = event_digest(nrc["events"], nrc["n_events"])
+    # the NRC RENDER pass and training data over that G-buffer
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_ref_integrator import nrc_cache_outputs
+    nn = nrc_cache_outputs(RES * RES, TRAIN, 4)
+    rr = rp.RefIntegrator(o, "nrc").nrc_render(nrc, nn, accum_id=ACCUM, every_nth=every_nth, n_train=TRAIN)
+    data["nrc_render_nn"] = nn
+    data["nrc_render_color"] = rr["accum"][:, :3]
+    data["nrc_render_train_in"] = rr["train_in"]
+    data["nrc_render_train_gt"] = rr["train_gt"]
     # the scene-sample training pass: 512 records on a 32-wide grid aiming at hair points
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from test_ref_integrator import hair_points

@@ -107,3 +107,31 @@ def test_nrc_training_renders_and_is_reproducible(R):
     assert np.array_equal(imgs[0], imgs[1])
     ls = np.array(losses[0])
     assert np.mean(ls[-4:]) < np.mean(ls[:4]), ls
+
+
+def test_nrc_render_pass_matches_oracle(R):
+    """The RENDER pass (colour = radiance + beta x max(cache, 0)) and the
+    training data (nrcGenerateTrainingData) of a GPU frame against the
+    oracle's restatement (pinned bit for bit to the reference's own nrc.cu,
+    tests/test_ref_integrator.py) applied to that frame's own G-buffer,
+    train buffers and cache outputs: bit for bit."""
+    res = 64
+    s = R.Scene(R.straight_hair_scene(res, res, strands=6000))
+    r = R.Renderer(s, R.NRC, train=False, seed=3, frames_in_flight=1)
+    r.frame()
+    P = res * res
+    st = r.stats()
+    gbuf, gbeta, nn, tinfo = r.buffer(4), r.buffer(8), r.buffer(1), r.buffer(10)
+    T = len(tinfo)
+    rec = r.buffer(9).reshape(T, 40, 5, 4)[:, :, :, :3].reshape(T, 40, 15)
+    tp = np.array([t * st.every_nth + po.feistel_perm(t, T, 0) % st.every_nth for t in range(T)])
+    assert np.array_equal(tinfo[:, 3], (gbuf[tp, 3] > 0.5).astype(np.int32))  # primary hit of each training pixel
+    color, tin, tgt = po.nrc_render(rad=gbuf[:, :3], beta=gbeta[:, :3], hit=gbuf[:, 3] > 0.5, cache=nn[:P + T],
+                                    train_px=tp, unbiased=tinfo[:, 2] != 0, t_bounces=tinfo[:, 0],
+                                    t_hit=tinfo[:, 1], records=rec)
+    assert (tinfo[:, 0] > 1).sum() > 20
+    img = r.read(R.IMAGE_FINAL).reshape(-1, 3)  # first frame: the FP64 sums hold the FP32 colours
+    assert np.array_equal(img, color.astype(np.float64))
+    g_in, g_out = r.buffer(2).reshape(T, 40, -1), r.buffer(3).reshape(T, 40, 3)
+    assert np.array_equal(g_in[:, :, :9].view(np.uint32), tin.view(np.uint32))
+    assert np.array_equal(g_out.view(np.uint32), tgt.view(np.uint32))

@@ -136,6 +136,22 @@ def test_oracle_traingen_matches_reference_golden(gold, gold_scene):
     assert np.array_equal(digest(ev, nev), gold["traingen_events"])
 
 
+def test_oracle_nrc_render_matches_reference_golden(gold):
+    """The NRC RENDER pass and training data of the oracle against the
+    reference's on the golden G-buffer."""
+    en = int(gold["every_nth"])
+    P = len(gold["nrc_gbuf"])
+    T = P // en
+    tp = gold["nrc_train_pixels"]
+    g = gold["nrc_gbuf"]
+    color, tin, tgt = po.nrc_render(rad=g[:, 1:4], beta=g[:, 4:7], hit=g[:, 0] != 0, cache=gold["nrc_render_nn"],
+                                    train_px=tp, unbiased=np.arange(T) % 16 == 0, t_bounces=gold["nrc_tinfo"][tp, 0],
+                                    t_hit=gold["nrc_tinfo"][tp, 1], records=gold["nrc_train"])
+    assert np.array_equal(bits(color), bits(gold["nrc_render_color"]))
+    assert np.array_equal(bits(tin), bits(gold["nrc_render_train_in"]))
+    assert np.array_equal(bits(tgt), bits(gold["nrc_render_train_gt"]))
+
+
 def test_golden_scene_exercises_the_branches(gold):
     """The fixture reaches the branches a frame bar would hide: head-surface
     (GGX) vertices, hair vertices, misses, training pixels, multi-bounce paths."""
@@ -274,3 +290,40 @@ def test_oracle_traingen_matches_reference_live(beta, rec_x):
     assert np.array_equal(bits(tout), bits(ref["train_out"]))
     assert np.array_equal(nev, ref["n_events"])
     assert np.array_equal(bits(events_as_reference(ev)), bits(ref["events"]))
+
+
+def nrc_render_inputs(g, P, en, n_train, accum_id):
+    """oracle nrc_render's arguments from the reference's G_BUFFER output."""
+    tp = np.array([t * en + po.feistel_perm(t, n_train, accum_id) % en for t in range(n_train)])
+    return dict(rad=g["gbuf"][:, 1:4], beta=g["gbuf"][:, 4:7], hit=g["gbuf"][:, 0] != 0, train_px=tp,
+                unbiased=np.arange(n_train) % 16 == 0, t_bounces=g["tinfo"][tp, 0], t_hit=g["tinfo"][tp, 1],
+                records=g["train"][tp])
+
+
+def nrc_cache_outputs(P, n_train, seed):
+    """Seeded cache outputs with negative values and NaNs (both handled by
+    the RENDER pass)."""
+    rng = np.random.default_rng(seed)
+    nn = rng.normal(0.3, 0.5, (P + n_train, 3)).astype(np.float32)
+    nn[rng.random(len(nn)) < 0.01] = np.nan
+    return nn
+
+
+@needs_ref
+def test_oracle_nrc_render_matches_reference_live():
+    """The NRC RENDER pass (nrc.cu:365-380: colour = radiance + beta x
+    max(cache, 0)) and nrcGenerateTrainingData (nrc.cu:70-133) of the oracle
+    against the reference's own, on the reference's G-buffer."""
+    o = _live_scene(6000)
+    P = o.width * o.height
+    en = 4
+    ref = refpath.RefIntegrator(o, "nrc")
+    g = ref.nrc_gbuffer(accum_id=2, every_nth=en, n_train=P // en, c=0.01, max_events=8)
+    nn = nrc_cache_outputs(P, P // en, 3)
+    # the same frame as the G-buffer (its trainIdxs); zero running sums: accum = colour
+    r = ref.nrc_render(g, nn, accum_id=2, every_nth=en, n_train=P // en)
+    color, tin, tgt = po.nrc_render(cache=nn, **nrc_render_inputs(g, P, en, P // en, 2))
+    assert (g["tinfo"][:, 0] > 1).sum() > 50  # multi-vertex training paths
+    assert np.array_equal(bits(color), bits(r["accum"][:, :3]))
+    assert np.array_equal(bits(tin), bits(r["train_in"]))
+    assert np.array_equal(bits(tgt), bits(r["train_gt"]))

@@ -132,6 +132,7 @@ def test_nrc_render_pass_matches_oracle(R):
     assert (tinfo[:, 0] > 1).sum() > 20
     img = r.read(R.IMAGE_FINAL).reshape(-1, 3)  # first frame: the FP64 sums hold the FP32 colours
     assert np.array_equal(img, color.astype(np.float64))
-    g_in, g_out = r.buffer(2).reshape(T, 40, -1), r.buffer(3).reshape(T, 40, 3)
+    # the record buffers hold numTrainingRecords rows; the T x 40 first are the training pixels'
+    g_in, g_out = r.buffer(2)[:T * 40].reshape(T, 40, -1), r.buffer(3)[:T * 40].reshape(T, 40, 3)
     assert np.array_equal(g_in[:, :, :9].view(np.uint32), tin.view(np.uint32))
     assert np.array_equal(g_out.view(np.uint32), tgt.view(np.uint32))

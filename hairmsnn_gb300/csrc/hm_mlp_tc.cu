@@ -67,8 +67,8 @@ HM_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-HM_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kTcWaitLimit; ++i)
+HM_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit = kTcWaitLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
@@ -1434,4 +1434,35 @@ int tc_backward(const MlpDims& d, const TcPack& pk, const TcTrainBufs& b, const 
   return HM_OK;
 }
 
+// ---- the bounded wait's expiry, exercised on purpose (tests)
+// One block: thread 0 sets up an mbarrier that expects one arrival, which
+// never comes, and waits on it with the kernels' bounded wait, `limit`
+// tries; the expiry is recorded in err and the kernel returns.  Any other
+// outcome (the wait completing) is recorded as 2.
+__global__ void tc_wait_expiry_kernel(uint32_t limit, int* err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+    *err = mbar_wait_bounded(&bar, 0u, limit) ? 2 : 1;
+  }
+}
+
 }  // namespace hm
+
+extern "C" int hm_debug_wait_expiry(int tries, void* stream) {
+  if (tries < 1 || tries > (1 << 20)) return hm_set_error("hm_debug_wait_expiry: tries out of range"), HM_EINVAL;
+  int* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(int));
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_debug_wait_expiry");
+  cudaMemsetAsync(d, 0, sizeof(int), (cudaStream_t)stream);
+  hm::tc_wait_expiry_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((uint32_t)tries, d);
+  int h = 0;
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize((cudaStream_t)stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return hm_cuda_status(e, "hm_debug_wait_expiry");
+  if (h == 1) return hm_set_error("hm_debug_wait_expiry: the bounded wait expired"), HM_ETIMEOUT;
+  return hm_set_error("hm_debug_wait_expiry: the wait did not expire (%d)", h), HM_EINVAL;
+}

@@ -165,6 +165,15 @@ int hm_mlp_inference(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, vo
  * other end of its primary context) while the library is loaded is not
  * supported by this entry point. */
 int hm_mlp_inference_noalloc(hm_mlp* mlp, const float* d_in, float* d_out, int64_t n, void* stream);
+/* The bounded device-side wait, run out on purpose (no reference
+ * counterpart; failure-detection tests).  Every wait of the tensor-core
+ * kernels on an mbarrier gives up after a fixed number of tries, records
+ * the fact in a host-visible flag and lets the kernel return, so that a
+ * lost completion shows as HM_ETIMEOUT instead of a hung GPU.  This call
+ * launches one block that waits `tries` times (1 .. 2^20) on a barrier
+ * nothing completes: it returns HM_ETIMEOUT when the wait expired and the
+ * kernel returned, and the context stays usable. */
+int hm_debug_wait_expiry(int tries, void* stream);
 /* Trainer::training_step + Trainer::loss (render_hair_msnn.cu:690-691),
  * split into its three phases and fused: forward keeps the activations
  * (d_out may be NULL; d_in must stay valid until backward), backward takes

@@ -222,6 +222,10 @@ int hm_mlp_load(hm_mlp* mlp, const char* path);
  *   surface.procedural {type ellipsoid, triangles, radii[3], diffuse[3], alpha}
  *   lights.sky         {turbidity, sun[3], width, height, scale, rotation}
  *                      (Preetham et al. 1999 sky baked to a lat-long map)
+ * As parseScene: a hair block without "type" keeps the default material
+ * (alpha 0.03 rad), and the bounds behind the scene scale of a HAIR file
+ * start at the origin (extractHairData's).  Unlike it, a missing integrator
+ * key takes its default, and a scene without any light is refused.
  * base_dir resolves relative file names (tcnn.config).  Returns NULL and a
  * status (HM_EPARSE for bad JSON or a malformed .hair/.obj file, HM_EINVAL for a
  * missing file, HM_EUNSUPPORTED for .exr environment maps).

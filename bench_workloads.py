@@ -57,7 +57,7 @@ class VertexWorkload:
         self.net = mlp.TinyMLP("c1_cache_w64.json", 16, 3, precision="fp16", seed=0)
         self.out = torch.empty((n, 3), device="cuda")
         self.net.inference(self.x, self.out)  # packs the FP16 weights once
-        self.kernels_per_step = 4  # eval, sample, encode, MLP
+        self.kernels_per_step = 3  # eval, sample, cache network (warp-specialised: encoding overlapped)
         # pinned host copies for the end-to-end leg
         self.host_in = [a.cpu().pin_memory() for a in (self.wo, self.wi, self.t, self.h, self.u)]
         self.h2d_bytes = sum(a.numel() * 4 for a in self.host_in) + self.x_host.numel() * 4
@@ -102,8 +102,8 @@ class VertexWorkload:
                                  seg_ms[0]),
             "bsdf_sample_kernel": ("hbm", BSDF_SAMPLE_BYTES * n / (seg_ms[1] * 1e-3) / 1e9, pk["hbm_gbs"], "GB/s",
                                    seg_ms[1]),
-            "tc_encode_kernel + mlp_tc_fwd_kernel<FP16, 64>": ("tensor", MLP_FLOP_W64 * n / (seg_ms[2] * 1e-3) / 1e12,
-                                                                pk["bf16_tflops"], "TFLOP/s", seg_ms[2]),
+            "mlp_tc_fused_kernel<FP16, 64>": ("tensor", MLP_FLOP_W64 * n / (seg_ms[2] * 1e-3) / 1e12,
+                                              pk["bf16_tflops"], "TFLOP/s", seg_ms[2]),
         }
         name = max(segs, key=lambda k: segs[k][4])
         bound, ach, peak, unit, ms = segs[name]
@@ -251,7 +251,8 @@ class PrecisionWorkload:
     def roofline(self, seg_ms, pk):
         ms = seg_ms[0]
         tf = self.flops(64) * self.n / (ms * 1e-3) / 1e12
-        return {"kernel": "mlp_tc_fwd_kernel<FP16, 64> (encoding fused)", "bound": "tensor",
+        return {"kernel": "mlp_tc_fused_kernel<FP16, 64> (warp-specialised: encoding overlapped with the layers)",
+                "bound": "tensor",
                 "achieved": round(tf, 3), "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": round(tf / pk["bf16_tflops"], 5), "traffic": None,
                 "flop_per_query": self.flops(64),

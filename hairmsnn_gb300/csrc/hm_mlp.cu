@@ -915,10 +915,11 @@ static int tc_prepare(Mlp* m) {
 }
 
 // Inference on the tensor cores (FP16 / BF16 / E4M3 operands, FP32
-// accumulation).  With allow_alloc the encoded operands go through a
-// workspace grown on demand (encode kernel, then the layers); without it
-// (hm_mlp_inference_noalloc) the encoding is fused into the layer kernel.  A
-// bounded wait that expired in an earlier call is reported here.
+// accumulation).  With allow_alloc, where tc_forward runs the encode kernel
+// before the layers, the encoded operands go through a workspace grown on
+// demand; without it (hm_mlp_inference_noalloc) the encoding runs inside
+// the layer kernels.  A bounded wait that expired in an earlier call is
+// reported here.
 static int tc_inference(Mlp* m, const float* d_in, float* d_out, int64_t n, cudaStream_t st, bool allow_alloc) {
   if (*(volatile int*)m->tc_err_host) {
     *m->tc_err_host = 0;
@@ -928,6 +929,7 @@ static int tc_inference(Mlp* m, const float* d_in, float* d_out, int64_t n, cuda
     if (int s = tc_pack(m->cfg.d, m->params, m->tc, st)) return s;
     m->packed_version = m->params_version;
   }
+  allow_alloc = allow_alloc && tc_wants_workspace(m->cfg.d, m->tc);
   if (allow_alloc) {
     const int64_t need = tc_encode_bytes(m->cfg.d, m->tc, n);
     if (need > m->tc_work_cap) {

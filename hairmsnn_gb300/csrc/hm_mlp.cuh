@@ -176,11 +176,17 @@ int tc_pack_alloc(const MlpDims& d, int precision, TcPack* pk);
 int tc_pack(const MlpDims& d, const float* params, TcPack& pk, cudaStream_t st);
 void tc_pack_free(TcPack* pk);
 // Encoding + all layers of n queries on the tensor cores: in [n][in_ch],
-// out [n][out_stride] (the first out_ch columns written).  With a workspace
-// of at least tc_encode_bytes the encoding runs first as its own kernel and
-// the layers load their input tiles by bulk copies; without one, the
-// encoding is fused into the layer kernel.
+// out [n][out_stride] (the first out_ch columns written).  Three forms, the
+// same bits: the warp-specialised kernel (16-bit operands, width 32 / 64:
+// encoder warps and layer warps overlapped in one CTA per SM, no
+// workspace); with a workspace of at least tc_encode_bytes, the encode
+// kernel and then the layer kernel loading its input tiles by bulk copies
+// (networks with a hash grid, E4M3, width 128); without one, the layer
+// kernel encoding its own tiles.
 int64_t tc_encode_bytes(const MlpDims& d, const TcPack& pk, int64_t n);
+// Whether tc_forward would use a workspace (false where the warp-specialised
+// kernel runs: no encoded operands in device memory).
+bool tc_wants_workspace(const MlpDims& d, const TcPack& pk);
 int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
                int out_stride, int64_t n, int* err_flag, cudaStream_t st, uint8_t* work = nullptr,
                int64_t work_bytes = 0);

@@ -73,6 +73,24 @@ HM_D bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t limit = kTc
   return false;
 }
 HM_D void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+HM_D void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// Named barrier over the nthreads threads (whole warps) of one warp group,
+// returning the OR of v over them.
+HM_D bool group_sync_or(int id, int nthreads, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 q, %1, 0;\n\t"
+      "bar.red.or.pred p, %2, %3, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(id), "r"(nthreads)
+      : "memory");
+  return r != 0;
+}
+HM_D void group_sync(int id, int nthreads) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory"); }
 // The barrier's phase completes once `bytes` of asynchronous copies have
 // landed (and the one arrival of this call).
 HM_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
@@ -427,6 +445,9 @@ struct TcArgs {
   const uint8_t* a_pre;
   const float* row_inv_pre;
   int64_t tile_bytes;
+  // warp-specialised inference: shared-memory bytes of the weights, of one
+  // layer-0 operand stage and of one hidden operand; number of stages
+  int fz_w, fz_a0, fz_h, fz_stages;
 };
 
 // Encoding of every row into the layer-0 operand, in the MMA's shared-memory
@@ -652,7 +673,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
 #pragma unroll
           for (int o = 0; o < 16; ++o) p.pred[q * 16 + o] = t[o] * sc;
         } else {
-          for (int o = 0; o < d.out_ch && o < p.out_stride; ++o) p.out[q * p.out_stride + o] = t[o] * sc;
+#pragma unroll
+          for (int o = 0; o < 16; ++o)
+            if (o < d.out_ch && o < p.out_stride) p.out[q * p.out_stride + o] = t[o] * sc;
         }
       }
     }
@@ -660,6 +683,200 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
     __syncthreads();
   }
   if (failed && tid == 0) atomicOr(p.err, 1);
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, p.ncols);
+}
+
+// ---------------------------------------------- warp-specialised inference
+// Encoding and layers overlapped inside one persistent CTA per SM (16-bit
+// operands).  24 encoder warps write layer-0 operands into a ring of NS
+// stages (each the whole K of one 128-row tile): they form NS teams of
+// 4 * P warps, team t encoding the CTA's tiles k = t (mod NS) into stage t
+// with P threads per row (each an equal contiguous range of the row's
+// 16-byte feature groups; P = 6 / NS with NS 6 or 2, the most stages that
+// fit next to the weights, so small operands get one thread per row as in
+// tc_encode_kernel).  Two lanes of 4 layer warps walk the layers: lane s
+// takes the tiles k = s (mod 2) (with NS even, stage t always feeds lane
+// t % 2), with its own hidden operand H[s] (128 x W)
+// and W columns of tensor memory; warp w reads tensor-memory lanes
+// 32 * (w % 4) .. (one thread per row) and the lane's first thread issues
+// the MMAs.  A team refills its stage as soon as the layer-0 MMAs of its
+// previous tile have read it, so encoding runs while the layer warps walk
+// layers 1..L, and the two lanes fill each other's waits.  Hand-offs:
+// full[t] (team -> layer lane, one arrival after the team's named barrier),
+// empty[t] (layer-0 MMAs done -> team), mma[s] (tcgen05.commit).  Every
+// mbarrier wait is bounded; an expired wait is reduced over the waiting
+// group through its named barrier, the group stops and the waits of the
+// groups that depend on it then expire too.  The encoded operands, the MMAs
+// and the epilogue arithmetic are those of mlp_tc_fwd_kernel, so the
+// outputs are the same bits.
+constexpr int kFzLanes = 2;
+constexpr int kFzLayWarps = 4;   // per lane
+constexpr int kFzEncWarps = 24;  // in all
+constexpr int kFzLayThreads = kFzLanes * kFzLayWarps * 32;
+constexpr int kFzThreads = kFzLayThreads + kFzEncWarps * 32;
+constexpr int kFzMaxStages = kFzEncWarps / 4;
+constexpr int kFzMisc = 128;  // 2 * kFzMaxStages + 2 mbarriers + the tensor-memory address
+
+template <int PREC, int W>
+__global__ void __launch_bounds__(kFzThreads, 1) mlp_tc_fused_kernel(const __grid_constant__ TcArgs p) {
+  static_assert(PREC != TC_E4M3, "16-bit operands only");
+  static_assert(8 * (2 * kFzMaxStages + 2) + 4 <= kFzMisc, "barrier area");
+  constexpr int CK = 8;  // elements per 16-byte core-matrix row
+  constexpr int FMT = PREC == TC_BF16 ? 1 : 0;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const int NS = p.fz_stages, P = kFzMaxStages / NS;
+  uint8_t* Wt = smem;
+  uint8_t* A0 = smem + p.fz_w;
+  uint8_t* Hb = A0 + NS * p.fz_a0;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Hb + kFzLanes * p.fz_h);
+  uint64_t* full = bars;                 // [NS]
+  uint64_t* empty = bars + kFzMaxStages;  // [NS]
+  uint64_t* mma = bars + 2 * kFzMaxStages;  // [2]
+  uint32_t* holder = reinterpret_cast<uint32_t*>(bars + 2 * kFzMaxStages + 2);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane_id = tid & 31;
+  const MlpDims& d = p.d;
+  const int L = p.n_layers - 1;
+  const int K0 = p.K[0];
+  const int64_t n_tiles = (p.n + kTcRows - 1) / kTcRows;
+
+  for (int64_t i = tid; i < p.blob_bytes / 16; i += kFzThreads)
+    reinterpret_cast<uint4*>(Wt)[i] = __ldg(reinterpret_cast<const uint4*>(p.blob) + i);
+  if (tid == 0) {
+    for (int b = 0; b < 2 * kFzMaxStages + 2; ++b) mbar_init(bars + b, 1);
+    fence_mbar_init();
+  }
+  if (warp == 0) tmem_alloc(holder, p.ncols);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *holder;
+  bool failed = false;
+
+  if (tid < kFzLayThreads) {
+    // ---------------- layer warps of lane s
+    const int s = warp / kFzLayWarps, quad = warp % 4, row = quad * 32 + lane_id;
+    const int bar_id = 1 + s;
+    const bool leader = (warp % kFzLayWarps) == 0 && lane_id == 0;
+    const uint32_t tm = tmem + (uint32_t)(s * W);
+    const uint32_t row_taddr = tm + ((uint32_t)(quad * 32) << 16);
+    uint8_t* Hs = Hb + s * p.fz_h;
+    uint64_t* mma_s = mma + s;
+    const uint32_t a_lbo = 16 * kTcRows;
+    const uint32_t h_base = smem_u32(Hs), w_base = smem_u32(Wt);
+    uint32_t ph_mma = 0;
+    // the MMAs of layer l over A (k_count elements of K), committed to mma_s
+    auto issue = [&](int l, uint32_t a_base, int k_count) {
+      tc_fence_after();
+      const uint32_t idesc = tc_idesc(kTcRows, p.N[l], FMT);
+      const uint32_t b_lbo = 16 * p.N[l];
+      const uint32_t b_base = w_base + (uint32_t)p.boff[l];
+      for (int ks = 0; ks < k_count / 16; ++ks) {
+        const uint64_t ad = tc_sdesc(a_base + (uint32_t)ks * 2 * a_lbo, a_lbo, 128);
+        const uint64_t bd = tc_sdesc(b_base + (uint32_t)ks * 2 * b_lbo, b_lbo, 128);
+        tc_mma<false>(tm, ad, bd, idesc, ks > 0 ? 1u : 0u);
+      }
+      tc_commit(mma_s);
+    };
+    for (int64_t k = s;; k += kFzLanes) {
+      const int64_t tile = blockIdx.x + k * (int64_t)gridDim.x;
+      if (tile >= n_tiles) break;
+      const int st = (int)(k % NS);
+      bool ok = true;
+      if (leader) {
+        ok = mbar_wait_bounded(full + st, (uint32_t)((k / NS) & 1));
+        if (ok) {
+          issue(0, smem_u32(A0 + st * p.fz_a0), K0);
+          ok = mbar_wait_bounded(mma_s, ph_mma);
+          if (ok) mbar_arrive(empty + st);  // the stage has been read
+        }
+      }
+      ph_mma ^= 1u;
+      if (group_sync_or(bar_id, kFzLayWarps * 32, !ok)) {
+        failed = true;
+        break;
+      }
+      tc_fence_after();
+      for (int l = 1; l <= L; ++l) {
+        // epilogue of layer l - 1: ReLU, rounded to the operand type, as the A of layer l
+#pragma unroll
+        for (int c = 0; c < W / 16; ++c) {
+          float t[16];
+          tmem_ld16(row_taddr + c * 16, t);
+#pragma unroll
+          for (int g = 0; g < 2; ++g) {
+            uint32_t word[4];
+#pragma unroll
+            for (int w2 = 0; w2 < 4; ++w2)
+              word[w2] = pack2<PREC>(fmaxf(t[g * 8 + 2 * w2], 0.f), fmaxf(t[g * 8 + 2 * w2 + 1], 0.f));
+            *reinterpret_cast<uint4*>(Hs + op_offset(kTcRows, row, (c * 16 + g * 8) * 2)) =
+                make_uint4(word[0], word[1], word[2], word[3]);
+          }
+        }
+        tc_fence_before();
+        fence_proxy_async_smem();
+        group_sync(bar_id, kFzLayWarps * 32);
+        if (leader) {
+          issue(l, h_base, p.K[l]);
+          ok = mbar_wait_bounded(mma_s, ph_mma);
+        }
+        ph_mma ^= 1u;
+        if (group_sync_or(bar_id, kFzLayWarps * 32, !ok)) {
+          failed = true;
+          break;
+        }
+        tc_fence_after();
+      }
+      if (failed) break;
+      // output layer accumulator -> out
+      float t[16];
+      tmem_ld16(row_taddr, t);
+      const int64_t q = tile * kTcRows + row;
+      if (q < p.n)
+        for (int o = 0; o < d.out_ch && o < p.out_stride; ++o) p.out[q * p.out_stride + o] = t[o];
+      // the next tile's layer-0 MMAs overwrite these columns
+      tc_fence_before();
+      group_sync(bar_id, kFzLayWarps * 32);
+    }
+  } else {
+    // ---------------- encoder team t (4 * P warps)
+    const int e = tid - kFzLayThreads;
+    const int team = e / (kTcRows * P), et = e % (kTcRows * P);
+    const int row = et % kTcRows, part = et / kTcRows;
+    const int bar_id = 3 + team;
+    const bool leader = et == 0;
+    uint8_t* As = A0 + team * p.fz_a0;
+    const int G = K0 / CK;
+    const int g0 = part * G / P, g1 = (part + 1) * G / P;
+    uint32_t ph_empty = 0;
+    for (int64_t k = team;; k += NS) {
+      const int64_t tile = blockIdx.x + k * (int64_t)gridDim.x;
+      if (tile >= n_tiles) break;
+      if (k >= NS) {  // wait until the layer-0 MMAs of the team's previous tile have read the stage
+        const bool ok = leader ? mbar_wait_bounded(empty + team, ph_empty) : true;
+        ph_empty ^= 1u;
+        if (group_sync_or(bar_id, kTcRows * P, !ok)) {
+          failed = true;
+          break;
+        }
+      }
+      const int64_t q = tile * kTcRows + row;
+      RowPacker<PREC> pk(As, row, g0, 1.f);
+      if (q < p.n) {
+        enc_range<PREC>(d, p.in + q * d.in_ch, p.enc_params, g0 * CK, g1 * CK, pk);
+      } else {
+        for (int kk = g0 * CK; kk < g1 * CK; ++kk) pk.push(0.f);
+      }
+      fence_proxy_async_smem();
+      group_sync(bar_id, kTcRows * P);
+      if (leader) mbar_arrive(full + team);
+    }
+  }
+  if (failed && lane_id == 0) atomicOr(p.err, 1);
+  tc_fence_before();
   __syncthreads();
   tc_fence_after();
   if (warp == 0) tmem_dealloc(tmem, p.ncols);
@@ -910,13 +1127,92 @@ int64_t tc_encode_bytes(const MlpDims& d, const TcPack& pk, int64_t n) {
   return tiles * tile_bytes + (pk.precision == HM_PREC_FP8_E4M3 ? ((n * 4 + 255) & ~(int64_t)255) : 0);
 }
 
+// Form of the 16-bit inferences: 0 automatic (below), 1 never the
+// warp-specialised kernel, 2 only it (HM_EUNSUPPORTED where it does not
+// fit).  Set by hm_debug_tc_path.
+static int g_tc_path = 0;
+
+static bool has_hash_grid(const MlpDims& d) {
+  for (int si = 0; si < d.n_segs; ++si)
+    if (d.segs[si].type == ENC_HASHGRID) return true;
+  return false;
+}
+
+// Shared memory of mlp_tc_fused_kernel (0: the network does not fit it).
+static int64_t tc_fused_smem(const MlpDims& d, const TcPack& pk, TcArgs* a) {
+  if (pk.precision == HM_PREC_FP8_E4M3 || (d.width != 32 && d.width != 64) || pk.N[pk.n_layers - 1] > d.width)
+    return 0;
+  const int64_t w = (pk.bytes + 1023) & ~(int64_t)1023;
+  const int64_t a0 = (int64_t)kTcRows * pk.K[0] * 2;
+  const int64_t h = (int64_t)kTcRows * d.width * 2;
+  // the most stages (the fewest encoder threads per row) that fit; an even
+  // count, so that each stage is read by one layer lane only and every
+  // parity wait on it is for the phase after the one that lane last saw
+  for (int ns : {6, 2}) {
+    const int64_t total = w + ns * a0 + kFzLanes * h + kFzMisc;
+    if (total > kTcSmemMax) continue;
+    if (a) {
+      a->fz_w = (int)w;
+      a->fz_a0 = (int)a0;
+      a->fz_h = (int)h;
+      a->fz_stages = ns;
+    }
+    return total;
+  }
+  return 0;
+}
+
+template <int PREC, int W>
+static int tc_fused_launch(const TcArgs& a, size_t smem, cudaStream_t st) {
+  auto kern = mlp_tc_fused_kernel<PREC, W>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return hm_cuda_status(e, "mlp_tc_fused_kernel smem");
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t tiles = (a.n + kTcRows - 1) / kTcRows;
+  const int blocks = (int)std::min<int64_t>(tiles, (int64_t)sms);
+  kern<<<blocks, kFzThreads, smem, st>>>(a);
+  HM_CHECK_LAUNCH("mlp_tc_fused_kernel");
+  return HM_OK;
+}
+
+bool tc_wants_workspace(const MlpDims& d, const TcPack& pk) {
+  if (g_tc_path == 2) return false;
+  return g_tc_path == 1 || has_hash_grid(d) || tc_fused_smem(d, pk, nullptr) == 0;
+}
+
 int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, const float* in, float* out,
                int out_stride, int64_t n, int* err_flag, cudaStream_t st, uint8_t* work, int64_t work_bytes) {
   if (n <= 0) return HM_OK;
   TcArgs a;
   size_t smem = 0;
   if (int e = tc_args(d, pk, enc_params, in, out, out_stride, n, err_flag, &a, &smem)) return e;
-  if (work && work_bytes >= tc_encode_bytes(d, pk, n)) {
+  const bool have_work = work && work_bytes >= tc_encode_bytes(d, pk, n);
+  // Automatic choice, from the measured times (2^18 and 2^20 queries, W 64):
+  // with a workspace, the encode kernel + layer kernel where the encoding
+  // holds a hash grid (its table gathers are latency-bound and want the
+  // encode kernel's occupancy: 0.17 / 0.68 ms against 0.22 / 0.77), else the
+  // warp-specialised kernel (Frequency / OneBlob: 0.132 / 0.497 ms against
+  // 0.152 / 0.516); without one, the warp-specialised kernel wherever it fits
+  // (the layer kernel encoding its own tiles: 0.17-0.27 / 0.64-1.02 ms).
+  const bool want_fz = g_tc_path == 2 || (g_tc_path == 0 && (!have_work || !has_hash_grid(d)));
+  if (want_fz) {
+    const int64_t fz = tc_fused_smem(d, pk, &a);
+    if (fz > 0) {
+      // both lanes' accumulators
+      int ncols = 32;
+      while (ncols < 2 * d.width) ncols *= 2;
+      a.ncols = ncols;
+      if (pk.precision == HM_PREC_BF16)
+        return d.width == 32 ? tc_fused_launch<TC_BF16, 32>(a, (size_t)fz, st)
+                             : tc_fused_launch<TC_BF16, 64>(a, (size_t)fz, st);
+      return d.width == 32 ? tc_fused_launch<TC_FP16, 32>(a, (size_t)fz, st)
+                           : tc_fused_launch<TC_FP16, 64>(a, (size_t)fz, st);
+    }
+    if (g_tc_path == 2) return hm_set_error("mlp: the warp-specialised kernel does not fit this network"), HM_EUNSUPPORTED;
+  }
+  if (have_work) {
     // encode every row first (high occupancy, no tensor work), then the
     // layers with the layer-0 operand loaded by bulk copies
     const int64_t tiles = (n + kTcRows - 1) / kTcRows;
@@ -1449,6 +1745,12 @@ __global__ void tc_wait_expiry_kernel(uint32_t limit, int* err) {
 }
 
 }  // namespace hm
+
+extern "C" int hm_debug_tc_path(int path) {
+  if (path < 0 || path > 2) return hm_set_error("hm_debug_tc_path: path out of range"), HM_EINVAL;
+  hm::g_tc_path = path;
+  return HM_OK;
+}
 
 extern "C" int hm_debug_wait_expiry(int tries, void* stream) {
   if (tries < 1 || tries > (1 << 20)) return hm_set_error("hm_debug_wait_expiry: tries out of range"), HM_EINVAL;

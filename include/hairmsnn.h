@@ -174,6 +174,20 @@ int hm_mlp_inference_noalloc(hm_mlp* mlp, const float* d_in, float* d_out, int64
  * nothing completes: it returns HM_ETIMEOUT when the wait expired and the
  * kernel returned, and the context stays usable. */
 int hm_debug_wait_expiry(int tries, void* stream);
+/* Form of the later FP16 / BF16 tensor-core inferences (no reference
+ * counterpart; tests and timing).  Three forms give the same bits: the
+ * warp-specialised kernel (encoder warps and layer warps overlapped in one
+ * CTA per SM, no workspace; width 32 or 64, where the weights, two or six
+ * layer-0 operand stages and two hidden operands fit in shared memory), the
+ * encode kernel followed by the layer kernel (a workspace of encoded
+ * operands), and the layer kernel encoding its own tiles.  0 (the default):
+ * hm_mlp_inference takes the warp-specialised kernel unless the encoding
+ * holds a hash grid (then the encode kernel + layer kernel, faster for
+ * latency-bound table gathers), hm_mlp_inference_noalloc takes it wherever
+ * it fits.  1: never the warp-specialised kernel.  2: only it
+ * (HM_EUNSUPPORTED where it does not fit, and for E4M3).  Process-wide; not
+ * synchronised with inferences in flight on other threads. */
+int hm_debug_tc_path(int path);
 /* Trainer::training_step + Trainer::loss (render_hair_msnn.cu:690-691),
  * split into its three phases and fused: forward keeps the activations
  * (d_out may be NULL; d_in must stay valid until backward), backward takes

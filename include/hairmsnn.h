@@ -181,10 +181,10 @@ int hm_debug_wait_expiry(int tries, void* stream);
  * layer-0 operand stages and two hidden operands fit in shared memory), the
  * encode kernel followed by the layer kernel (a workspace of encoded
  * operands), and the layer kernel encoding its own tiles.  0 (the default):
- * hm_mlp_inference takes the warp-specialised kernel unless the encoding
- * holds a hash grid (then the encode kernel + layer kernel, faster for
- * latency-bound table gathers), hm_mlp_inference_noalloc takes it wherever
- * it fits.  1: never the warp-specialised kernel.  2: only it
+ * the warp-specialised kernel where it fits, except that an inference with
+ * a workspace on a network whose encoding holds a hash grid takes the
+ * encode kernel + layer kernel (faster for latency-bound table gathers).
+ * 1: never the warp-specialised kernel.  2: only it
  * (HM_EUNSUPPORTED where it does not fit, and for E4M3).  Process-wide; not
  * synchronised with inferences in flight on other threads. */
 int hm_debug_tc_path(int path);

@@ -356,6 +356,7 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
       }
     } else {  // hash grid
       const float* table = enc_params + s.param_off;
+      const bool pair_table = s.n_feat == 2 && (reinterpret_cast<uintptr_t>(table) & 7) == 0;
       const float px = xin[s.in_off], py = xin[s.in_off + 1], pz = xin[s.in_off + 2];
       int l = j0 / s.n_feat, f0 = j0 - l * s.n_feat;
       for (int j = j0; j < j1; ++l) {
@@ -367,15 +368,35 @@ HM_D void enc_range(const MlpDims& d, const float* __restrict__ xin, const float
         float acc[8];
 #pragma unroll
         for (int q = 0; q < 8; ++q) acc[q] = 0.f;
-        for (int c = 0; c < 8; ++c) {
-          const uint32_t cx = ix + (c & 1), cy = iy + ((c >> 1) & 1), cz = iz + ((c >> 2) & 1);
-          const float w = ((c & 1) ? wx : 1.f - wx) * (((c >> 1) & 1) ? wy : 1.f - wy) *
-                          (((c >> 2) & 1) ? wz : 1.f - wz);
-          const uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
-          const float* tv = table + (int64_t)e * s.n_feat;
+        if (pair_table) {
+          // two features per entry: the eight corners' entries are loaded
+          // first (eight 8-byte gathers in flight), then accumulated in
+          // corner order as below
+          float2 tv[8];
 #pragma unroll
-          for (int q = 0; q < 8; ++q)
-            if (q < s.n_feat) acc[q] += w * __ldg(tv + q);
+          for (int c = 0; c < 8; ++c) {
+            const uint32_t cx = ix + (c & 1), cy = iy + ((c >> 1) & 1), cz = iz + ((c >> 2) & 1);
+            const uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
+            tv[c] = __ldg(reinterpret_cast<const float2*>(table) + e);
+          }
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            const float w = ((c & 1) ? wx : 1.f - wx) * (((c >> 1) & 1) ? wy : 1.f - wy) *
+                            (((c >> 2) & 1) ? wz : 1.f - wz);
+            acc[0] += w * tv[c].x;
+            acc[1] += w * tv[c].y;
+          }
+        } else {
+          for (int c = 0; c < 8; ++c) {
+            const uint32_t cx = ix + (c & 1), cy = iy + ((c >> 1) & 1), cz = iz + ((c >> 2) & 1);
+            const float w = ((c & 1) ? wx : 1.f - wx) * (((c >> 1) & 1) ? wy : 1.f - wy) *
+                            (((c >> 2) & 1) ? wz : 1.f - wz);
+            const uint32_t e = s.level_off[l] + grid_index(s, l, cx, cy, cz);
+            const float* tv = table + (int64_t)e * s.n_feat;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+              if (q < s.n_feat) acc[q] += w * __ldg(tv + q);
+          }
         }
 #pragma unroll
         for (int q = 0; q < 8; q += 2) {
@@ -1192,10 +1213,11 @@ int tc_forward(const MlpDims& d, const TcPack& pk, const float* enc_params, cons
   // Automatic choice, from the measured times (2^18 and 2^20 queries, W 64):
   // with a workspace, the encode kernel + layer kernel where the encoding
   // holds a hash grid (its table gathers are latency-bound and want the
-  // encode kernel's occupancy: 0.17 / 0.68 ms against 0.22 / 0.77), else the
-  // warp-specialised kernel (Frequency / OneBlob: 0.132 / 0.497 ms against
-  // 0.152 / 0.516); without one, the warp-specialised kernel wherever it fits
-  // (the layer kernel encoding its own tiles: 0.17-0.27 / 0.64-1.02 ms).
+  // encode kernel's occupancy: 0.127 / 0.437 ms against 0.136 / 0.510), else
+  // the warp-specialised kernel (Frequency / OneBlob: 0.134 / 0.494 ms
+  // against 0.151 / 0.515); without one, the warp-specialised kernel
+  // wherever it fits (the layer kernel encoding its own tiles: 0.17 /
+  // 0.64 ms on either network).
   const bool want_fz = g_tc_path == 2 || (g_tc_path == 0 && (!have_work || !has_hash_grid(d)));
   if (want_fz) {
     const int64_t fz = tc_fused_smem(d, pk, &a);

@@ -719,10 +719,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) mlp_tc_fwd_kernel(const __grid_
 // fit next to the weights, so small operands get one thread per row as in
 // tc_encode_kernel).  Two lanes of 4 layer warps walk the layers: lane s
 // takes the tiles k = s (mod 2) (with NS even, stage t always feeds lane
-// t % 2), with its own hidden operand H[s] (128 x W)
-// and W columns of tensor memory; warp w reads tensor-memory lanes
-// 32 * (w % 4) .. (one thread per row) and the lane's first thread issues
-// the MMAs.  A team refills its stage as soon as the layer-0 MMAs of its
+// t % 2), with its own hidden operand H[s] (128 x W) and W columns of
+// tensor memory; warp w reads tensor-memory lanes 32 * (w % 4) .. (one
+// thread per row) and the lane's first thread issues the MMAs.  A team refills its stage as soon as the layer-0 MMAs of its
 // previous tile have read it, so encoding runs while the layer warps walk
 // layers 1..L, and the two lanes fill each other's waits.  Hand-offs:
 // full[t] (team -> layer lane, one arrival after the team's named barrier),

@@ -48,3 +48,15 @@ def test_bad_arguments_are_rejected_without_touching_the_device(L):
     bad = hm.hair_params([0.1, 0.1, 0.1, 0.0, 0.3, 0.0, 1, 1, 1, 1])
     assert L.hm_bsdf_eval(ctypes.byref(q), None, None, 0, ctypes.byref(bad), None) == 1
     assert L.hm_hair_setup(None, None) == 1
+
+
+def test_inference_form_selector_checks_its_range(L):
+    """hm_debug_tc_path only sets the form of later inferences: no device
+    call, so it runs without a GPU."""
+    L.hm_debug_tc_path.argtypes = [ctypes.c_int]
+    L.hm_debug_tc_path.restype = ctypes.c_int
+    for bad in (-1, 3, 7):
+        assert L.hm_debug_tc_path(bad) == 1  # HM_EINVAL
+    assert b"out of range" in L.hm_last_error()
+    for ok in (2, 1, 0):
+        assert L.hm_debug_tc_path(ok) == 0
